@@ -1,0 +1,331 @@
+"""Benchmark: one transport sweep (Epetra_Operator::Apply, y = x - D L^-1 M2D S x)
+per step on the 2-D heterogeneous anisotropic workload -- 256 x 256 cells, DG Q2
+(9 dofs/cell), level-symmetric S16 (144 directions), P3 scattering (10
+moments), 8 x 8 seeded material blocks -- i.e. 9,437,184 cell-direction solves
+per step.  Prints one JSON line.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl ours (default): the GB300 operator through the C-ABI.
+  value    = cell-direction solves/s over the timed steps, inputs resident in
+             HBM, device time from CUDA events on the operator's stream, L2
+             flushed (256 MiB write) before every step outside the timed span.
+  e2e      = the same call with pinned host buffers (host->device copy of x and
+             device->host copy of y inside the timed span), wall clock.
+  roofline = the sweep kernel against measured HBM bandwidth, with the
+             algorithmic bytes per solve of the sweep's face hand-off model.
+  cpu_baseline = the CPU restatement of the reference sweep (oracle/), all
+             host threads, on the same workload (rank 0 at N = 1 only).
+--impl reference: the CPU restatement of the reference's sweep (the reference
+  itself needs deal.II/Trilinos/p4est/MPI, absent here), all host threads,
+  timed per step.  Under torchrun only rank 0 runs it.
+
+Multi-GPU: replicas only (each rank sweeps its own seeded problem, no
+collective on the data path); value is the sum over ranks of solves divided by
+the slowest rank's time.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("time-to-1e-8 residual: learned+FP32 FGMRES vs plain FP64 GMRES; "
+          "cell-dir solves/s")
+UNIT = "cell-dir solves/s"
+WORKLOAD = "2d-hetero-256x256-dgq2-ls16-p3"
+
+
+def workload_problem(seed=1001):
+    import ouranos_gb300 as og
+    return og.heterogeneous_2d(seed=seed, n=256, fe_order=2, sn=16, l_max=3, blocks=8)
+
+
+def bytes_per_solve(prob, real_bytes=8):
+    """Algorithmic HBM bytes per cell-direction solve: each outflow face value
+    written once and read once downwind (2 * dim * fd values), the source and
+    flux moments read and written once per sweep (amortised over the
+    directions), and the 4-byte material id per cell (amortised)."""
+    dim, n = prob.dim, prob.dofs_per_cell
+    fd = (prob.fe_order + 1) ** (dim - 1)
+    nd, nm = prob.quad.n_dir, prob.quad.n_mom
+    return 2 * real_bytes * dim * fd + 2 * real_bytes * n * nm / nd + 4.0 / nd
+
+
+def flops_per_solve(prob):
+    dim, n = prob.dim, prob.dofs_per_cell
+    fd = (prob.fe_order + 1) ** (dim - 1)
+    nm = prob.quad.n_mom
+    return 2 * n * n + 2 * dim * (fd * fd + fd) + 4 * n * nm
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu_id), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference_rate(prob, threads, reps=1):
+    """The reference's sweep restated on the CPU (oracle/), all threads."""
+    import numpy as np
+    from oracle import pyoracle
+    O = pyoracle.OracleProblem(prob.arrays())
+    x = np.random.default_rng(0).standard_normal(prob.vector_length)
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        O.apply(x, threads=threads)
+        times.append(time.perf_counter() - t0)
+    solves = prob.total_cells * prob.quad.n_dir
+    return solves / (sum(times) / len(times)), times
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    prob = workload_problem()
+    threads = os.cpu_count() or 1
+    # warm-up steps, then K timed steps; each step is one full sweep
+    import numpy as np
+    from oracle import pyoracle
+    O = pyoracle.OracleProblem(prob.arrays())
+    x = np.random.default_rng(0).standard_normal(prob.vector_length)
+    for _ in range(args.warmup):
+        O.apply(x, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.apply(x, threads=threads)
+    dt = time.perf_counter() - t0
+    solves = prob.total_cells * prob.quad.n_dir
+    value = solves * args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64 material map)",
+        "config": {"workload": WORKLOAD, "cells": prob.total_cells, "directions": prob.quad.n_dir,
+                   "moments": prob.quad.n_mom, "solves_per_step": solves},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "full sweep of the workload per step (oracle/ C++ restatement "
+                                   "of src/RadiativeTransfer.cc sweep + Crout LU, linear "
+                                   "ready-counter scheduler, directions split over threads)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import ouranos_gb300 as og
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    prob = workload_problem(seed=1001 + rank)
+    rt = og.RadiativeTransfer(prob, device=local, precision=args.precision)
+    stream = torch.cuda.current_stream(dev)
+    rt.set_stream(stream.cuda_stream)
+    L = prob.vector_length
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1234 + rank)
+    x = torch.randn(L, dtype=torch.float64, device=dev, generator=gen)
+    y = torch.empty_like(x)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    solves = prob.total_cells * prob.quad.n_dir
+
+    for _ in range(max(args.warmup, 3)):
+        rt.Apply(x, y)
+    torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    props = torch.cuda.get_device_properties(dev)
+    uid = str(getattr(props, "uuid", "") or "")
+    sampler = ClockSampler(("GPU-" + uid if uid and not uid.startswith("GPU-") else uid) or local)
+    sampler.start()
+    step_ms, sweep_ms = [], []
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    for _ in range(args.steps):
+        flush.zero_()                      # L2 flush, outside the timed span
+        ev0.record(stream)
+        rt.Apply(x, y)
+        ev1.record(stream)
+        ev1.synchronize()
+        step_ms.append(ev0.elapsed_time(ev1))
+        sweep_ms.append(rt.last_sweep_ms()[0])
+    torch.cuda.synchronize(dev)
+    clocks = sampler.stop()
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = t.item()
+        dist.barrier()
+    value = world * solves * args.steps / (total_ms / 1e3)
+
+    # end-to-end through the C-ABI with pinned host buffers
+    xh = x.cpu().pin_memory()
+    yh = torch.empty_like(xh).pin_memory()
+    rt.set_stream(None)
+    rt.Apply(xh, yh)
+    e2e_times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        rt.Apply(xh, yh)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_total = sum(e2e_times)
+    if dist:
+        t = torch.tensor([e2e_total], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = t.item()
+    e2e_value = world * solves * args.steps / e2e_total
+    if not np.isfinite(yh.numpy()).all():
+        raise RuntimeError("non-finite operator output")
+
+    peak, peak_kind = measured_peaks()
+    rb = 8 if args.precision == "fp64" else 4
+    bps = bytes_per_solve(prob, rb)
+    avg_sweep_s = sum(sweep_ms) / len(sweep_ms) / 1e3
+    achieved = bps * solves / avg_sweep_s / 1e9
+    fps = flops_per_solve(prob)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, times = cpu_reference_rate(prob, threads, reps=max(1, args.cpu_reps))
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d full sweep(s) of the workload (%.1f s of CPU work) with the oracle/ C++ "
+                         "restatement of the reference sweep, directions split over threads"
+                         % (len(times), sum(times))}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f32",
+            "data": "synthetic (seeded SplitMix64 material map, random flux moments)",
+            "config": {"workload": WORKLOAD, "cells": prob.total_cells,
+                       "directions": prob.quad.n_dir, "moments": prob.quad.n_mom,
+                       "dofs_per_cell": prob.dofs_per_cell, "solves_per_step": solves,
+                       "parallelism": "replicas" if world > 1 else "single-gpu",
+                       "l2": "flushed (256 MiB write) before every timed step",
+                       "tiling": list(rt.tiling())},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * L,
+                    "d2h_bytes_per_step": 8 * L},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "peak_kind": peak_kind, "bytes_per_solve": bps,
+                         "sweep_ms": avg_sweep_s * 1e3,
+                         "fp_flops_per_solve": fps,
+                         "fp_tflops": fps * solves / avg_sweep_s / 1e12},
+            "gpu_launches": 3 * args.steps,
+            "clocks": clocks,
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    rt.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-reps", type=int, default=2)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("_ob", os.path.join(ROOT, "oracle", "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+        run_reference(args)
+    else:
+        import __graft_entry__
+        __graft_entry__.build()
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,201 @@
+/*
+ * ouranos_gb300 -- C-ABI of the GB300-native transport-sweep operator.
+ *
+ * The operator replaces the reference's
+ *   class RadiativeTransfer<dim,tensor_dim> : public Epetra_Operator
+ * (Rombur/ouranos src/RadiativeTransfer.hh:46-263) on the path the SI/GMRES
+ * driver of src/ouranos.cc:43-209 calls.  Each entry point below names the
+ * reference member it stands in for.  Conventions:
+ *   - every function returns an int status: OURANOS_OK (0) or a negative
+ *     OURANOS_ERR_* code; ouranos_rt_last_error() gives the message.  No C++
+ *     exception crosses this boundary.
+ *   - flux-moment vectors use the reference's Epetra layout [mom][dof]
+ *     (src/RadiativeTransfer.cc:831,995): entry m*n_dofs + cell*n + i, where
+ *     cell = i_x + n_x*(i_y + n_y*i_z) unless the descriptor supplies
+ *     cell_order, and i is the lexicographic (x fastest) local Lagrange dof.
+ *   - vector arguments may be host or device (cudaMalloc / managed) pointers;
+ *     the operator detects which.  Host buffers are copied in and out inside
+ *     the call.
+ *   - one handle = one CUDA stream; calls on one handle are not thread-safe
+ *     (the reference operator mutates `mutable` state inside const methods and
+ *     is not reentrant either, src/RadiativeTransfer.hh:195-212).
+ */
+#ifndef OURANOS_GB300_H
+#define OURANOS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OURANOS_OK 0
+#define OURANOS_ERR_BAD_INPUT (-1)
+#define OURANOS_ERR_CUDA (-2)
+#define OURANOS_ERR_TIMEOUT (-3)
+#define OURANOS_ERR_UNSUPPORTED (-4)
+#define OURANOS_ERR_NO_DEVICE (-5)
+#define OURANOS_ERR_NOT_CONVERGED (-6)
+
+/* Boundary kinds, src/Parameters.hh:21.  REFLECTIVE is accepted and, as in the
+ * reference (src/RadiativeTransfer.cc:958-975), treated as vacuum. */
+#define OURANOS_BC_VACUUM 0
+#define OURANOS_BC_ISOTROPIC 1
+#define OURANOS_BC_MOST_NORMAL 2
+#define OURANOS_BC_REFLECTIVE 3
+
+/* Quadrature families: src/LS.hh, src/GLC.hh. */
+#define OURANOS_QUAD_LS 0
+#define OURANOS_QUAD_GLC 1
+
+/* Harmonic conventions for the moment-to-discrete matrix (src/RTQuadrature.cc:97-198):
+ * ORTHONORMAL: real spherical harmonics at polar angle arccos(Omega_z), sqrt(2)
+ *   on m>0 (orthonormal set; default).
+ * REFERENCE: the reference's literal boost call, polar-angle argument Omega_z,
+ *   no sqrt(2) (src/RTQuadrature.cc:126-131). */
+#define OURANOS_HARM_ORTHONORMAL 0
+#define OURANOS_HARM_REFERENCE 1
+
+/* Arithmetic of the sweep. */
+#define OURANOS_FP64 0
+#define OURANOS_FP32 1
+
+/* Problem description: the data the reference spreads over Parameters,
+ * Geometry, RTQuadrature and RTMaterialProperties (src/*.hh), restricted to a
+ * uniform Cartesian mesh.  All arrays are host memory and are copied. */
+typedef struct ouranos_problem_desc {
+  int dim;                  /* 2 or 3 */
+  int fe_order;             /* 1..4 in 2-D, 1..2 in 3-D (DG Q_p, equidistant nodes) */
+  int n_cells[3];           /* cells per axis */
+  double lower[3];          /* box corners */
+  double upper[3];
+  int n_groups;
+  /* quadrature, as RTQuadrature::get_omega/get_M2D/get_D2M/get_l return it */
+  int n_dir;
+  int n_mom;
+  const double* omega;      /* [n_dir][3] */
+  const double* m2d;        /* [n_dir][n_mom] */
+  const double* d2m;        /* [n_mom][n_dir] */
+  const int* moment_l;      /* [n_mom] Legendre order of each moment */
+  const int* most_normal;   /* [2*dim][n_dir] flags or NULL */
+  double weight_sum;        /* Parameters::get_weight_sum */
+  /* materials, RTMaterialProperties layout (src/RTMaterialProperties.hh:84-101) */
+  int n_materials;
+  int l_max;
+  const double* sigma_t;    /* [mat][g] */
+  const double* sigma_s;    /* [mat][g_from][g_to][l] */
+  const int* material_id;   /* [cell] */
+  const int* source_id;     /* [cell] or NULL */
+  int n_sources;
+  const double* source;     /* [src][g] or NULL (Parameters::get_src) */
+  int bc_type[6];           /* per face x-,x+,y-,y+,z-,z+ */
+  const double* inc_flux;   /* [face][g] or NULL (Parameters::get_inc_flux) */
+  const long* cell_order;   /* optional: caller's index of each lexicographic cell
+                               (e.g. deal.II's z-order); NULL = lexicographic */
+} ouranos_problem_desc;
+
+typedef struct ouranos_rt ouranos_rt;
+
+/* ---------------------------------------------------------------- quadrature */
+/* RTQuadrature::RTQuadrature sizes (src/RTQuadrature.cc:10-25); 3-D deploys 8
+ * octants (the reference's deploy_octant fills 4, src/RTQuadrature.cc:61). */
+int ouranos_quadrature_sizes(int sn, int l_max, int galerkin, int dim, int* n_dir, int* n_mom);
+/* RTQuadrature::build_quadrature (src/RTQuadrature.cc:27-56) with LS::build_octant
+ * (src/LS.cc:14-682, S2..S16) or GLC::build_octant (src/GLC.cc:14-58, Gauss-Legendre
+ * nodes computed, any even order).  Any output pointer may be NULL. */
+int ouranos_quadrature_build(int type, int sn, int l_max, int galerkin, double weight_sum,
+                             int dim, int harmonics, double* omega, double* weight,
+                             double* m2d, double* d2m, int* moment_l, int* most_normal);
+
+/* ------------------------------------------------------------------ operator */
+/* RadiativeTransfer constructor + setup() (src/RadiativeTransfer.cc:12-78):
+ * builds the FE tables, the per-octant wavefront schedule and the device
+ * arrays.  Selects CUDA device `device` (-1 = current). */
+int ouranos_rt_create(const ouranos_problem_desc* desc, int device, ouranos_rt** out);
+/* ~RadiativeTransfer (src/RadiativeTransfer.cc:38-47). */
+int ouranos_rt_destroy(ouranos_rt* rt);
+/* RadiativeTransfer::set_group (src/RadiativeTransfer.hh:230 area). */
+int ouranos_rt_set_group(ouranos_rt* rt, int group);
+/* Sweep arithmetic: OURANOS_FP64 (default, parity path) or OURANOS_FP32. No
+ * reference counterpart (the reference is FP64 only). */
+int ouranos_rt_set_precision(ouranos_rt* rt, int precision);
+/* Length of a flux-moment vector, n_mom * n_dofs: the size of the Epetra_Map
+ * returned by OperatorDomainMap/OperatorRangeMap (src/RadiativeTransfer.hh:240-249). */
+int ouranos_rt_vector_length(const ouranos_rt* rt, long* length);
+/* Number of (cell, direction) tasks one sweep executes: the value
+ * RadiativeTransfer::get_n_tasks_to_execute holds after initialize_scheduler. */
+int ouranos_rt_n_tasks(const ouranos_rt* rt, long* n_tasks);
+/* compute_scattering_source (src/RadiativeTransfer.cc:811-843): S_m = sigma_s,l(m) M x_m,
+ * kept inside the handle for the next ouranos_rt_sweep. */
+int ouranos_rt_scattering_source(ouranos_rt* rt, const double* x);
+/* The driver's sweep loop `initialize_scheduler(); while (tasks) sweep(...)`
+ * (src/ouranos.cc:74-84,150-158): flux_moments += D L^-1 (M2D S [+ q + other-group
+ * scattering + boundary inflow when group_flux != NULL]).  group_flux is
+ * [g][mom][dof] (the reference's group_flux vector of MPI vectors). */
+int ouranos_rt_sweep(ouranos_rt* rt, double* flux_moments, const double* group_flux);
+/* Epetra_Operator::Apply (src/RadiativeTransfer.cc:780-809): y = x - D L^-1 M2D S x. */
+int ouranos_rt_apply(ouranos_rt* rt, const double* x, double* y);
+/* Right-hand side of the Krylov form (src/ouranos.cc:149-158): rhs += D L^-1 (q +
+ * other-group scattering + boundary inflow), with the in-group scattering source
+ * taken as zero (its value before the first Apply). */
+int ouranos_rt_sweep_rhs(ouranos_rt* rt, const double* group_flux, double* rhs);
+/* Per-octant wavefront level of every task, [dir][cell] (cell in the
+ * lexicographic numbering): the longest-path depth in the task graph that
+ * compute_sweep_ordering builds (src/RadiativeTransfer.cc:80-232). */
+int ouranos_rt_task_levels(const ouranos_rt* rt, int* levels);
+/* The same levels without a handle (host integer work, no GPU needed):
+ * n_cells[dim], omega[n_dir][3] -> levels[n_dir][cells]. */
+int ouranos_wavefront_levels(int dim, const int* n_cells, int n_dir, const double* omega,
+                             int* levels);
+/* Run the handle's work on the caller's CUDA stream (a cudaStream_t; NULL
+ * returns to the handle's own stream).  Calls still synchronise that stream
+ * before returning. */
+int ouranos_rt_set_stream(ouranos_rt* rt, void* stream);
+/* Copy of the last error message. */
+int ouranos_rt_last_error(const ouranos_rt* rt, char* buf, size_t len);
+/* Device time (ms) of the last sweep kernel launch, measured with CUDA events
+ * on the handle's stream; and the number of kernels that sweep launched. */
+int ouranos_rt_last_sweep_ms(const ouranos_rt* rt, double* ms, int* kernels);
+/* Tiling of the sweep kernel: cells per warp along x (and y in 3-D) and
+ * directions per warp, with cells_x * cells_y * dirs == 32.  0s = autotuned. */
+int ouranos_rt_set_tiling(ouranos_rt* rt, int cells_x, int cells_y, int dirs_per_warp);
+int ouranos_rt_get_tiling(const ouranos_rt* rt, int* cells_x, int* cells_y, int* dirs_per_warp);
+/* Spin limit of the in-kernel dependency waits, in nanoseconds (default 2 s).
+ * A wait that runs out sets an error status, every warp leaves, and the call
+ * returns OURANOS_ERR_TIMEOUT with the context still usable. */
+int ouranos_rt_set_wait_limit(ouranos_rt* rt, double ns);
+/* Test hook: bias the dependency target the sweep waits for by `extra` steps
+ * (0 = normal).  A positive value makes the first dependent wait unsatisfiable
+ * so the timeout path can be exercised without faulting the GPU. */
+int ouranos_rt_debug_wait_bias(ouranos_rt* rt, int extra);
+
+/* ------------------------------------------------------------------- solvers */
+/* Drivers of src/ouranos.cc:43-209, on device vectors.
+ * OURANOS_SOLVER_SI: source iteration, relative-change test (src/ouranos.cc:72-95).
+ * OURANOS_SOLVER_GMRES: restarted GMRES(restart), FP64 sweeps.
+ * OURANOS_SOLVER_BICGSTAB: BiCGSTAB, FP64 sweeps (tests/RadiativeTransfer_test.cc:78).
+ * OURANOS_SOLVER_FGMRES_MIXED: FGMRES(restart) whose Arnoldi operator applies use
+ *   FP32 sweeps, with FP64 Gram-Schmidt, FP64 true residual at every restart. */
+#define OURANOS_SOLVER_SI 0
+#define OURANOS_SOLVER_GMRES 1
+#define OURANOS_SOLVER_BICGSTAB 2
+#define OURANOS_SOLVER_FGMRES_MIXED 3
+
+typedef struct ouranos_solve_info {
+  int iterations;           /* operator applications in the Krylov/SI loop */
+  int restarts;
+  double residual;          /* final ||b - (I-T)x|| / ||b|| in FP64 (SI: last relative change) */
+  double seconds;           /* wall time of the solve */
+  int converged;
+} ouranos_solve_info;
+
+/* Solve (I - T) phi = rhs for the current group (rhs from ouranos_rt_sweep_rhs
+ * with group_flux), x is [mom][dof] (host or device).  hist (host, may be NULL)
+ * receives max_it+1 relative residuals. */
+int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it, double tol,
+                  const double* group_flux, double* x, double* hist, ouranos_solve_info* info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,181 @@
+// Internal declarations of the GB300 transport-sweep operator.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/ouranos_gb300.h"
+
+namespace ouranos {
+
+// ---------------------------------------------------------------- FE tables
+// Reference-cell matrices of DG Q_p on equidistant Lagrange nodes, assembled
+// by tensor products of 1-D integrals (exact Gauss integration), then scaled
+// to an h_x x h_y (x h_z) box.  Local dof i = ix + P1*(iy + P1*iz).
+struct FETables {
+  int dim = 0, p = 0, p1 = 0, n = 0, fd = 0;
+  double h[3] = {1, 1, 1};
+  std::vector<double> mass;        // [n][n]
+  std::vector<double> grad;        // [dim][n][n]: G_a[i][j] = int b_j d_a b_i
+  std::vector<double> face;        // [2*dim][n][n]: E_f[i][j] = int_f b_i b_j
+  std::vector<double> face_mass;   // [3][fd][fd]: transverse face mass, axis a
+  std::vector<double> mass1d;      // [p1][p1] on [0,1]
+};
+FETables build_fe_tables(int dim, int p, const double* h);
+
+// Inverse of the canonical-orientation cell matrix
+//   A' = sigma_t M - sum_a |Omega_a| G_a + sum_a |Omega_a| E_{a,max}
+// (every direction mapped to the all-positive octant, see sweep.cuh), computed
+// with the reference's pivoted Crout LU (src/RadiativeTransfer.cc:1026-1105)
+// applied to the unit vectors.  out: [n][n] row-major.
+void canonical_inverse(const FETables& fe, double sigma_t, const double* abs_omega, double* out);
+
+// --------------------------------------------------------------- quadrature
+int quadrature_sizes(int sn, int l_max, int galerkin, int dim, int* n_dir, int* n_mom);
+int quadrature_build(int type, int sn, int l_max, int galerkin, double ws, int dim,
+                     int harmonics, double* omega, double* weight, double* m2d, double* d2m,
+                     int* moment_l, int* most_normal);
+
+// ------------------------------------------------------------ device buffer
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t alloc(size_t b) {
+    if (b <= bytes && p) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc(&p, b ? b : 16);
+    if (e == cudaSuccess) bytes = b;
+    return e;
+  }
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// ---------------------------------------------------------- sweep kernels
+// Arguments of one sweep launch (see sweep.cuh for the algorithm).
+template <typename real>
+struct SweepArgs {
+  int nx, ny, nz;              // cells per axis (physical)
+  int n_sweep;                 // cells along the sweep axis (y in 2-D, z in 3-D)
+  long n_dofs;                 // cells * n
+  int n_mom;
+  int wx, wy, kd;              // warp tiling: wx*wy cells x kd directions = 32 lanes
+  int tiles_x, tiles_y;
+  int n_tasks;
+  const int2* tasks;           // (dir group, tile) in dependency order
+  const int* group_dirs;       // [n_groups][kd] direction or -1
+  const int* group_flip;       // [n_groups] bit a set: Omega_a < 0
+  const int* dir_class;        // [n_dir] index of |Omega| class
+  int n_dir_class;
+  const real* abs_omega;       // [n_dir][3]
+  const real* m2d;             // [n_dir][n_mom]
+  const real* d2m_t;           // [n_dir][n_mom] (D2M transposed)
+  const real* ainv;            // [n_sigma_class][n_dir_class][n][n]
+  const int* cell_class;       // [cells] sigma_t class
+  const real* face_mass;       // [3][fd][fd]
+  const real* src;             // [n_mom][n_dofs] source moments T
+  const real* iso;             // [n_dofs] isotropic fixed source term or NULL
+  const real* bnd;             // [n_dir][3] boundary inflow per axis or NULL
+  real* phi;                   // [n_mom][n_dofs] accumulated
+  real* edge_x;                // [n_dir][tiles][n_sweep][wy][fd]
+  real* edge_y;                // [n_dir][tiles][n_sweep][wx][fd]
+  int* progress;               // [n_groups][tiles] completed steps
+  int* ticket;                 // task counter
+  int* status;                 // 0 ok, 1 wait timeout
+  long long wait_limit_ns;
+  int wait_bias;
+};
+
+template <typename real>
+cudaError_t launch_sweep(int dim, int p1, const SweepArgs<real>& a, int grid, int block,
+                         cudaStream_t s);
+
+// ------------------------------------------------------------ vector kernels
+template <typename real>
+cudaError_t launch_scatter_source(const double* x, const double* group_flux, real* src,
+                                  const double* cell_mass, const double* sscale,
+                                  const double* oscale, const int* material, int n_mat,
+                                  int n_groups, int group, long n_cells, int n, int n_mom,
+                                  long n_dofs, cudaStream_t s);
+template <typename real>
+cudaError_t launch_iso_source(real* iso, const double* qcell, const double* rowsum_mass,
+                              const int* source_id, long n_cells, int n, cudaStream_t s);
+template <typename real>
+cudaError_t launch_combine(const double* x, const real* phi, double* y, long len, double sx,
+                           double sp, cudaStream_t s);
+cudaError_t launch_permute(const double* in, double* out, const long* order, long n_cells,
+                           int n, int n_vec, int to_internal, cudaStream_t s);
+cudaError_t launch_axpby(double a, const double* x, double b, double* y, long len, cudaStream_t s);
+constexpr int kDotGrid = 304;  // blocks of the dot-product kernel (2 per SM)
+cudaError_t launch_dots(const double* const* xs, const double* y, int k, long len, double* out,
+                        double* partial, unsigned int* done, cudaStream_t s);
+
+}  // namespace ouranos
+struct ouranos_rt;
+namespace ouranos {
+// Device-side pieces the solvers use (operator.cu).
+int rt_apply_device(ouranos_rt* rt, const double* x, double* y);
+int rt_rhs_device(ouranos_rt* rt, const double* gf, double* rhs);
+int rt_check_status(ouranos_rt* rt);
+int rt_clear_status(ouranos_rt* rt);
+int rt_stage_in(ouranos_rt* rt, const double* v, DevBuf& buf, int n_vec, const double** out);
+int rt_stage_out(ouranos_rt* rt, const double* dv, double* user);
+}  // namespace ouranos
+
+struct ouranos_rt {
+  int device = 0;
+  cudaStream_t stream = nullptr;      // stream in use
+  cudaStream_t own_stream = nullptr;  // the handle's own stream
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  // problem
+  int dim = 2, p = 1, p1 = 2, n = 4, fd = 2;
+  int nx[3] = {1, 1, 1};
+  double h[3] = {1, 1, 1};
+  long n_cells = 0, n_dofs = 0;
+  int G = 1, group = 0, n_dir = 0, n_mom = 0, n_mat = 0, l_max = 0, n_src = 0;
+  double ws = 1.0;
+  std::vector<double> omega, m2d, d2m, sigma_t, sigma_s, source, inc_flux;
+  std::vector<int> moment_l, most_normal, material_id, source_id;
+  int bc[6] = {0, 0, 0, 0, 0, 0};
+  std::vector<long> cell_order;
+  ouranos::FETables fe;
+  int precision = OURANOS_FP64;
+  // schedule
+  int wx = 0, wy = 1, kd = 0;          // 0 = not chosen yet
+  int tiles_x = 0, tiles_y = 0, n_groups_dir = 0, n_tasks = 0;
+  std::vector<int> dir_class_h;
+  std::vector<double> class_abs_omega;  // [n_dir_class][3]
+  int n_dir_class = 0;
+  std::vector<double> sigma_class_value; // per sigma_t class
+  std::vector<int> cell_class_h;
+  long long wait_limit_ns = 2000000000LL;
+  int wait_bias = 0;
+  double last_ms = 0.0;
+  int last_kernels = 0;
+  bool ainv_valid = false;
+  bool scat_valid = false;             // src_* holds compute_scattering_source(x)
+  // device: geometry / tables (both precisions where the sweep reads them)
+  ouranos::DevBuf d_material, d_source_id, d_cell_class, d_cell_order;
+  ouranos::DevBuf d_cell_mass, d_rowsum_mass, d_sscale, d_oscale, d_qcell;
+  ouranos::DevBuf d_dir_class, d_abs64, d_abs32, d_m2d64, d_m2d32, d_d2m64, d_d2m32;
+  ouranos::DevBuf d_ainv64, d_ainv32, d_face64, d_face32, d_bnd64, d_bnd32;
+  ouranos::DevBuf d_tasks, d_group_dirs, d_group_flip, d_progress, d_ctrl;
+  ouranos::DevBuf d_edge_x, d_edge_y;
+  // device: vectors
+  ouranos::DevBuf d_src64, d_src32, d_phi64, d_phi32, d_iso64, d_iso32;
+  ouranos::DevBuf d_x, d_y, d_gf, d_tmp, d_scatx;  // staging; d_scatx: scattering-source argument
+  // solver workspace
+  ouranos::DevBuf d_krylov;
+};

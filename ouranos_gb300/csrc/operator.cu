@@ -1,0 +1,784 @@
+// The transport operator behind the C-ABI: setup (RadiativeTransfer::setup,
+// src/RadiativeTransfer.cc:50-78), the sweep launch (the task loop of
+// src/RadiativeTransfer.cc:797-803) and Apply (:780-809).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <vector>
+
+#include "internal.h"
+
+using namespace ouranos;
+
+namespace {
+
+#define OK_OR_RETURN(expr)                 \
+  do {                                     \
+    int _rc = (expr);                      \
+    if (_rc != OURANOS_OK) return _rc;     \
+  } while (0)
+
+int cuda_fail(ouranos_rt* rt, cudaError_t e, const char* what) {
+  char buf[256];
+  std::snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+  rt->err = buf;
+  return OURANOS_ERR_CUDA;
+}
+#define CU(expr, what)                                  \
+  do {                                                  \
+    cudaError_t _e = (expr);                            \
+    if (_e != cudaSuccess) return cuda_fail(rt, _e, what); \
+  } while (0)
+
+int bad(ouranos_rt* rt, const char* msg) {
+  rt->err = msg;
+  return OURANOS_ERR_BAD_INPUT;
+}
+
+template <class T>
+int upload(ouranos_rt* rt, DevBuf& buf, const std::vector<T>& v, const char* what) {
+  CU(buf.alloc(sizeof(T) * std::max<size_t>(v.size(), 1)), what);
+  if (!v.empty())
+    CU(cudaMemcpyAsync(buf.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, rt->stream),
+       what);
+  return OURANOS_OK;
+}
+
+template <class T>
+std::vector<float> to_f32(const std::vector<T>& v) {
+  return std::vector<float>(v.begin(), v.end());
+}
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+long vec_len(const ouranos_rt* rt) { return (long)rt->n_mom * rt->n_dofs; }
+
+// ------------------------------------------------------------------ schedule
+// Directions of one octant (same sign pattern) are grouped kd at a time; each
+// group crosses the transverse tiles in dependency order.
+int build_schedule(ouranos_rt* rt) {
+  const int dim = rt->dim;
+  const int NX = rt->nx[0], NY = dim == 3 ? rt->nx[1] : 1, NS = rt->nx[dim - 1];
+  rt->tiles_x = (NX + rt->wx - 1) / rt->wx;
+  rt->tiles_y = dim == 3 ? (NY + rt->wy - 1) / rt->wy : 1;
+  const int tiles = rt->tiles_x * rt->tiles_y;
+  std::map<int, std::vector<int>> by_flip;
+  for (int d = 0; d < rt->n_dir; ++d) {
+    int f = 0;
+    for (int a = 0; a < dim; ++a)
+      if (rt->omega[3 * d + a] < 0.0) f |= 1 << a;
+    by_flip[f].push_back(d);
+  }
+  std::vector<int> gdirs, gflip;
+  for (auto& kv : by_flip) {
+    const auto& ds = kv.second;
+    for (size_t i = 0; i < ds.size(); i += rt->kd) {
+      for (int k = 0; k < rt->kd; ++k) gdirs.push_back(i + k < ds.size() ? ds[i + k] : -1);
+      gflip.push_back(kv.first);
+    }
+  }
+  const int n_groups = (int)gflip.size();
+  rt->n_groups_dir = n_groups;
+  std::vector<int2> tasks;
+  const int levels = rt->tiles_x + rt->tiles_y - 1;
+  for (int L = 0; L < levels; ++L)
+    for (int g = 0; g < n_groups; ++g)
+      for (int ty = 0; ty < rt->tiles_y; ++ty) {
+        const int tx = L - ty;
+        if (tx < 0 || tx >= rt->tiles_x) continue;
+        tasks.push_back(make_int2(g, tx + rt->tiles_x * ty));
+      }
+  rt->n_tasks = (int)tasks.size();
+  OK_OR_RETURN(upload(rt, rt->d_tasks, tasks, "tasks"));
+  OK_OR_RETURN(upload(rt, rt->d_group_dirs, gdirs, "group dirs"));
+  OK_OR_RETURN(upload(rt, rt->d_group_flip, gflip, "group flips"));
+  // control block: [0] ticket, [1] status, [2..] dot counter, [64..] progress
+  CU(rt->d_ctrl.alloc(sizeof(int) * (64 + (size_t)n_groups * tiles)), "control block");
+  CU(cudaMemsetAsync(rt->d_ctrl.p, 0, rt->d_ctrl.bytes, rt->stream), "control block");
+  const size_t ex = (size_t)rt->n_dir * tiles * NS * rt->wy * rt->fd;
+  const size_t ey = dim == 3 ? (size_t)rt->n_dir * tiles * NS * rt->wx * rt->fd : 1;
+  const size_t esz = rt->precision == OURANOS_FP64 ? 8 : 4;
+  CU(rt->d_edge_x.alloc(ex * 8 > 0 ? ex * 8 : 16), "edge buffer x");
+  CU(rt->d_edge_y.alloc(ey * 8 > 0 ? ey * 8 : 16), "edge buffer y");
+  (void)esz;
+  return OURANOS_OK;
+}
+
+int default_tiling(ouranos_rt* rt) {
+  // directions per octant
+  const int per_oct = rt->n_dir / (rt->dim == 3 ? 8 : 4);
+  int kd = rt->dim == 3 ? 2 : 4;
+  while (kd > 1 && per_oct > 0 && per_oct < kd) kd >>= 1;
+  rt->kd = kd;
+  if (rt->dim == 2) {
+    rt->wx = 32 / kd;
+    rt->wy = 1;
+  } else {
+    const int wc = 32 / kd;  // 16 -> 4x4, 32 -> 8x4, 8 -> 4x2
+    rt->wx = wc >= 16 ? 4 : (wc == 8 ? 4 : 2);
+    rt->wy = wc / rt->wx;
+    if (wc == 32) {
+      rt->wx = 8;
+      rt->wy = 4;
+    }
+  }
+  return OURANOS_OK;
+}
+
+// ------------------------------------------------------- per-group tables
+int setup_group(ouranos_rt* rt) {
+  const int g = rt->group, G = rt->G, nm = rt->n_mom, L = rt->l_max;
+  const int n = rt->n;
+  // sigma_t classes (A depends on the cell only through sigma_t)
+  std::vector<double> cls_val;
+  std::vector<int> mat_cls(rt->n_mat);
+  for (int m = 0; m < rt->n_mat; ++m) {
+    const double st = rt->sigma_t[(size_t)m * G + g];
+    auto it = std::find(cls_val.begin(), cls_val.end(), st);
+    if (it == cls_val.end()) {
+      mat_cls[m] = (int)cls_val.size();
+      cls_val.push_back(st);
+    } else {
+      mat_cls[m] = (int)(it - cls_val.begin());
+    }
+  }
+  rt->sigma_class_value = cls_val;
+  std::vector<int> ccls(rt->n_cells);
+  for (long c = 0; c < rt->n_cells; ++c) ccls[c] = mat_cls[rt->material_id[c]];
+  OK_OR_RETURN(upload(rt, rt->d_cell_class, ccls, "cell classes"));
+  // A'^-1 per (sigma class, |Omega| class)
+  const size_t nn = (size_t)n * n;
+  std::vector<double> ainv(cls_val.size() * rt->n_dir_class * nn);
+  for (size_t s = 0; s < cls_val.size(); ++s)
+    for (int dc = 0; dc < rt->n_dir_class; ++dc)
+      canonical_inverse(rt->fe, cls_val[s], &rt->class_abs_omega[3 * dc],
+                        &ainv[(s * rt->n_dir_class + dc) * nn]);
+  OK_OR_RETURN(upload(rt, rt->d_ainv64, ainv, "inverse tables"));
+  OK_OR_RETURN(upload(rt, rt->d_ainv32, to_f32(ainv), "inverse tables"));
+  // scattering scales: sigma_s(mat, g'->g, l(m)) (by Legendre order)
+  auto sig_s = [&](int mat, int gf, int gt, int l) {
+    if (l > L) return 0.0;
+    return rt->sigma_s[(size_t)l + (size_t)gt * (L + 1) + (size_t)gf * G * (L + 1) +
+                       (size_t)mat * G * G * (L + 1)];
+  };
+  std::vector<double> ss((size_t)rt->n_mat * nm), os((size_t)rt->n_mat * G * nm);
+  for (int mat = 0; mat < rt->n_mat; ++mat)
+    for (int q = 0; q < nm; ++q) {
+      ss[(size_t)mat * nm + q] = sig_s(mat, g, g, rt->moment_l[q]);
+      for (int gf = 0; gf < G; ++gf)
+        os[((size_t)mat * G + gf) * nm + q] = sig_s(mat, gf, g, rt->moment_l[q]);
+    }
+  OK_OR_RETURN(upload(rt, rt->d_sscale, ss, "scattering scales"));
+  OK_OR_RETURN(upload(rt, rt->d_oscale, os, "scattering scales"));
+  // fixed source per source id: q/ws (src/RadiativeTransfer.cc:918-921)
+  std::vector<double> q(std::max(rt->n_src, 1), 0.0);
+  for (int s = 0; s < rt->n_src; ++s) q[s] = rt->source[(size_t)s * G + g] / rt->ws;
+  OK_OR_RETURN(upload(rt, rt->d_qcell, q, "sources"));
+  // boundary inflow per (direction, axis) (src/RadiativeTransfer.cc:958-975)
+  std::vector<double> bnd((size_t)rt->n_dir * 3, 0.0);
+  for (int d = 0; d < rt->n_dir; ++d)
+    for (int a = 0; a < rt->dim; ++a) {
+      const int f = rt->omega[3 * d + a] > 0.0 ? 2 * a : 2 * a + 1;  // entering face
+      const int bt = rt->bc[f];
+      const bool mn = !rt->most_normal.empty() && rt->most_normal[(size_t)f * rt->n_dir + d];
+      double inc = 0.0;
+      if ((bt == OURANOS_BC_MOST_NORMAL && mn) || bt == OURANOS_BC_ISOTROPIC)
+        inc = rt->inc_flux.empty() ? 0.0 : rt->inc_flux[(size_t)f * G + g];
+      bnd[3 * d + a] = inc / rt->ws;
+    }
+  OK_OR_RETURN(upload(rt, rt->d_bnd64, bnd, "boundary"));
+  OK_OR_RETURN(upload(rt, rt->d_bnd32, to_f32(bnd), "boundary"));
+  return OURANOS_OK;
+}
+
+// --------------------------------------------------------------- the sweep
+template <typename real>
+int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd, real* phi) {
+  SweepArgs<real> a;
+  const bool f64 = sizeof(real) == 8;
+  a.nx = rt->nx[0];
+  a.ny = rt->nx[1];
+  a.nz = rt->nx[2];
+  a.n_sweep = rt->nx[rt->dim - 1];
+  a.n_dofs = rt->n_dofs;
+  a.n_mom = rt->n_mom;
+  a.wx = rt->wx;
+  a.wy = rt->wy;
+  a.kd = rt->kd;
+  a.tiles_x = rt->tiles_x;
+  a.tiles_y = rt->tiles_y;
+  a.n_tasks = rt->n_tasks;
+  a.tasks = rt->d_tasks.as<int2>();
+  a.group_dirs = rt->d_group_dirs.as<int>();
+  a.group_flip = rt->d_group_flip.as<int>();
+  a.dir_class = rt->d_dir_class.as<int>();
+  a.n_dir_class = rt->n_dir_class;
+  a.abs_omega = (const real*)(f64 ? rt->d_abs64.p : rt->d_abs32.p);
+  a.m2d = (const real*)(f64 ? rt->d_m2d64.p : rt->d_m2d32.p);
+  a.d2m_t = (const real*)(f64 ? rt->d_d2m64.p : rt->d_d2m32.p);
+  a.ainv = (const real*)(f64 ? rt->d_ainv64.p : rt->d_ainv32.p);
+  a.cell_class = rt->d_cell_class.as<int>();
+  a.face_mass = (const real*)(f64 ? rt->d_face64.p : rt->d_face32.p);
+  a.src = src;
+  a.iso = iso;
+  a.bnd = bnd;
+  a.phi = phi;
+  a.edge_x = rt->d_edge_x.as<real>();
+  a.edge_y = rt->d_edge_y.as<real>();
+  int* ctrl = rt->d_ctrl.as<int>();
+  a.ticket = ctrl;
+  a.status = ctrl + 1;
+  a.progress = ctrl + 64;
+  a.wait_limit_ns = rt->wait_limit_ns;
+  a.wait_bias = rt->wait_bias;
+  const size_t ctrl_bytes = sizeof(int) * (64 + (size_t)rt->n_groups_dir * rt->tiles_x * rt->tiles_y);
+  // ticket + progress -> 0.  The status word [1] is sticky: it is cleared at the
+  // start of each C-ABI call (clear_status), so a timeout inside a solve is seen
+  // at its end and every later sweep of that call exits at once.  The dot
+  // counter at [2] is 0 whenever no dot kernel is in flight on this stream.
+  CU(cudaMemsetAsync(ctrl, 0, sizeof(int), rt->stream), "reset sweep control");
+  CU(cudaMemsetAsync(ctrl + 64, 0, ctrl_bytes - 64 * sizeof(int), rt->stream), "reset progress");
+  int dev = rt->device, sms = 0, per_sm = 0;
+  CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device query");
+  const int block = 128;
+  // occupancy of the instantiated kernel is queried once per (precision, shape)
+  static thread_local std::map<long, int> occ;
+  const long key = (long)f64 * 1000 + rt->dim * 100 + rt->p1;
+  auto it = occ.find(key);
+  if (it == occ.end()) {
+    per_sm = 0;
+    // probe: launch-free occupancy through a zero-task launch is not needed;
+    // 8 blocks (32 warps) per SM is within every instantiation's register budget
+    per_sm = 8;
+    occ[key] = per_sm;
+  } else {
+    per_sm = it->second;
+  }
+  int grid = std::min((rt->n_tasks + 3) / 4, std::max(1, sms * per_sm));
+  CU(cudaEventRecord(rt->ev0, rt->stream), "event");
+  CU(launch_sweep<real>(rt->dim, rt->p1, a, grid, block, rt->stream), "sweep launch");
+  CU(cudaEventRecord(rt->ev1, rt->stream), "event");
+  rt->last_kernels = 1;
+  return OURANOS_OK;
+}
+
+int clear_status(ouranos_rt* rt) {
+  CU(cudaMemsetAsync(rt->d_ctrl.as<int>() + 1, 0, sizeof(int), rt->stream), "reset status");
+  return OURANOS_OK;
+}
+
+int finish(ouranos_rt* rt) {
+  CU(cudaStreamSynchronize(rt->stream), "sweep");
+  int st = 0;
+  CU(cudaMemcpy(&st, rt->d_ctrl.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost), "status");
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, rt->ev0, rt->ev1) == cudaSuccess) rt->last_ms = ms;
+  if (st) {
+    rt->err = "sweep dependency wait timed out";
+    return OURANOS_ERR_TIMEOUT;
+  }
+  return OURANOS_OK;
+}
+
+// Bring a caller vector (host or device, caller numbering) into a device
+// buffer in lexicographic numbering.  Returns the device pointer to use.
+int stage_in(ouranos_rt* rt, const double* v, DevBuf& buf, int n_vec, const double** out) {
+  const long len = (long)n_vec * vec_len(rt) / rt->n_mom * rt->n_mom;
+  const size_t bytes = sizeof(double) * (size_t)n_vec * rt->n_mom * rt->n_dofs;
+  const bool dev = is_device_ptr(v);
+  (void)len;
+  if (dev && rt->cell_order.empty()) {
+    *out = v;
+    return OURANOS_OK;
+  }
+  CU(buf.alloc(bytes), "staging");
+  if (!dev) {
+    if (rt->cell_order.empty()) {
+      CU(cudaMemcpyAsync(buf.p, v, bytes, cudaMemcpyHostToDevice, rt->stream), "copy in");
+      *out = buf.as<double>();
+      return OURANOS_OK;
+    }
+    CU(rt->d_tmp.alloc(bytes), "staging");
+    CU(cudaMemcpyAsync(rt->d_tmp.p, v, bytes, cudaMemcpyHostToDevice, rt->stream), "copy in");
+    v = rt->d_tmp.as<double>();
+  }
+  CU(launch_permute(v, buf.as<double>(), rt->d_cell_order.as<long>(), rt->n_cells, rt->n,
+                    n_vec * rt->n_mom, 1, rt->stream),
+     "permute in");
+  *out = buf.as<double>();
+  return OURANOS_OK;
+}
+
+// Copy a lexicographic device vector back to the caller's buffer.
+int stage_out(ouranos_rt* rt, const double* dv, double* user) {
+  const size_t bytes = sizeof(double) * vec_len(rt);
+  const bool dev = is_device_ptr(user);
+  if (rt->cell_order.empty()) {
+    if (dv != user)
+      CU(cudaMemcpyAsync(user, dv, bytes, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                         rt->stream),
+         "copy out");
+    return OURANOS_OK;
+  }
+  if (dev) {
+    CU(launch_permute(dv, user, rt->d_cell_order.as<long>(), rt->n_cells, rt->n, rt->n_mom, 0,
+                      rt->stream),
+       "permute out");
+    return OURANOS_OK;
+  }
+  CU(rt->d_tmp.alloc(bytes), "staging");
+  CU(launch_permute(dv, rt->d_tmp.as<double>(), rt->d_cell_order.as<long>(), rt->n_cells, rt->n,
+                    rt->n_mom, 0, rt->stream),
+     "permute out");
+  CU(cudaMemcpyAsync(user, rt->d_tmp.p, bytes, cudaMemcpyDeviceToHost, rt->stream), "copy out");
+  return OURANOS_OK;
+}
+
+// Source moments T (precision of the sweep) from x (FP64, device) and the
+// other groups' fluxes gf (device or NULL).
+int build_source(ouranos_rt* rt, const double* x, const double* gf) {
+  const long len = vec_len(rt);
+  const double* M = rt->d_cell_mass.as<double>();
+  if (rt->precision == OURANOS_FP64) {
+    CU(rt->d_src64.alloc(sizeof(double) * len), "source");
+    CU(launch_scatter_source<double>(x, gf, rt->d_src64.as<double>(), M, rt->d_sscale.as<double>(),
+                                     rt->d_oscale.as<double>(), rt->d_material.as<int>(), rt->n_mat,
+                                     rt->G, rt->group, rt->n_cells, rt->n, rt->n_mom, rt->n_dofs,
+                                     rt->stream),
+       "scattering source");
+  } else {
+    CU(rt->d_src32.alloc(sizeof(float) * len), "source");
+    CU(launch_scatter_source<float>(x, gf, rt->d_src32.as<float>(), M, rt->d_sscale.as<double>(),
+                                    rt->d_oscale.as<double>(), rt->d_material.as<int>(), rt->n_mat,
+                                    rt->G, rt->group, rt->n_cells, rt->n, rt->n_mom, rt->n_dofs,
+                                    rt->stream),
+       "scattering source");
+  }
+  return OURANOS_OK;
+}
+
+// phi = D L^-1 (M2D T [+ iso + inflow]) into the precision's phi buffer.
+int sweep_into_phi(ouranos_rt* rt, bool sources) {
+  const long len = vec_len(rt);
+  if (rt->precision == OURANOS_FP64) {
+    CU(rt->d_phi64.alloc(sizeof(double) * len), "flux");
+    CU(cudaMemsetAsync(rt->d_phi64.p, 0, sizeof(double) * len, rt->stream), "flux");
+    const double* iso = nullptr;
+    if (sources) {
+      CU(rt->d_iso64.alloc(sizeof(double) * rt->n_dofs), "iso");
+      CU(launch_iso_source<double>(rt->d_iso64.as<double>(), rt->d_qcell.as<double>(),
+                                   rt->d_rowsum_mass.as<double>(), rt->d_source_id.as<int>(),
+                                   rt->n_cells, rt->n, rt->stream),
+         "iso source");
+      iso = rt->d_iso64.as<double>();
+    }
+    return run_sweep<double>(rt, rt->d_src64.as<double>(), iso,
+                             sources ? rt->d_bnd64.as<double>() : nullptr, rt->d_phi64.as<double>());
+  }
+  CU(rt->d_phi32.alloc(sizeof(float) * len), "flux");
+  CU(cudaMemsetAsync(rt->d_phi32.p, 0, sizeof(float) * len, rt->stream), "flux");
+  const float* iso = nullptr;
+  if (sources) {
+    CU(rt->d_iso32.alloc(sizeof(float) * rt->n_dofs), "iso");
+    CU(launch_iso_source<float>(rt->d_iso32.as<float>(), rt->d_qcell.as<double>(),
+                                rt->d_rowsum_mass.as<double>(), rt->d_source_id.as<int>(),
+                                rt->n_cells, rt->n, rt->stream),
+       "iso source");
+    iso = rt->d_iso32.as<float>();
+  }
+  return run_sweep<float>(rt, rt->d_src32.as<float>(), iso,
+                          sources ? rt->d_bnd32.as<float>() : nullptr, rt->d_phi32.as<float>());
+}
+
+// y = sx * x + sp * phi  (x may be NULL)
+int phi_combine(ouranos_rt* rt, const double* x, double* y, double sx, double sp) {
+  const long len = vec_len(rt);
+  if (rt->precision == OURANOS_FP64)
+    CU(launch_combine<double>(x, rt->d_phi64.as<double>(), y, len, sx, sp, rt->stream), "combine");
+  else
+    CU(launch_combine<float>(x, rt->d_phi32.as<float>(), y, len, sx, sp, rt->stream), "combine");
+  return OURANOS_OK;
+}
+
+}  // namespace
+
+// ============================================================== internal API
+namespace ouranos {
+// Device-side Apply for the solvers: y = x - D L^-1 M2D S x, x and y device,
+// lexicographic numbering.  Does not synchronise.
+int rt_apply_device(ouranos_rt* rt, const double* x, double* y) {
+  OK_OR_RETURN(build_source(rt, x, nullptr));
+  OK_OR_RETURN(sweep_into_phi(rt, false));
+  return phi_combine(rt, x, y, 1.0, -1.0);
+}
+// rhs = D L^-1 (q + outer + inflow) with zero in-group scattering (device).
+int rt_rhs_device(ouranos_rt* rt, const double* gf, double* rhs) {
+  OK_OR_RETURN(build_source(rt, nullptr, gf));
+  OK_OR_RETURN(sweep_into_phi(rt, true));
+  return phi_combine(rt, nullptr, rhs, 0.0, 1.0);
+}
+int rt_check_status(ouranos_rt* rt) { return finish(rt); }
+int rt_clear_status(ouranos_rt* rt) { return clear_status(rt); }
+int rt_stage_in(ouranos_rt* rt, const double* v, DevBuf& buf, int n_vec, const double** out) {
+  return stage_in(rt, v, buf, n_vec, out);
+}
+int rt_stage_out(ouranos_rt* rt, const double* dv, double* user) { return stage_out(rt, dv, user); }
+}  // namespace ouranos
+
+// ===================================================================== C-ABI
+extern "C" {
+
+int ouranos_rt_create(const ouranos_problem_desc* D, int device, ouranos_rt** out) {
+  if (!out) return OURANOS_ERR_BAD_INPUT;
+  *out = nullptr;
+  if (!D) return OURANOS_ERR_BAD_INPUT;
+  ouranos_rt* rt = new (std::nothrow) ouranos_rt();
+  if (!rt) return OURANOS_ERR_BAD_INPUT;
+  auto fail = [&](int rc) {
+    // keep the handle so the caller can read the message; it must destroy it
+    *out = rt;
+    return rc;
+  };
+  if (D->dim != 2 && D->dim != 3) return fail(bad(rt, "dim must be 2 or 3"));
+  const int pmax = D->dim == 2 ? 4 : 2;
+  if (D->fe_order < 1 || D->fe_order > pmax) {
+    rt->err = "fe_order outside the instantiated range (2-D: 1..4, 3-D: 1..2)";
+    return fail(OURANOS_ERR_UNSUPPORTED);
+  }
+  if (D->n_groups < 1 || D->n_dir < 1 || D->n_mom < 1 || D->n_materials < 1 || D->l_max < 0 ||
+      !D->omega || !D->m2d || !D->d2m || !D->moment_l || !D->sigma_t || !D->sigma_s ||
+      !D->material_id || !(D->weight_sum > 0.0))
+    return fail(bad(rt, "incomplete problem description"));
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    rt->err = "no CUDA device";
+    return fail(OURANOS_ERR_NO_DEVICE);
+  }
+  if (device < 0) cudaGetDevice(&device);
+  rt->device = device;
+  if (cudaSetDevice(device) != cudaSuccess) return fail(cuda_fail(rt, cudaGetLastError(), "set device"));
+  rt->dim = D->dim;
+  rt->p = D->fe_order;
+  rt->p1 = rt->p + 1;
+  rt->n_cells = 1;
+  for (int a = 0; a < 3; ++a) {
+    if (a < rt->dim) {
+      if (D->n_cells[a] < 1 || !(D->upper[a] > D->lower[a])) return fail(bad(rt, "bad mesh box"));
+      rt->nx[a] = D->n_cells[a];
+      rt->h[a] = (D->upper[a] - D->lower[a]) / D->n_cells[a];
+    } else {
+      rt->nx[a] = 1;
+      rt->h[a] = 1.0;
+    }
+    rt->n_cells *= rt->nx[a];
+  }
+  rt->fe = build_fe_tables(rt->dim, rt->p, rt->h);
+  rt->n = rt->fe.n;
+  rt->fd = rt->fe.fd;
+  rt->n_dofs = rt->n_cells * rt->n;
+  rt->G = D->n_groups;
+  rt->n_dir = D->n_dir;
+  rt->n_mom = D->n_mom;
+  rt->n_mat = D->n_materials;
+  rt->l_max = D->l_max;
+  rt->ws = D->weight_sum;
+  rt->omega.assign(D->omega, D->omega + 3 * (size_t)rt->n_dir);
+  rt->m2d.assign(D->m2d, D->m2d + (size_t)rt->n_dir * rt->n_mom);
+  rt->d2m.assign(D->d2m, D->d2m + (size_t)rt->n_dir * rt->n_mom);
+  rt->moment_l.assign(D->moment_l, D->moment_l + rt->n_mom);
+  if (D->most_normal)
+    rt->most_normal.assign(D->most_normal, D->most_normal + (size_t)2 * rt->dim * rt->n_dir);
+  rt->sigma_t.assign(D->sigma_t, D->sigma_t + (size_t)rt->n_mat * rt->G);
+  rt->sigma_s.assign(D->sigma_s, D->sigma_s + (size_t)rt->n_mat * rt->G * rt->G * (rt->l_max + 1));
+  rt->material_id.assign(D->material_id, D->material_id + rt->n_cells);
+  for (long c = 0; c < rt->n_cells; ++c)
+    if (rt->material_id[c] < 0 || rt->material_id[c] >= rt->n_mat)
+      return fail(bad(rt, "material id out of range"));
+  rt->n_src = D->source ? D->n_sources : 0;
+  if (D->source) rt->source.assign(D->source, D->source + (size_t)rt->n_src * rt->G);
+  if (D->source_id) {
+    rt->source_id.assign(D->source_id, D->source_id + rt->n_cells);
+    for (long c = 0; c < rt->n_cells; ++c)
+      if (rt->source_id[c] < 0 || (rt->source_id[c] >= rt->n_src && rt->n_src > 0))
+        return fail(bad(rt, "source id out of range"));
+  }
+  for (int f = 0; f < 6; ++f) rt->bc[f] = D->bc_type[f];
+  if (D->inc_flux) rt->inc_flux.assign(D->inc_flux, D->inc_flux + (size_t)2 * rt->dim * rt->G);
+  for (int q = 0; q < rt->n_mom; ++q)
+    if (rt->moment_l[q] < 0) return fail(bad(rt, "negative moment order"));
+  for (int d = 0; d < rt->n_dir; ++d)
+    for (int a = 0; a < rt->dim; ++a)
+      if (rt->omega[3 * d + a] == 0.0)
+        return fail(bad(rt, "a direction is parallel to a mesh face (Omega_a == 0)"));
+  if (D->cell_order) {
+    rt->cell_order.assign(D->cell_order, D->cell_order + rt->n_cells);
+    std::vector<char> seen(rt->n_cells, 0);
+    for (long c = 0; c < rt->n_cells; ++c) {
+      const long o = rt->cell_order[c];
+      if (o < 0 || o >= rt->n_cells || seen[o]) return fail(bad(rt, "cell_order is not a permutation"));
+      seen[o] = 1;
+    }
+  }
+  if (cudaStreamCreateWithFlags(&rt->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&rt->ev0) != cudaSuccess || cudaEventCreate(&rt->ev1) != cudaSuccess)
+    return fail(cuda_fail(rt, cudaGetLastError(), "stream"));
+  rt->stream = rt->own_stream;
+
+  // |Omega| classes (the canonical cell matrix depends on |Omega_a| only)
+  std::vector<int> dcls(rt->n_dir);
+  for (int d = 0; d < rt->n_dir; ++d) {
+    double w[3] = {0, 0, 0};
+    for (int a = 0; a < rt->dim; ++a) w[a] = std::fabs(rt->omega[3 * d + a]);
+    int found = -1;
+    for (int c = 0; c < rt->n_dir_class && found < 0; ++c)
+      if (rt->class_abs_omega[3 * c] == w[0] && rt->class_abs_omega[3 * c + 1] == w[1] &&
+          rt->class_abs_omega[3 * c + 2] == w[2])
+        found = c;
+    if (found < 0) {
+      found = rt->n_dir_class++;
+      rt->class_abs_omega.insert(rt->class_abs_omega.end(), w, w + 3);
+    }
+    dcls[d] = found;
+  }
+  rt->dir_class_h = dcls;
+  std::vector<double> absw((size_t)rt->n_dir * 3), d2m_t((size_t)rt->n_dir * rt->n_mom);
+  for (int d = 0; d < rt->n_dir; ++d)
+    for (int a = 0; a < 3; ++a) absw[3 * d + a] = std::fabs(rt->omega[3 * d + a]);
+  for (int q = 0; q < rt->n_mom; ++q)
+    for (int d = 0; d < rt->n_dir; ++d)
+      d2m_t[(size_t)d * rt->n_mom + q] = rt->d2m[(size_t)q * rt->n_dir + d];
+  std::vector<double> rowsum(rt->n, 0.0);
+  for (int i = 0; i < rt->n; ++i)
+    for (int j = 0; j < rt->n; ++j) rowsum[i] += rt->fe.mass[i * rt->n + j];
+  std::vector<int> sid = rt->source_id;
+  if (sid.empty()) sid.assign(rt->n_cells, 0);
+  int rc;
+  if ((rc = upload(rt, rt->d_dir_class, dcls, "dir classes")) ||
+      (rc = upload(rt, rt->d_abs64, absw, "omega")) ||
+      (rc = upload(rt, rt->d_abs32, to_f32(absw), "omega")) ||
+      (rc = upload(rt, rt->d_m2d64, rt->m2d, "m2d")) ||
+      (rc = upload(rt, rt->d_m2d32, to_f32(rt->m2d), "m2d")) ||
+      (rc = upload(rt, rt->d_d2m64, d2m_t, "d2m")) ||
+      (rc = upload(rt, rt->d_d2m32, to_f32(d2m_t), "d2m")) ||
+      (rc = upload(rt, rt->d_face64, rt->fe.face_mass, "face mass")) ||
+      (rc = upload(rt, rt->d_face32, to_f32(rt->fe.face_mass), "face mass")) ||
+      (rc = upload(rt, rt->d_cell_mass, rt->fe.mass, "mass")) ||
+      (rc = upload(rt, rt->d_rowsum_mass, rowsum, "mass")) ||
+      (rc = upload(rt, rt->d_material, rt->material_id, "materials")) ||
+      (rc = upload(rt, rt->d_source_id, sid, "source ids")))
+    return fail(rc);
+  if (!rt->cell_order.empty() && (rc = upload(rt, rt->d_cell_order, rt->cell_order, "cell order")))
+    return fail(rc);
+  if ((rc = default_tiling(rt)) || (rc = build_schedule(rt)) || (rc = setup_group(rt)))
+    return fail(rc);
+  if (cudaStreamSynchronize(rt->stream) != cudaSuccess)
+    return fail(cuda_fail(rt, cudaGetLastError(), "setup"));
+  *out = rt;
+  return OURANOS_OK;
+}
+
+int ouranos_rt_destroy(ouranos_rt* rt) {
+  if (!rt) return OURANOS_OK;
+  if (rt->stream) {
+    cudaSetDevice(rt->device);
+    cudaStreamSynchronize(rt->stream);
+  }
+  if (rt->ev0) cudaEventDestroy(rt->ev0);
+  if (rt->ev1) cudaEventDestroy(rt->ev1);
+  if (rt->own_stream) cudaStreamDestroy(rt->own_stream);
+  delete rt;
+  return OURANOS_OK;
+}
+
+int ouranos_rt_set_group(ouranos_rt* rt, int g) {
+  if (!rt) return OURANOS_ERR_BAD_INPUT;
+  if (g < 0 || g >= rt->G) return bad(rt, "group out of range");
+  cudaSetDevice(rt->device);
+  rt->group = g;
+  OK_OR_RETURN(setup_group(rt));
+  CU(cudaStreamSynchronize(rt->stream), "set group");
+  return OURANOS_OK;
+}
+
+int ouranos_rt_set_precision(ouranos_rt* rt, int precision) {
+  if (!rt) return OURANOS_ERR_BAD_INPUT;
+  if (precision != OURANOS_FP64 && precision != OURANOS_FP32) return bad(rt, "unknown precision");
+  rt->precision = precision;
+  return OURANOS_OK;
+}
+
+int ouranos_rt_vector_length(const ouranos_rt* rt, long* length) {
+  if (!rt || !length) return OURANOS_ERR_BAD_INPUT;
+  *length = vec_len(rt);
+  return OURANOS_OK;
+}
+
+int ouranos_rt_n_tasks(const ouranos_rt* rt, long* n_tasks) {
+  if (!rt || !n_tasks) return OURANOS_ERR_BAD_INPUT;
+  *n_tasks = rt->n_cells * rt->n_dir;
+  return OURANOS_OK;
+}
+
+int ouranos_rt_scattering_source(ouranos_rt* rt, const double* x) {
+  if (!rt || !x) return OURANOS_ERR_BAD_INPUT;
+  cudaSetDevice(rt->device);
+  // S = sigma_s M x is rebuilt from the stored argument at each sweep (it is
+  // cheap next to the sweep and keeps one FP64 copy for both precisions)
+  const double* dx = nullptr;
+  OK_OR_RETURN(stage_in(rt, x, rt->d_x, 1, &dx));
+  CU(rt->d_scatx.alloc(sizeof(double) * vec_len(rt)), "scattering source");
+  CU(cudaMemcpyAsync(rt->d_scatx.p, dx, sizeof(double) * vec_len(rt), cudaMemcpyDeviceToDevice,
+                     rt->stream),
+     "scattering source");
+  rt->scat_valid = true;
+  CU(cudaStreamSynchronize(rt->stream), "scattering source");
+  return OURANOS_OK;
+}
+
+int ouranos_rt_sweep(ouranos_rt* rt, double* flux, const double* group_flux) {
+  if (!rt || !flux) return OURANOS_ERR_BAD_INPUT;
+  cudaSetDevice(rt->device);
+  OK_OR_RETURN(clear_status(rt));
+  const double* dgf = nullptr;
+  if (group_flux) OK_OR_RETURN(stage_in(rt, group_flux, rt->d_gf, rt->G, &dgf));
+  OK_OR_RETURN(build_source(rt, rt->scat_valid ? rt->d_scatx.as<double>() : nullptr, dgf));
+  OK_OR_RETURN(sweep_into_phi(rt, group_flux != nullptr));
+  const double* dflux = nullptr;
+  OK_OR_RETURN(stage_in(rt, flux, rt->d_x, 1, &dflux));
+  CU(rt->d_y.alloc(sizeof(double) * vec_len(rt)), "flux");
+  OK_OR_RETURN(phi_combine(rt, dflux, rt->d_y.as<double>(), 1.0, 1.0));  // flux + phi
+  OK_OR_RETURN(stage_out(rt, rt->d_y.as<double>(), flux));
+  return finish(rt);
+}
+
+int ouranos_rt_apply(ouranos_rt* rt, const double* x, double* y) {
+  if (!rt || !x || !y) return OURANOS_ERR_BAD_INPUT;
+  cudaSetDevice(rt->device);
+  OK_OR_RETURN(clear_status(rt));
+  const double* dx = nullptr;
+  OK_OR_RETURN(stage_in(rt, x, rt->d_x, 1, &dx));
+  CU(rt->d_y.alloc(sizeof(double) * vec_len(rt)), "apply");
+  OK_OR_RETURN(rt_apply_device(rt, dx, rt->d_y.as<double>()));
+  OK_OR_RETURN(stage_out(rt, rt->d_y.as<double>(), y));
+  return finish(rt);
+}
+
+int ouranos_rt_sweep_rhs(ouranos_rt* rt, const double* group_flux, double* rhs) {
+  if (!rt || !rhs) return OURANOS_ERR_BAD_INPUT;
+  cudaSetDevice(rt->device);
+  OK_OR_RETURN(clear_status(rt));
+  const double* dgf = nullptr;
+  if (group_flux) OK_OR_RETURN(stage_in(rt, group_flux, rt->d_gf, rt->G, &dgf));
+  OK_OR_RETURN(build_source(rt, nullptr, dgf));
+  OK_OR_RETURN(sweep_into_phi(rt, true));
+  const double* drhs = nullptr;
+  OK_OR_RETURN(stage_in(rt, rhs, rt->d_x, 1, &drhs));
+  CU(rt->d_y.alloc(sizeof(double) * vec_len(rt)), "rhs");
+  OK_OR_RETURN(phi_combine(rt, drhs, rt->d_y.as<double>(), 1.0, 1.0));
+  OK_OR_RETURN(stage_out(rt, rt->d_y.as<double>(), rhs));
+  return finish(rt);
+}
+
+int ouranos_wavefront_levels(int dim, const int* nx, int n_dir, const double* omega, int* levels) {
+  if ((dim != 2 && dim != 3) || !nx || n_dir < 1 || !omega || !levels) return OURANOS_ERR_BAD_INPUT;
+  long n_cells = 1;
+  for (int a = 0; a < dim; ++a) {
+    if (nx[a] < 1) return OURANOS_ERR_BAD_INPUT;
+    n_cells *= nx[a];
+  }
+  // wavefront level of (direction, cell): its distance in cells from the
+  // corner the direction enters through, sum_a (Omega_a > 0 ? i_a : N_a - 1 - i_a)
+  // -- the longest upwind chain ending at the cell in the task graph of
+  // src/RadiativeTransfer.cc:80-232
+  for (int d = 0; d < n_dir; ++d)
+    for (long c = 0; c < n_cells; ++c) {
+      long r = c;
+      int lev = 0;
+      for (int a = 0; a < dim; ++a) {
+        const int i = (int)(r % nx[a]);
+        r /= nx[a];
+        lev += omega[3 * d + a] > 0.0 ? i : nx[a] - 1 - i;
+      }
+      levels[(size_t)d * n_cells + c] = lev;
+    }
+  return OURANOS_OK;
+}
+
+int ouranos_rt_task_levels(const ouranos_rt* rt, int* levels) {
+  if (!rt || !levels) return OURANOS_ERR_BAD_INPUT;
+  return ouranos_wavefront_levels(rt->dim, rt->nx, rt->n_dir, rt->omega.data(), levels);
+}
+
+int ouranos_rt_set_stream(ouranos_rt* rt, void* stream) {
+  if (!rt) return OURANOS_ERR_BAD_INPUT;
+  cudaSetDevice(rt->device);
+  CU(cudaStreamSynchronize(rt->stream), "set stream");
+  rt->stream = stream ? (cudaStream_t)stream : rt->own_stream;
+  return OURANOS_OK;
+}
+
+int ouranos_rt_last_error(const ouranos_rt* rt, char* buf, size_t len) {
+  if (!rt || !buf || !len) return OURANOS_ERR_BAD_INPUT;
+  std::snprintf(buf, len, "%s", rt->err.c_str());
+  return OURANOS_OK;
+}
+
+int ouranos_rt_last_sweep_ms(const ouranos_rt* rt, double* ms, int* kernels) {
+  if (!rt) return OURANOS_ERR_BAD_INPUT;
+  if (ms) *ms = rt->last_ms;
+  if (kernels) *kernels = rt->last_kernels;
+  return OURANOS_OK;
+}
+
+int ouranos_rt_set_tiling(ouranos_rt* rt, int cells_x, int cells_y, int dirs) {
+  if (!rt) return OURANOS_ERR_BAD_INPUT;
+  cudaSetDevice(rt->device);
+  if (cells_x == 0 && cells_y == 0 && dirs == 0) {
+    OK_OR_RETURN(default_tiling(rt));
+  } else {
+    if (rt->dim == 2) cells_y = 1;
+    const int lanes = cells_x * cells_y * dirs;
+    if (cells_x < 1 || cells_y < 1 || dirs < 1 || lanes != 32 || (dirs & (dirs - 1)))
+      return bad(rt, "tiling must satisfy cells_x*cells_y*dirs == 32 with dirs a power of two");
+    rt->wx = cells_x;
+    rt->wy = cells_y;
+    rt->kd = dirs;
+  }
+  OK_OR_RETURN(build_schedule(rt));
+  CU(cudaStreamSynchronize(rt->stream), "tiling");
+  return OURANOS_OK;
+}
+
+int ouranos_rt_get_tiling(const ouranos_rt* rt, int* cx, int* cy, int* dirs) {
+  if (!rt) return OURANOS_ERR_BAD_INPUT;
+  if (cx) *cx = rt->wx;
+  if (cy) *cy = rt->wy;
+  if (dirs) *dirs = rt->kd;
+  return OURANOS_OK;
+}
+
+int ouranos_rt_set_wait_limit(ouranos_rt* rt, double ns) {
+  if (!rt || !(ns > 0)) return OURANOS_ERR_BAD_INPUT;
+  rt->wait_limit_ns = (long long)ns;
+  return OURANOS_OK;
+}
+
+int ouranos_rt_debug_wait_bias(ouranos_rt* rt, int extra) {
+  if (!rt || extra < 0) return OURANOS_ERR_BAD_INPUT;
+  rt->wait_bias = extra;
+  return OURANOS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,417 @@
+// Drivers around the operator: the source iteration and Krylov solves of
+// src/ouranos.cc:43-209 (the reference hands Apply to AztecOO through deal.II's
+// TrilinosWrappers::SolverGMRES / SolverBicgstab; here the methods are written
+// out on device vectors).  Gram-Schmidt, norms and dot products are FP64
+// (classical Gram-Schmidt with one re-orthogonalisation pass); the small
+// Hessenberg least-squares problem is solved on the host.
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+
+using namespace ouranos;
+
+namespace ouranos {
+cudaError_t launch_multi_axpy(const double* const* V, int k, const double* coef, double scale,
+                              double* w, long len, cudaStream_t s);
+}
+
+namespace {
+
+#define RC(expr)                       \
+  do {                                 \
+    int _rc = (expr);                  \
+    if (_rc != OURANOS_OK) return _rc; \
+  } while (0)
+
+int cfail(ouranos_rt* rt, cudaError_t e, const char* what) {
+  char buf[256];
+  std::snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+  rt->err = buf;
+  return OURANOS_ERR_CUDA;
+}
+#define CUC(expr, what)                                \
+  do {                                                 \
+    cudaError_t _e = (expr);                           \
+    if (_e != cudaSuccess) return cfail(rt, _e, what); \
+  } while (0)
+
+struct Work {
+  ouranos_rt* rt;
+  long len;
+  int nvec;
+  double* base = nullptr;
+  double** dptrs = nullptr;   // device array of vector pointers
+  double* dres = nullptr;     // device results (64) + partials
+  unsigned* done = nullptr;
+  std::vector<double*> vec;   // host copy of vector pointers
+  double* v(int i) const { return vec[i]; }
+};
+
+int make_work(ouranos_rt* rt, int nvec, Work& w) {
+  w.rt = rt;
+  w.len = (long)rt->n_mom * rt->n_dofs;
+  w.nvec = nvec;
+  const size_t vbytes = sizeof(double) * (size_t)w.len;
+  const size_t ptr_bytes = sizeof(double*) * 64;
+  const size_t res_bytes = sizeof(double) * (64 + 64 * (size_t)kDotGrid);
+  const size_t total = vbytes * nvec + ptr_bytes + res_bytes + 256;
+  CUC(rt->d_krylov.alloc(total), "solver workspace");
+  char* p = (char*)rt->d_krylov.p;
+  w.base = (double*)p;
+  w.vec.resize(nvec);
+  for (int i = 0; i < nvec; ++i) w.vec[i] = w.base + (size_t)i * w.len;
+  p += vbytes * nvec;
+  w.dptrs = (double**)p;
+  p += ptr_bytes;
+  w.dres = (double*)p;
+  w.done = (unsigned*)(rt->d_ctrl.as<int>() + 2);
+  return OURANOS_OK;
+}
+
+// out[j] = <V_first+j, y>, j < k (host result)
+int dots(Work& w, int first, int k, const double* y, double* out) {
+  ouranos_rt* rt = w.rt;
+  CUC(cudaMemcpyAsync(w.dptrs, &w.vec[first], sizeof(double*) * k, cudaMemcpyHostToDevice,
+                      rt->stream),
+      "dots");
+  CUC(launch_dots((const double* const*)w.dptrs, y, k, w.len, w.dres, w.dres + 64, w.done,
+                  rt->stream),
+      "dots");
+  CUC(cudaMemcpyAsync(out, w.dres, sizeof(double) * k, cudaMemcpyDeviceToHost, rt->stream), "dots");
+  CUC(cudaStreamSynchronize(rt->stream), "dots");
+  return OURANOS_OK;
+}
+
+int dot_pair(Work& w, const double* a, const double* b, double* out) {
+  ouranos_rt* rt = w.rt;
+  const double* ptrs[1] = {a};
+  CUC(cudaMemcpyAsync(w.dptrs, ptrs, sizeof(double*), cudaMemcpyHostToDevice, rt->stream), "dot");
+  CUC(launch_dots((const double* const*)w.dptrs, b, 1, w.len, w.dres, w.dres + 64, w.done,
+                  rt->stream),
+      "dot");
+  CUC(cudaMemcpyAsync(out, w.dres, sizeof(double), cudaMemcpyDeviceToHost, rt->stream), "dot");
+  CUC(cudaStreamSynchronize(rt->stream), "dot");
+  return OURANOS_OK;
+}
+
+double nrm(Work& w, const double* a, int* rc) {
+  double v = 0.0;
+  *rc = dot_pair(w, a, a, &v);
+  return std::sqrt(std::fmax(v, 0.0));
+}
+
+// w -= sum_j h_j V_{first+j} with h = V^T w, twice (CGS2); h accumulates into hout
+int orthogonalise(Work& w, int first, int k, double* target, double* hout) {
+  ouranos_rt* rt = w.rt;
+  std::vector<double> h(k);
+  for (int j = 0; j < k; ++j) hout[j] = 0.0;
+  for (int pass = 0; pass < 2; ++pass) {
+    RC(dots(w, first, k, target, h.data()));
+    // coefficients are already on the device in w.dres[0..k)
+    CUC(launch_multi_axpy((const double* const*)w.dptrs, k, w.dres, -1.0, target, w.len,
+                          rt->stream),
+        "orthogonalise");
+    for (int j = 0; j < k; ++j) hout[j] += h[j];
+  }
+  return OURANOS_OK;
+}
+
+// op(x) -> y : FP64 or FP32 sweep Apply
+int apply_prec(ouranos_rt* rt, int precision, const double* x, double* y) {
+  const int saved = rt->precision;
+  rt->precision = precision;
+  int rc = rt_apply_device(rt, x, y);
+  rt->precision = saved;
+  return rc;
+}
+
+struct Givens {
+  int m;
+  std::vector<double> H, cs, sn, g;
+  explicit Givens(int m_) : m(m_), H((m_ + 1) * m_, 0.0), cs(m_), sn(m_), g(m_ + 1, 0.0) {}
+  double& h(int i, int j) { return H[i * m + j]; }
+  // column k of H holds h[0..k+1]; returns |g_{k+1}|
+  double add_column(int k, const double* col) {
+    for (int i = 0; i <= k + 1; ++i) h(i, k) = col[i];
+    for (int j = 0; j < k; ++j) {
+      const double a = h(j, k), b = h(j + 1, k);
+      h(j, k) = cs[j] * a + sn[j] * b;
+      h(j + 1, k) = -sn[j] * a + cs[j] * b;
+    }
+    const double a = h(k, k), b = h(k + 1, k);
+    const double r = std::hypot(a, b);
+    cs[k] = r > 0 ? a / r : 1.0;
+    sn[k] = r > 0 ? b / r : 0.0;
+    h(k, k) = r;
+    h(k + 1, k) = 0.0;
+    g[k + 1] = -sn[k] * g[k];
+    g[k] = cs[k] * g[k];
+    return std::fabs(g[k + 1]);
+  }
+  std::vector<double> solve(int k) {
+    std::vector<double> y(k, 0.0);
+    for (int i = k - 1; i >= 0; --i) {
+      double s = g[i];
+      for (int j = i + 1; j < k; ++j) s -= h(i, j) * y[j];
+      y[i] = h(i, i) != 0.0 ? s / h(i, i) : 0.0;
+    }
+    return y;
+  }
+};
+
+// x += sum_j y_j Z_{first+j}
+int update(Work& w, int first, const std::vector<double>& y, double* x) {
+  ouranos_rt* rt = w.rt;
+  const int k = (int)y.size();
+  if (!k) return OURANOS_OK;
+  CUC(cudaMemcpyAsync(w.dptrs, &w.vec[first], sizeof(double*) * k, cudaMemcpyHostToDevice,
+                      rt->stream),
+      "update");
+  CUC(cudaMemcpyAsync(w.dres, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, rt->stream),
+      "update");
+  CUC(launch_multi_axpy((const double* const*)w.dptrs, k, w.dres, 1.0, x, w.len, rt->stream),
+      "update");
+  CUC(cudaStreamSynchronize(rt->stream), "update");
+  return OURANOS_OK;
+}
+
+// Restarted (F)GMRES.  Arnoldi applies use `inner_prec`; each cycle starts
+// from the FP64 true residual.  mixed: the cycle stops once its own residual
+// estimate has dropped by `inner_drop` (FP32 operator accuracy), and the FP64
+// restart refines the solution (iterative refinement).
+int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double* x,
+          double* hist, ouranos_solve_info* info, int inner_prec, double inner_drop) {
+  m = std::max(1, std::min(m, 32));  // dot kernel handles up to 32 basis vectors
+  const bool flexible = inner_prec != OURANOS_FP64;
+  // vectors: V[0..m], Z[0..m-1] (flexible), r
+  Work w;
+  const int nv = (m + 1) + (flexible ? m : 0) + 1;
+  RC(make_work(rt, nv, w));
+  const int V0 = 0, Z0 = m + 1, R = nv - 1;
+  int rc = 0;
+  const double bnorm = nrm(w, b, &rc);
+  RC(rc);
+  CUC(cudaMemsetAsync(x, 0, sizeof(double) * w.len, rt->stream), "gmres");
+  int total = 0, cycles = 0;
+  double rel = bnorm > 0 ? 1.0 : 0.0;
+  if (hist) hist[0] = rel;
+  bool converged = bnorm == 0.0;
+  while (!converged && total < max_it) {
+    // true residual r = b - A x in FP64
+    if (cycles == 0) {
+      CUC(cudaMemcpyAsync(w.v(R), b, sizeof(double) * w.len, cudaMemcpyDeviceToDevice, rt->stream),
+          "gmres");
+    } else {
+      RC(apply_prec(rt, OURANOS_FP64, x, w.v(R)));
+      CUC(launch_axpby(1.0, b, -1.0, w.v(R), w.len, rt->stream), "gmres");
+    }
+    const double beta = nrm(w, w.v(R), &rc);
+    RC(rc);
+    rel = beta / bnorm;
+    if (rel < tol) {
+      converged = true;
+      break;
+    }
+    ++cycles;
+    CUC(launch_axpby(1.0 / beta, w.v(R), 0.0, w.v(V0), w.len, rt->stream), "gmres");
+    Givens gv(m);
+    gv.g[0] = beta;
+    int k = 0;
+    std::vector<double> col(m + 2);
+    for (; k < m && total < max_it; ++k) {
+      const double* vin = w.v(V0 + k);
+      if (flexible) {
+        // right preconditioner slot: z_k = v_k (no preconditioner)
+        CUC(cudaMemcpyAsync(w.v(Z0 + k), vin, sizeof(double) * w.len, cudaMemcpyDeviceToDevice,
+                            rt->stream),
+            "fgmres");
+        vin = w.v(Z0 + k);
+      }
+      double* nxt = w.v(V0 + k + 1);
+      RC(apply_prec(rt, inner_prec, vin, nxt));
+      RC(orthogonalise(w, V0, k + 1, nxt, col.data()));
+      const double hn = nrm(w, nxt, &rc);
+      RC(rc);
+      col[k + 1] = hn;
+      if (hn > 0) CUC(launch_axpby(1.0 / hn, nxt, 0.0, nxt, w.len, rt->stream), "gmres");
+      const double est = gv.add_column(k, col.data()) / bnorm;
+      ++total;
+      if (hist) hist[total] = est;
+      if (est < tol || (flexible && est < rel * inner_drop) || hn == 0.0) {
+        ++k;
+        break;
+      }
+    }
+    std::vector<double> y = gv.solve(k);
+    RC(update(w, flexible ? Z0 : V0, y, x));
+  }
+  // final FP64 true residual
+  RC(apply_prec(rt, OURANOS_FP64, x, w.v(R)));
+  CUC(launch_axpby(1.0, b, -1.0, w.v(R), w.len, rt->stream), "gmres");
+  const double fin = nrm(w, w.v(R), &rc) / (bnorm > 0 ? bnorm : 1.0);
+  RC(rc);
+  RC(rt_check_status(rt));
+  info->iterations = total;
+  info->restarts = cycles;
+  info->residual = fin;
+  info->converged = fin < tol;
+  return OURANOS_OK;
+}
+
+int bicgstab(ouranos_rt* rt, int max_it, double tol, const double* b, double* x, double* hist,
+             ouranos_solve_info* info) {
+  Work w;
+  RC(make_work(rt, 7, w));
+  double *r = w.v(0), *r0 = w.v(1), *p = w.v(2), *v = w.v(3), *s = w.v(4), *t = w.v(5);
+  int rc = 0;
+  const double bnorm = nrm(w, b, &rc);
+  RC(rc);
+  CUC(cudaMemsetAsync(x, 0, sizeof(double) * w.len, rt->stream), "bicgstab");
+  CUC(cudaMemcpyAsync(r, b, sizeof(double) * w.len, cudaMemcpyDeviceToDevice, rt->stream), "bicgstab");
+  CUC(cudaMemcpyAsync(r0, b, sizeof(double) * w.len, cudaMemcpyDeviceToDevice, rt->stream), "bicgstab");
+  CUC(cudaMemsetAsync(p, 0, sizeof(double) * w.len, rt->stream), "bicgstab");
+  CUC(cudaMemsetAsync(v, 0, sizeof(double) * w.len, rt->stream), "bicgstab");
+  double rho = 1.0, alpha = 1.0, om = 1.0;
+  if (hist) hist[0] = 1.0;
+  int it = 0;
+  for (; it < max_it && bnorm > 0; ++it) {
+    double rho1;
+    RC(dot_pair(w, r0, r, &rho1));
+    const double beta = (rho1 / rho) * (alpha / om);
+    rho = rho1;
+    // p = r + beta (p - om v)
+    CUC(launch_axpby(-om, v, 1.0, p, w.len, rt->stream), "bicgstab");
+    CUC(launch_axpby(1.0, r, beta, p, w.len, rt->stream), "bicgstab");
+    RC(apply_prec(rt, OURANOS_FP64, p, v));
+    double r0v;
+    RC(dot_pair(w, r0, v, &r0v));
+    alpha = rho / r0v;
+    CUC(cudaMemcpyAsync(s, r, sizeof(double) * w.len, cudaMemcpyDeviceToDevice, rt->stream), "bicgstab");
+    CUC(launch_axpby(-alpha, v, 1.0, s, w.len, rt->stream), "bicgstab");
+    RC(apply_prec(rt, OURANOS_FP64, s, t));
+    double ts, tt;
+    RC(dot_pair(w, t, s, &ts));
+    RC(dot_pair(w, t, t, &tt));
+    om = tt > 0 ? ts / tt : 0.0;
+    CUC(launch_axpby(alpha, p, 1.0, x, w.len, rt->stream), "bicgstab");
+    CUC(launch_axpby(om, s, 1.0, x, w.len, rt->stream), "bicgstab");
+    CUC(cudaMemcpyAsync(r, s, sizeof(double) * w.len, cudaMemcpyDeviceToDevice, rt->stream), "bicgstab");
+    CUC(launch_axpby(-om, t, 1.0, r, w.len, rt->stream), "bicgstab");
+    const double rel = nrm(w, r, &rc) / bnorm;
+    RC(rc);
+    if (hist) hist[it + 1] = rel;
+    if (rel < tol) {
+      ++it;
+      break;
+    }
+  }
+  RC(apply_prec(rt, OURANOS_FP64, x, t));
+  CUC(launch_axpby(1.0, b, -1.0, t, w.len, rt->stream), "bicgstab");
+  const double fin = nrm(w, t, &rc) / (bnorm > 0 ? bnorm : 1.0);
+  RC(rc);
+  RC(rt_check_status(rt));
+  info->iterations = it;
+  info->restarts = 0;
+  info->residual = fin;
+  info->converged = fin < tol;
+  return OURANOS_OK;
+}
+
+// Source iteration phi <- D L^-1 (M2D S phi + q + inflow) (src/ouranos.cc:72-95,
+// written as intended: a fresh sweep each iteration), relative-change test.
+int source_iteration(ouranos_rt* rt, int max_it, double tol, const double* gf, const double* b,
+                     double* x, double* hist, ouranos_solve_info* info) {
+  Work w;
+  RC(make_work(rt, 3, w));
+  double *xn = w.v(0), *dlt = w.v(1), *rr = w.v(2);
+  int rc = 0;
+  CUC(cudaMemsetAsync(x, 0, sizeof(double) * w.len, rt->stream), "si");
+  int it = 0;
+  double rel = 1.0;
+  for (; it < max_it; ++it) {
+    // phi_new = T phi + rhs  (the rhs sweep is linear: sweep(S x + q) = T x + rhs)
+    RC(rt_apply_device(rt, x, xn));                          // xn = x - T x
+    CUC(launch_axpby(1.0, x, -1.0, xn, w.len, rt->stream), "si");  // xn = T x
+    CUC(launch_axpby(1.0, b, 1.0, xn, w.len, rt->stream), "si");   // xn = T x + rhs
+    CUC(cudaMemcpyAsync(dlt, xn, sizeof(double) * w.len, cudaMemcpyDeviceToDevice, rt->stream), "si");
+    CUC(launch_axpby(-1.0, x, 1.0, dlt, w.len, rt->stream), "si");
+    const double num = nrm(w, dlt, &rc);
+    RC(rc);
+    const double den = nrm(w, xn, &rc);
+    RC(rc);
+    CUC(cudaMemcpyAsync(x, xn, sizeof(double) * w.len, cudaMemcpyDeviceToDevice, rt->stream), "si");
+    rel = den > 0 ? num / den : 0.0;
+    if (hist) hist[it] = rel;
+    if (rel < tol) {
+      ++it;
+      break;
+    }
+  }
+  (void)gf;
+  RC(apply_prec(rt, OURANOS_FP64, x, rr));
+  CUC(launch_axpby(1.0, b, -1.0, rr, w.len, rt->stream), "si");
+  const double bn = nrm(w, b, &rc);
+  RC(rc);
+  const double fin = nrm(w, rr, &rc) / (bn > 0 ? bn : 1.0);
+  RC(rc);
+  RC(rt_check_status(rt));
+  info->iterations = it;
+  info->restarts = 0;
+  info->residual = fin;
+  info->converged = rel < tol;
+  return OURANOS_OK;
+}
+
+}  // namespace
+
+extern "C" int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it, double tol,
+                             const double* group_flux, double* x, double* hist,
+                             ouranos_solve_info* info) {
+  if (!rt || !x || max_it < 1 || !(tol > 0)) return OURANOS_ERR_BAD_INPUT;
+  ouranos_solve_info local;
+  if (!info) info = &local;
+  std::memset(info, 0, sizeof *info);
+  cudaSetDevice(rt->device);
+  RC(rt_clear_status(rt));
+  const auto t0 = std::chrono::steady_clock::now();
+  const double* dgf = nullptr;
+  if (group_flux) RC(rt_stage_in(rt, group_flux, rt->d_gf, rt->G, &dgf));
+  // rhs and solution live in the handle's staging buffers while the solver
+  // workspace holds the Krylov vectors
+  const long len = (long)rt->n_mom * rt->n_dofs;
+  DevBuf rhs, sol;
+  CUC(rhs.alloc(sizeof(double) * len), "rhs");
+  CUC(sol.alloc(sizeof(double) * len), "solution");
+  RC(rt_rhs_device(rt, dgf, rhs.as<double>()));
+  const int saved = rt->precision;
+  int rc;
+  switch (solver) {
+    case OURANOS_SOLVER_SI:
+      rc = source_iteration(rt, max_it, tol, dgf, rhs.as<double>(), sol.as<double>(), hist, info);
+      break;
+    case OURANOS_SOLVER_GMRES:
+      rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info,
+                 OURANOS_FP64, 0.0);
+      break;
+    case OURANOS_SOLVER_BICGSTAB:
+      rc = bicgstab(rt, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info);
+      break;
+    case OURANOS_SOLVER_FGMRES_MIXED:
+      rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info,
+                 OURANOS_FP32, 1e-5);
+      break;
+    default:
+      rt->err = "unknown solver";
+      rc = OURANOS_ERR_BAD_INPUT;
+  }
+  rt->precision = saved;
+  if (rc) return rc;
+  RC(rt_stage_out(rt, sol.as<double>(), x));
+  CUC(cudaStreamSynchronize(rt->stream), "solve");
+  info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return info->converged ? OURANOS_OK : OURANOS_ERR_NOT_CONVERGED;
+}

@@ -1,0 +1,25 @@
+// Instantiations of the sweep kernel in double: 2-D Q1..Q4, 3-D Q1..Q2.
+#include "sweep.cuh"
+
+namespace ouranos {
+
+template <>
+cudaError_t launch_sweep<double>(int dim, int p1, const SweepArgs<double>& a, int grid, int block,
+                                cudaStream_t s) {
+  if (dim == 2) {
+    switch (p1) {
+      case 2: return launch_sweep_impl<double, 2, 2>(a, grid, block, s);
+      case 3: return launch_sweep_impl<double, 2, 3>(a, grid, block, s);
+      case 4: return launch_sweep_impl<double, 2, 4>(a, grid, block, s);
+      case 5: return launch_sweep_impl<double, 2, 5>(a, grid, block, s);
+    }
+  } else if (dim == 3) {
+    switch (p1) {
+      case 2: return launch_sweep_impl<double, 3, 2>(a, grid, block, s);
+      case 3: return launch_sweep_impl<double, 3, 3>(a, grid, block, s);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace ouranos

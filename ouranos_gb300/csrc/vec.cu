@@ -1,0 +1,239 @@
+// Vector kernels around the sweep: scattering source, fixed source, the
+// residual form of Apply, layout permutations and the FP64 BLAS-1 pieces of
+// the Krylov drivers.  All are HBM-streaming, one grid-stride loop each.
+#include "internal.h"
+
+namespace ouranos {
+namespace {
+
+constexpr int kBlock = 256;
+
+inline int grid_for(long n) {
+  long g = (n + kBlock - 1) / kBlock;
+  if (g > 152L * 32) g = 152L * 32;  // 152 SMs x 32 resident blocks of 256 threads at most
+  return g < 1 ? 1 : (int)g;
+}
+
+// compute_scattering_source (src/RadiativeTransfer.cc:811-843) and, for the
+// right-hand side, compute_outer_scattering_source (:845-876):
+//   T_m[c] = s(mat_c, g->g, l(m)) M x_m[c] + sum_{g' != g} s(mat_c, g'->g, l(m)) M phi_{g',m}[c]
+// One thread per (moment, cell, local dof i).
+template <typename real>
+__global__ void scatter_source_kernel(const double* __restrict__ x, const double* __restrict__ gf,
+                                      real* __restrict__ src, const double* __restrict__ M,
+                                      const double* __restrict__ sscale,
+                                      const double* __restrict__ oscale,
+                                      const int* __restrict__ material, int n_groups, int group,
+                                      long n_cells, int n, int n_mom, long n_dofs) {
+  const long total = (long)n_mom * n_cells * n;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
+       e += (long)gridDim.x * blockDim.x) {
+    const int i = e % n;
+    const long c = (e / n) % n_cells;
+    const int m = e / ((long)n * n_cells);
+    const int mat = material[c];
+    const double* row = M + i * n;
+    double acc = 0.0;
+    if (x) {
+      const double* xc = x + (size_t)m * n_dofs + c * n;
+      double r = 0.0;
+      for (int j = 0; j < n; ++j) r += row[j] * xc[j];
+      acc = sscale[(size_t)mat * n_mom + m] * r;
+    }
+    if (gf) {
+      for (int g = 0; g < n_groups; ++g) {
+        if (g == group) continue;
+        const double* xg = gf + ((size_t)g * n_mom + m) * n_dofs + c * n;
+        double r = 0.0;
+        for (int j = 0; j < n; ++j) r += row[j] * xg[j];
+        acc += oscale[((size_t)mat * n_groups + g) * n_mom + m] * r;
+      }
+    }
+    src[(size_t)m * n_dofs + c * n + i] = (real)acc;
+  }
+}
+
+// b += M q/ws for the right-hand side (src/RadiativeTransfer.cc:914-922):
+// iso[c*n+i] = (q_{src(c)}/ws) * sum_j M_ij.
+template <typename real>
+__global__ void iso_source_kernel(real* iso, const double* qcell, const double* rowsum,
+                                  const int* source_id, long n_cells, int n) {
+  const long total = n_cells * n;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
+       e += (long)gridDim.x * blockDim.x) {
+    const long c = e / n;
+    const int i = e % n;
+    const int sid = source_id ? source_id[c] : 0;
+    iso[e] = (real)(qcell[sid] * rowsum[i]);
+  }
+}
+
+// y = sx * x + sp * phi; Apply uses (1, -1): y = x - D L^-1 M2D S x
+// (src/RadiativeTransfer.cc:805-806); the driver's sweep uses (1, 1).
+template <typename real>
+__global__ void combine_kernel(const double* x, const real* phi, double* y, long len, double sx,
+                               double sp) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len;
+       e += (long)gridDim.x * blockDim.x)
+    y[e] = (x ? sx * x[e] : 0.0) + sp * (double)phi[e];
+}
+
+// Gather between the caller's cell numbering and the lexicographic one.
+__global__ void permute_kernel(const double* in, double* out, const long* order, long n_cells,
+                               int n, int n_vec, int to_internal) {
+  const long total = (long)n_vec * n_cells * n;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
+       e += (long)gridDim.x * blockDim.x) {
+    const int i = e % n;
+    const long c = (e / n) % n_cells;
+    const long v = e / ((long)n * n_cells);
+    const long ext = (v * n_cells + order[c]) * n + i;
+    if (to_internal)
+      out[e] = in[ext];
+    else
+      out[ext] = in[e];
+  }
+}
+
+// w += scale * sum_j coef[j] V_j  (coef on the device)
+__global__ void multi_axpy_kernel(const double* const* V, int k, const double* coef, double scale,
+                                  double* w, long len) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len;
+       e += (long)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int j = 0; j < k; ++j) acc += coef[j] * V[j][e];
+    w[e] += scale * acc;
+  }
+}
+
+__global__ void axpby_kernel(double a, const double* x, double b, double* y, long len) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len;
+       e += (long)gridDim.x * blockDim.x)
+    y[e] = b == 0.0 ? a * x[e] : a * x[e] + b * y[e];  // y may be uninitialised when b == 0
+}
+
+// out[j] = sum_i xs[j][i] * y[i], j < k; one block per chunk writes partial
+// sums, the last block to finish reduces them in a fixed order (deterministic).
+template <int KMAX>
+__global__ void dots_kernel(const double* const* xs, const double* y, int k, long len,
+                            double* partial, double* out, unsigned int* done) {
+  __shared__ double red[KMAX][kBlock / 32];
+  __shared__ bool last;
+  double acc[KMAX];
+#pragma unroll
+  for (int j = 0; j < KMAX; ++j) acc[j] = 0.0;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len;
+       e += (long)gridDim.x * blockDim.x) {
+    const double yv = y[e];
+#pragma unroll
+    for (int j = 0; j < KMAX; ++j)
+      if (j < k) acc[j] += xs[j][e] * yv;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < KMAX; ++j) {
+    double v = acc[j];
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[j][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < k) {
+    double v = 0.0;
+    for (int w = 0; w < kBlock / 32; ++w) v += red[threadIdx.x][w];
+    partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = v;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(done, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    for (int j = threadIdx.x; j < k; j += blockDim.x) {
+      double v = 0.0;
+      for (unsigned b = 0; b < gridDim.x; ++b) v += partial[(size_t)j * gridDim.x + b];
+      out[j] = v;
+    }
+    if (threadIdx.x == 0) *done = 0;
+  }
+}
+
+}  // namespace
+
+template <typename real>
+cudaError_t launch_scatter_source(const double* x, const double* gf, real* src,
+                                  const double* M, const double* sscale, const double* oscale,
+                                  const int* material, int n_mat, int n_groups, int group,
+                                  long n_cells, int n, int n_mom, long n_dofs, cudaStream_t s) {
+  (void)n_mat;
+  scatter_source_kernel<real><<<grid_for((long)n_mom * n_cells * n), kBlock, 0, s>>>(
+      x, gf, src, M, sscale, oscale, material, n_groups, group, n_cells, n, n_mom, n_dofs);
+  return cudaGetLastError();
+}
+template cudaError_t launch_scatter_source<double>(const double*, const double*, double*,
+                                                   const double*, const double*, const double*,
+                                                   const int*, int, int, int, long, int, int,
+                                                   long, cudaStream_t);
+template cudaError_t launch_scatter_source<float>(const double*, const double*, float*,
+                                                  const double*, const double*, const double*,
+                                                  const int*, int, int, int, long, int, int, long,
+                                                  cudaStream_t);
+
+template <typename real>
+cudaError_t launch_iso_source(real* iso, const double* qcell, const double* rowsum,
+                              const int* source_id, long n_cells, int n, cudaStream_t s) {
+  iso_source_kernel<real><<<grid_for(n_cells * n), kBlock, 0, s>>>(iso, qcell, rowsum, source_id,
+                                                                   n_cells, n);
+  return cudaGetLastError();
+}
+template cudaError_t launch_iso_source<double>(double*, const double*, const double*, const int*,
+                                               long, int, cudaStream_t);
+template cudaError_t launch_iso_source<float>(float*, const double*, const double*, const int*,
+                                              long, int, cudaStream_t);
+
+template <typename real>
+cudaError_t launch_combine(const double* x, const real* phi, double* y, long len, double sx,
+                           double sp, cudaStream_t s) {
+  combine_kernel<real><<<grid_for(len), kBlock, 0, s>>>(x, phi, y, len, sx, sp);
+  return cudaGetLastError();
+}
+template cudaError_t launch_combine<double>(const double*, const double*, double*, long, double,
+                                            double, cudaStream_t);
+template cudaError_t launch_combine<float>(const double*, const float*, double*, long, double,
+                                           double, cudaStream_t);
+
+cudaError_t launch_permute(const double* in, double* out, const long* order, long n_cells, int n,
+                           int n_vec, int to_internal, cudaStream_t s) {
+  permute_kernel<<<grid_for((long)n_vec * n_cells * n), kBlock, 0, s>>>(in, out, order, n_cells,
+                                                                        n, n_vec, to_internal);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_multi_axpy(const double* const* V, int k, const double* coef, double scale,
+                              double* w, long len, cudaStream_t s) {
+  multi_axpy_kernel<<<grid_for(len), kBlock, 0, s>>>(V, k, coef, scale, w, len);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_axpby(double a, const double* x, double b, double* y, long len,
+                         cudaStream_t s) {
+  axpby_kernel<<<grid_for(len), kBlock, 0, s>>>(a, x, b, y, len);
+  return cudaGetLastError();
+}
+
+// xs: device array of k device pointers; out: k doubles; partial: k * kDotGrid
+// doubles; done: a zeroed counter that the kernel leaves zeroed.
+cudaError_t launch_dots(const double* const* xs, const double* y, int k, long len, double* out,
+                        double* partial, unsigned int* done, cudaStream_t s) {
+  const int grid = kDotGrid;
+  if (k <= 1)
+    dots_kernel<1><<<grid, kBlock, 0, s>>>(xs, y, k, len, partial, out, done);
+  else if (k <= 8)
+    dots_kernel<8><<<grid, kBlock, 0, s>>>(xs, y, k, len, partial, out, done);
+  else if (k <= 32)
+    dots_kernel<32><<<grid, kBlock, 0, s>>>(xs, y, k, len, partial, out, done);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+}  // namespace ouranos

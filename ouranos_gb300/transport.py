@@ -1,0 +1,182 @@
+"""Python mirror of the reference operator ``RadiativeTransfer<dim,tensor_dim>``
+(src/RadiativeTransfer.hh:46-263) over the C-ABI.
+
+Method names and argument meanings follow the reference so that a driver
+written against it (src/ouranos.cc:43-209) reads the same:
+
+    rt = RadiativeTransfer(problem)       # constructor + setup()
+    rt.set_group(0)
+    rhs = np.zeros(rt.length)
+    rt.sweep(rhs, group_flux)             # RHS sweep (src/ouranos.cc:152-158)
+    rt.Apply(x, y)                        # Epetra_Operator::Apply, returns 0
+
+Vectors are numpy arrays (host) or CUDA tensors (anything with
+``data_ptr()``, i.e. device memory), in the [mom][dof] layout.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from .problem import Problem
+
+
+def _ptr(v):
+    if v is None:
+        return None
+    if hasattr(v, "data_ptr"):
+        if not v.is_contiguous() or str(v.dtype) != "torch.float64":
+            raise ValueError("device vectors must be contiguous float64 tensors")
+        return v.data_ptr()
+    if not (isinstance(v, np.ndarray) and v.dtype == np.float64 and v.flags["C_CONTIGUOUS"]):
+        raise ValueError("host vectors must be C-contiguous float64 numpy arrays")
+    return v.ctypes.data
+
+
+class RadiativeTransfer:
+    """The transport operator y = x - D L^-1 M2D S x on one GPU."""
+
+    def __init__(self, problem: Problem, device: int = -1, precision: str = "fp64"):
+        self.problem = problem
+        L = _capi.lib()
+        desc, keep = problem.desc()
+        h = C.c_void_p()
+        rc = L.ouranos_rt_create(C.byref(desc), device, C.byref(h))
+        self._h = h.value
+        if rc != _capi.OK:
+            msg = _capi.last_error(self._h)
+            if self._h:
+                L.ouranos_rt_destroy(self._h)
+                self._h = None
+            raise _capi.OuranosError(rc, msg)
+        del keep
+        n = C.c_long()
+        _capi.check(L.ouranos_rt_vector_length(self._h, C.byref(n)), self._h)
+        self.length = n.value
+        _capi.check(L.ouranos_rt_n_tasks(self._h, C.byref(n)), self._h)
+        self.n_tasks = n.value
+        self.set_precision(precision)
+
+    # ---- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            _capi.lib().ouranos_rt_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        return _capi.check(rc, self._h)
+
+    # ---- reference surface
+    def setup(self):
+        """RadiativeTransfer::setup -- done by the constructor; kept for drivers."""
+
+    def set_group(self, g):
+        self._check(_capi.lib().ouranos_rt_set_group(self._h, g))
+
+    def set_precision(self, precision):
+        p = {"fp64": _capi.FP64, "fp32": _capi.FP32}[precision]
+        self._check(_capi.lib().ouranos_rt_set_precision(self._h, p))
+        self.precision = precision
+
+    def get_n_tasks_to_execute(self):
+        return self.n_tasks
+
+    def compute_scattering_source(self, x):
+        self._check(_capi.lib().ouranos_rt_scattering_source(self._h, _ptr(x)))
+
+    def sweep(self, flux_moments, group_flux=None):
+        """flux_moments += D L^-1 (M2D S [+ q + other groups + inflow])."""
+        self._check(_capi.lib().ouranos_rt_sweep(self._h, _ptr(flux_moments), _ptr(group_flux)))
+        return flux_moments
+
+    def Apply(self, x, y):
+        """Epetra_Operator::Apply: y = x - D L^-1 M2D S x; returns 0."""
+        self._check(_capi.lib().ouranos_rt_apply(self._h, _ptr(x), _ptr(y)))
+        return 0
+
+    def apply(self, x):
+        y = np.empty_like(x) if isinstance(x, np.ndarray) else x.new_empty(x.shape)
+        self.Apply(x, y)
+        return y
+
+    def rhs(self, group_flux=None, out=None):
+        """Right-hand side of the Krylov form, in-group scattering taken as zero."""
+        if out is None:
+            out = np.zeros(self.length)
+        self._check(_capi.lib().ouranos_rt_sweep_rhs(self._h, _ptr(group_flux), _ptr(out)))
+        return out
+
+    # Epetra_Operator trivia (src/RadiativeTransfer.hh:97-118)
+    def UseTranspose(self):
+        return False
+
+    def SetUseTranspose(self, flag):
+        return 0
+
+    def ApplyInverse(self, x, y):
+        return 0
+
+    def NormInf(self):
+        return 0.0
+
+    def HasNormInf(self):
+        return False
+
+    def Label(self):
+        return "radiative_transfer"
+
+    # ---- extensions
+    def task_levels(self):
+        out = np.zeros(self.n_tasks, dtype=np.int32)
+        self._check(_capi.lib().ouranos_rt_task_levels(self._h, out.ctypes.data))
+        return out.reshape(self.problem.quad.n_dir, self.problem.total_cells)
+
+    def last_sweep_ms(self):
+        ms, k = C.c_double(), C.c_int()
+        self._check(_capi.lib().ouranos_rt_last_sweep_ms(self._h, C.byref(ms), C.byref(k)))
+        return ms.value, k.value
+
+    def set_tiling(self, cells_x=0, cells_y=0, dirs=0):
+        self._check(_capi.lib().ouranos_rt_set_tiling(self._h, cells_x, cells_y, dirs))
+
+    def tiling(self):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        self._check(_capi.lib().ouranos_rt_get_tiling(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def set_stream(self, stream):
+        """Run on a caller's cudaStream_t (an int handle, e.g. torch's
+        ``torch.cuda.current_stream().cuda_stream``); None = own stream."""
+        self._check(_capi.lib().ouranos_rt_set_stream(self._h, stream or None))
+
+    def set_wait_limit(self, ns):
+        self._check(_capi.lib().ouranos_rt_set_wait_limit(self._h, float(ns)))
+
+    def debug_wait_bias(self, extra):
+        self._check(_capi.lib().ouranos_rt_debug_wait_bias(self._h, int(extra)))
+
+    def solve(self, method="gmres", tol=1e-8, max_it=1000, restart=30, group_flux=None, x=None):
+        """Drivers of src/ouranos.cc:43-209. Returns (x, info dict, residual history)."""
+        kind = {"si": _capi.SOLVER_SI, "gmres": _capi.SOLVER_GMRES,
+                "bicgstab": _capi.SOLVER_BICGSTAB, "fgmres_mixed": _capi.SOLVER_FGMRES_MIXED}[method]
+        if x is None:
+            x = np.zeros(self.length)
+        hist = np.zeros(max_it + 2)
+        info = _capi.SolveInfo()
+        rc = _capi.lib().ouranos_solve(self._h, kind, restart, max_it, tol, _ptr(group_flux),
+                                       _ptr(x), hist.ctypes.data, C.byref(info))
+        if rc not in (_capi.OK, _capi.ERR_NOT_CONVERGED):
+            self._check(rc)
+        n = info.iterations + 1
+        return x, dict(iterations=info.iterations, restarts=info.restarts,
+                       residual=info.residual, seconds=info.seconds,
+                       converged=bool(info.converged)), hist[:n]

@@ -1,0 +1,130 @@
+"""C-ABI surface that needs no GPU: exported symbols, host-side level sets,
+error paths, the input-file reader."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from helpers import golden
+from oracle import pyoracle as po
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_declared_symbol():
+    from ouranos_gb300 import _capi
+    L = _capi.lib()
+    declared = []
+    for name in os.listdir(os.path.join(ROOT, "include")):
+        if name.endswith(".h"):
+            with open(os.path.join(ROOT, "include", name)) as f:
+                src = re.sub(r"/\*.*?\*/", "", f.read(), flags=re.S)
+            declared += re.findall(r"^\s*int\s+(ouranos_\w+)\s*\(", src, flags=re.M)
+    assert declared
+    for sym in declared:
+        assert hasattr(L, sym), sym
+    assert sorted(set(declared)) == sorted(set(_capi.EXPORTS))
+
+
+@pytest.mark.parametrize("dim,n,sn", [(2, (5, 7), 4), (2, (8, 8), 8), (3, (3, 4, 5), 4), (3, (4, 4, 4), 6)])
+def test_wavefront_levels_bit_exact(dim, n, sn):
+    """Per-octant levels equal the longest-path depths of the reference's task DAG
+    (compute_sweep_ordering + required/waiting maps), and the oracle's FIFO
+    execution order never runs a task before a task of a lower level it depends on."""
+    import ouranos_gb300 as og
+    from ouranos_gb300 import _capi
+    q = og.build_quadrature("LS", sn, 0, False, 4 * np.pi, dim)
+    nc = int(np.prod(n))
+    lv = np.zeros(q.n_dir * nc, dtype=np.int32)
+    arr = np.array(list(n), dtype=np.int32)
+    assert _capi.lib().ouranos_wavefront_levels(dim, arr.ctypes.data, q.n_dir,
+                                                 np.ascontiguousarray(q.omega).ctypes.data,
+                                                 lv.ctypes.data) == 0
+    lv = lv.reshape(q.n_dir, nc)
+    p = og.uniform_problem(dim, 1, n, (0,) * dim, (1.0,) * dim, q, 1.0, 0.5, 1.0)
+    P = po.OracleProblem(p.arrays())
+    assert (P.task_levels() == lv).all()
+    P.scattering_source(np.zeros(P.length))
+    P.sweep()
+    order = P.last_order()
+    dirs, cells = order // nc, order % nc
+    # per direction, levels along the execution order are non-decreasing in the
+    # sense of dependencies: a task at level L runs after all its upwind tasks
+    done = np.zeros((q.n_dir, nc), bool)
+    for d, c in zip(dirs, cells):
+        ijk = np.unravel_index(c, n[::-1])[::-1]
+        for a in range(dim):
+            up = list(ijk)
+            up[a] += -1 if q.omega[d, a] > 0 else 1
+            if 0 <= up[a] < n[a]:
+                uc = np.ravel_multi_index(tuple(up[::-1]), n[::-1])
+                assert done[d, uc]
+        done[d, c] = True
+
+
+def test_create_without_device_or_bad_input():
+    """No GPU here: ouranos_rt_create must fail cleanly, never crash."""
+    import ouranos_gb300 as og
+    from ouranos_gb300 import _capi
+    p = og.config_small(n=4, sn=4)
+    desc, keep = p.desc()
+    h = C.c_void_p()
+    rc = _capi.lib().ouranos_rt_create(C.byref(desc), -1, C.byref(h))
+    try:
+        assert rc in (_capi.OK, _capi.ERR_NO_DEVICE, _capi.ERR_CUDA)
+        if rc != _capi.OK:
+            assert _capi.last_error(h.value)
+    finally:
+        if h.value:
+            _capi.lib().ouranos_rt_destroy(h.value)
+    desc.dim = 4
+    h = C.c_void_p()
+    rc = _capi.lib().ouranos_rt_create(C.byref(desc), -1, C.byref(h))
+    assert rc == _capi.ERR_BAD_INPUT
+    assert "dim" in _capi.last_error(h.value)
+    _capi.lib().ouranos_rt_destroy(h.value)
+
+
+def test_parameters_reader():
+    """tests/Parameters_test.cc through the input reader."""
+    import math
+    import ouranos_gb300.inp as inp
+    m = golden("inputs.json")
+    p = inp.read_parameters(m["files"]["parameters.inp"])
+    enums = {"VACUUM": 0, "ISOTROPIC": 1, "MOST_NORMAL": 2, "REFLECTIVE": 3, "BICGSTAB": "BICGSTAB",
+             "GMRES": "GMRES", "SI": "SI", "GLC_QUAD": "GLC", "LS_QUAD": "LS",
+             "false": False, "true": True}
+    for name, args, val in m["parameters"]:
+        if name in ("bc_type",):
+            got = p.bc_type[args[0]]
+        elif name in ("inc_flux", "src"):
+            got = getattr(p, "get_" + name)(*args)
+        elif name == "n_src":
+            got = p.n_src
+        elif name == "max_outer_it":
+            got = p.max_outer_it
+        else:
+            got = getattr(p, {"quad_type": "quad_type", "solver_type": "solver_type"}.get(name, name))
+        if val in enums:
+            exp = enums[val]
+        elif val.startswith('"'):
+            exp = val.strip('"')
+        else:
+            exp = eval(val.replace("M_PI", "math.pi").replace("2.*", "2.0*"), {"math": math})
+        assert got == exp, (name, got, exp)
+
+
+def test_inp_problem_matches_golden_problem(tmp_path):
+    """The reference's RT deck replayed through the reader gives the golden test's problem."""
+    import ouranos_gb300.inp as inp
+    m = golden("inputs.json")["files"]
+    d = tmp_path / "tests"
+    d.mkdir()
+    for k in ("rt_parameters.inp", "rt_geometry.inp", "rt_xs.inp"):
+        (d / k).write_text(m[k])
+    prob = inp.problem_from_files("tests/rt_parameters.inp", base_dir=str(tmp_path))
+    assert prob.n_cells == (4, 4) and prob.fe_order == 1 and prob.quad.n_dir == 12
+    assert prob.quad.weight_sum == 1.0 and prob.sigma_t[0, 0] == 1.0 and prob.sigma_s[0, 0, 0, 0] == 0.5
+    assert prob.source[0, 0] == 1.0 and tuple(prob.bc_type[:4]) == (0, 0, 0, 0)
