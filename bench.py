@@ -217,6 +217,7 @@ def run_ours(args):
     sampler = ClockSampler(("GPU-" + uid if uid and not uid.startswith("GPU-") else uid) or local)
     sampler.start()
     step_ms, sweep_ms = [], []
+    launches = 0
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize(dev)
@@ -227,7 +228,9 @@ def run_ours(args):
         ev1.record(stream)
         ev1.synchronize()
         step_ms.append(ev0.elapsed_time(ev1))
-        sweep_ms.append(rt.last_sweep_ms()[0])
+        ms, k = rt.last_sweep_ms()
+        sweep_ms.append(ms)
+        launches += k + 2  # sweep-side kernels + scattering source + combine
     torch.cuda.synchronize(dev)
     clocks = sampler.stop()
     total_ms = sum(step_ms)
@@ -293,7 +296,7 @@ def run_ours(args):
                          "sweep_ms": avg_sweep_s * 1e3,
                          "fp_flops_per_solve": fps,
                          "fp_tflops": fps * solves / avg_sweep_s / 1e12},
-            "gpu_launches": 3 * args.steps,
+            "gpu_launches": launches,
             "clocks": clocks,
         }
         if cpu:

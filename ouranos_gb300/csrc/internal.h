@@ -79,15 +79,15 @@ struct SweepArgs {
   const int* dir_class;        // [n_dir] index of |Omega| class
   int n_dir_class;
   const real* abs_omega;       // [n_dir][3]
-  const real* m2d;             // [n_dir][n_mom]
-  const real* d2m_t;           // [n_dir][n_mom] (D2M transposed)
+  const real* m2d;             // [n_dir][n_mom]      (moment-fused form)
   const real* ainv;            // [n_sigma_class][n_dir_class][n][n]
   const int* cell_class;       // [cells] sigma_t class
   const real* face_mass;       // [3][fd][fd]
-  const real* src;             // [n_mom][n_dofs] source moments T
-  const real* iso;             // [n_dofs] isotropic fixed source term or NULL
+  const real* src;             // [n_mom][n_dofs] source moments T (moment-fused form)
+  const real* iso;             // [n_dofs] isotropic fixed source or NULL (moment-fused form)
+  const real* q;               // [n_dir][n_dofs] per-direction source (expanded form)
   const real* bnd;             // [n_dir][3] boundary inflow per axis or NULL
-  real* phi;                   // [n_mom][n_dofs] accumulated
+  real* psi;                   // [n_dir][n_dofs] angular flux out
   real* edge_x;                // [n_dir][tiles][n_sweep][wy][fd]
   real* edge_y;                // [n_dir][tiles][n_sweep][wx][fd]
   int* progress;               // [n_groups][tiles] completed steps
@@ -97,9 +97,19 @@ struct SweepArgs {
   int wait_bias;
 };
 
+// fused_moments: 0 = read the expanded per-direction source q; 1 or 2 = apply
+// M2D to that many source moments inside the sweep.
 template <typename real>
-cudaError_t launch_sweep(int dim, int p1, const SweepArgs<real>& a, int grid, int block,
-                         cudaStream_t s);
+cudaError_t launch_sweep(int dim, int p1, int fused_moments, const SweepArgs<real>& a, int grid,
+                         int block, cudaStream_t s);
+// q[d][e] = sum_m M2D[d][m] T[m][e] (+ iso[e])  -- moment -> direction expansion
+template <typename real>
+cudaError_t launch_expand_source(const real* T, const real* iso, const real* m2d, real* q,
+                                 int n_dir, int n_mom, long n_dofs, cudaStream_t s);
+// phi[m][e] = sum_d D2M[m][d] psi[d][e]  -- direction -> moment reduction
+template <typename real>
+cudaError_t launch_reduce_moments(const real* psi, const real* d2m_t, real* phi, int n_dir,
+                                  int n_mom, long n_dofs, cudaStream_t s);
 
 // ------------------------------------------------------------ vector kernels
 template <typename real>
@@ -174,7 +184,7 @@ struct ouranos_rt {
   ouranos::DevBuf d_tasks, d_group_dirs, d_group_flip, d_progress, d_ctrl;
   ouranos::DevBuf d_edge_x, d_edge_y;
   // device: vectors
-  ouranos::DevBuf d_src64, d_src32, d_phi64, d_phi32, d_iso64, d_iso32;
+  ouranos::DevBuf d_src64, d_src32, d_phi64, d_phi32, d_iso64, d_iso32, d_q, d_psi;
   ouranos::DevBuf d_x, d_y, d_gf, d_tmp, d_scatx;  // staging; d_scatx: scattering-source argument
   // solver workspace
   ouranos::DevBuf d_krylov;

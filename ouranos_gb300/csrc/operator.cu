@@ -203,10 +203,16 @@ int setup_group(ouranos_rt* rt) {
 }
 
 // --------------------------------------------------------------- the sweep
+// Source moments with at most this many entries are applied inside the sweep;
+// more are first expanded to per-direction sources (a dense contraction over
+// the moment axis that streams better than a per-step loop over moments).
+constexpr int kFusedMomentsMax = 2;
+
 template <typename real>
 int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd, real* phi) {
   SweepArgs<real> a;
   const bool f64 = sizeof(real) == 8;
+  const long len_dir = (long)rt->n_dir * rt->n_dofs;
   a.nx = rt->nx[0];
   a.ny = rt->nx[1];
   a.nz = rt->nx[2];
@@ -226,14 +232,15 @@ int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd,
   a.n_dir_class = rt->n_dir_class;
   a.abs_omega = (const real*)(f64 ? rt->d_abs64.p : rt->d_abs32.p);
   a.m2d = (const real*)(f64 ? rt->d_m2d64.p : rt->d_m2d32.p);
-  a.d2m_t = (const real*)(f64 ? rt->d_d2m64.p : rt->d_d2m32.p);
   a.ainv = (const real*)(f64 ? rt->d_ainv64.p : rt->d_ainv32.p);
   a.cell_class = rt->d_cell_class.as<int>();
   a.face_mass = (const real*)(f64 ? rt->d_face64.p : rt->d_face32.p);
   a.src = src;
   a.iso = iso;
+  a.q = nullptr;
   a.bnd = bnd;
-  a.phi = phi;
+  CU(rt->d_psi.alloc(sizeof(real) * len_dir), "angular flux");
+  a.psi = rt->d_psi.as<real>();
   a.edge_x = rt->d_edge_x.as<real>();
   a.edge_y = rt->d_edge_y.as<real>();
   int* ctrl = rt->d_ctrl.as<int>();
@@ -242,6 +249,17 @@ int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd,
   a.progress = ctrl + 64;
   a.wait_limit_ns = rt->wait_limit_ns;
   a.wait_bias = rt->wait_bias;
+  int kernels = 0;
+  // (the fused form holds (moments + 1) prefetched values per dof in registers)
+  const int fm = (rt->n_mom <= kFusedMomentsMax && rt->n * (rt->n_mom + 1) <= 32) ? rt->n_mom : 0;
+  if (fm == 0) {
+    CU(rt->d_q.alloc(sizeof(real) * len_dir), "expanded source");
+    CU(launch_expand_source<real>(src, iso, a.m2d, rt->d_q.as<real>(), rt->n_dir, rt->n_mom,
+                                  rt->n_dofs, rt->stream),
+       "source expansion");
+    kernels += (rt->n_mom + 15) / 16;
+    a.q = rt->d_q.as<real>();
+  }
   const size_t ctrl_bytes = sizeof(int) * (64 + (size_t)rt->n_groups_dir * rt->tiles_x * rt->tiles_y);
   // ticket + progress -> 0.  The status word [1] is sticky: it is cleared at the
   // start of each C-ABI call (clear_status), so a timeout inside a solve is seen
@@ -249,27 +267,21 @@ int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd,
   // counter at [2] is 0 whenever no dot kernel is in flight on this stream.
   CU(cudaMemsetAsync(ctrl, 0, sizeof(int), rt->stream), "reset sweep control");
   CU(cudaMemsetAsync(ctrl + 64, 0, ctrl_bytes - 64 * sizeof(int), rt->stream), "reset progress");
-  int dev = rt->device, sms = 0, per_sm = 0;
-  CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device query");
+  int sms = 0;
+  CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, rt->device), "device query");
   const int block = 128;
-  // occupancy of the instantiated kernel is queried once per (precision, shape)
-  static thread_local std::map<long, int> occ;
-  const long key = (long)f64 * 1000 + rt->dim * 100 + rt->p1;
-  auto it = occ.find(key);
-  if (it == occ.end()) {
-    per_sm = 0;
-    // probe: launch-free occupancy through a zero-task launch is not needed;
-    // 8 blocks (32 warps) per SM is within every instantiation's register budget
-    per_sm = 8;
-    occ[key] = per_sm;
-  } else {
-    per_sm = it->second;
-  }
-  int grid = std::min((rt->n_tasks + 3) / 4, std::max(1, sms * per_sm));
+  // tasks are handed out by ticket, so any grid is deadlock-free; 8 blocks of
+  // 4 warps per SM covers every instantiation's register budget
+  const int grid = std::min((rt->n_tasks + 3) / 4, std::max(1, sms * 8));
   CU(cudaEventRecord(rt->ev0, rt->stream), "event");
-  CU(launch_sweep<real>(rt->dim, rt->p1, a, grid, block, rt->stream), "sweep launch");
+  CU(launch_sweep<real>(rt->dim, rt->p1, fm, a, grid, block, rt->stream), "sweep launch");
   CU(cudaEventRecord(rt->ev1, rt->stream), "event");
-  rt->last_kernels = 1;
+  ++kernels;
+  CU(launch_reduce_moments<real>(a.psi, (const real*)(f64 ? rt->d_d2m64.p : rt->d_d2m32.p), phi,
+                                 rt->n_dir, rt->n_mom, rt->n_dofs, rt->stream),
+     "moment reduction");
+  kernels += (rt->n_mom + 15) / 16;
+  rt->last_kernels = kernels;
   return OURANOS_OK;
 }
 
@@ -373,7 +385,6 @@ int sweep_into_phi(ouranos_rt* rt, bool sources) {
   const long len = vec_len(rt);
   if (rt->precision == OURANOS_FP64) {
     CU(rt->d_phi64.alloc(sizeof(double) * len), "flux");
-    CU(cudaMemsetAsync(rt->d_phi64.p, 0, sizeof(double) * len, rt->stream), "flux");
     const double* iso = nullptr;
     if (sources) {
       CU(rt->d_iso64.alloc(sizeof(double) * rt->n_dofs), "iso");
@@ -387,7 +398,6 @@ int sweep_into_phi(ouranos_rt* rt, bool sources) {
                              sources ? rt->d_bnd64.as<double>() : nullptr, rt->d_phi64.as<double>());
   }
   CU(rt->d_phi32.alloc(sizeof(float) * len), "flux");
-  CU(cudaMemsetAsync(rt->d_phi32.p, 0, sizeof(float) * len, rt->stream), "flux");
   const float* iso = nullptr;
   if (sources) {
     CU(rt->d_iso32.alloc(sizeof(float) * rt->n_dofs), "iso");

@@ -29,10 +29,14 @@
 // hold: any grid size is deadlock-free.  Every wait is bounded (iteration cap
 // and %globaltimer); a wait that runs out sets `status`, and all warps leave.
 //
-// Per lane and step: b = sum_m M2D(d,m) T_m[cell] (+ isotropic source) +
-// |Omega_a| F_a psi_up,a over the inflow faces; x = A'^-1 b; outflow faces are
-// the c_a = p entries of x; phi_m[cell] += D2M(m,d) x, reduced over the kd
-// directions of the warp by shuffles and added with one atomic per entry.
+// Per lane and step: b = q_d[cell] (the source expanded to this direction by
+// the expansion kernel, or sum_m M2D(d,m) T_m[cell] + isotropic source for one
+// or two moments) + |Omega_a| F_a psi_up,a over the inflow faces; x = A'^-1 b;
+// the outflow faces are the c_a = p entries of x; x is stored as psi_d[cell].
+// The next step's source values are loaded one step ahead, so their memory
+// latency overlaps the current solve.  The moments phi = D2M psi are formed
+// afterwards by the reduction kernel over the direction axis (no atomics: the
+// sweep is deterministic).
 #pragma once
 
 #include "internal.h"
@@ -91,7 +95,7 @@ struct Cell {
   static __device__ __forceinline__ constexpr int s_out(int t) { return t + N - PN; }
 };
 
-template <typename real, int DIM, int P1>
+template <typename real, int DIM, int P1, int FM>
 __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
   using C = Cell<DIM, P1>;
   constexpr int N = C::N;
@@ -136,6 +140,9 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
       if (DIM == 3) bY = a.bnd[dd * 3 + 1];
       bS = a.bnd[dd * 3 + AS];
     }
+    real w0 = 0, w1 = 0;  // M2D row (moment-fused form)
+    if (FM >= 1) w0 = a.m2d[(size_t)dd * a.n_mom + 0];
+    if (FM >= 2) w1 = a.m2d[(size_t)dd * a.n_mom + 1];
     const int dcls = a.dir_class[dd];
     // mirrored local dof offsets: phys(i') = base + c0*s0 + c1*s1 + c2*s2
     int base = 0, st0 = 1, st1 = P1, st2 = P1 * P1;
@@ -145,10 +152,14 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
 
     const int xc = tx * a.wx + lx;  // canonical transverse coordinates
     const int yc = ty * a.wy + ly;
-    const bool col_ok = xc < NX && (DIM == 2 || yc < NY);
+    const bool col_ok = dir_ok && xc < NX && (DIM == 2 || yc < NY);
     const int xp = (flip & 1) ? NX - 1 - xc : xc;  // physical
     const int yp = DIM == 3 ? ((flip & 2) ? NY - 1 - yc : yc) : 0;
     const int sflip = DIM == 3 ? (flip & 4) : (flip & 2);
+    const long colbase = DIM == 2 ? (long)xp : (long)xp + (long)NX * yp;
+    const long plane = DIM == 2 ? (long)NX : (long)NX * NY;  // cells per sweep-axis layer
+    auto cell_of = [&](int sc) { return colbase + plane * (sflip ? NS - 1 - sc : sc); };
+    const size_t dirbase = (size_t)dd * a.n_dofs;
 
     const int* prog_x = a.progress + grp * tiles + tile - 1;
     const int* prog_y = a.progress + grp * tiles + tile - a.tiles_x;
@@ -157,18 +168,38 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
     const bool pub_y = DIM == 3 && ty + 1 < a.tiles_y;
     const bool publish = pub_x || pub_y;
 
+    // source values of the lane's next cell, loaded one step ahead
+    real nq[N], nt1[FM >= 2 ? N : 1], niso[FM >= 1 ? N : 1];
+    int ncls = 0;
+    auto load_next = [&](int sc) {
+      const long cb = cell_of(sc) * N + base;
+      ncls = __ldg(a.cell_class + cell_of(sc));
+      if (FM == 0) {
+        const real* Q = a.q + dirbase + cb;
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+          nq[i] = __ldg(Q + C::comp(i, 0) * st0 + C::comp(i, 1) * st1 + (DIM == 3 ? C::comp(i, 2) * st2 : 0));
+      } else {
+        const real* T = a.src + cb;
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          const int off = C::comp(i, 0) * st0 + C::comp(i, 1) * st1 + (DIM == 3 ? C::comp(i, 2) * st2 : 0);
+          nq[i] = __ldg(T + off);
+          if (FM >= 2) nt1[i] = __ldg(T + a.n_dofs + off);
+          if (FM >= 1) niso[i] = a.iso ? __ldg(a.iso + cb + off) : real(0);
+        }
+      }
+    };
+    // the lane's first active step is s = lx + ly (plane 0)
+    if (col_ok) load_next(0);
+
     real psiS[FD], psiX[FD], psiY[FD];
 #pragma unroll
     for (int t = 0; t < FD; ++t) psiS[t] = psiX[t] = psiY[t] = real(0);
 
     for (int s = 0; s < nsteps; ++s) {
       const int sc = s - lx - ly;
-      const bool cell_ok = col_ok && sc >= 0 && sc < NS;
-      const bool act = cell_ok && dir_ok;
-      const int sp = sflip ? NS - 1 - sc : sc;
-      const long cell = DIM == 2 ? (long)xp + (long)NX * sp
-                                 : (long)xp + (long)NX * (yp + (long)NY * sp);
-      const long cbase = cell * N;
+      const bool act = col_ok && sc >= 0 && sc < NS;
 
       // ---- upwind face values.  Edge-buffer waits run first (divergent), the
       // shuffles after them (converged), and the boundary / edge / neighbour
@@ -213,31 +244,19 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
         upS[t] = sc == 0 ? bS : psiS[t];
       }
 
-      real x[N];
-#pragma unroll
-      for (int i = 0; i < N; ++i) x[i] = real(0);
       if (act) {
+        const long cell = cell_of(sc);
+        const long cbase = cell * N + base;
+        const int cls = ncls;
         real b[N];
 #pragma unroll
-        for (int i = 0; i < N; ++i) b[i] = real(0);
-        // scattering / fixed source moments
-        for (int m = 0; m < a.n_mom; ++m) {
-          const real w = __ldg(a.m2d + (size_t)d * a.n_mom + m);
-          const real* T = a.src + (size_t)m * a.n_dofs + cbase + base;
-#pragma unroll
-          for (int i = 0; i < N; ++i) {
-            const int off = C::comp(i, 0) * st0 + C::comp(i, 1) * st1 + (DIM == 3 ? C::comp(i, 2) * st2 : 0);
-            b[i] += w * __ldg(T + off);
-          }
+        for (int i = 0; i < N; ++i) {
+          if (FM == 0) b[i] = nq[i];
+          else if (FM == 1) b[i] = w0 * nq[i] + niso[i];
+          else b[i] = w0 * nq[i] + w1 * nt1[i] + niso[i];
         }
-        if (a.iso) {
-          const real* Q = a.iso + cbase + base;
-#pragma unroll
-          for (int i = 0; i < N; ++i) {
-            const int off = C::comp(i, 0) * st0 + C::comp(i, 1) * st1 + (DIM == 3 ? C::comp(i, 2) * st2 : 0);
-            b[i] += __ldg(Q + off);
-          }
-        }
+        // prefetch the next plane's source while this one is solved
+        if (sc + 1 < NS) load_next(sc + 1);
         // inflow faces: b_face += |Omega_a| F_a psi_up
         const real* FX = a.face_mass + 0 * FD * FD;
         const real* FS = a.face_mass + AS * FD * FD;
@@ -263,7 +282,8 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
           }
         }
         // x = A'^-1 b
-        const real* Ai = a.ainv + ((size_t)a.cell_class[cell] * a.n_dir_class + dcls) * (N * N);
+        const real* Ai = a.ainv + ((size_t)cls * a.n_dir_class + dcls) * (N * N);
+        real x[N];
 #pragma unroll
         for (int i = 0; i < N; ++i) {
           real acc = 0;
@@ -271,6 +291,10 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
           for (int j = 0; j < N; ++j) acc += __ldg(Ai + i * N + j) * b[j];
           x[i] = acc;
         }
+        real* P = a.psi + dirbase + cbase;
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+          P[C::comp(i, 0) * st0 + C::comp(i, 1) * st1 + (DIM == 3 ? C::comp(i, 2) * st2 : 0)] = x[i];
 #pragma unroll
         for (int t = 0; t < FD; ++t) {
           psiX[t] = x[C::x_out(t)];
@@ -293,35 +317,21 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
         __syncwarp();
         if (lane == 0) st_release_gpu(prog_self, s + 1);
       }
-
-      // ---- phi_m += D2M(m, d) x, reduced over the kd directions of the cell
-      for (int m = 0; m < a.n_mom; ++m) {
-        const real w = act ? __ldg(a.d2m_t + (size_t)d * a.n_mom + m) : real(0);
-        real v[N];
-#pragma unroll
-        for (int i = 0; i < N; ++i) v[i] = w * x[i];
-        for (int o = wc; o < 32; o <<= 1) {
-#pragma unroll
-          for (int i = 0; i < N; ++i) v[i] += __shfl_xor_sync(FULL, v[i], o);
-        }
-        if (cell_ok) {
-          real* P = a.phi + (size_t)m * a.n_dofs + cbase + base;
-#pragma unroll
-          for (int i = 0; i < N; ++i) {
-            if ((i & (a.kd - 1)) == kslot) {
-              const int off = C::comp(i, 0) * st0 + C::comp(i, 1) * st1 + (DIM == 3 ? C::comp(i, 2) * st2 : 0);
-              atomicAdd(P + off, v[i]);
-            }
-          }
-        }
-      }
     }
   }
 }
 
 template <typename real, int DIM, int P1>
-cudaError_t launch_sweep_impl(const SweepArgs<real>& a, int grid, int block, cudaStream_t s) {
-  sweep_kernel<real, DIM, P1><<<grid, block, 0, s>>>(a);
+cudaError_t launch_sweep_impl(int fm, const SweepArgs<real>& a, int grid, int block,
+                              cudaStream_t s) {
+  if (fm == 0)
+    sweep_kernel<real, DIM, P1, 0><<<grid, block, 0, s>>>(a);
+  else if (fm == 1)
+    sweep_kernel<real, DIM, P1, 1><<<grid, block, 0, s>>>(a);
+  else if (fm == 2)
+    sweep_kernel<real, DIM, P1, 2><<<grid, block, 0, s>>>(a);
+  else
+    return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 

@@ -4,19 +4,19 @@
 namespace ouranos {
 
 template <>
-cudaError_t launch_sweep<double>(int dim, int p1, const SweepArgs<double>& a, int grid, int block,
+cudaError_t launch_sweep<double>(int dim, int p1, int fm, const SweepArgs<double>& a, int grid, int block,
                                 cudaStream_t s) {
   if (dim == 2) {
     switch (p1) {
-      case 2: return launch_sweep_impl<double, 2, 2>(a, grid, block, s);
-      case 3: return launch_sweep_impl<double, 2, 3>(a, grid, block, s);
-      case 4: return launch_sweep_impl<double, 2, 4>(a, grid, block, s);
-      case 5: return launch_sweep_impl<double, 2, 5>(a, grid, block, s);
+      case 2: return launch_sweep_impl<double, 2, 2>(fm, a, grid, block, s);
+      case 3: return launch_sweep_impl<double, 2, 3>(fm, a, grid, block, s);
+      case 4: return launch_sweep_impl<double, 2, 4>(fm, a, grid, block, s);
+      case 5: return launch_sweep_impl<double, 2, 5>(fm, a, grid, block, s);
     }
   } else if (dim == 3) {
     switch (p1) {
-      case 2: return launch_sweep_impl<double, 3, 2>(a, grid, block, s);
-      case 3: return launch_sweep_impl<double, 3, 3>(a, grid, block, s);
+      case 2: return launch_sweep_impl<double, 3, 2>(fm, a, grid, block, s);
+      case 3: return launch_sweep_impl<double, 3, 3>(fm, a, grid, block, s);
     }
   }
   return cudaErrorInvalidValue;

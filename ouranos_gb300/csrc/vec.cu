@@ -157,7 +157,111 @@ __global__ void dots_kernel(const double* const* xs, const double* y, int k, lon
   }
 }
 
+// Moment <-> direction contractions over the direction axis.  Both are
+// HBM-streaming: each thread owns one dof column e and loops over the short
+// axis with the coefficient table in shared memory.
+//   expand:  q[d][e] (+)= sum_{m<nm} m2d[d*ld + m] T[m][e] (+ iso[e])
+//   reduce:  phi[m][e]   = sum_d d2m_t[d*ld + m] psi[d][e],  m < nm
+template <typename real, int NM>
+__global__ void expand_kernel(const real* __restrict__ T, const real* __restrict__ iso,
+                              const real* __restrict__ m2d, int ld, real* __restrict__ q,
+                              int n_dir, int nm, long n_dofs, int accumulate) {
+  extern __shared__ unsigned char smem_raw[];
+  real* sm = reinterpret_cast<real*>(smem_raw);
+  for (int k = threadIdx.x; k < n_dir * nm; k += blockDim.x) sm[k] = m2d[(k / nm) * ld + k % nm];
+  __syncthreads();
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n_dofs;
+       e += (long)gridDim.x * blockDim.x) {
+    real t[NM];
+#pragma unroll
+    for (int m = 0; m < NM; ++m) t[m] = m < nm ? T[(size_t)m * n_dofs + e] : real(0);
+    const real is = iso ? iso[e] : real(0);
+    for (int d = 0; d < n_dir; ++d) {
+      real acc = accumulate ? q[(size_t)d * n_dofs + e] : is;
+#pragma unroll
+      for (int m = 0; m < NM; ++m)
+        if (m < nm) acc += sm[d * nm + m] * t[m];
+      q[(size_t)d * n_dofs + e] = acc;
+    }
+  }
+}
+
+template <typename real, int NM>
+__global__ void reduce_kernel(const real* __restrict__ psi, const real* __restrict__ d2m_t, int ld,
+                              real* __restrict__ phi, int n_dir, int nm, long n_dofs) {
+  extern __shared__ unsigned char smem_raw[];
+  real* sm = reinterpret_cast<real*>(smem_raw);
+  for (int k = threadIdx.x; k < n_dir * nm; k += blockDim.x) sm[k] = d2m_t[(k / nm) * ld + k % nm];
+  __syncthreads();
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n_dofs;
+       e += (long)gridDim.x * blockDim.x) {
+    real acc[NM];
+#pragma unroll
+    for (int m = 0; m < NM; ++m) acc[m] = real(0);
+    for (int d = 0; d < n_dir; ++d) {
+      const real v = psi[(size_t)d * n_dofs + e];
+#pragma unroll
+      for (int m = 0; m < NM; ++m)
+        if (m < nm) acc[m] += sm[d * nm + m] * v;
+    }
+#pragma unroll
+    for (int m = 0; m < NM; ++m)
+      if (m < nm) phi[(size_t)m * n_dofs + e] = acc[m];
+  }
+}
+
 }  // namespace
+
+template <typename real>
+cudaError_t launch_expand_source(const real* T, const real* iso, const real* m2d, real* q,
+                                 int n_dir, int n_mom, long n_dofs, cudaStream_t s) {
+  // moments in chunks of at most 16 (Galerkin sets have n_mom = n_dir)
+  for (int m0 = 0; m0 < n_mom; m0 += 16) {
+    const int nm = n_mom - m0 < 16 ? n_mom - m0 : 16;
+    const size_t sh = sizeof(real) * (size_t)n_dir * nm;
+    const real* Tm = T + (size_t)m0 * n_dofs;
+    const int acc = m0 > 0;
+    const real* is = m0 == 0 ? iso : nullptr;
+    if (nm <= 4)
+      expand_kernel<real, 4><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+    else if (nm <= 10)
+      expand_kernel<real, 10><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+    else
+      expand_kernel<real, 16><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+template cudaError_t launch_expand_source<double>(const double*, const double*, const double*,
+                                                  double*, int, int, long, cudaStream_t);
+template cudaError_t launch_expand_source<float>(const float*, const float*, const float*, float*,
+                                                 int, int, long, cudaStream_t);
+
+template <typename real>
+cudaError_t launch_reduce_moments(const real* psi, const real* d2m_t, real* phi, int n_dir,
+                                  int n_mom, long n_dofs, cudaStream_t s) {
+  for (int m0 = 0; m0 < n_mom; m0 += 16) {
+    const int nm = n_mom - m0 < 16 ? n_mom - m0 : 16;
+    const size_t sh = sizeof(real) * (size_t)n_dir * nm;
+    real* ph = phi + (size_t)m0 * n_dofs;
+    if (nm <= 1)
+      reduce_kernel<real, 1><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+    else if (nm <= 4)
+      reduce_kernel<real, 4><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+    else if (nm <= 10)
+      reduce_kernel<real, 10><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+    else
+      reduce_kernel<real, 16><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+template cudaError_t launch_reduce_moments<double>(const double*, const double*, double*, int, int,
+                                                   long, cudaStream_t);
+template cudaError_t launch_reduce_moments<float>(const float*, const float*, float*, int, int,
+                                                  long, cudaStream_t);
 
 template <typename real>
 cudaError_t launch_scatter_source(const double* x, const double* gf, real* src,

@@ -128,3 +128,19 @@ def test_inp_problem_matches_golden_problem(tmp_path):
     assert prob.n_cells == (4, 4) and prob.fe_order == 1 and prob.quad.n_dir == 12
     assert prob.quad.weight_sum == 1.0 and prob.sigma_t[0, 0] == 1.0 and prob.sigma_s[0, 0, 0, 0] == 0.5
     assert prob.source[0, 0] == 1.0 and tuple(prob.bc_type[:4]) == (0, 0, 0, 0)
+
+
+def test_vtk_writer_roundtrip(tmp_path):
+    """Headless VTK output of the flux (src/ouranos.cc:211-253 counterpart)."""
+    import ouranos_gb300 as og
+    from ouranos_gb300.vtk import read_vtk_point_data, write_vtk
+    for prob in (og.config_small(n=3, sn=2), og.uniform_problem(3, 1, (2, 2, 2), (0, 0, 0), (1, 1, 1),
+                                                                og.build_quadrature("LS", 2, 0, dim=3),
+                                                                1.0, 0.5, 1.0)):
+        x = np.arange(prob.vector_length, dtype=np.float64)
+        path = write_vtk(str(tmp_path / "out.vtk"), prob, x)
+        data = read_vtk_point_data(path)
+        vals = data["phi_0_g0"]
+        assert vals.size == prob.total_cells * 2 ** prob.dim
+        # first cell, first corner is local dof 0, second corner local dof 1
+        assert vals[0] == 0.0 and vals[1] == 1.0
