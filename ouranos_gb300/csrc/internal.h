@@ -88,9 +88,10 @@ struct SweepArgs {
   const real* q;               // [n_dir][n_dofs] per-direction source (expanded form)
   const real* bnd;             // [n_dir][3] boundary inflow per axis or NULL
   real* psi;                   // [n_dir][n_dofs] angular flux out
-  real* edge_x;                // [n_dir][tiles][n_sweep][wy][fd]
-  real* edge_y;                // [n_dir][tiles][n_sweep][wx][fd]
-  int* progress;               // [n_groups][tiles] completed steps
+  // edge buffers of tagged 64-bit words (1 per FP32 value, 2 per FP64 value)
+  unsigned long long* edge_x;  // [n_dir][tiles][n_sweep][wy][fd][words]
+  unsigned long long* edge_y;  // [n_dir][tiles][n_sweep][wx][fd][words]
+  unsigned epoch;              // sweep epoch in [1, 0x7fff], tags edge words
   int* ticket;                 // task counter
   int* status;                 // 0 ok, 1 wait timeout
   long long wait_limit_ns;
@@ -172,6 +173,7 @@ struct ouranos_rt {
   std::vector<int> cell_class_h;
   long long wait_limit_ns = 2000000000LL;
   int wait_bias = 0;
+  unsigned epoch = 0;                  // sweep counter, tags edge-buffer words
   double last_ms = 0.0;
   int last_kernels = 0;
   bool ainv_valid = false;

@@ -109,29 +109,25 @@ int build_schedule(ouranos_rt* rt) {
   const size_t ex = (size_t)rt->n_dir * tiles * NS * rt->wy * rt->fd;
   const size_t ey = dim == 3 ? (size_t)rt->n_dir * tiles * NS * rt->wx * rt->fd : 1;
   const size_t esz = rt->precision == OURANOS_FP64 ? 8 : 4;
-  CU(rt->d_edge_x.alloc(ex * 8 > 0 ? ex * 8 : 16), "edge buffer x");
-  CU(rt->d_edge_y.alloc(ey * 8 > 0 ? ey * 8 : 16), "edge buffer y");
+  // two 64-bit tagged words per value cover both precisions
+  CU(rt->d_edge_x.alloc(ex * 16 > 0 ? ex * 16 : 16), "edge buffer x");
+  CU(rt->d_edge_y.alloc(ey * 16 > 0 ? ey * 16 : 16), "edge buffer y");
+  CU(cudaMemsetAsync(rt->d_edge_x.p, 0, rt->d_edge_x.bytes, rt->stream), "edge buffer x");
+  CU(cudaMemsetAsync(rt->d_edge_y.p, 0, rt->d_edge_y.bytes, rt->stream), "edge buffer y");
   (void)esz;
   return OURANOS_OK;
 }
 
 int default_tiling(ouranos_rt* rt) {
-  // directions per octant
-  const int per_oct = rt->n_dir / (rt->dim == 3 ? 8 : 4);
-  int kd = rt->dim == 3 ? 2 : 4;
-  while (kd > 1 && per_oct > 0 && per_oct < kd) kd >>= 1;
-  rt->kd = kd;
+  // one direction per warp: every lane of a warp reads the same inverse table
+  // (broadcast loads); 32 cells per warp (2-D: 32 x 1, 3-D: 8 x 4)
+  rt->kd = 1;
   if (rt->dim == 2) {
-    rt->wx = 32 / kd;
+    rt->wx = 32;
     rt->wy = 1;
   } else {
-    const int wc = 32 / kd;  // 16 -> 4x4, 32 -> 8x4, 8 -> 4x2
-    rt->wx = wc >= 16 ? 4 : (wc == 8 ? 4 : 2);
-    rt->wy = wc / rt->wx;
-    if (wc == 32) {
-      rt->wx = 8;
-      rt->wy = 4;
-    }
+    rt->wx = 8;
+    rt->wy = 4;
   }
   return OURANOS_OK;
 }
@@ -241,12 +237,15 @@ int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd,
   a.bnd = bnd;
   CU(rt->d_psi.alloc(sizeof(real) * len_dir), "angular flux");
   a.psi = rt->d_psi.as<real>();
-  a.edge_x = rt->d_edge_x.as<real>();
-  a.edge_y = rt->d_edge_y.as<real>();
+  a.edge_x = rt->d_edge_x.as<unsigned long long>();
+  a.edge_y = rt->d_edge_y.as<unsigned long long>();
+  // epochs cycle through [1, 0x7fff]; every sweep rewrites every edge word it
+  // reads, so a stale word carries the previous epoch and never matches
+  rt->epoch = rt->epoch % 0x7fffu + 1u;
+  a.epoch = rt->epoch;
   int* ctrl = rt->d_ctrl.as<int>();
   a.ticket = ctrl;
   a.status = ctrl + 1;
-  a.progress = ctrl + 64;
   a.wait_limit_ns = rt->wait_limit_ns;
   a.wait_bias = rt->wait_bias;
   int kernels = 0;
@@ -260,13 +259,11 @@ int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd,
     kernels += (rt->n_mom + 15) / 16;
     a.q = rt->d_q.as<real>();
   }
-  const size_t ctrl_bytes = sizeof(int) * (64 + (size_t)rt->n_groups_dir * rt->tiles_x * rt->tiles_y);
-  // ticket + progress -> 0.  The status word [1] is sticky: it is cleared at the
-  // start of each C-ABI call (clear_status), so a timeout inside a solve is seen
-  // at its end and every later sweep of that call exits at once.  The dot
-  // counter at [2] is 0 whenever no dot kernel is in flight on this stream.
+  // ticket -> 0.  The status word [1] is sticky: it is cleared at the start of
+  // each C-ABI call (clear_status), so a timeout inside a solve is seen at its
+  // end and every later sweep of that call exits at once.  The dot counter at
+  // [2] is 0 whenever no dot kernel is in flight on this stream.
   CU(cudaMemsetAsync(ctrl, 0, sizeof(int), rt->stream), "reset sweep control");
-  CU(cudaMemsetAsync(ctrl + 64, 0, ctrl_bytes - 64 * sizeof(int), rt->stream), "reset progress");
   int sms = 0;
   CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, rt->device), "device query");
   const int block = 128;
@@ -494,6 +491,7 @@ int ouranos_rt_create(const ouranos_problem_desc* D, int device, ouranos_rt** ou
     }
     rt->n_cells *= rt->nx[a];
   }
+  if (rt->nx[rt->dim - 1] > 0xffff) return fail(bad(rt, "at most 65535 cells along the sweep axis"));
   rt->fe = build_fe_tables(rt->dim, rt->p, rt->h);
   rt->n = rt->fe.n;
   rt->fd = rt->fe.fd;

@@ -20,10 +20,14 @@
 // the warp).  Upwind face values arrive
 //   - along S: from the lane's own previous step (registers),
 //   - along x/y inside the tile: from lane-1 / lane-wx by warp shuffle,
-//   - across tiles: from an HBM edge buffer written by the upwind tile's warp,
-//     guarded by a per-(group, tile) progress counter (release store /
-//     acquire load) -- the GPU form of the reference's MPI_Isend/Iprobe of
-//     outflow faces (src/RadiativeTransfer.cc:633-750).
+//   - across tiles: from an HBM edge buffer written by the upwind tile's warp
+//     -- the GPU form of the reference's MPI_Isend/Iprobe of outflow faces
+//     (src/RadiativeTransfer.cc:633-750).  Every edge value travels in a
+//     64-bit word together with a 32-bit tag (sweep epoch, plane); an FP64
+//     value is split into two tagged halves.  The consumer polls the words it
+//     needs until the tags match: single-copy atomicity of aligned 64-bit
+//     accesses makes each word self-validating, so no fence or counter is
+//     needed on the producer side.
 // Tasks are handed out through one atomic ticket in dependency order (tile
 // level first), so a warp only ever waits on tasks that live warps already
 // hold: any grid size is deadlock-free.  Every wait is bounded (iteration cap
@@ -33,8 +37,9 @@
 // the expansion kernel, or sum_m M2D(d,m) T_m[cell] + isotropic source for one
 // or two moments) + |Omega_a| F_a psi_up,a over the inflow faces; x = A'^-1 b;
 // the outflow faces are the c_a = p entries of x; x is stored as psi_d[cell].
-// The next step's source values are loaded one step ahead, so their memory
-// latency overlaps the current solve.  The moments phi = D2M psi are formed
+// The source values of the next kPrefetch planes stream into a per-warp
+// shared-memory ring with cp.async, so their memory latency overlaps the
+// solves of the planes before them.  The moments phi = D2M psi are formed
 // afterwards by the reduction kernel over the direction axis (no atomics: the
 // sweep is deterministic).
 #pragma once
@@ -57,23 +62,87 @@ __device__ __forceinline__ long long global_ns() {
   return t;
 }
 
-// Wait until *flag >= target.  Returns false when the wait ran out (and then
-// records status 1) or when another warp has already recorded an error.
-static __device__ __forceinline__ bool wait_at_least(const int* flag, int target, int* status,
-                                                     long long limit_ns) {
-  if (ld_acquire_gpu(flag) >= target) return true;
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Tagged edge words: value bits in the low half, tag in the high half.
+template <typename real>
+struct Tagged;
+template <>
+struct Tagged<float> {
+  static constexpr int W = 1;  // 64-bit words per value
+  static __device__ __forceinline__ void put(unsigned long long* w, float v, unsigned tag) {
+    st_relaxed_u64(w, ((unsigned long long)tag << 32) | __float_as_uint(v));
+  }
+  static __device__ __forceinline__ bool get(const unsigned long long* w, unsigned tag, float& v) {
+    const unsigned long long a = ld_relaxed_u64(w);
+    v = __uint_as_float((unsigned)a);
+    return (unsigned)(a >> 32) == tag;
+  }
+};
+template <>
+struct Tagged<double> {
+  static constexpr int W = 2;
+  static __device__ __forceinline__ void put(unsigned long long* w, double v, unsigned tag) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    st_relaxed_u64(w, ((unsigned long long)tag << 32) | (b & 0xffffffffull));
+    st_relaxed_u64(w + 1, ((unsigned long long)tag << 32) | (b >> 32));
+  }
+  static __device__ __forceinline__ bool get(const unsigned long long* w, unsigned tag, double& v) {
+    const unsigned long long lo = ld_relaxed_u64(w), hi = ld_relaxed_u64(w + 1);
+    v = __longlong_as_double((long long)((hi << 32) | (lo & 0xffffffffull)));
+    return (unsigned)(lo >> 32) == tag && (unsigned)(hi >> 32) == tag;
+  }
+};
+
+// Read FD tagged values; poll until every tag matches.  Returns false when the
+// wait ran out (and then records status 1) or when another warp has already
+// recorded an error.
+template <typename real, int FD>
+static __device__ __forceinline__ bool fetch_edge(const unsigned long long* w, unsigned tag,
+                                                  real* out, int* status, long long limit_ns) {
+  constexpr int W = Tagged<real>::W;
+  bool ok = true;
+#pragma unroll
+  for (int t = 0; t < FD; ++t) ok &= Tagged<real>::get(w + t * W, tag, out[t]);
+  if (ok) return true;
   const long long t0 = global_ns();
-  unsigned sleep_ns = 32;
+  unsigned sleep_ns = 16;
   for (unsigned it = 0; it < (1u << 26); ++it) {
-    if (ld_acquire_gpu(flag) >= target) return true;
+    __nanosleep(sleep_ns);
+    if (sleep_ns < 256) sleep_ns <<= 1;
+    ok = true;
+#pragma unroll
+    for (int t = 0; t < FD; ++t) ok &= Tagged<real>::get(w + t * W, tag, out[t]);
+    if (ok) return true;
     if (*(volatile int*)status) return false;
     if (global_ns() - t0 > limit_ns) break;
-    __nanosleep(sleep_ns);
-    if (sleep_ns < 512) sleep_ns <<= 1;
   }
   atomicCAS(status, 0, 1);
   return false;
 }
+
+// cp.async of one 4- or 8-byte element into shared memory
+template <typename real>
+__device__ __forceinline__ void cp_async_elem(real* smem_dst, const real* gsrc) {
+  const unsigned dst = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(dst), "l"(gsrc), "n"(sizeof(real))
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// planes prefetched ahead of the one being solved; the ring has one more slot
+// so the slot being refilled was consumed a step earlier
+constexpr int kPrefetch = 3;
+constexpr int kRing = kPrefetch + 1;
 
 template <int DIM, int P1>
 struct Cell {
@@ -95,13 +164,27 @@ struct Cell {
   static __device__ __forceinline__ constexpr int s_out(int t) { return t + N - PN; }
 };
 
+template <typename real, int FM, int N>
+struct Stream {
+  // values streamed per plane and lane: the expanded source (FM = 0) or FM
+  // moments plus the isotropic source
+  static constexpr int NV = FM == 0 ? N : (FM + 1) * N;
+  static constexpr size_t warp_bytes = (size_t)kRing * 32 * (NV * sizeof(real) + sizeof(int));
+};
+
 template <typename real, int DIM, int P1, int FM>
 __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
   using C = Cell<DIM, P1>;
   constexpr int N = C::N;
   constexpr int FD = C::FD;
+  constexpr int NV = Stream<real, FM, N>::NV;
+  constexpr int W = Tagged<real>::W;
   constexpr unsigned FULL = 0xffffffffu;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  real* ring = reinterpret_cast<real*>(smem_raw + warp * Stream<real, FM, N>::warp_bytes);
+  int* cring = reinterpret_cast<int*>(ring + kRing * 32 * NV);
   const int wc = a.wx * a.wy;
   const int kslot = lane / wc;
   const int cl = lane - kslot * wc;
@@ -113,6 +196,7 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
   const int NY = DIM == 3 ? a.ny : 1;
   const int nsteps = NS + (a.wx - 1) + (a.wy - 1);
   constexpr int AS = DIM - 1;  // physical axis of the sweep direction
+  const unsigned want_epoch = a.epoch ^ (a.wait_bias ? 0x8000u : 0u);
 
   for (;;) {
     int task = 0, stop = 0;
@@ -149,6 +233,9 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
     if (flip & 1) { base += (P1 - 1); st0 = -1; }
     if (flip & 2) { base += (P1 - 1) * P1; st1 = -P1; }
     if (DIM == 3 && (flip & 4)) { base += (P1 - 1) * P1 * P1; st2 = -P1 * P1; }
+    auto off = [&](int i) {
+      return C::comp(i, 0) * st0 + C::comp(i, 1) * st1 + (DIM == 3 ? C::comp(i, 2) * st2 : 0);
+    };
 
     const int xc = tx * a.wx + lx;  // canonical transverse coordinates
     const int yc = ty * a.wy + ly;
@@ -160,38 +247,39 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
     const long plane = DIM == 2 ? (long)NX : (long)NX * NY;  // cells per sweep-axis layer
     auto cell_of = [&](int sc) { return colbase + plane * (sflip ? NS - 1 - sc : sc); };
     const size_t dirbase = (size_t)dd * a.n_dofs;
+    const bool pub_x = tx + 1 < a.tiles_x && lx == a.wx - 1;
+    const bool pub_y = DIM == 3 && ty + 1 < a.tiles_y && ly == a.wy - 1;
 
-    const int* prog_x = a.progress + grp * tiles + tile - 1;
-    const int* prog_y = a.progress + grp * tiles + tile - a.tiles_x;
-    int* prog_self = a.progress + grp * tiles + tile;
-    const bool pub_x = tx + 1 < a.tiles_x;
-    const bool pub_y = DIM == 3 && ty + 1 < a.tiles_y;
-    const bool publish = pub_x || pub_y;
-
-    // source values of the lane's next cell, loaded one step ahead
-    real nq[N], nt1[FM >= 2 ? N : 1], niso[FM >= 1 ? N : 1];
-    int ncls = 0;
-    auto load_next = [&](int sc) {
-      const long cb = cell_of(sc) * N + base;
-      ncls = __ldg(a.cell_class + cell_of(sc));
-      if (FM == 0) {
-        const real* Q = a.q + dirbase + cb;
+    // stream the source of plane pl into ring slot pl % kRing (one cp.async group per plane)
+    auto issue = [&](int pl) {
+      if (col_ok && pl < NS) {
+        real* v = ring + ((pl % kRing) * 32 + lane) * NV;
+        const long cell = cell_of(pl);
+        const long cb = cell * N + base;
+        const unsigned cdst = (unsigned)__cvta_generic_to_shared(cring + (pl % kRing) * 32 + lane);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(cdst), "l"(a.cell_class + cell)
+                     : "memory");
+        if (FM == 0) {
+          const real* Q = a.q + dirbase + cb;
 #pragma unroll
-        for (int i = 0; i < N; ++i)
-          nq[i] = __ldg(Q + C::comp(i, 0) * st0 + C::comp(i, 1) * st1 + (DIM == 3 ? C::comp(i, 2) * st2 : 0));
-      } else {
-        const real* T = a.src + cb;
+          for (int i = 0; i < N; ++i) cp_async_elem(v + i, Q + off(i));
+        } else {
+          const real* T = a.src + cb;
 #pragma unroll
-        for (int i = 0; i < N; ++i) {
-          const int off = C::comp(i, 0) * st0 + C::comp(i, 1) * st1 + (DIM == 3 ? C::comp(i, 2) * st2 : 0);
-          nq[i] = __ldg(T + off);
-          if (FM >= 2) nt1[i] = __ldg(T + a.n_dofs + off);
-          if (FM >= 1) niso[i] = a.iso ? __ldg(a.iso + cb + off) : real(0);
+          for (int i = 0; i < N; ++i) {
+            cp_async_elem(v + i, T + off(i));
+            if (FM >= 2) cp_async_elem(v + N + i, T + a.n_dofs + off(i));
+            if (a.iso)
+              cp_async_elem(v + FM * N + i, a.iso + cb + off(i));
+            else
+              v[FM * N + i] = real(0);
+          }
         }
       }
+      cp_async_commit();
     };
-    // the lane's first active step is s = lx + ly (plane 0)
-    if (col_ok) load_next(0);
+#pragma unroll
+    for (int pl = 0; pl < kPrefetch; ++pl) issue(pl);
 
     real psiS[FD], psiX[FD], psiY[FD];
 #pragma unroll
@@ -201,35 +289,28 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
       const int sc = s - lx - ly;
       const bool act = col_ok && sc >= 0 && sc < NS;
 
-      // ---- upwind face values.  Edge-buffer waits run first (divergent), the
+      // ---- upwind face values.  Edge-buffer polls run first (divergent), the
       // shuffles after them (converged), and the boundary / edge / neighbour
       // choice is a branch-free select.
       real eX[FD], eY[FD];
 #pragma unroll
       for (int t = 0; t < FD; ++t) eX[t] = eY[t] = real(0);
       bool failed = false;
-      const bool need_x = act && lx == 0 && tx > 0;
-      const bool need_y = DIM == 3 && act && ly == 0 && ty > 0;
-      if (need_x) {
-        if (wait_at_least(prog_x, sc + a.wx + ly + a.wait_bias, a.status, a.wait_limit_ns)) {
-          const real* e = a.edge_x + ((((size_t)d * tiles + tile - 1) * NS + sc) * a.wy + ly) * FD;
-#pragma unroll
-          for (int t = 0; t < FD; ++t) eX[t] = e[t];
-        } else {
-          failed = true;
-        }
+      const unsigned tag = (want_epoch << 16) | ((unsigned)sc & 0xffffu);
+      if (act && lx == 0 && tx > 0) {
+        const unsigned long long* e =
+            a.edge_x + ((((size_t)d * tiles + tile - 1) * NS + sc) * a.wy + ly) * (FD * W);
+        failed |= !fetch_edge<real, FD>(e, tag, eX, a.status, a.wait_limit_ns);
       }
-      if (need_y) {
-        if (wait_at_least(prog_y, sc + lx + a.wy + a.wait_bias, a.status, a.wait_limit_ns)) {
-          const real* e =
-              a.edge_y + ((((size_t)d * tiles + tile - a.tiles_x) * NS + sc) * a.wx + lx) * FD;
-#pragma unroll
-          for (int t = 0; t < FD; ++t) eY[t] = e[t];
-        } else {
-          failed = true;
-        }
+      if (DIM == 3 && act && ly == 0 && ty > 0) {
+        const unsigned long long* e =
+            a.edge_y + ((((size_t)d * tiles + tile - a.tiles_x) * NS + sc) * a.wx + lx) * (FD * W);
+        failed |= !fetch_edge<real, FD>(e, tag, eY, a.status, a.wait_limit_ns);
       }
-      if (__any_sync(FULL, failed)) break;  // status is set; every warp drains
+      if (__any_sync(FULL, failed)) {  // status is set; drain own copies, leave
+        cp_async_wait<0>();
+        break;
+      }
       const bool x_edge = lx == 0;
       const bool y_edge = ly == 0;
       real upX[FD], upY[FD], upS[FD];
@@ -245,18 +326,17 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
       }
 
       if (act) {
-        const long cell = cell_of(sc);
-        const long cbase = cell * N + base;
-        const int cls = ncls;
+        cp_async_wait<kPrefetch - 1>();  // plane sc has landed
+        const real* v = ring + ((sc % kRing) * 32 + lane) * NV;
+        const int cls = cring[(sc % kRing) * 32 + lane];
         real b[N];
 #pragma unroll
         for (int i = 0; i < N; ++i) {
-          if (FM == 0) b[i] = nq[i];
-          else if (FM == 1) b[i] = w0 * nq[i] + niso[i];
-          else b[i] = w0 * nq[i] + w1 * nt1[i] + niso[i];
+          if (FM == 0) b[i] = v[i];
+          else if (FM == 1) b[i] = w0 * v[i] + v[N + i];
+          else b[i] = w0 * v[i] + w1 * v[N + i] + v[2 * N + i];
         }
-        // prefetch the next plane's source while this one is solved
-        if (sc + 1 < NS) load_next(sc + 1);
+        issue(sc + kPrefetch);  // refills the slot consumed one step ago
         // inflow faces: b_face += |Omega_a| F_a psi_up
         const real* FX = a.face_mass + 0 * FD * FD;
         const real* FS = a.face_mass + AS * FD * FD;
@@ -291,48 +371,56 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
           for (int j = 0; j < N; ++j) acc += __ldg(Ai + i * N + j) * b[j];
           x[i] = acc;
         }
-        real* P = a.psi + dirbase + cbase;
-#pragma unroll
-        for (int i = 0; i < N; ++i)
-          P[C::comp(i, 0) * st0 + C::comp(i, 1) * st1 + (DIM == 3 ? C::comp(i, 2) * st2 : 0)] = x[i];
 #pragma unroll
         for (int t = 0; t < FD; ++t) {
           psiX[t] = x[C::x_out(t)];
           psiS[t] = x[C::s_out(t)];
           if (DIM == 3) psiY[t] = x[C::y_out(t)];
         }
-        if (lx == a.wx - 1 && pub_x) {
-          real* e = a.edge_x + ((((size_t)d * tiles + tile) * NS + sc) * a.wy + ly) * FD;
+        // edge values first, so the downwind tile can start; then the angular flux
+        const unsigned ptag = (a.epoch << 16) | ((unsigned)sc & 0xffffu);
+        if (pub_x) {
+          unsigned long long* e =
+              a.edge_x + ((((size_t)d * tiles + tile) * NS + sc) * a.wy + ly) * (FD * W);
 #pragma unroll
-          for (int t = 0; t < FD; ++t) e[t] = psiX[t];
+          for (int t = 0; t < FD; ++t) Tagged<real>::put(e + t * W, psiX[t], ptag);
         }
-        if (DIM == 3 && ly == a.wy - 1 && pub_y) {
-          real* e = a.edge_y + ((((size_t)d * tiles + tile) * NS + sc) * a.wx + lx) * FD;
+        if (pub_y) {
+          unsigned long long* e =
+              a.edge_y + ((((size_t)d * tiles + tile) * NS + sc) * a.wx + lx) * (FD * W);
 #pragma unroll
-          for (int t = 0; t < FD; ++t) e[t] = psiY[t];
+          for (int t = 0; t < FD; ++t) Tagged<real>::put(e + t * W, psiY[t], ptag);
         }
-      }
-      if (publish) {
-        __threadfence();
-        __syncwarp();
-        if (lane == 0) st_release_gpu(prog_self, s + 1);
+        real* P = a.psi + dirbase + cell_of(sc) * N + base;
+#pragma unroll
+        for (int i = 0; i < N; ++i) P[off(i)] = x[i];
       }
     }
   }
 }
 
+template <typename real, int DIM, int P1, int FM>
+cudaError_t launch_sweep_fm(const SweepArgs<real>& a, int grid, int block, cudaStream_t s) {
+  constexpr int N = Cell<DIM, P1>::N;
+  const size_t smem = (size_t)(block / 32) * Stream<real, FM, N>::warp_bytes;
+  static bool configured = false;  // opt in to > 48 KB once per instantiation
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(sweep_kernel<real, DIM, P1, FM>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  sweep_kernel<real, DIM, P1, FM><<<grid, block, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
 template <typename real, int DIM, int P1>
 cudaError_t launch_sweep_impl(int fm, const SweepArgs<real>& a, int grid, int block,
                               cudaStream_t s) {
-  if (fm == 0)
-    sweep_kernel<real, DIM, P1, 0><<<grid, block, 0, s>>>(a);
-  else if (fm == 1)
-    sweep_kernel<real, DIM, P1, 1><<<grid, block, 0, s>>>(a);
-  else if (fm == 2)
-    sweep_kernel<real, DIM, P1, 2><<<grid, block, 0, s>>>(a);
-  else
-    return cudaErrorInvalidValue;
-  return cudaGetLastError();
+  if (fm == 0) return launch_sweep_fm<real, DIM, P1, 0>(a, grid, block, s);
+  if (fm == 1) return launch_sweep_fm<real, DIM, P1, 1>(a, grid, block, s);
+  if (fm == 2) return launch_sweep_fm<real, DIM, P1, 2>(a, grid, block, s);
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace ouranos
