@@ -169,6 +169,21 @@ int ouranos_rt_set_wait_limit(ouranos_rt* rt, double ns);
  * so the timeout path can be exercised without faulting the GPU. */
 int ouranos_rt_debug_wait_bias(ouranos_rt* rt, int extra);
 
+/* Apply, y = x - D L^-1 M2D S x, that allocates no device memory during the
+ * call.  No counterpart in the reference.  For callers that cannot allocate
+ * device memory when they apply the operator -- a solver framework that owns
+ * the device memory pool and forbids allocations inside its operator
+ * callbacks, or a driver that allows allocations only at set-up.  Every
+ * scratch buffer of the Apply lives in one file-scope device array of
+ * OURANOS_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * the process exits; problems needing more scratch are rejected with
+ * OURANOS_ERR_BAD_INPUT.  x and y must be device pointers.  The first call on a
+ * device looks up the array's address (cudaGetSymbolAddress): make it before
+ * any stream capture.  All calls share the array, so calls whose GPU work
+ * overlaps (two streams, threads or handles) race. */
+#define OURANOS_NOALLOC_SCRATCH_BYTES (32u << 20)
+int ouranos_rt_apply_noalloc(ouranos_rt* rt, const double* x, double* y);
+
 /* ------------------------------------------------------------------- solvers */
 /* Drivers of src/ouranos.cc:43-209, on device vectors.
  * OURANOS_SOLVER_SI: source iteration, relative-change test (src/ouranos.cc:72-95).

@@ -33,6 +33,7 @@ EXPORTS = [
     "ouranos_rt_set_stream", "ouranos_rt_last_error",
     "ouranos_rt_last_sweep_ms", "ouranos_rt_set_tiling", "ouranos_rt_get_tiling",
     "ouranos_rt_set_wait_limit", "ouranos_rt_debug_wait_bias", "ouranos_solve",
+    "ouranos_rt_apply_noalloc",
 ]
 
 
@@ -98,6 +99,7 @@ def lib():
         "ouranos_rt_set_wait_limit": [vp, d],
         "ouranos_rt_debug_wait_bias": [vp, i],
         "ouranos_solve": [vp, i, i, i, d, vp, vp, vp, C.POINTER(SolveInfo)],
+        "ouranos_rt_apply_noalloc": [vp, vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
