@@ -307,6 +307,35 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_solve(args):
+    """Time to a 1e-8 relative residual on the 3-D thick diffusive workload
+    (64^3 hexes, DG Q1, GLC S12 = 168 directions, 4^3-cell blocks of
+    (sigma_t, c) = (100, 0.999) or (1, 0.9)): plain FP64 GMRES(30) against
+    FGMRES(30) with FP32 sweeps and FP64 refinement.  Reports wall time,
+    iterations, the FP64 true residual and the scalar-flux error of the mixed
+    solve against the FP64 solve."""
+    import numpy as np
+    import ouranos_gb300 as og
+    n = args.solve_n
+    prob = og.thick_3d(seed=2000, n=n, sn=12)
+    out = {"workload": "3d-thick-%d^3-dgq1-glc12" % n, "tol": args.tol}
+    with og.RadiativeTransfer(prob) as rt:
+        res = {}
+        for method in args.methods.split(","):
+            x, info, hist = rt.solve(method, tol=args.tol, max_it=args.max_it, restart=30)
+            res[method] = (x, info)
+            out[method] = {k: info[k] for k in ("iterations", "restarts", "residual", "seconds",
+                                                "converged")}
+        if "gmres" in res:
+            ref = res["gmres"][0]
+            for m, (x, info) in res.items():
+                if m != "gmres":
+                    out[m]["flux_rel_l2_vs_fp64"] = float(np.linalg.norm(x - ref) / np.linalg.norm(ref))
+                    out[m]["flux_max_abs_vs_fp64"] = float(np.abs(x - ref).max())
+                    out[m]["speedup_vs_fp64_gmres"] = res["gmres"][1]["seconds"] / info["seconds"]
+    print(json.dumps({"solve": out}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -316,7 +345,17 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-reps", type=int, default=2)
+    ap.add_argument("--solve", action="store_true", help="time-to-solution mode")
+    ap.add_argument("--solve-n", type=int, default=64)
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--max-it", type=int, default=3000)
+    ap.add_argument("--methods", default="gmres,fgmres_mixed")
     args = ap.parse_args()
+    if args.solve:
+        import __graft_entry__
+        __graft_entry__.build()
+        run_solve(args)
+        return
     if args.impl == "reference":
         import importlib.util
         spec = importlib.util.spec_from_file_location("_ob", os.path.join(ROOT, "oracle", "build.py"))
