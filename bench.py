@@ -317,11 +317,21 @@ def run_solve(args):
     import numpy as np
     import ouranos_gb300 as og
     n = args.solve_n
-    prob = og.thick_3d(seed=2000, n=n, sn=12)
+    prob = og.thick_3d(seed=args.solve_seed, n=n, sn=12)
     out = {"workload": "3d-thick-%d^3-dgq1-glc12" % n, "tol": args.tol}
     with og.RadiativeTransfer(prob) as rt:
         res = {}
-        for method in args.methods.split(","):
+        methods = args.methods.split(",")
+        if "fgmres_learned" in methods:
+            from ouranos_gb300.learned import Network, install
+            wpath = os.path.join(ROOT, "ouranos_gb300", "weights", "precond_thick3d.npz")
+            if os.path.exists(wpath):
+                install(rt, Network.load(wpath, (n, n, n)))
+                out["learned_weights"] = os.path.relpath(wpath, ROOT)
+            else:
+                methods.remove("fgmres_learned")
+                out["learned_weights"] = None
+        for method in methods:
             x, info, hist = rt.solve(method, tol=args.tol, max_it=args.max_it, restart=30)
             res[method] = (x, info)
             out[method] = {k: info[k] for k in ("iterations", "restarts", "residual", "seconds",
@@ -347,9 +357,10 @@ def main():
     ap.add_argument("--cpu-reps", type=int, default=2)
     ap.add_argument("--solve", action="store_true", help="time-to-solution mode")
     ap.add_argument("--solve-n", type=int, default=64)
+    ap.add_argument("--solve-seed", type=int, default=7000, help="evaluation map (training uses 2000+)")
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--max-it", type=int, default=3000)
-    ap.add_argument("--methods", default="gmres,fgmres_mixed")
+    ap.add_argument("--methods", default="gmres,fgmres_mixed,fgmres_learned")
     args = ap.parse_args()
     if args.solve:
         import __graft_entry__

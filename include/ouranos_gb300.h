@@ -59,6 +59,11 @@ extern "C" {
 /* Arithmetic of the sweep. */
 #define OURANOS_FP64 0
 #define OURANOS_FP32 1
+/* How the FP64 path evaluates its moment <-> direction contractions: native
+ * FP64 instructions, or double-float pairs on the FP32 pipes (about 48
+ * significant bits, FP32 exponent range; the default). */
+#define OURANOS_FP64_NATIVE 0
+#define OURANOS_FP64_DF64 1
 
 /* Problem description: the data the reference spreads over Parameters,
  * Geometry, RTQuadrature and RTMaterialProperties (src/*.hh), restricted to a
@@ -119,6 +124,9 @@ int ouranos_rt_set_group(ouranos_rt* rt, int group);
 /* Sweep arithmetic: OURANOS_FP64 (default, parity path) or OURANOS_FP32. No
  * reference counterpart (the reference is FP64 only). */
 int ouranos_rt_set_precision(ouranos_rt* rt, int precision);
+/* Select OURANOS_FP64_NATIVE or OURANOS_FP64_DF64 for the FP64 path's moment
+ * contractions.  No reference counterpart. */
+int ouranos_rt_set_fp64_contractions(ouranos_rt* rt, int mode);
 /* Length of a flux-moment vector, n_mom * n_dofs: the size of the Epetra_Map
  * returned by OperatorDomainMap/OperatorRangeMap (src/RadiativeTransfer.hh:240-249). */
 int ouranos_rt_vector_length(const ouranos_rt* rt, long* length);
@@ -195,6 +203,10 @@ int ouranos_rt_apply_noalloc(ouranos_rt* rt, const double* x, double* y);
 #define OURANOS_SOLVER_GMRES 1
 #define OURANOS_SOLVER_BICGSTAB 2
 #define OURANOS_SOLVER_FGMRES_MIXED 3
+/* FGMRES_MIXED with the learned right preconditioner installed by
+ * ouranos_rt_set_preconditioner; falls back to the plain method for the rest of
+ * the solve when a preconditioned restart cycle stagnates. */
+#define OURANOS_SOLVER_FGMRES_LEARNED 4
 
 typedef struct ouranos_solve_info {
   int iterations;           /* operator applications in the Krylov/SI loop */
@@ -209,6 +221,39 @@ typedef struct ouranos_solve_info {
  * receives max_it+1 relative residuals. */
 int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it, double tol,
                   const double* group_flux, double* x, double* hist, ouranos_solve_info* info);
+
+/* ------------------------------------------------- learned preconditioner
+ * No counterpart in the reference (its Krylov solves use an identity
+ * preconditioner, src/ouranos.cc:160-171).  A 3-D convolutional network on the
+ * cell grid maps (residual scalar-flux cell averages, log sigma_t, scattering
+ * ratio) to a scalar-flux correction -- a learned synthetic acceleration used
+ * as the right preconditioner of FGMRES.  Grid sides must be multiples of 4. */
+typedef struct ouranos_cnn ouranos_cnn;
+int ouranos_cnn_create(int nx, int ny, int nz, unsigned long long seed, ouranos_cnn** out);
+int ouranos_cnn_destroy(ouranos_cnn* net);
+int ouranos_cnn_n_params(const ouranos_cnn* net, long* n);
+int ouranos_cnn_get_params(const ouranos_cnn* net, float* host);
+int ouranos_cnn_set_params(ouranos_cnn* net, const float* host);
+/* features: device [cells][3] FP32; out: device [cells] FP32 */
+int ouranos_cnn_forward(ouranos_cnn* net, const float* features, float* out);
+/* MSE loss of forward(features) against target ([cells], device); gradients of
+ * all parameters to grads_host (may be NULL), no update */
+int ouranos_cnn_gradients(ouranos_cnn* net, const float* features, const float* target,
+                          float* grads_host, float* loss);
+/* one Adam step (beta 0.9/0.999) on that loss */
+int ouranos_cnn_train_step(ouranos_cnn* net, const float* features, const float* target, float lr,
+                           float* loss);
+int ouranos_cnn_last_error(const ouranos_cnn* net, char* buf, size_t len);
+/* install (or, with NULL, remove) the network as the handle's preconditioner */
+int ouranos_rt_set_preconditioner(ouranos_rt* rt, ouranos_cnn* net);
+/* network features of a residual v ([mom][dof], device FP64) into features
+ * (device [cells][3]); scale (host, may be NULL) gets the normalisation */
+int ouranos_rt_pc_features(ouranos_rt* rt, const double* v, float* features, double* scale);
+/* training target for the pair (v, e = A^-1 v): cell averages of (e - v) over
+ * the normalisation of v (device [cells]) */
+int ouranos_rt_pc_target(ouranos_rt* rt, const double* v, const double* e, float* target);
+/* z = v + network correction (device vectors) */
+int ouranos_rt_pc_apply(ouranos_rt* rt, const double* v, double* z);
 
 #ifdef __cplusplus
 }

@@ -21,19 +21,24 @@ BC_VACUUM, BC_ISOTROPIC, BC_MOST_NORMAL, BC_REFLECTIVE = 0, 1, 2, 3
 QUAD_LS, QUAD_GLC = 0, 1
 HARM_ORTHONORMAL, HARM_REFERENCE = 0, 1
 FP64, FP32 = 0, 1
-SOLVER_SI, SOLVER_GMRES, SOLVER_BICGSTAB, SOLVER_FGMRES_MIXED = 0, 1, 2, 3
+FP64_NATIVE, FP64_DF64 = 0, 1
+SOLVER_SI, SOLVER_GMRES, SOLVER_BICGSTAB, SOLVER_FGMRES_MIXED, SOLVER_FGMRES_LEARNED = 0, 1, 2, 3, 4
 
 # every symbol include/ouranos_gb300.h declares
 EXPORTS = [
     "ouranos_quadrature_sizes", "ouranos_quadrature_build",
     "ouranos_rt_create", "ouranos_rt_destroy", "ouranos_rt_set_group",
-    "ouranos_rt_set_precision", "ouranos_rt_vector_length", "ouranos_rt_n_tasks",
+    "ouranos_rt_set_precision", "ouranos_rt_set_fp64_contractions", "ouranos_rt_vector_length", "ouranos_rt_n_tasks",
     "ouranos_rt_scattering_source", "ouranos_rt_sweep", "ouranos_rt_apply",
     "ouranos_rt_sweep_rhs", "ouranos_rt_task_levels", "ouranos_wavefront_levels",
     "ouranos_rt_set_stream", "ouranos_rt_last_error",
     "ouranos_rt_last_sweep_ms", "ouranos_rt_set_tiling", "ouranos_rt_get_tiling",
     "ouranos_rt_set_wait_limit", "ouranos_rt_debug_wait_bias", "ouranos_solve",
     "ouranos_rt_apply_noalloc",
+    "ouranos_cnn_create", "ouranos_cnn_destroy", "ouranos_cnn_n_params", "ouranos_cnn_get_params",
+    "ouranos_cnn_set_params", "ouranos_cnn_forward", "ouranos_cnn_gradients",
+    "ouranos_cnn_train_step", "ouranos_cnn_last_error", "ouranos_rt_set_preconditioner",
+    "ouranos_rt_pc_features", "ouranos_rt_pc_target", "ouranos_rt_pc_apply",
 ]
 
 
@@ -83,6 +88,7 @@ def lib():
         "ouranos_rt_destroy": [vp],
         "ouranos_rt_set_group": [vp, i],
         "ouranos_rt_set_precision": [vp, i],
+        "ouranos_rt_set_fp64_contractions": [vp, i],
         "ouranos_rt_vector_length": [vp, C.POINTER(l)],
         "ouranos_rt_n_tasks": [vp, C.POINTER(l)],
         "ouranos_rt_scattering_source": [vp, vp],

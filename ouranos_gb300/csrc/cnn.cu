@@ -1,0 +1,503 @@
+// The learned preconditioner's network: a three-level 3-D U-Net on the cell
+// grid, BF16 activations, FP32 master weights, Adam.  No counterpart in the
+// reference (its Krylov solves are unpreconditioned, src/ouranos.cc:160-171).
+//
+//   level 0 (n^3):   x0(16) -a0-> h_a0(16) -b0-> s0(16)
+//   level 1 (n/2):   pool(s0) -a1-> h_a1(32) -b1-> s1(32)
+//   level 2 (n/4):   pool(s1) -a2-> h_a2(32) -b2-> h_b2(32)
+//   level 1:         up(h_b2)+s1 -c1-> h_c1(32) -d1-> h_d1(16)
+//   level 0:         up(h_d1)+s0 -c0-> h_c0(16) -out-> y (linear, channel 0 used)
+// every conv is 3x3x3 + bias + ReLU except `out`.  Inputs: channel 0 the
+// normalised cell average of the residual's scalar moment, 1 log(sigma_t)/log(100),
+// 2 the scattering ratio; channels 3..15 are zero.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "cnn_kernels.cuh"
+#include "internal.h"
+
+using namespace ouranos;
+using ouranos::cnn::Grid;
+
+namespace {
+
+constexpr int kCin0 = 16;  // padded input channels
+constexpr int kFeatures = 3;
+
+__global__ void features_kernel(const float* feat, int nf, __nv_bfloat16* x0, long V) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < V * kCin0;
+       e += (long)gridDim.x * blockDim.x) {
+    const long v = e / kCin0;
+    const int c = (int)(e % kCin0);
+    x0[e] = __float2bfloat16(c < nf ? feat[v * nf + c] : 0.f);
+  }
+}
+__global__ void relu_mask_kernel(const __nv_bfloat16* act, const __nv_bfloat16* g, __nv_bfloat16* out,
+                                 long n) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+    out[e] = __bfloat162float(act[e]) > 0.f ? g[e] : __float2bfloat16(0.f);
+}
+__global__ void add_kernel(const __nv_bfloat16* a, const __nv_bfloat16* b, __nv_bfloat16* out, long n) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+    out[e] = __float2bfloat16(__bfloat162float(a[e]) + __bfloat162float(b[e]));
+}
+// 2x2x2 average pool (fine -> coarse) and its adjoint
+__global__ void pool_kernel(Grid fine, const __nv_bfloat16* in, __nv_bfloat16* out, int C) {
+  const Grid co{fine.nx / 2, fine.ny / 2, fine.nz / 2};
+  const long n = co.voxels() * C;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    const long v = e / C;
+    const int c = (int)(e % C);
+    const int x = (int)(v % co.nx), y = (int)((v / co.nx) % co.ny), z = (int)(v / ((long)co.nx * co.ny));
+    float s = 0.f;
+    for (int k = 0; k < 8; ++k) {
+      const long fv = (2 * x + (k & 1)) + (long)fine.nx * ((2 * y + ((k >> 1) & 1)) + (long)fine.ny * (2 * z + (k >> 2)));
+      s += __bfloat162float(in[fv * C + c]);
+    }
+    out[e] = __float2bfloat16(0.125f * s);
+  }
+}
+__global__ void pool_bwd_kernel(Grid fine, const __nv_bfloat16* gco, __nv_bfloat16* gfine, int C) {
+  const Grid co{fine.nx / 2, fine.ny / 2, fine.nz / 2};
+  const long n = fine.voxels() * C;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    const long v = e / C;
+    const int c = (int)(e % C);
+    const int x = (int)(v % fine.nx) / 2, y = (int)((v / fine.nx) % fine.ny) / 2,
+              z = (int)(v / ((long)fine.nx * fine.ny)) / 2;
+    gfine[e] = __float2bfloat16(0.125f * __bfloat162float(gco[(x + (long)co.nx * (y + (long)co.ny * z)) * C + c]));
+  }
+}
+// nearest upsample (coarse -> fine) plus a skip tensor on the fine grid
+__global__ void up_add_kernel(Grid fine, const __nv_bfloat16* co_in, const __nv_bfloat16* skip,
+                              __nv_bfloat16* out, int C) {
+  const Grid co{fine.nx / 2, fine.ny / 2, fine.nz / 2};
+  const long n = fine.voxels() * C;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    const long v = e / C;
+    const int c = (int)(e % C);
+    const int x = (int)(v % fine.nx) / 2, y = (int)((v / fine.nx) % fine.ny) / 2,
+              z = (int)(v / ((long)fine.nx * fine.ny)) / 2;
+    out[e] = __float2bfloat16(__bfloat162float(co_in[(x + (long)co.nx * (y + (long)co.ny * z)) * C + c]) +
+                              __bfloat162float(skip[e]));
+  }
+}
+// adjoint of nearest upsample: sum the 8 children
+__global__ void up_bwd_kernel(Grid fine, const __nv_bfloat16* gfine, __nv_bfloat16* gco, int C) {
+  const Grid co{fine.nx / 2, fine.ny / 2, fine.nz / 2};
+  const long n = co.voxels() * C;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    const long v = e / C;
+    const int c = (int)(e % C);
+    const int x = (int)(v % co.nx), y = (int)((v / co.nx) % co.ny), z = (int)(v / ((long)co.nx * co.ny));
+    float s = 0.f;
+    for (int k = 0; k < 8; ++k) {
+      const long fv = (2 * x + (k & 1)) + (long)fine.nx * ((2 * y + ((k >> 1) & 1)) + (long)fine.ny * (2 * z + (k >> 2)));
+      s += __bfloat162float(gfine[fv * C + c]);
+    }
+    gco[e] = __float2bfloat16(s);
+  }
+}
+// mean-squared error on output channel 0 and its gradient (BF16, channel 0 only)
+__global__ void mse_kernel(const float* out, int cout, const float* target, long V,
+                           __nv_bfloat16* grad, float* loss_acc) {
+  float local = 0.f;
+  for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < V; v += (long)gridDim.x * blockDim.x) {
+    const float d = out[v * cout] - target[v];
+    local += d * d;
+    for (int c = 0; c < cout; ++c) grad[v * cout + c] = __float2bfloat16(c == 0 ? 2.f * d / (float)V : 0.f);
+  }
+  for (int o = 16; o; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss_acc, local / (float)V);
+}
+__global__ void adam_kernel(float* w, const float* g, float* m, float* v, long n, float lr, float b1,
+                            float b2, float eps, float c1, float c2) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    const float gg = g[e];
+    m[e] = b1 * m[e] + (1.f - b1) * gg;
+    v[e] = b2 * v[e] + (1.f - b2) * gg * gg;
+    w[e] -= lr * (m[e] / c1) / (sqrtf(v[e] / c2) + eps);
+  }
+}
+// master [tap][cin][cout] -> forward copy [tap][cout][cin] and mirrored-tap copy [26-tap][cin][cout]
+__global__ void weight_copies_kernel(const float* w, int cin, int cout, __nv_bfloat16* fwd,
+                                     __nv_bfloat16* bwd) {
+  const long n = 27L * cin * cout;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    const int tap = (int)(e / ((long)cin * cout));
+    const int ci = (int)((e / cout) % cin), co = (int)(e % cout);
+    const __nv_bfloat16 b = __float2bfloat16(w[e]);
+    fwd[((long)tap * cout + co) * cin + ci] = b;
+    bwd[((long)(26 - tap) * cin + ci) * cout + co] = b;
+  }
+}
+
+inline int blocks_for(long n) {
+  long b = (n + 255) / 256;
+  return (int)(b < 1 ? 1 : (b > 152L * 16 ? 152L * 16 : b));
+}
+
+struct Layer {
+  int cin, cout;
+  bool relu;
+  Grid grid;
+  size_t woff, boff;  // offsets into the parameter arrays
+};
+
+template <int CIN, int COUT, bool RELU>
+cudaError_t conv_fwd_t(const Grid& g, const __nv_bfloat16* in, const __nv_bfloat16* wt,
+                       const float* bias, __nv_bfloat16* ob, float* of, cudaStream_t s) {
+  const long warps = (g.voxels() + 15) / 16;
+  cnn::conv3_fwd<CIN, COUT, RELU><<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(g, in, wt, bias, ob, of);
+  return cudaGetLastError();
+}
+
+cudaError_t conv_fwd(int cin, int cout, bool relu, const Grid& g, const __nv_bfloat16* in,
+                     const __nv_bfloat16* wt, const float* bias, __nv_bfloat16* ob, float* of,
+                     cudaStream_t s) {
+#define CASE(CI, CO)                                                                    \
+  if (cin == CI && cout == CO)                                                          \
+    return relu ? conv_fwd_t<CI, CO, true>(g, in, wt, bias, ob, of, s)                  \
+                : conv_fwd_t<CI, CO, false>(g, in, wt, bias, ob, of, s);
+  CASE(16, 16)
+  CASE(16, 32)
+  CASE(32, 32)
+  CASE(32, 16)
+#undef CASE
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t conv_wgrad(int cin, int cout, const Grid& g, const __nv_bfloat16* in,
+                       const __nv_bfloat16* grad, float* dw, float* db, cudaStream_t s) {
+  const int chunk = 2048;
+  dim3 grid((unsigned)((g.voxels() + chunk - 1) / chunk), 27);
+#define CASE(CI, CO) \
+  if (cin == CI && cout == CO) { cnn::conv3_wgrad<CI, CO><<<grid, 256, 0, s>>>(g, in, grad, dw, db, chunk); return cudaGetLastError(); }
+  CASE(16, 16)
+  CASE(16, 32)
+  CASE(32, 32)
+  CASE(32, 16)
+#undef CASE
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+struct ouranos_cnn {
+  Grid g0, g1, g2;
+  std::vector<Layer> L;  // a0 b0 a1 b1 a2 b2 c1 d1 c0 out
+  size_t n_w = 0, n_b = 0;
+  float *w = nullptr, *b = nullptr, *gw = nullptr, *gb = nullptr;
+  float *mw = nullptr, *vw = nullptr, *mb = nullptr, *vb = nullptr;
+  __nv_bfloat16 *wf = nullptr, *wb = nullptr;  // BF16 forward / mirrored copies (n_w each)
+  // activations and gradient scratch
+  __nv_bfloat16 *x0, *ha0, *s0, *p0, *ha1, *s1, *p1, *ha2, *hb2, *u1, *hc1, *hd1, *u0, *hc0;
+  __nv_bfloat16 *ga, *gb_, *gc, *gskip0, *gskip1, *gout;  // gradients
+  float* out = nullptr;
+  float* dloss = nullptr;
+  long step = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+enum { A0, B0, A1, B1, A2, B2, C1, D1, C0, OUT };
+
+int cnn_fail(ouranos_cnn* n, cudaError_t e, const char* what) {
+  char buf[256];
+  std::snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+  n->err = buf;
+  return OURANOS_ERR_CUDA;
+}
+#define CN(expr, what)                                      \
+  do {                                                      \
+    cudaError_t _e = (expr);                                \
+    if (_e != cudaSuccess) return cnn_fail(net, _e, what);  \
+  } while (0)
+
+template <class T>
+cudaError_t dalloc(ouranos_cnn* net, T** p, size_t count) {
+  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+  if (e == cudaSuccess) {
+    net->allocs.push_back(*p);
+    cudaMemset(*p, 0, sizeof(T) * (count ? count : 1));
+  }
+  return e;
+}
+
+const __nv_bfloat16* wf_of(const ouranos_cnn* n, int l) { return n->wf + n->L[l].woff; }
+const __nv_bfloat16* wb_of(const ouranos_cnn* n, int l) { return n->wb + n->L[l].woff; }
+
+int refresh_copies(ouranos_cnn* net) {
+  for (const Layer& l : net->L)
+    weight_copies_kernel<<<blocks_for(27L * l.cin * l.cout), 256, 0, net->stream>>>(
+        net->w + l.woff, l.cin, l.cout, net->wf + l.woff, net->wb + l.woff);
+  CN(cudaGetLastError(), "weight copies");
+  return OURANOS_OK;
+}
+
+int conv_layer(ouranos_cnn* net, int l, const __nv_bfloat16* in, __nv_bfloat16* ob, float* of) {
+  const Layer& L = net->L[l];
+  CN(conv_fwd(L.cin, L.cout, L.relu, L.grid, in, wf_of(net, l), net->b + L.boff, ob, of, net->stream),
+     "conv forward");
+  return OURANOS_OK;
+}
+
+int forward(ouranos_cnn* net, const float* feat) {
+  cudaStream_t s = net->stream;
+  const long V0 = net->g0.voxels();
+  features_kernel<<<blocks_for(V0 * kCin0), 256, 0, s>>>(feat, kFeatures, net->x0, V0);
+  int rc;
+  if ((rc = conv_layer(net, A0, net->x0, net->ha0, nullptr)) || (rc = conv_layer(net, B0, net->ha0, net->s0, nullptr)))
+    return rc;
+  pool_kernel<<<blocks_for(net->g1.voxels() * 16), 256, 0, s>>>(net->g0, net->s0, net->p0, 16);
+  if ((rc = conv_layer(net, A1, net->p0, net->ha1, nullptr)) || (rc = conv_layer(net, B1, net->ha1, net->s1, nullptr)))
+    return rc;
+  pool_kernel<<<blocks_for(net->g2.voxels() * 32), 256, 0, s>>>(net->g1, net->s1, net->p1, 32);
+  if ((rc = conv_layer(net, A2, net->p1, net->ha2, nullptr)) || (rc = conv_layer(net, B2, net->ha2, net->hb2, nullptr)))
+    return rc;
+  up_add_kernel<<<blocks_for(net->g1.voxels() * 32), 256, 0, s>>>(net->g1, net->hb2, net->s1, net->u1, 32);
+  if ((rc = conv_layer(net, C1, net->u1, net->hc1, nullptr)) || (rc = conv_layer(net, D1, net->hc1, net->hd1, nullptr)))
+    return rc;
+  up_add_kernel<<<blocks_for(V0 * 16), 256, 0, s>>>(net->g0, net->hd1, net->s0, net->u0, 16);
+  if ((rc = conv_layer(net, C0, net->u0, net->hc0, nullptr)) || (rc = conv_layer(net, OUT, net->hc0, nullptr, net->out)))
+    return rc;
+  CN(cudaGetLastError(), "forward");
+  return OURANOS_OK;
+}
+
+// gradient of conv layer l: given the output gradient g_out (already masked by
+// the layer's ReLU), accumulate its weight/bias gradients and, if g_in is not
+// NULL, produce the input gradient
+int conv_backward(ouranos_cnn* net, int l, const __nv_bfloat16* in, const __nv_bfloat16* g_out,
+                  __nv_bfloat16* g_in) {
+  const Layer& L = net->L[l];
+  CN(conv_wgrad(L.cin, L.cout, L.grid, in, g_out, net->gw + L.woff, net->gb + L.boff, net->stream),
+     "weight gradient");
+  if (g_in)
+    CN(conv_fwd(L.cout, L.cin, false, L.grid, g_out, wb_of(net, l), nullptr, g_in, nullptr, net->stream),
+       "data gradient");
+  return OURANOS_OK;
+}
+
+int mask(ouranos_cnn* net, const __nv_bfloat16* act, __nv_bfloat16* g, long n) {
+  relu_mask_kernel<<<blocks_for(n), 256, 0, net->stream>>>(act, g, g, n);
+  CN(cudaGetLastError(), "relu mask");
+  return OURANOS_OK;
+}
+
+int backward(ouranos_cnn* net, const float* target, float* loss_host) {
+  cudaStream_t s = net->stream;
+  const long V0 = net->g0.voxels(), V1 = net->g1.voxels(), V2 = net->g2.voxels();
+  CN(cudaMemsetAsync(net->gw, 0, sizeof(float) * net->n_w, s), "zero grads");
+  CN(cudaMemsetAsync(net->gb, 0, sizeof(float) * net->n_b, s), "zero grads");
+  CN(cudaMemsetAsync(net->dloss, 0, sizeof(float), s), "zero loss");
+  mse_kernel<<<blocks_for(V0), 256, 0, s>>>(net->out, 16, target, V0, net->gout, net->dloss);
+  int rc;
+  __nv_bfloat16 *ga = net->ga, *gb = net->gb_, *gc = net->gc;
+  // out (linear) and c0
+  if ((rc = conv_backward(net, OUT, net->hc0, net->gout, ga))) return rc;      // ga = d hc0
+  if ((rc = mask(net, net->hc0, ga, V0 * 16))) return rc;
+  if ((rc = conv_backward(net, C0, net->u0, ga, gb))) return rc;               // gb = d u0
+  CN(cudaMemcpyAsync(net->gskip0, gb, sizeof(__nv_bfloat16) * V0 * 16, cudaMemcpyDeviceToDevice, s), "skip");
+  up_bwd_kernel<<<blocks_for(V1 * 16), 256, 0, s>>>(net->g0, gb, ga, 16);      // ga = d hd1
+  if ((rc = mask(net, net->hd1, ga, V1 * 16))) return rc;
+  if ((rc = conv_backward(net, D1, net->hc1, ga, gb))) return rc;              // gb = d hc1
+  if ((rc = mask(net, net->hc1, gb, V1 * 32))) return rc;
+  if ((rc = conv_backward(net, C1, net->u1, gb, ga))) return rc;               // ga = d u1
+  CN(cudaMemcpyAsync(net->gskip1, ga, sizeof(__nv_bfloat16) * V1 * 32, cudaMemcpyDeviceToDevice, s), "skip");
+  up_bwd_kernel<<<blocks_for(V2 * 32), 256, 0, s>>>(net->g1, ga, gb, 32);      // gb = d hb2
+  if ((rc = mask(net, net->hb2, gb, V2 * 32))) return rc;
+  if ((rc = conv_backward(net, B2, net->ha2, gb, ga))) return rc;              // ga = d ha2
+  if ((rc = mask(net, net->ha2, ga, V2 * 32))) return rc;
+  if ((rc = conv_backward(net, A2, net->p1, ga, gb))) return rc;               // gb = d p1
+  pool_bwd_kernel<<<blocks_for(V1 * 32), 256, 0, s>>>(net->g1, gb, gc, 32);    // gc = d s1 (pool path)
+  add_kernel<<<blocks_for(V1 * 32), 256, 0, s>>>(gc, net->gskip1, gc, V1 * 32);
+  if ((rc = mask(net, net->s1, gc, V1 * 32))) return rc;
+  if ((rc = conv_backward(net, B1, net->ha1, gc, ga))) return rc;              // ga = d ha1
+  if ((rc = mask(net, net->ha1, ga, V1 * 32))) return rc;
+  if ((rc = conv_backward(net, A1, net->p0, ga, gb))) return rc;               // gb = d p0
+  pool_bwd_kernel<<<blocks_for(V0 * 16), 256, 0, s>>>(net->g0, gb, gc, 16);    // gc = d s0 (pool path)
+  add_kernel<<<blocks_for(V0 * 16), 256, 0, s>>>(gc, net->gskip0, gc, V0 * 16);
+  if ((rc = mask(net, net->s0, gc, V0 * 16))) return rc;
+  if ((rc = conv_backward(net, B0, net->ha0, gc, ga))) return rc;              // ga = d ha0
+  if ((rc = mask(net, net->ha0, ga, V0 * 16))) return rc;
+  if ((rc = conv_backward(net, A0, net->x0, ga, nullptr))) return rc;
+  CN(cudaGetLastError(), "backward");
+  if (loss_host) {
+    CN(cudaMemcpyAsync(loss_host, net->dloss, sizeof(float), cudaMemcpyDeviceToHost, s), "loss");
+    CN(cudaStreamSynchronize(s), "loss");
+  }
+  return OURANOS_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- C-ABI
+extern "C" {
+
+int ouranos_cnn_create(int nx, int ny, int nz, unsigned long long seed, ouranos_cnn** out) {
+  if (!out) return OURANOS_ERR_BAD_INPUT;
+  *out = nullptr;
+  if (nx < 4 || ny < 4 || nz < 4 || nx % 4 || ny % 4 || nz % 4) return OURANOS_ERR_BAD_INPUT;
+  ouranos_cnn* net = new ouranos_cnn();
+  *out = net;
+  net->g0 = {nx, ny, nz};
+  net->g1 = {nx / 2, ny / 2, nz / 2};
+  net->g2 = {nx / 4, ny / 4, nz / 4};
+  struct Spec { int cin, cout; bool relu; int level; };
+  const Spec spec[] = {{16, 16, true, 0}, {16, 16, true, 0}, {16, 32, true, 1}, {32, 32, true, 1},
+                       {32, 32, true, 2}, {32, 32, true, 2}, {32, 32, true, 1}, {32, 16, true, 1},
+                       {16, 16, true, 0}, {16, 16, false, 0}};
+  const Grid grids[3] = {net->g0, net->g1, net->g2};
+  for (const Spec& sp : spec) {
+    Layer l{sp.cin, sp.cout, sp.relu, grids[sp.level], net->n_w, net->n_b};
+    net->n_w += 27L * sp.cin * sp.cout;
+    net->n_b += sp.cout;
+    net->L.push_back(l);
+  }
+  if (cudaStreamCreateWithFlags(&net->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return cnn_fail(net, cudaGetLastError(), "stream");
+  const long V0 = net->g0.voxels(), V1 = net->g1.voxels(), V2 = net->g2.voxels();
+  CN(dalloc(net, &net->w, net->n_w), "params");
+  CN(dalloc(net, &net->b, net->n_b), "params");
+  CN(dalloc(net, &net->gw, net->n_w), "grads");
+  CN(dalloc(net, &net->gb, net->n_b), "grads");
+  CN(dalloc(net, &net->mw, net->n_w), "adam");
+  CN(dalloc(net, &net->vw, net->n_w), "adam");
+  CN(dalloc(net, &net->mb, net->n_b), "adam");
+  CN(dalloc(net, &net->vb, net->n_b), "adam");
+  CN(dalloc(net, &net->wf, net->n_w), "weights");
+  CN(dalloc(net, &net->wb, net->n_w), "weights");
+  __nv_bfloat16** a16[] = {&net->x0, &net->ha0, &net->s0, &net->u0, &net->hc0};
+  for (auto p : a16) CN(dalloc(net, p, V0 * 16), "activations");
+  CN(dalloc(net, &net->p0, V1 * 16), "activations");
+  CN(dalloc(net, &net->hd1, V1 * 16), "activations");
+  __nv_bfloat16** a1[] = {&net->ha1, &net->s1, &net->u1, &net->hc1};
+  for (auto p : a1) CN(dalloc(net, p, V1 * 32), "activations");
+  CN(dalloc(net, &net->p1, V2 * 32), "activations");
+  CN(dalloc(net, &net->ha2, V2 * 32), "activations");
+  CN(dalloc(net, &net->hb2, V2 * 32), "activations");
+  const long gmax = V0 * 16 > V1 * 32 ? V0 * 16 : V1 * 32;
+  CN(dalloc(net, &net->ga, gmax), "gradients");
+  CN(dalloc(net, &net->gb_, gmax), "gradients");
+  CN(dalloc(net, &net->gc, gmax), "gradients");
+  CN(dalloc(net, &net->gskip0, V0 * 16), "gradients");
+  CN(dalloc(net, &net->gskip1, V1 * 32), "gradients");
+  CN(dalloc(net, &net->gout, V0 * 16), "gradients");
+  CN(dalloc(net, &net->out, V0 * 16), "output");
+  CN(dalloc(net, &net->dloss, 1), "loss");
+  // He-normal initialisation from a SplitMix64 stream, Box-Muller
+  std::vector<float> w(net->n_w, 0.f), b(net->n_b, 0.f);
+  unsigned long long st = seed;
+  auto next = [&]() {
+    st += 0x9E3779B97F4A7C15ull;
+    unsigned long long z = st;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return ((z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+  };
+  for (size_t li = 0; li < net->L.size(); ++li) {
+    const Layer& l = net->L[li];
+    const double sd = std::sqrt(2.0 / (27.0 * l.cin)) * (li == OUT ? 0.1 : 1.0);
+    for (long k = 0; k < 27L * l.cin * l.cout; ++k) {
+      const double u1 = next(), u2 = next();
+      w[l.woff + k] = (float)(sd * std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * M_PI * u2));
+    }
+  }
+  CN(cudaMemcpy(net->w, w.data(), sizeof(float) * net->n_w, cudaMemcpyHostToDevice), "params");
+  CN(cudaMemcpy(net->b, b.data(), sizeof(float) * net->n_b, cudaMemcpyHostToDevice), "params");
+  int rc = refresh_copies(net);
+  if (rc) return rc;
+  CN(cudaStreamSynchronize(net->stream), "init");
+  return OURANOS_OK;
+}
+
+int ouranos_cnn_destroy(ouranos_cnn* net) {
+  if (!net) return OURANOS_OK;
+  if (net->stream) cudaStreamSynchronize(net->stream);
+  for (void* p : net->allocs) cudaFree(p);
+  if (net->stream) cudaStreamDestroy(net->stream);
+  delete net;
+  return OURANOS_OK;
+}
+
+int ouranos_cnn_n_params(const ouranos_cnn* net, long* n) {
+  if (!net || !n) return OURANOS_ERR_BAD_INPUT;
+  *n = (long)(net->n_w + net->n_b);
+  return OURANOS_OK;
+}
+
+int ouranos_cnn_get_params(const ouranos_cnn* cnet, float* host) {
+  ouranos_cnn* net = const_cast<ouranos_cnn*>(cnet);
+  if (!net || !host) return OURANOS_ERR_BAD_INPUT;
+  CN(cudaStreamSynchronize(net->stream), "params");
+  CN(cudaMemcpy(host, net->w, sizeof(float) * net->n_w, cudaMemcpyDeviceToHost), "params");
+  CN(cudaMemcpy(host + net->n_w, net->b, sizeof(float) * net->n_b, cudaMemcpyDeviceToHost), "params");
+  return OURANOS_OK;
+}
+
+int ouranos_cnn_set_params(ouranos_cnn* net, const float* host) {
+  if (!net || !host) return OURANOS_ERR_BAD_INPUT;
+  CN(cudaStreamSynchronize(net->stream), "params");
+  CN(cudaMemcpy(net->w, host, sizeof(float) * net->n_w, cudaMemcpyHostToDevice), "params");
+  CN(cudaMemcpy(net->b, host + net->n_w, sizeof(float) * net->n_b, cudaMemcpyHostToDevice), "params");
+  int rc = refresh_copies(net);
+  if (rc) return rc;
+  CN(cudaStreamSynchronize(net->stream), "params");
+  return OURANOS_OK;
+}
+
+// features: device [voxel][3] FP32; out: device [voxel] FP32 (channel 0)
+int ouranos_cnn_forward(ouranos_cnn* net, const float* features, float* out) {
+  if (!net || !features || !out) return OURANOS_ERR_BAD_INPUT;
+  int rc = forward(net, features);
+  if (rc) return rc;
+  CN(cudaMemcpy2DAsync(out, sizeof(float), net->out, 16 * sizeof(float), sizeof(float),
+                       net->g0.voxels(), cudaMemcpyDeviceToDevice, net->stream),
+     "output");
+  CN(cudaStreamSynchronize(net->stream), "forward");
+  return OURANOS_OK;
+}
+
+// loss and gradients without an update; grads_host (may be NULL) receives [n_params]
+int ouranos_cnn_gradients(ouranos_cnn* net, const float* features, const float* target,
+                          float* grads_host, float* loss) {
+  if (!net || !features || !target) return OURANOS_ERR_BAD_INPUT;
+  int rc;
+  if ((rc = forward(net, features)) || (rc = backward(net, target, loss))) return rc;
+  if (grads_host) {
+    CN(cudaStreamSynchronize(net->stream), "grads");
+    CN(cudaMemcpy(grads_host, net->gw, sizeof(float) * net->n_w, cudaMemcpyDeviceToHost), "grads");
+    CN(cudaMemcpy(grads_host + net->n_w, net->gb, sizeof(float) * net->n_b, cudaMemcpyDeviceToHost), "grads");
+  }
+  return OURANOS_OK;
+}
+
+// one Adam step on the MSE loss of (features -> target)
+int ouranos_cnn_train_step(ouranos_cnn* net, const float* features, const float* target, float lr,
+                           float* loss) {
+  if (!net || !features || !target || !(lr > 0)) return OURANOS_ERR_BAD_INPUT;
+  int rc;
+  if ((rc = forward(net, features)) || (rc = backward(net, target, loss))) return rc;
+  ++net->step;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  const float c1 = 1.f - std::pow(b1, (float)net->step), c2 = 1.f - std::pow(b2, (float)net->step);
+  adam_kernel<<<blocks_for(net->n_w), 256, 0, net->stream>>>(net->w, net->gw, net->mw, net->vw, net->n_w, lr, b1, b2, eps, c1, c2);
+  adam_kernel<<<blocks_for(net->n_b), 256, 0, net->stream>>>(net->b, net->gb, net->mb, net->vb, net->n_b, lr, b1, b2, eps, c1, c2);
+  CN(cudaGetLastError(), "adam");
+  return refresh_copies(net);
+}
+
+int ouranos_cnn_last_error(const ouranos_cnn* net, char* buf, size_t len) {
+  if (!net || !buf || !len) return OURANOS_ERR_BAD_INPUT;
+  std::snprintf(buf, len, "%s", net->err.c_str());
+  return OURANOS_OK;
+}
+
+}  // extern "C"

@@ -107,6 +107,11 @@ cudaError_t launch_sweep(int dim, int p1, int fused_moments, const SweepArgs<rea
 template <typename real>
 cudaError_t launch_expand_source(const real* T, const real* iso, const real* m2d, real* q,
                                  int n_dir, int n_mom, long n_dofs, cudaStream_t s);
+// the same two contractions for FP64 data in double-float arithmetic (df64.cuh)
+cudaError_t launch_expand_source_df64(const double* T, const double* iso, const double* m2d,
+                                      double* q, int n_dir, int n_mom, long n_dofs, cudaStream_t s);
+cudaError_t launch_reduce_moments_df64(const double* psi, const double* d2m_t, double* phi,
+                                       int n_dir, int n_mom, long n_dofs, cudaStream_t s);
 // phi[m][e] = sum_d D2M[m][d] psi[d][e]  -- direction -> moment reduction
 template <typename real>
 cudaError_t launch_reduce_moments(const real* psi, const real* d2m_t, real* phi, int n_dir,
@@ -134,7 +139,11 @@ cudaError_t launch_dots(const double* const* xs, const double* y, int k, long le
 
 }  // namespace ouranos
 struct ouranos_rt;
+struct ouranos_cnn;
 namespace ouranos {
+// learned preconditioner glue (precond.cu)
+int rt_pc_features(ouranos_rt* rt, const double* v, float* feat);
+int rt_pc_correct(ouranos_rt* rt, const double* v, const float* y, double* z);
 // Device-side pieces the solvers use (operator.cu).
 int rt_apply_device(ouranos_rt* rt, const double* x, double* y);
 int rt_rhs_device(ouranos_rt* rt, const double* gf, double* rhs);
@@ -163,6 +172,7 @@ struct ouranos_rt {
   std::vector<long> cell_order;
   ouranos::FETables fe;
   int precision = OURANOS_FP64;
+  int fp64_contract = OURANOS_FP64_DF64;  // arithmetic of the FP64 moment contractions
   // schedule
   int wx = 0, wy = 1, kd = 0;          // 0 = not chosen yet
   int tiles_x = 0, tiles_y = 0, n_groups_dir = 0, n_tasks = 0;
@@ -190,4 +200,8 @@ struct ouranos_rt {
   ouranos::DevBuf d_x, d_y, d_gf, d_tmp, d_scatx;  // staging; d_scatx: scattering-source argument
   // solver workspace
   ouranos::DevBuf d_krylov;
+  // learned preconditioner
+  ouranos_cnn* cnn = nullptr;
+  int pc_group = -1;
+  ouranos::DevBuf d_pc_prop, d_pc_wavg, d_pc_work, d_pc_feat;
 };

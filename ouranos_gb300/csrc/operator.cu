@@ -253,9 +253,15 @@ int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd,
   const int fm = (rt->n_mom <= kFusedMomentsMax && rt->n * (rt->n_mom + 1) <= 32) ? rt->n_mom : 0;
   if (fm == 0) {
     CU(rt->d_q.alloc(sizeof(real) * len_dir), "expanded source");
-    CU(launch_expand_source<real>(src, iso, a.m2d, rt->d_q.as<real>(), rt->n_dir, rt->n_mom,
-                                  rt->n_dofs, rt->stream),
-       "source expansion");
+    if (f64 && rt->fp64_contract == OURANOS_FP64_DF64)
+      CU(launch_expand_source_df64((const double*)src, (const double*)iso, (const double*)a.m2d,
+                                   rt->d_q.as<double>(), rt->n_dir, rt->n_mom, rt->n_dofs,
+                                   rt->stream),
+         "source expansion");
+    else
+      CU(launch_expand_source<real>(src, iso, a.m2d, rt->d_q.as<real>(), rt->n_dir, rt->n_mom,
+                                    rt->n_dofs, rt->stream),
+         "source expansion");
     kernels += (rt->n_mom + 15) / 16;
     a.q = rt->d_q.as<real>();
   }
@@ -274,9 +280,14 @@ int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd,
   CU(launch_sweep<real>(rt->dim, rt->p1, fm, a, grid, block, rt->stream), "sweep launch");
   CU(cudaEventRecord(rt->ev1, rt->stream), "event");
   ++kernels;
-  CU(launch_reduce_moments<real>(a.psi, (const real*)(f64 ? rt->d_d2m64.p : rt->d_d2m32.p), phi,
-                                 rt->n_dir, rt->n_mom, rt->n_dofs, rt->stream),
-     "moment reduction");
+  if (f64 && rt->fp64_contract == OURANOS_FP64_DF64)
+    CU(launch_reduce_moments_df64((const double*)a.psi, rt->d_d2m64.as<double>(), (double*)phi,
+                                  rt->n_dir, rt->n_mom, rt->n_dofs, rt->stream),
+       "moment reduction");
+  else
+    CU(launch_reduce_moments<real>(a.psi, (const real*)(f64 ? rt->d_d2m64.p : rt->d_d2m32.p), phi,
+                                   rt->n_dir, rt->n_mom, rt->n_dofs, rt->stream),
+       "moment reduction");
   kernels += (rt->n_mom + 15) / 16;
   rt->last_kernels = kernels;
   return OURANOS_OK;
@@ -624,6 +635,13 @@ int ouranos_rt_set_precision(ouranos_rt* rt, int precision) {
   if (!rt) return OURANOS_ERR_BAD_INPUT;
   if (precision != OURANOS_FP64 && precision != OURANOS_FP32) return bad(rt, "unknown precision");
   rt->precision = precision;
+  return OURANOS_OK;
+}
+
+int ouranos_rt_set_fp64_contractions(ouranos_rt* rt, int mode) {
+  if (!rt) return OURANOS_ERR_BAD_INPUT;
+  if (mode != OURANOS_FP64_NATIVE && mode != OURANOS_FP64_DF64) return bad(rt, "unknown FP64 mode");
+  rt->fp64_contract = mode;
   return OURANOS_OK;
 }
 

@@ -184,7 +184,8 @@ int update(Work& w, int first, const std::vector<double>& y, double* x) {
 // estimate has dropped by `inner_drop` (FP32 operator accuracy), and the FP64
 // restart refines the solution (iterative refinement).
 int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double* x,
-          double* hist, ouranos_solve_info* info, int inner_prec, double inner_drop) {
+          double* hist, ouranos_solve_info* info, int inner_prec, double inner_drop,
+          bool learned = false) {
   m = std::max(1, std::min(m, 32));  // dot kernel handles up to 32 basis vectors
   const bool flexible = inner_prec != OURANOS_FP64;
   // vectors: V[0..m], Z[0..m-1] (flexible), r
@@ -197,6 +198,7 @@ int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double
   RC(rc);
   CUC(cudaMemsetAsync(x, 0, sizeof(double) * w.len, rt->stream), "gmres");
   int total = 0, cycles = 0;
+  bool use_pc = learned && rt->cnn;
   double rel = bnorm > 0 ? 1.0 : 0.0;
   if (hist) hist[0] = rel;
   bool converged = bnorm == 0.0;
@@ -225,10 +227,14 @@ int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double
     for (; k < m && total < max_it; ++k) {
       const double* vin = w.v(V0 + k);
       if (flexible) {
-        // right preconditioner slot: z_k = v_k (no preconditioner)
-        CUC(cudaMemcpyAsync(w.v(Z0 + k), vin, sizeof(double) * w.len, cudaMemcpyDeviceToDevice,
-                            rt->stream),
-            "fgmres");
+        // right preconditioner: z_k = P(v_k), learned correction or identity
+        if (use_pc) {
+          RC(ouranos_rt_pc_apply(rt, vin, w.v(Z0 + k)));
+        } else {
+          CUC(cudaMemcpyAsync(w.v(Z0 + k), vin, sizeof(double) * w.len, cudaMemcpyDeviceToDevice,
+                              rt->stream),
+              "fgmres");
+        }
         vin = w.v(Z0 + k);
       }
       double* nxt = w.v(V0 + k + 1);
@@ -248,6 +254,12 @@ int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double
     }
     std::vector<double> y = gv.solve(k);
     RC(update(w, flexible ? Z0 : V0, y, x));
+    // fallback: a preconditioned cycle that used all m steps without halving
+    // its residual estimate counts as stagnation -> plain FGMRES from here on
+    if (use_pc && k == m && total < max_it) {
+      const double est = std::fabs(gv.g[k]) / bnorm;
+      if (est > 0.5 * rel) use_pc = false;
+    }
   }
   // final FP64 true residual
   RC(apply_prec(rt, OURANOS_FP64, x, w.v(R)));
@@ -403,6 +415,15 @@ extern "C" int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it
     case OURANOS_SOLVER_FGMRES_MIXED:
       rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info,
                  OURANOS_FP32, 1e-5);
+      break;
+    case OURANOS_SOLVER_FGMRES_LEARNED:
+      if (!rt->cnn) {
+        rt->err = "no preconditioner installed (ouranos_rt_set_preconditioner)";
+        rc = OURANOS_ERR_BAD_INPUT;
+        break;
+      }
+      rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info,
+                 OURANOS_FP32, 1e-5, true);
       break;
     default:
       rt->err = "unknown solver";

@@ -1,6 +1,7 @@
 // Vector kernels around the sweep: scattering source, fixed source, the
 // residual form of Apply, layout permutations and the FP64 BLAS-1 pieces of
 // the Krylov drivers.  All are HBM-streaming, one grid-stride loop each.
+#include "df64.cuh"
 #include "internal.h"
 
 namespace ouranos {
@@ -210,7 +211,98 @@ __global__ void reduce_kernel(const real* __restrict__ psi, const real* __restri
   }
 }
 
+// FP64 contractions in double-float arithmetic on the FP32 pipes (see df64.cuh):
+// same inputs and outputs as expand_kernel<double> / reduce_kernel<double>.
+template <int NM>
+__global__ void expand_df64_kernel(const double* __restrict__ T, const double* __restrict__ iso,
+                                   const double* __restrict__ m2d, int ld, double* __restrict__ q,
+                                   int n_dir, int nm, long n_dofs, int accumulate) {
+  extern __shared__ unsigned char smem_raw[];
+  df64* sm = reinterpret_cast<df64*>(smem_raw);
+  for (int k = threadIdx.x; k < n_dir * nm; k += blockDim.x) sm[k] = df64_from(m2d[(k / nm) * ld + k % nm]);
+  __syncthreads();
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n_dofs;
+       e += (long)gridDim.x * blockDim.x) {
+    df64 t[NM];
+#pragma unroll
+    for (int m = 0; m < NM; ++m) t[m] = df64_from(m < nm ? T[(size_t)m * n_dofs + e] : 0.0);
+    const df64 is = df64_from(iso ? iso[e] : 0.0);
+    for (int d = 0; d < n_dir; ++d) {
+      df64_acc acc = acc_from(accumulate ? df64_from(q[(size_t)d * n_dofs + e]) : is);
+#pragma unroll
+      for (int m = 0; m < NM; ++m)
+        if (m < nm) acc_fma(acc, sm[d * nm + m], t[m]);
+      q[(size_t)d * n_dofs + e] = df64_to(acc_result(acc));
+    }
+  }
+}
+
+template <int NM>
+__global__ void reduce_df64_kernel(const double* __restrict__ psi, const double* __restrict__ d2m_t,
+                                   int ld, double* __restrict__ phi, int n_dir, int nm, long n_dofs) {
+  extern __shared__ unsigned char smem_raw[];
+  df64* sm = reinterpret_cast<df64*>(smem_raw);
+  for (int k = threadIdx.x; k < n_dir * nm; k += blockDim.x) sm[k] = df64_from(d2m_t[(k / nm) * ld + k % nm]);
+  __syncthreads();
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n_dofs;
+       e += (long)gridDim.x * blockDim.x) {
+    df64_acc acc[NM];
+#pragma unroll
+    for (int m = 0; m < NM; ++m) acc[m] = acc_zero();
+    for (int d = 0; d < n_dir; ++d) {
+      const df64 v = df64_from(psi[(size_t)d * n_dofs + e]);
+#pragma unroll
+      for (int m = 0; m < NM; ++m)
+        if (m < nm) acc_fma(acc[m], sm[d * nm + m], v);
+    }
+#pragma unroll
+    for (int m = 0; m < NM; ++m)
+      if (m < nm) phi[(size_t)m * n_dofs + e] = df64_to(acc_result(acc[m]));
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_expand_source_df64(const double* T, const double* iso, const double* m2d,
+                                      double* q, int n_dir, int n_mom, long n_dofs,
+                                      cudaStream_t s) {
+  for (int m0 = 0; m0 < n_mom; m0 += 16) {
+    const int nm = n_mom - m0 < 16 ? n_mom - m0 : 16;
+    const size_t sh = sizeof(df64) * (size_t)n_dir * nm;
+    const double* Tm = T + (size_t)m0 * n_dofs;
+    const int acc = m0 > 0;
+    const double* is = m0 == 0 ? iso : nullptr;
+    if (nm <= 4)
+      expand_df64_kernel<4><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+    else if (nm <= 10)
+      expand_df64_kernel<10><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+    else
+      expand_df64_kernel<16><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_reduce_moments_df64(const double* psi, const double* d2m_t, double* phi,
+                                       int n_dir, int n_mom, long n_dofs, cudaStream_t s) {
+  for (int m0 = 0; m0 < n_mom; m0 += 16) {
+    const int nm = n_mom - m0 < 16 ? n_mom - m0 : 16;
+    const size_t sh = sizeof(df64) * (size_t)n_dir * nm;
+    double* ph = phi + (size_t)m0 * n_dofs;
+    if (nm <= 1)
+      reduce_df64_kernel<1><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+    else if (nm <= 4)
+      reduce_df64_kernel<4><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+    else if (nm <= 10)
+      reduce_df64_kernel<10><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+    else
+      reduce_df64_kernel<16><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
 
 template <typename real>
 cudaError_t launch_expand_source(const real* T, const real* iso, const real* m2d, real* q,

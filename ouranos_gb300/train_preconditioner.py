@@ -1,0 +1,43 @@
+"""Train the learned preconditioner on the GPU and write its weights.
+
+    python -m ouranos_gb300.train_preconditioner [--n 64] [--maps 128] [--fields 4]
+        [--epochs 8] [--out ouranos_gb300/weights/precond_thick3d.npz]
+
+Training maps are the seeded 3-D thick diffusive material maps (seeds
+2000, 2001, ...; GLC S12); evaluation maps use other seeds.
+"""
+import argparse
+import json
+import os
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--maps", type=int, default=128)
+    ap.add_argument("--fields", type=int, default=4)
+    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--sn", type=int, default=12)
+    ap.add_argument("--out", default=os.path.join(HERE, "weights", "precond_thick3d.npz"))
+    args = ap.parse_args()
+    import ouranos_gb300
+    ouranos_gb300.build()
+    from ouranos_gb300.learned import train
+    t0 = time.time()
+    net, hist = train(n=args.n, maps=args.maps, fields_per_map=args.fields, epochs=args.epochs,
+                      lr=args.lr, sn=args.sn, log=lambda s: print(s, flush=True))
+    dt = time.time() - t0
+    os.makedirs(os.path.dirname(args.out), exist_ok=True)
+    net.save(args.out, meta={"loss_history": hist, "maps": args.maps, "fields": args.fields,
+                             "epochs": args.epochs, "train_seconds": dt, "n": args.n})
+    print(json.dumps({"trained": args.out, "seconds": dt, "final_loss": hist[-1]}))
+
+
+if __name__ == "__main__":
+    main()

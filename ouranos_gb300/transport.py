@@ -87,6 +87,11 @@ class RadiativeTransfer:
         self._check(_capi.lib().ouranos_rt_set_precision(self._h, p))
         self.precision = precision
 
+    def set_fp64_contractions(self, mode):
+        """'df64' (double-float on the FP32 pipes, default) or 'native' FP64."""
+        m = {"native": _capi.FP64_NATIVE, "df64": _capi.FP64_DF64}[mode]
+        self._check(_capi.lib().ouranos_rt_set_fp64_contractions(self._h, m))
+
     def get_n_tasks_to_execute(self):
         return self.n_tasks
 
@@ -167,7 +172,8 @@ class RadiativeTransfer:
     def solve(self, method="gmres", tol=1e-8, max_it=1000, restart=30, group_flux=None, x=None):
         """Drivers of src/ouranos.cc:43-209. Returns (x, info dict, residual history)."""
         kind = {"si": _capi.SOLVER_SI, "gmres": _capi.SOLVER_GMRES,
-                "bicgstab": _capi.SOLVER_BICGSTAB, "fgmres_mixed": _capi.SOLVER_FGMRES_MIXED}[method]
+                "bicgstab": _capi.SOLVER_BICGSTAB, "fgmres_mixed": _capi.SOLVER_FGMRES_MIXED,
+                "fgmres_learned": _capi.SOLVER_FGMRES_LEARNED}[method]
         if x is None:
             x = np.zeros(self.length)
         hist = np.zeros(max_it + 2)

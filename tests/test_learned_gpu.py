@@ -1,0 +1,97 @@
+"""Learned preconditioner: GPU network kernels against the CPU oracle, and the
+preconditioner inside FGMRES."""
+import numpy as np
+import pytest
+
+from oracle import cnn_oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.mark.parametrize("grid", [(8, 8, 8), (12, 8, 4)])
+def test_network_forward_and_gradients_match_oracle(grid):
+    torch = pytest.importorskip("torch")
+    from ouranos_gb300.learned import Network
+    nx, ny, nz = grid
+    V = nx * ny * nz
+    net = Network(nx, ny, nz, seed=11)
+    rng = np.random.default_rng(5)
+    p = net.params()
+    nb = sum(c for _, c, _, _ in cnn_oracle.LAYERS)
+    p[-nb:] = rng.uniform(-0.05, 0.05, nb)  # nonzero biases
+    net.set_params(p)
+    feat = rng.standard_normal((V, 3)).astype(np.float32)
+    target = rng.standard_normal(V).astype(np.float32)
+    fd = torch.from_numpy(feat.reshape(-1)).cuda()
+    td = torch.from_numpy(target).cuda()
+    out = torch.empty(V, dtype=torch.float32, device="cuda")
+    net.forward(fd, out)
+    loss, grads = net.gradients(fd, td)
+    loss_o, grads_o, out_o = cnn_oracle.gradients(p.astype(np.float64), feat.astype(np.float64),
+                                                  target.astype(np.float64), grid)
+    # BF16 activations/gradients: only FP32 vs FP64 accumulation order differs
+    assert _rel(out.cpu().numpy(), out_o) < 1e-2
+    assert abs(loss - loss_o) / loss_o < 1e-2
+    off = 0
+    for li, (cin, cout, _, _) in enumerate(cnn_oracle.LAYERS):
+        n = 27 * cin * cout
+        assert _rel(grads[off:off + n], grads_o[off:off + n]) < 5e-2, ("weights", li)
+        off += n
+    assert _rel(grads[off:], grads_o[off:]) < 5e-2
+
+
+def test_training_reduces_loss():
+    torch = pytest.importorskip("torch")
+    from ouranos_gb300.learned import Network
+    net = Network(8, 8, 8, seed=3)
+    rng = np.random.default_rng(9)
+    feat = torch.from_numpy(rng.standard_normal(8 ** 3 * 3).astype(np.float32)).cuda()
+    target = torch.from_numpy(np.tanh(rng.standard_normal(8 ** 3)).astype(np.float32)).cuda()
+    first = net.train_step(feat, target, 1e-3)
+    for _ in range(200):
+        last = net.train_step(feat, target, 1e-3)
+    assert last < 0.5 * first
+
+
+def test_preconditioner_features_and_target():
+    """Features/targets of a known pair: e constant in space -> cell averages."""
+    torch = pytest.importorskip("torch")
+    import ouranos_gb300 as og
+    from ouranos_gb300 import learned
+    prob = og.thick_3d(seed=2100, n=8, sn=4, block=4, width=2.0)
+    L = learned._lib()
+    with og.RadiativeTransfer(prob) as rt:
+        e = torch.full((prob.vector_length,), 2.0, dtype=torch.float64, device="cuda")
+        v = torch.full_like(e, 0.5)
+        feat = torch.empty(prob.total_cells * 3, dtype=torch.float32, device="cuda")
+        tgt = torch.empty(prob.total_cells, dtype=torch.float32, device="cuda")
+        import ctypes as C
+        scale = C.c_double()
+        assert L.ouranos_rt_pc_features(rt._h, v.data_ptr(), feat.data_ptr(), C.byref(scale)) == 0
+        assert L.ouranos_rt_pc_target(rt._h, v.data_ptr(), e.data_ptr(), tgt.data_ptr()) == 0
+        f = feat.cpu().numpy().reshape(-1, 3)
+        assert abs(scale.value - 0.5) < 1e-12
+        assert np.allclose(f[:, 0], 1.0, rtol=1e-6)
+        st = prob.sigma_t[prob.material_id, 0]
+        assert np.allclose(f[:, 1], np.log(st) / np.log(100.0), rtol=1e-6)
+        assert np.allclose(tgt.cpu().numpy(), (2.0 - 0.5) / 0.5, rtol=1e-6)
+
+
+def test_learned_fgmres_converges_and_falls_back():
+    """FGMRES with an (untrained) network still converges to 1e-8: a stagnating
+    preconditioned cycle hands over to the plain method."""
+    pytest.importorskip("torch")
+    import ouranos_gb300 as og
+    from ouranos_gb300.learned import Network, install
+    prob = og.thick_3d(seed=2101, n=8, sn=4, block=2, width=2.0)
+    with og.RadiativeTransfer(prob) as rt:
+        xg, ig, _ = rt.solve("gmres", tol=1e-8, max_it=800)
+        net = Network(8, 8, 8, seed=1)
+        install(rt, net)
+        xl, il, _ = rt.solve("fgmres_learned", tol=1e-8, max_it=800)
+    assert il["converged"] and il["residual"] < 1e-8
+    assert _rel(xl, xg) < 1e-6

@@ -232,3 +232,18 @@ def test_wait_timeout_reports_error_and_recovers():
         rt.set_wait_limit(2e9)
         y = rt.apply(x)
     assert rel_err(y, ref) < TOL64
+
+
+@pytest.mark.parametrize("mode", ["native", "df64"])
+def test_fp64_contraction_modes_match_oracle(mode):
+    """Both FP64 contraction arithmetics (native FP64, double-float on the FP32
+    pipes) keep the 1e-12 parity bar, on P3 (expanded source) and P0 (fused)."""
+    import ouranos_gb300 as og
+    for prob in (og.heterogeneous_2d(seed=61, n=20, fe_order=2, sn=8, l_max=3, blocks=4),
+                 og.thick_3d(seed=2061, n=6, sn=4, block=2, width=2.0)):
+        x = np.random.default_rng(61).standard_normal(prob.vector_length)
+        ref = po.OracleProblem(prob.arrays()).apply(x)
+        with og.RadiativeTransfer(prob) as rt:
+            rt.set_fp64_contractions(mode)
+            y = rt.apply(x)
+        assert rel_err(y, ref) < TOL64
