@@ -225,18 +225,23 @@ int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it, double to
 /* ------------------------------------------------- learned preconditioner
  * No counterpart in the reference (its Krylov solves use an identity
  * preconditioner, src/ouranos.cc:160-171).  A 3-D convolutional network on the
- * cell grid maps (residual scalar-flux cell averages, log sigma_t, scattering
- * ratio) to a scalar-flux correction -- a learned synthetic acceleration used
- * as the right preconditioner of FGMRES.  Grid sides must be multiples of 4. */
+ * cell grid of a 3-D DG Q1 mesh maps (the residual's normalised scalar-flux
+ * nodal values, 8 per cell; log sigma_t / log 100; scattering ratio) to a
+ * nodal scalar-flux correction -- a learned synthetic acceleration used as the
+ * right preconditioner of FGMRES.  Grid sides must be multiples of 4. */
+#define OURANOS_CNN_FEATURES 10 /* input channels per cell */
+#define OURANOS_CNN_OUTPUTS 8   /* output channels per cell (Q1 nodes) */
 typedef struct ouranos_cnn ouranos_cnn;
 int ouranos_cnn_create(int nx, int ny, int nz, unsigned long long seed, ouranos_cnn** out);
 int ouranos_cnn_destroy(ouranos_cnn* net);
 int ouranos_cnn_n_params(const ouranos_cnn* net, long* n);
 int ouranos_cnn_get_params(const ouranos_cnn* net, float* host);
 int ouranos_cnn_set_params(ouranos_cnn* net, const float* host);
-/* features: device [cells][3] FP32; out: device [cells] FP32 */
+/* features: device [cells][OURANOS_CNN_FEATURES] FP32; out: device
+ * [cells][OURANOS_CNN_OUTPUTS] FP32 */
 int ouranos_cnn_forward(ouranos_cnn* net, const float* features, float* out);
-/* MSE loss of forward(features) against target ([cells], device); gradients of
+/* MSE loss of forward(features) against target ([cells][OURANOS_CNN_OUTPUTS],
+ * device), averaged over all entries; gradients of
  * all parameters to grads_host (may be NULL), no update */
 int ouranos_cnn_gradients(ouranos_cnn* net, const float* features, const float* target,
                           float* grads_host, float* loss);
@@ -244,15 +249,18 @@ int ouranos_cnn_gradients(ouranos_cnn* net, const float* features, const float* 
 int ouranos_cnn_train_step(ouranos_cnn* net, const float* features, const float* target, float lr,
                            float* loss);
 int ouranos_cnn_last_error(const ouranos_cnn* net, char* buf, size_t len);
-/* install (or, with NULL, remove) the network as the handle's preconditioner */
+/* install (or, with NULL, remove) the network as the handle's preconditioner;
+ * UNSUPPORTED unless the mesh is 3-D DG Q1, BAD_INPUT if the grids differ */
 int ouranos_rt_set_preconditioner(ouranos_rt* rt, ouranos_cnn* net);
 /* network features of a residual v ([mom][dof], device FP64) into features
- * (device [cells][3]); scale (host, may be NULL) gets the normalisation */
+ * (device [cells][OURANOS_CNN_FEATURES]); scale (host, may be NULL) gets the
+ * normalisation s = RMS of v's scalar-moment values */
 int ouranos_rt_pc_features(ouranos_rt* rt, const double* v, float* features, double* scale);
-/* training target for the pair (v, e = A^-1 v): cell averages of (e - v) over
- * the normalisation of v (device [cells]) */
+/* training target for the pair (v, e = A^-1 v): the scalar-moment nodal
+ * values of (e - v) / (s g_c), g_c = 1/(1 - sigma_s0/sigma_t) of the cell
+ * (device [cells][OURANOS_CNN_OUTPUTS]) */
 int ouranos_rt_pc_target(ouranos_rt* rt, const double* v, const double* e, float* target);
-/* z = v + network correction (device vectors) */
+/* z = v + s g_c y, y the network output on v's features (device vectors) */
 int ouranos_rt_pc_apply(ouranos_rt* rt, const double* v, double* z);
 
 #ifdef __cplusplus

@@ -6,10 +6,19 @@
 //   level 1 (n/2):   pool(s0) -a1-> h_a1(32) -b1-> s1(32)
 //   level 2 (n/4):   pool(s1) -a2-> h_a2(32) -b2-> h_b2(32)
 //   level 1:         up(h_b2)+s1 -c1-> h_c1(32) -d1-> h_d1(16)
-//   level 0:         up(h_d1)+s0 -c0-> h_c0(16) -out-> y (linear, channel 0 used)
-// every conv is 3x3x3 + bias + ReLU except `out`.  Inputs: channel 0 the
-// normalised cell average of the residual's scalar moment, 1 log(sigma_t)/log(100),
-// 2 the scattering ratio; channels 3..15 are zero.
+//   level 0:         up(h_d1)+s0 -c0-> h_c0(16) -out-> o (channels 0..7 used)
+//   continuity:      y = S o, S the projection onto continuous nodal fields
+//                    (values at a shared mesh vertex averaged)
+// Every layer is gated-linear: h = (W * x) . gamma, a 3x3x3 convolution with
+// no bias followed by a per-voxel, per-channel gate gamma = a0 + a1 m0 + a2 m1
+// that is affine in the local material features m = (log(sigma_t)/log(100),
+// scattering ratio), average-pooled to the layer's level.  The network is
+// therefore linear in the residual it is given -- like A^-1 itself -- while
+// its coefficients follow the material map, and it answers consistently on
+// any mix of the error modes it was fitted on.
+// Inputs: channels 0..7 of x0 the residual's normalised scalar-flux values at
+// the cell's eight Q1 nodes (features 0..7) rounded to BF16, channels 8..15
+// the rounding remainders; features 8 and 9 are m.  Outputs: the eight nodal values of the continuous correction.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -24,20 +33,84 @@ using ouranos::cnn::Grid;
 namespace {
 
 constexpr int kCin0 = 16;  // padded input channels
-constexpr int kFeatures = 3;
+constexpr int kFeatures = OURANOS_CNN_FEATURES;
+constexpr int kNodal = 8;  // features 0..7: the residual's nodal values; 8, 9: materials
+constexpr int kOut = OURANOS_CNN_OUTPUTS;
+static_assert(kFeatures == kNodal + 2 && 2 * kNodal == kCin0 && kOut == 8,
+              "features are 8 nodal values + 2 material fields; outputs are the 8 Q1 corners");
 
-__global__ void features_kernel(const float* feat, int nf, __nv_bfloat16* x0, long V) {
+__global__ void features_kernel(const float* feat, __nv_bfloat16* x0, float2* mat, long V) {
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < V * kCin0;
        e += (long)gridDim.x * blockDim.x) {
     const long v = e / kCin0;
     const int c = (int)(e % kCin0);
-    x0[e] = __float2bfloat16(c < nf ? feat[v * nf + c] : 0.f);
+    // channels 0..7: BF16 of the nodal values; 8..15: BF16 of what that
+    // rounding lost, so the first layer sees the residual to ~16 bits
+    const float f = feat[v * kFeatures + (c & 7)];
+    const float hi = __bfloat162float(__float2bfloat16(f));
+    x0[e] = __float2bfloat16(c < kNodal ? hi : f - hi);
+    if (c == 0) mat[v] = make_float2(feat[v * kFeatures + kNodal], feat[v * kFeatures + kNodal + 1]);
   }
 }
-__global__ void relu_mask_kernel(const __nv_bfloat16* act, const __nv_bfloat16* g, __nv_bfloat16* out,
-                                 long n) {
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
-    out[e] = __bfloat162float(act[e]) > 0.f ? g[e] : __float2bfloat16(0.f);
+// 2x2x2 average pool of the material features
+__global__ void mat_pool_kernel(Grid fine, const float2* in, float2* out) {
+  const Grid co{fine.nx / 2, fine.ny / 2, fine.nz / 2};
+  for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < co.voxels(); v += (long)gridDim.x * blockDim.x) {
+    const int x = (int)(v % co.nx), y = (int)((v / co.nx) % co.ny), z = (int)(v / ((long)co.nx * co.ny));
+    float sx = 0.f, sy = 0.f;
+    for (int k = 0; k < 8; ++k) {
+      const float2 m = in[(2 * x + (k & 1)) + (long)fine.nx * ((2 * y + ((k >> 1) & 1)) + (long)fine.ny * (2 * z + (k >> 2)))];
+      sx += m.x;
+      sy += m.y;
+    }
+    out[v] = make_float2(0.125f * sx, 0.125f * sy);
+  }
+}
+// gate: x[v,c] = o[v,c] * (a[3c] + a[3c+1] m[v].x + a[3c+2] m[v].y)
+template <typename T>
+__device__ __forceinline__ float to_f(T v);
+template <>
+__device__ __forceinline__ float to_f<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ float to_f<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+template <typename T>
+__device__ __forceinline__ T from_f(float v);
+template <>
+__device__ __forceinline__ float from_f<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return __float2bfloat16(v); }
+
+__device__ __forceinline__ float gate_of(const float* a, int c, float2 m) {
+  return a[3 * c] + a[3 * c + 1] * m.x + a[3 * c + 2] * m.y;
+}
+template <typename T>
+__global__ void gate_fwd_kernel(const T* o, const float2* mat, const float* a, int C, long V, T* x) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < V * C; e += (long)gridDim.x * blockDim.x) {
+    const int c = (int)(e % C);
+    x[e] = from_f<T>(to_f<T>(o[e]) * gate_of(a, c, mat[e / C]));
+  }
+}
+// backward of the gate: g_o = g . gamma (BF16, may alias g) and
+// da[3c+j] += sum_v g[v,c] o[v,c] (1, m0, m1)_j
+template <typename T>
+__global__ void __launch_bounds__(256) gate_bwd_kernel(const __nv_bfloat16* g, const T* o, const float2* mat,
+                                                       const float* a, int C, long V, __nv_bfloat16* g_o,
+                                                       float* da) {
+  __shared__ float s_da[3 * 32];
+  for (int i = threadIdx.x; i < 3 * C; i += blockDim.x) s_da[i] = 0.f;
+  __syncthreads();
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < V * C; e += (long)gridDim.x * blockDim.x) {
+    const int c = (int)(e % C);
+    const float2 m = mat[e / C];
+    const float gv = __bfloat162float(g[e]);
+    const float go = gv * to_f<T>(o[e]);
+    g_o[e] = __float2bfloat16(gv * gate_of(a, c, m));
+    atomicAdd(&s_da[3 * c], go);
+    atomicAdd(&s_da[3 * c + 1], go * m.x);
+    atomicAdd(&s_da[3 * c + 2], go * m.y);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 3 * C; i += blockDim.x) atomicAdd(da + i, s_da[i]);
 }
 __global__ void add_kernel(const __nv_bfloat16* a, const __nv_bfloat16* b, __nv_bfloat16* out, long n) {
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
@@ -100,17 +173,25 @@ __global__ void up_bwd_kernel(Grid fine, const __nv_bfloat16* gfine, __nv_bfloat
     gco[e] = __float2bfloat16(s);
   }
 }
-// mean-squared error on output channel 0 and its gradient (BF16, channel 0 only)
-__global__ void mse_kernel(const float* out, int cout, const float* target, long V,
-                           __nv_bfloat16* grad, float* loss_acc) {
+// residual r = y - target over all V*kOut entries, loss = mean(r^2)
+__global__ void resid_kernel(const float* y, const float* target, long n, float* resid, float* loss_acc) {
   float local = 0.f;
-  for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < V; v += (long)gridDim.x * blockDim.x) {
-    const float d = out[v * cout] - target[v];
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    const float d = y[e] - target[e];
+    resid[e] = d;
     local += d * d;
-    for (int c = 0; c < cout; ++c) grad[v * cout + c] = __float2bfloat16(c == 0 ? 2.f * d / (float)V : 0.f);
   }
   for (int o = 16; o; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(loss_acc, local / (float)V);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss_acc, local / (float)n);
+}
+// d loss / d o = S (2 r / n): the vertex averages of 2r/n scattered to channels
+// 0..7 of the output layer's gradient (BF16), zero on channels 8..15
+__global__ void grad_scatter_kernel(Grid g, const float* vert, __nv_bfloat16* grad) {
+  const long n = g.voxels() * 16;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    const int c = (int)(e & 15);
+    grad[e] = __float2bfloat16(c < kOut ? vert[ouranos::cnn::corner_vertex(g, e >> 4, c)] : 0.f);
+  }
 }
 __global__ void adam_kernel(float* w, const float* g, float* m, float* v, long n, float lr, float b1,
                             float b2, float eps, float c1, float c2) {
@@ -141,9 +222,9 @@ inline int blocks_for(long n) {
 
 struct Layer {
   int cin, cout;
-  bool relu;
+  int level;          // 0, 1, 2: grid n, n/2, n/4
   Grid grid;
-  size_t woff, boff;  // offsets into the parameter arrays
+  size_t woff, goff;  // offsets into the weight and gate arrays
 };
 
 template <int CIN, int COUT, bool RELU>
@@ -188,14 +269,20 @@ cudaError_t conv_wgrad(int cin, int cout, const Grid& g, const __nv_bfloat16* in
 struct ouranos_cnn {
   Grid g0, g1, g2;
   std::vector<Layer> L;  // a0 b0 a1 b1 a2 b2 c1 d1 c0 out
-  size_t n_w = 0, n_b = 0;
-  float *w = nullptr, *b = nullptr, *gw = nullptr, *gb = nullptr;
-  float *mw = nullptr, *vw = nullptr, *mb = nullptr, *vb = nullptr;
+  size_t n_w = 0, n_g = 0;  // conv weights, gate coefficients (3 per output channel)
+  float *w = nullptr, *gt = nullptr, *dw = nullptr, *dgt = nullptr;
+  float *mw = nullptr, *vw = nullptr, *mg = nullptr, *vg = nullptr;
   __nv_bfloat16 *wf = nullptr, *wb = nullptr;  // BF16 forward / mirrored copies (n_w each)
-  // activations and gradient scratch
+  // gated activations (inputs of the next layer) and the pre-gate conv outputs
   __nv_bfloat16 *x0, *ha0, *s0, *p0, *ha1, *s1, *p1, *ha2, *hb2, *u1, *hc1, *hd1, *u0, *hc0;
+  __nv_bfloat16 *o[9];                                    // pre-gate outputs of a0 .. c0
+  float2 *mat[3];                                         // material features per level
   __nv_bfloat16 *ga, *gb_, *gc, *gskip0, *gskip1, *gout;  // gradients
-  float* out = nullptr;
+  float* out = nullptr;    // output layer before its gate, [voxel][16]
+  float* outg = nullptr;   // output layer after its gate, [voxel][16]
+  float* outp = nullptr;   // projected output y = S outg, [voxel][kOut]
+  float* resid = nullptr;  // y - target, [voxel][kOut]
+  float* vert = nullptr;   // one value per mesh vertex
   float* dloss = nullptr;
   long step = 0;
   cudaStream_t stream = nullptr;
@@ -240,92 +327,115 @@ int refresh_copies(ouranos_cnn* net) {
   return OURANOS_OK;
 }
 
-int conv_layer(ouranos_cnn* net, int l, const __nv_bfloat16* in, __nv_bfloat16* ob, float* of) {
+// layer l on `in`: o_l = W_l * in, then the gated activation into `out`
+int conv_layer(ouranos_cnn* net, int l, const __nv_bfloat16* in, __nv_bfloat16* out) {
   const Layer& L = net->L[l];
-  CN(conv_fwd(L.cin, L.cout, L.relu, L.grid, in, wf_of(net, l), net->b + L.boff, ob, of, net->stream),
+  CN(conv_fwd(L.cin, L.cout, false, L.grid, in, wf_of(net, l), nullptr, net->o[l], nullptr, net->stream),
      "conv forward");
+  gate_fwd_kernel<__nv_bfloat16><<<blocks_for(L.grid.voxels() * L.cout), 256, 0, net->stream>>>(
+      net->o[l], net->mat[L.level], net->gt + L.goff, L.cout, L.grid.voxels(), out);
+  CN(cudaGetLastError(), "gate");
   return OURANOS_OK;
 }
 
 int forward(ouranos_cnn* net, const float* feat) {
   cudaStream_t s = net->stream;
   const long V0 = net->g0.voxels();
-  features_kernel<<<blocks_for(V0 * kCin0), 256, 0, s>>>(feat, kFeatures, net->x0, V0);
+  features_kernel<<<blocks_for(V0 * kCin0), 256, 0, s>>>(feat, net->x0, net->mat[0], V0);
+  mat_pool_kernel<<<blocks_for(net->g1.voxels()), 256, 0, s>>>(net->g0, net->mat[0], net->mat[1]);
+  mat_pool_kernel<<<blocks_for(net->g2.voxels()), 256, 0, s>>>(net->g1, net->mat[1], net->mat[2]);
   int rc;
-  if ((rc = conv_layer(net, A0, net->x0, net->ha0, nullptr)) || (rc = conv_layer(net, B0, net->ha0, net->s0, nullptr)))
+  if ((rc = conv_layer(net, A0, net->x0, net->ha0)) || (rc = conv_layer(net, B0, net->ha0, net->s0)))
     return rc;
   pool_kernel<<<blocks_for(net->g1.voxels() * 16), 256, 0, s>>>(net->g0, net->s0, net->p0, 16);
-  if ((rc = conv_layer(net, A1, net->p0, net->ha1, nullptr)) || (rc = conv_layer(net, B1, net->ha1, net->s1, nullptr)))
+  if ((rc = conv_layer(net, A1, net->p0, net->ha1)) || (rc = conv_layer(net, B1, net->ha1, net->s1)))
     return rc;
   pool_kernel<<<blocks_for(net->g2.voxels() * 32), 256, 0, s>>>(net->g1, net->s1, net->p1, 32);
-  if ((rc = conv_layer(net, A2, net->p1, net->ha2, nullptr)) || (rc = conv_layer(net, B2, net->ha2, net->hb2, nullptr)))
+  if ((rc = conv_layer(net, A2, net->p1, net->ha2)) || (rc = conv_layer(net, B2, net->ha2, net->hb2)))
     return rc;
   up_add_kernel<<<blocks_for(net->g1.voxels() * 32), 256, 0, s>>>(net->g1, net->hb2, net->s1, net->u1, 32);
-  if ((rc = conv_layer(net, C1, net->u1, net->hc1, nullptr)) || (rc = conv_layer(net, D1, net->hc1, net->hd1, nullptr)))
+  if ((rc = conv_layer(net, C1, net->u1, net->hc1)) || (rc = conv_layer(net, D1, net->hc1, net->hd1)))
     return rc;
   up_add_kernel<<<blocks_for(V0 * 16), 256, 0, s>>>(net->g0, net->hd1, net->s0, net->u0, 16);
-  if ((rc = conv_layer(net, C0, net->u0, net->hc0, nullptr)) || (rc = conv_layer(net, OUT, net->hc0, nullptr, net->out)))
-    return rc;
+  if ((rc = conv_layer(net, C0, net->u0, net->hc0))) return rc;
+  const Layer& LO = net->L[OUT];
+  CN(conv_fwd(LO.cin, LO.cout, false, LO.grid, net->hc0, wf_of(net, OUT), nullptr, nullptr, net->out, s),
+     "conv forward");
+  gate_fwd_kernel<float><<<blocks_for(V0 * 16), 256, 0, s>>>(net->out, net->mat[0], net->gt + LO.goff, 16, V0,
+                                                              net->outg);
+  const long NV = ouranos::cnn::n_vertices(net->g0);
+  ouranos::cnn::vertex_average_kernel<<<blocks_for(NV), 256, 0, s>>>(net->g0, net->outg, 16, 1.f, net->vert);
+  ouranos::cnn::vertex_scatter_kernel<<<blocks_for(V0 * kOut), 256, 0, s>>>(net->g0, net->vert, net->outp);
   CN(cudaGetLastError(), "forward");
   return OURANOS_OK;
 }
 
-// gradient of conv layer l: given the output gradient g_out (already masked by
-// the layer's ReLU), accumulate its weight/bias gradients and, if g_in is not
-// NULL, produce the input gradient
-int conv_backward(ouranos_cnn* net, int l, const __nv_bfloat16* in, const __nv_bfloat16* g_out,
+// gradient of conv layer l: given the gradient g_o of its pre-gate output,
+// accumulate its weight gradients and, if g_in is not NULL, produce the input
+// gradient
+int conv_backward(ouranos_cnn* net, int l, const __nv_bfloat16* in, const __nv_bfloat16* g_o,
                   __nv_bfloat16* g_in) {
   const Layer& L = net->L[l];
-  CN(conv_wgrad(L.cin, L.cout, L.grid, in, g_out, net->gw + L.woff, net->gb + L.boff, net->stream),
-     "weight gradient");
+  CN(conv_wgrad(L.cin, L.cout, L.grid, in, g_o, net->dw + L.woff, nullptr, net->stream), "weight gradient");
   if (g_in)
-    CN(conv_fwd(L.cout, L.cin, false, L.grid, g_out, wb_of(net, l), nullptr, g_in, nullptr, net->stream),
+    CN(conv_fwd(L.cout, L.cin, false, L.grid, g_o, wb_of(net, l), nullptr, g_in, nullptr, net->stream),
        "data gradient");
   return OURANOS_OK;
 }
 
-int mask(ouranos_cnn* net, const __nv_bfloat16* act, __nv_bfloat16* g, long n) {
-  relu_mask_kernel<<<blocks_for(n), 256, 0, net->stream>>>(act, g, g, n);
-  CN(cudaGetLastError(), "relu mask");
+// gate backward of layer l in place: g (gradient of the gated activation)
+// becomes the gradient of the pre-gate output; gate gradients accumulate
+int gate_backward(ouranos_cnn* net, int l, __nv_bfloat16* g) {
+  const Layer& L = net->L[l];
+  gate_bwd_kernel<__nv_bfloat16><<<blocks_for(L.grid.voxels() * L.cout), 256, 0, net->stream>>>(
+      g, net->o[l], net->mat[L.level], net->gt + L.goff, L.cout, L.grid.voxels(), g, net->dgt + L.goff);
+  CN(cudaGetLastError(), "gate gradient");
   return OURANOS_OK;
 }
 
 int backward(ouranos_cnn* net, const float* target, float* loss_host) {
   cudaStream_t s = net->stream;
   const long V0 = net->g0.voxels(), V1 = net->g1.voxels(), V2 = net->g2.voxels();
-  CN(cudaMemsetAsync(net->gw, 0, sizeof(float) * net->n_w, s), "zero grads");
-  CN(cudaMemsetAsync(net->gb, 0, sizeof(float) * net->n_b, s), "zero grads");
+  CN(cudaMemsetAsync(net->dw, 0, sizeof(float) * net->n_w, s), "zero grads");
+  CN(cudaMemsetAsync(net->dgt, 0, sizeof(float) * net->n_g, s), "zero grads");
   CN(cudaMemsetAsync(net->dloss, 0, sizeof(float), s), "zero loss");
-  mse_kernel<<<blocks_for(V0), 256, 0, s>>>(net->out, 16, target, V0, net->gout, net->dloss);
+  const long n_out = V0 * kOut;
+  resid_kernel<<<blocks_for(n_out), 256, 0, s>>>(net->outp, target, n_out, net->resid, net->dloss);
+  ouranos::cnn::vertex_average_kernel<<<blocks_for(ouranos::cnn::n_vertices(net->g0)), 256, 0, s>>>(
+      net->g0, net->resid, kOut, 2.f / (float)n_out, net->vert);
+  grad_scatter_kernel<<<blocks_for(V0 * 16), 256, 0, s>>>(net->g0, net->vert, net->gout);  // d outg
+  const Layer& LO = net->L[OUT];
+  gate_bwd_kernel<float><<<blocks_for(V0 * 16), 256, 0, s>>>(net->gout, net->out, net->mat[0],
+                                                             net->gt + LO.goff, 16, V0, net->gout,
+                                                             net->dgt + LO.goff);
   int rc;
   __nv_bfloat16 *ga = net->ga, *gb = net->gb_, *gc = net->gc;
-  // out (linear) and c0
-  if ((rc = conv_backward(net, OUT, net->hc0, net->gout, ga))) return rc;      // ga = d hc0
-  if ((rc = mask(net, net->hc0, ga, V0 * 16))) return rc;
-  if ((rc = conv_backward(net, C0, net->u0, ga, gb))) return rc;               // gb = d u0
+  if ((rc = conv_backward(net, OUT, net->hc0, net->gout, ga))) return rc;     // ga = d hc0
+  if ((rc = gate_backward(net, C0, ga))) return rc;
+  if ((rc = conv_backward(net, C0, net->u0, ga, gb))) return rc;              // gb = d u0
   CN(cudaMemcpyAsync(net->gskip0, gb, sizeof(__nv_bfloat16) * V0 * 16, cudaMemcpyDeviceToDevice, s), "skip");
-  up_bwd_kernel<<<blocks_for(V1 * 16), 256, 0, s>>>(net->g0, gb, ga, 16);      // ga = d hd1
-  if ((rc = mask(net, net->hd1, ga, V1 * 16))) return rc;
-  if ((rc = conv_backward(net, D1, net->hc1, ga, gb))) return rc;              // gb = d hc1
-  if ((rc = mask(net, net->hc1, gb, V1 * 32))) return rc;
-  if ((rc = conv_backward(net, C1, net->u1, gb, ga))) return rc;               // ga = d u1
+  up_bwd_kernel<<<blocks_for(V1 * 16), 256, 0, s>>>(net->g0, gb, ga, 16);     // ga = d hd1
+  if ((rc = gate_backward(net, D1, ga))) return rc;
+  if ((rc = conv_backward(net, D1, net->hc1, ga, gb))) return rc;             // gb = d hc1
+  if ((rc = gate_backward(net, C1, gb))) return rc;
+  if ((rc = conv_backward(net, C1, net->u1, gb, ga))) return rc;              // ga = d u1
   CN(cudaMemcpyAsync(net->gskip1, ga, sizeof(__nv_bfloat16) * V1 * 32, cudaMemcpyDeviceToDevice, s), "skip");
-  up_bwd_kernel<<<blocks_for(V2 * 32), 256, 0, s>>>(net->g1, ga, gb, 32);      // gb = d hb2
-  if ((rc = mask(net, net->hb2, gb, V2 * 32))) return rc;
-  if ((rc = conv_backward(net, B2, net->ha2, gb, ga))) return rc;              // ga = d ha2
-  if ((rc = mask(net, net->ha2, ga, V2 * 32))) return rc;
-  if ((rc = conv_backward(net, A2, net->p1, ga, gb))) return rc;               // gb = d p1
-  pool_bwd_kernel<<<blocks_for(V1 * 32), 256, 0, s>>>(net->g1, gb, gc, 32);    // gc = d s1 (pool path)
+  up_bwd_kernel<<<blocks_for(V2 * 32), 256, 0, s>>>(net->g1, ga, gb, 32);     // gb = d hb2
+  if ((rc = gate_backward(net, B2, gb))) return rc;
+  if ((rc = conv_backward(net, B2, net->ha2, gb, ga))) return rc;             // ga = d ha2
+  if ((rc = gate_backward(net, A2, ga))) return rc;
+  if ((rc = conv_backward(net, A2, net->p1, ga, gb))) return rc;              // gb = d p1
+  pool_bwd_kernel<<<blocks_for(V1 * 32), 256, 0, s>>>(net->g1, gb, gc, 32);   // gc = d s1 (pool path)
   add_kernel<<<blocks_for(V1 * 32), 256, 0, s>>>(gc, net->gskip1, gc, V1 * 32);
-  if ((rc = mask(net, net->s1, gc, V1 * 32))) return rc;
-  if ((rc = conv_backward(net, B1, net->ha1, gc, ga))) return rc;              // ga = d ha1
-  if ((rc = mask(net, net->ha1, ga, V1 * 32))) return rc;
-  if ((rc = conv_backward(net, A1, net->p0, ga, gb))) return rc;               // gb = d p0
-  pool_bwd_kernel<<<blocks_for(V0 * 16), 256, 0, s>>>(net->g0, gb, gc, 16);    // gc = d s0 (pool path)
+  if ((rc = gate_backward(net, B1, gc))) return rc;
+  if ((rc = conv_backward(net, B1, net->ha1, gc, ga))) return rc;             // ga = d ha1
+  if ((rc = gate_backward(net, A1, ga))) return rc;
+  if ((rc = conv_backward(net, A1, net->p0, ga, gb))) return rc;              // gb = d p0
+  pool_bwd_kernel<<<blocks_for(V0 * 16), 256, 0, s>>>(net->g0, gb, gc, 16);   // gc = d s0 (pool path)
   add_kernel<<<blocks_for(V0 * 16), 256, 0, s>>>(gc, net->gskip0, gc, V0 * 16);
-  if ((rc = mask(net, net->s0, gc, V0 * 16))) return rc;
-  if ((rc = conv_backward(net, B0, net->ha0, gc, ga))) return rc;              // ga = d ha0
-  if ((rc = mask(net, net->ha0, ga, V0 * 16))) return rc;
+  if ((rc = gate_backward(net, B0, gc))) return rc;
+  if ((rc = conv_backward(net, B0, net->ha0, gc, ga))) return rc;             // ga = d ha0
+  if ((rc = gate_backward(net, A0, ga))) return rc;
   if ((rc = conv_backward(net, A0, net->x0, ga, nullptr))) return rc;
   CN(cudaGetLastError(), "backward");
   if (loss_host) {
@@ -336,6 +446,14 @@ int backward(ouranos_cnn* net, const float* target, float* loss_host) {
 }
 
 }  // namespace
+
+namespace ouranos {
+void cnn_grid(const ouranos_cnn* net, int* nx, int* ny, int* nz) {
+  *nx = net->g0.nx;
+  *ny = net->g0.ny;
+  *nz = net->g0.nz;
+}
+}  // namespace ouranos
 
 // ---------------------------------------------------------------- C-ABI
 extern "C" {
@@ -349,28 +467,29 @@ int ouranos_cnn_create(int nx, int ny, int nz, unsigned long long seed, ouranos_
   net->g0 = {nx, ny, nz};
   net->g1 = {nx / 2, ny / 2, nz / 2};
   net->g2 = {nx / 4, ny / 4, nz / 4};
-  struct Spec { int cin, cout; bool relu; int level; };
-  const Spec spec[] = {{16, 16, true, 0}, {16, 16, true, 0}, {16, 32, true, 1}, {32, 32, true, 1},
-                       {32, 32, true, 2}, {32, 32, true, 2}, {32, 32, true, 1}, {32, 16, true, 1},
-                       {16, 16, true, 0}, {16, 16, false, 0}};
+  struct Spec { int cin, cout, level; };
+  const Spec spec[] = {{16, 16, 0}, {16, 16, 0}, {16, 32, 1}, {32, 32, 1}, {32, 32, 2},
+                       {32, 32, 2}, {32, 32, 1}, {32, 16, 1}, {16, 16, 0}, {16, 16, 0}};
   const Grid grids[3] = {net->g0, net->g1, net->g2};
   for (const Spec& sp : spec) {
-    Layer l{sp.cin, sp.cout, sp.relu, grids[sp.level], net->n_w, net->n_b};
+    Layer l{sp.cin, sp.cout, sp.level, grids[sp.level], net->n_w, net->n_g};
     net->n_w += 27L * sp.cin * sp.cout;
-    net->n_b += sp.cout;
+    net->n_g += 3L * sp.cout;
     net->L.push_back(l);
   }
-  if (cudaStreamCreateWithFlags(&net->stream, cudaStreamNonBlocking) != cudaSuccess)
+  // blocking: ordered against the legacy default stream the caller's tensors
+  // are usually written on
+  if (cudaStreamCreateWithFlags(&net->stream, cudaStreamDefault) != cudaSuccess)
     return cnn_fail(net, cudaGetLastError(), "stream");
   const long V0 = net->g0.voxels(), V1 = net->g1.voxels(), V2 = net->g2.voxels();
   CN(dalloc(net, &net->w, net->n_w), "params");
-  CN(dalloc(net, &net->b, net->n_b), "params");
-  CN(dalloc(net, &net->gw, net->n_w), "grads");
-  CN(dalloc(net, &net->gb, net->n_b), "grads");
+  CN(dalloc(net, &net->gt, net->n_g), "params");
+  CN(dalloc(net, &net->dw, net->n_w), "grads");
+  CN(dalloc(net, &net->dgt, net->n_g), "grads");
   CN(dalloc(net, &net->mw, net->n_w), "adam");
   CN(dalloc(net, &net->vw, net->n_w), "adam");
-  CN(dalloc(net, &net->mb, net->n_b), "adam");
-  CN(dalloc(net, &net->vb, net->n_b), "adam");
+  CN(dalloc(net, &net->mg, net->n_g), "adam");
+  CN(dalloc(net, &net->vg, net->n_g), "adam");
   CN(dalloc(net, &net->wf, net->n_w), "weights");
   CN(dalloc(net, &net->wb, net->n_w), "weights");
   __nv_bfloat16** a16[] = {&net->x0, &net->ha0, &net->s0, &net->u0, &net->hc0};
@@ -382,6 +501,8 @@ int ouranos_cnn_create(int nx, int ny, int nz, unsigned long long seed, ouranos_
   CN(dalloc(net, &net->p1, V2 * 32), "activations");
   CN(dalloc(net, &net->ha2, V2 * 32), "activations");
   CN(dalloc(net, &net->hb2, V2 * 32), "activations");
+  for (int l = A0; l < OUT; ++l) CN(dalloc(net, &net->o[l], net->L[l].grid.voxels() * net->L[l].cout), "activations");
+  for (int k = 0; k < 3; ++k) CN(dalloc(net, &net->mat[k], grids[k].voxels()), "materials");
   const long gmax = V0 * 16 > V1 * 32 ? V0 * 16 : V1 * 32;
   CN(dalloc(net, &net->ga, gmax), "gradients");
   CN(dalloc(net, &net->gb_, gmax), "gradients");
@@ -390,9 +511,15 @@ int ouranos_cnn_create(int nx, int ny, int nz, unsigned long long seed, ouranos_
   CN(dalloc(net, &net->gskip1, V1 * 32), "gradients");
   CN(dalloc(net, &net->gout, V0 * 16), "gradients");
   CN(dalloc(net, &net->out, V0 * 16), "output");
+  CN(dalloc(net, &net->outg, V0 * 16), "output");
+  CN(dalloc(net, &net->outp, V0 * kOut), "output");
+  CN(dalloc(net, &net->resid, V0 * kOut), "output");
+  CN(dalloc(net, &net->vert, ouranos::cnn::n_vertices(net->g0)), "output");
   CN(dalloc(net, &net->dloss, 1), "loss");
-  // He-normal initialisation from a SplitMix64 stream, Box-Muller
-  std::vector<float> w(net->n_w, 0.f), b(net->n_b, 0.f);
+  // weights: normal with variance 1/fan_in (a linear network keeps the signal
+  // scale), the output layer 0.1x so the initial correction is small; gates
+  // start at gamma = 1.  SplitMix64 stream, Box-Muller.
+  std::vector<float> w(net->n_w, 0.f), gt(net->n_g, 0.f);
   unsigned long long st = seed;
   auto next = [&]() {
     st += 0x9E3779B97F4A7C15ull;
@@ -404,14 +531,15 @@ int ouranos_cnn_create(int nx, int ny, int nz, unsigned long long seed, ouranos_
   };
   for (size_t li = 0; li < net->L.size(); ++li) {
     const Layer& l = net->L[li];
-    const double sd = std::sqrt(2.0 / (27.0 * l.cin)) * (li == OUT ? 0.1 : 1.0);
+    const double sd = std::sqrt(1.0 / (27.0 * l.cin)) * (li == OUT ? 0.1 : 1.0);
     for (long k = 0; k < 27L * l.cin * l.cout; ++k) {
       const double u1 = next(), u2 = next();
       w[l.woff + k] = (float)(sd * std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * M_PI * u2));
     }
+    for (int c = 0; c < l.cout; ++c) gt[l.goff + 3 * c] = 1.f;
   }
   CN(cudaMemcpy(net->w, w.data(), sizeof(float) * net->n_w, cudaMemcpyHostToDevice), "params");
-  CN(cudaMemcpy(net->b, b.data(), sizeof(float) * net->n_b, cudaMemcpyHostToDevice), "params");
+  CN(cudaMemcpy(net->gt, gt.data(), sizeof(float) * net->n_g, cudaMemcpyHostToDevice), "params");
   int rc = refresh_copies(net);
   if (rc) return rc;
   CN(cudaStreamSynchronize(net->stream), "init");
@@ -429,16 +557,18 @@ int ouranos_cnn_destroy(ouranos_cnn* net) {
 
 int ouranos_cnn_n_params(const ouranos_cnn* net, long* n) {
   if (!net || !n) return OURANOS_ERR_BAD_INPUT;
-  *n = (long)(net->n_w + net->n_b);
+  *n = (long)(net->n_w + net->n_g);
   return OURANOS_OK;
 }
 
+// parameter vector: all conv weights ([tap][cin][cout] per layer, layers in
+// order), then all gate coefficients ([cout][3] per layer)
 int ouranos_cnn_get_params(const ouranos_cnn* cnet, float* host) {
   ouranos_cnn* net = const_cast<ouranos_cnn*>(cnet);
   if (!net || !host) return OURANOS_ERR_BAD_INPUT;
   CN(cudaStreamSynchronize(net->stream), "params");
   CN(cudaMemcpy(host, net->w, sizeof(float) * net->n_w, cudaMemcpyDeviceToHost), "params");
-  CN(cudaMemcpy(host + net->n_w, net->b, sizeof(float) * net->n_b, cudaMemcpyDeviceToHost), "params");
+  CN(cudaMemcpy(host + net->n_w, net->gt, sizeof(float) * net->n_g, cudaMemcpyDeviceToHost), "params");
   return OURANOS_OK;
 }
 
@@ -446,20 +576,20 @@ int ouranos_cnn_set_params(ouranos_cnn* net, const float* host) {
   if (!net || !host) return OURANOS_ERR_BAD_INPUT;
   CN(cudaStreamSynchronize(net->stream), "params");
   CN(cudaMemcpy(net->w, host, sizeof(float) * net->n_w, cudaMemcpyHostToDevice), "params");
-  CN(cudaMemcpy(net->b, host + net->n_w, sizeof(float) * net->n_b, cudaMemcpyHostToDevice), "params");
+  CN(cudaMemcpy(net->gt, host + net->n_w, sizeof(float) * net->n_g, cudaMemcpyHostToDevice), "params");
   int rc = refresh_copies(net);
   if (rc) return rc;
   CN(cudaStreamSynchronize(net->stream), "params");
   return OURANOS_OK;
 }
 
-// features: device [voxel][3] FP32; out: device [voxel] FP32 (channel 0)
+// features: device [voxel][kFeatures] FP32; out: device [voxel][kOut] FP32
 int ouranos_cnn_forward(ouranos_cnn* net, const float* features, float* out) {
   if (!net || !features || !out) return OURANOS_ERR_BAD_INPUT;
   int rc = forward(net, features);
   if (rc) return rc;
-  CN(cudaMemcpy2DAsync(out, sizeof(float), net->out, 16 * sizeof(float), sizeof(float),
-                       net->g0.voxels(), cudaMemcpyDeviceToDevice, net->stream),
+  CN(cudaMemcpyAsync(out, net->outp, sizeof(float) * kOut * net->g0.voxels(), cudaMemcpyDeviceToDevice,
+                     net->stream),
      "output");
   CN(cudaStreamSynchronize(net->stream), "forward");
   return OURANOS_OK;
@@ -473,8 +603,8 @@ int ouranos_cnn_gradients(ouranos_cnn* net, const float* features, const float* 
   if ((rc = forward(net, features)) || (rc = backward(net, target, loss))) return rc;
   if (grads_host) {
     CN(cudaStreamSynchronize(net->stream), "grads");
-    CN(cudaMemcpy(grads_host, net->gw, sizeof(float) * net->n_w, cudaMemcpyDeviceToHost), "grads");
-    CN(cudaMemcpy(grads_host + net->n_w, net->gb, sizeof(float) * net->n_b, cudaMemcpyDeviceToHost), "grads");
+    CN(cudaMemcpy(grads_host, net->dw, sizeof(float) * net->n_w, cudaMemcpyDeviceToHost), "grads");
+    CN(cudaMemcpy(grads_host + net->n_w, net->dgt, sizeof(float) * net->n_g, cudaMemcpyDeviceToHost), "grads");
   }
   return OURANOS_OK;
 }
@@ -488,8 +618,9 @@ int ouranos_cnn_train_step(ouranos_cnn* net, const float* features, const float*
   ++net->step;
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   const float c1 = 1.f - std::pow(b1, (float)net->step), c2 = 1.f - std::pow(b2, (float)net->step);
-  adam_kernel<<<blocks_for(net->n_w), 256, 0, net->stream>>>(net->w, net->gw, net->mw, net->vw, net->n_w, lr, b1, b2, eps, c1, c2);
-  adam_kernel<<<blocks_for(net->n_b), 256, 0, net->stream>>>(net->b, net->gb, net->mb, net->vb, net->n_b, lr, b1, b2, eps, c1, c2);
+  adam_kernel<<<blocks_for(net->n_w), 256, 0, net->stream>>>(net->w, net->dw, net->mw, net->vw, net->n_w, lr, b1, b2, eps, c1, c2);
+  // gates multiply through all ten layers: a tenth of the weights' step
+  adam_kernel<<<blocks_for(net->n_g), 256, 0, net->stream>>>(net->gt, net->dgt, net->mg, net->vg, net->n_g, 0.1f * lr, b1, b2, eps, c1, c2);
   CN(cudaGetLastError(), "adam");
   return refresh_copies(net);
 }

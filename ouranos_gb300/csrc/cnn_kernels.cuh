@@ -185,5 +185,44 @@ __global__ void conv3_wgrad(Grid g, const __nv_bfloat16* __restrict__ in,
   if (tap == 13 && threadIdx.x < COUT && dbias) atomicAdd(dbias + threadIdx.x, bacc);
 }
 
+// ---------------------------------------------------------------- continuity projection
+// Nodal fields on a grid of Q1 cells: value k (0..7) of a cell sits at its
+// corner (k&1, (k>>1)&1, k>>2).  The projection S onto continuous fields
+// averages the values that share a mesh vertex and copies the average back
+// to each of them (S is symmetric and S S = S).
+__host__ __device__ inline long n_vertices(const Grid& g) {
+  return (long)(g.nx + 1) * (g.ny + 1) * (g.nz + 1);
+}
+
+// vert[v] = scale * mean of nodal[cell*ld + corner] over the pairs at vertex v
+static __global__ void vertex_average_kernel(Grid g, const float* nodal, int ld, float scale, float* vert) {
+  const long nv = n_vertices(g);
+  for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < nv; v += (long)gridDim.x * blockDim.x) {
+    const int vx = (int)(v % (g.nx + 1)), vy = (int)((v / (g.nx + 1)) % (g.ny + 1));
+    const int vz = (int)(v / ((long)(g.nx + 1) * (g.ny + 1)));
+    float s = 0.f;
+    int n = 0;
+    for (int k = 0; k < 8; ++k) {
+      const int cx = vx - (k & 1), cy = vy - ((k >> 1) & 1), cz = vz - (k >> 2);
+      if (cx < 0 || cy < 0 || cz < 0 || cx >= g.nx || cy >= g.ny || cz >= g.nz) continue;
+      s += nodal[(cx + (long)g.nx * (cy + (long)g.ny * cz)) * ld + k];
+      ++n;
+    }
+    vert[v] = n ? scale * s / (float)n : 0.f;
+  }
+}
+
+__device__ __forceinline__ long corner_vertex(const Grid& g, long cell, int k) {
+  const int x = (int)(cell % g.nx), y = (int)((cell / g.nx) % g.ny), z = (int)(cell / ((long)g.nx * g.ny));
+  return (x + (k & 1)) + (long)(g.nx + 1) * ((y + ((k >> 1) & 1)) + (long)(g.ny + 1) * (z + (k >> 2)));
+}
+
+// nodal[cell*8 + k] = vert[vertex of (cell, k)]
+static __global__ void vertex_scatter_kernel(Grid g, const float* vert, float* nodal) {
+  const long n = g.voxels() * 8;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+    nodal[e] = vert[corner_vertex(g, e >> 3, (int)(e & 7))];
+}
+
 }  // namespace cnn
 }  // namespace ouranos

@@ -144,6 +144,8 @@ namespace ouranos {
 // learned preconditioner glue (precond.cu)
 int rt_pc_features(ouranos_rt* rt, const double* v, float* feat);
 int rt_pc_correct(ouranos_rt* rt, const double* v, const float* y, double* z);
+// the network's cell grid
+void cnn_grid(const ouranos_cnn* net, int* nx, int* ny, int* nz);
 // Device-side pieces the solvers use (operator.cu).
 int rt_apply_device(ouranos_rt* rt, const double* x, double* y);
 int rt_rhs_device(ouranos_rt* rt, const double* gf, double* rhs);
@@ -203,5 +205,5 @@ struct ouranos_rt {
   // learned preconditioner
   ouranos_cnn* cnn = nullptr;
   int pc_group = -1;
-  ouranos::DevBuf d_pc_prop, d_pc_wavg, d_pc_work, d_pc_feat;
+  ouranos::DevBuf d_pc_prop, d_pc_work, d_pc_feat, d_pc_nodal, d_pc_vert;
 };

@@ -550,7 +550,10 @@ int ouranos_rt_create(const ouranos_problem_desc* D, int device, ouranos_rt** ou
       seen[o] = 1;
     }
   }
-  if (cudaStreamCreateWithFlags(&rt->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+  // A blocking stream: work on it is ordered after work already issued to the
+  // legacy default stream (and before work issued there later), so device
+  // vectors a caller has just written on that stream are read complete.
+  if (cudaStreamCreateWithFlags(&rt->own_stream, cudaStreamDefault) != cudaSuccess ||
       cudaEventCreate(&rt->ev0) != cudaSuccess || cudaEventCreate(&rt->ev1) != cudaSuccess)
     return fail(cuda_fail(rt, cudaGetLastError(), "stream"));
   rt->stream = rt->own_stream;

@@ -1,63 +1,87 @@
 // Learned preconditioner glue: per-cell features of a residual vector, the
 // network's training target, and the correction it applies.
 //
-// For a residual v ([mom][dof], FP64) on a handle's mesh:
-//   a[c]  = cell average of the scalar moment, sum_i (sum_j M_ij / |cell|) v_0[c,i]
-//   s     = sqrt(mean_c a[c]^2)  (normalisation, kept on the device)
-//   feature[c] = (a[c]/s, log(sigma_t,c)/log(100), sigma_s0,c/sigma_t,c)
-// The network predicts y[c] ~ cell average of (A^-1 v - v)[c] / s, and the
-// preconditioner returns z = v + s*y on the scalar moment (piecewise constant
-// per cell) -- a learned synthetic acceleration of the scalar flux.
+// For a residual v ([mom][dof], FP64) on a 3-D DG Q1 mesh (8 nodes per cell):
+//   s          = sqrt(mean over all scalar-moment dofs of v_0^2)  (kept on the device)
+//   c_c        = sigma_s0,c / sigma_t,c,   g_c = 1 / (1 - min(c_c, 1 - 1e-6))
+//   feature[c] = (v_0[c,0..7]/s, log(sigma_t,c)/log(100), c_c)
+// The network predicts y[c,i] ~ (A^-1 v - v)_0[c,i] / (s g_c), and the
+// preconditioner returns z = v + s g_c y on the scalar moment's nodal values --
+// a learned synthetic acceleration of the scalar flux.  g_c is the
+// infinite-medium gain of source iteration in cell c (sum_k c^k); dividing it
+// out keeps the regression targets O(1) although A^-1 amplifies the slow modes
+// of thick, scattering cells by up to ~g_c.  The correction is per node, not
+// per cell: in optically thick cells the slow error modes are continuous
+// across faces, and a piecewise-constant correction of them leaves intra-cell
+// residuals larger than the one it corrects.
 #include <cmath>
 #include <cstdio>
 #include <vector>
 
+#include "cnn_kernels.cuh"
 #include "internal.h"
 
 using namespace ouranos;
 
 namespace {
 
-__global__ void cell_avg_kernel(const double* v, const double* wavg, int n, long n_cells, double* avg,
-                                double* sumsq) {
+constexpr int kNodes = OURANOS_CNN_OUTPUTS;
+constexpr int kFeat = OURANOS_CNN_FEATURES;
+constexpr int kPartials = 304;  // fixed grid of the deterministic sum of squares
+constexpr double kGain = 64.0;  // output scale K of the correction
+
+// partial sums of v[0..n) squared, one per block (fixed grid, fixed order)
+__global__ void __launch_bounds__(256) sumsq_partial_kernel(const double* v, long n, double* partial) {
+  __shared__ double red[8];
   double local = 0.0;
-  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n_cells; c += (long)gridDim.x * blockDim.x) {
-    double a = 0.0;
-    for (int i = 0; i < n; ++i) a += wavg[i] * v[c * n + i];
-    avg[c] = a;
-    local += a * a;
-  }
+  for (long e = blockIdx.x * 256L + threadIdx.x; e < n; e += 256L * kPartials) local += v[e] * v[e];
   for (int o = 16; o; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
-  if ((threadIdx.x & 31) == 0 && sumsq) atomicAdd(sumsq, local);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = local;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[w];
+    partial[blockIdx.x] = t;
+  }
+}
+// partial[kPartials] -> scale = sqrt(sum / n)
+__global__ void __launch_bounds__(32) sumsq_final_kernel(double* partial, long n) {
+  double t = 0.0;
+  for (int i = threadIdx.x; i < kPartials; i += 32) t += partial[i];
+  for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (threadIdx.x == 0) partial[kPartials] = n > 0 ? sqrt(t / (double)n) : 0.0;
 }
 
-__global__ void features_kernel(const double* avg, const double* sumsq, long n_cells, const float2* prop,
+__global__ void features_kernel(const double* v, const double* scale, long n_cells, const float2* prop,
                                 float* feat) {
-  const double s = sqrt(*sumsq / (double)n_cells);
+  const double s = *scale;
   const double inv = s > 0 ? 1.0 / s : 0.0;
-  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n_cells; c += (long)gridDim.x * blockDim.x) {
-    feat[c * 3 + 0] = (float)(avg[c] * inv);
-    feat[c * 3 + 1] = prop[c].x;
-    feat[c * 3 + 2] = prop[c].y;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n_cells * kFeat;
+       e += (long)gridDim.x * blockDim.x) {
+    const long c = e / kFeat;
+    const int k = (int)(e % kFeat);
+    float f;
+    if (k < kNodes) f = (float)(v[c * kNodes + k] * inv);
+    else f = k == kNodes ? prop[c].x : prop[c].y;
+    feat[e] = f;
   }
 }
 
-// target[c] = (avg(e)[c] - avg(v)[c]) / s
-__global__ void target_kernel(const double* avg_e, const double* avg_v, const double* sumsq, long n_cells,
-                              float* target) {
-  const double s = sqrt(*sumsq / (double)n_cells);
-  const double inv = s > 0 ? 1.0 / s : 0.0;
-  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n_cells; c += (long)gridDim.x * blockDim.x)
-    target[c] = (float)((avg_e[c] - avg_v[c]) * inv);
+// d[c,i] = (e_0 - v_0)[c,i] / (s K)  (before the continuity projection)
+__global__ void target_kernel(const double* v, const double* e, const double* scale, long n, float* d) {
+  const double s = *scale;
+  const double inv = s > 0 ? 1.0 / (s * kGain) : 0.0;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
+    d[k] = (float)((e[k] - v[k]) * inv);
 }
 
-// z = v; z_0[c,i] += s * y[c]
-__global__ void correct_kernel(const double* v, double* z, long len, const float* y, const double* sumsq,
-                               int n, long n_cells) {
-  const double s = sqrt(*sumsq / (double)n_cells);
+// z = v; z_0[c,i] += s K y[c,i]
+__global__ void correct_kernel(const double* v, double* z, long len, const float* y, const double* scale,
+                               long n0) {
+  const double sk = *scale * kGain;
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len; e += (long)gridDim.x * blockDim.x) {
     double val = v[e];
-    if (e < n_cells * n) val += s * (double)y[e / n];
+    if (e < n0) val += sk * (double)y[e];
     z[e] = val;
   }
 }
@@ -79,8 +103,14 @@ int pfail(ouranos_rt* rt, cudaError_t e, const char* what) {
     if (_e != cudaSuccess) return pfail(rt, _e, what);  \
   } while (0)
 
-// per-cell properties and averaging weights (uploaded once per handle/group)
+cnn::Grid pc_grid(const ouranos_rt* rt) { return cnn::Grid{rt->nx[0], rt->nx[1], rt->nx[2]}; }
+
+// per-cell properties (uploaded once per handle/group) and the work area
 int ensure_tables(ouranos_rt* rt) {
+  if (rt->dim != 3 || rt->n != kNodes) {
+    rt->err = "learned preconditioner: needs a 3-D DG Q1 mesh (8 nodes per cell)";
+    return OURANOS_ERR_UNSUPPORTED;
+  }
   if (rt->pc_group == rt->group && rt->d_pc_prop.p) return OURANOS_OK;
   std::vector<float2> prop(rt->n_cells);
   const int G = rt->G, L = rt->l_max;
@@ -92,45 +122,46 @@ int ensure_tables(ouranos_rt* rt) {
     prop[c] = make_float2((float)(std::log(st > 0 ? st : 1e-30) / std::log(100.0)),
                           (float)(st > 0 ? ss / st : 0.0));
   }
-  double vol = 1.0;
-  for (int a = 0; a < rt->dim; ++a) vol *= rt->h[a];
-  std::vector<double> w(rt->n, 0.0);
-  for (int i = 0; i < rt->n; ++i)
-    for (int j = 0; j < rt->n; ++j) w[i] += rt->fe.mass[j * rt->n + i] / vol;
   PC(rt->d_pc_prop.alloc(sizeof(float2) * rt->n_cells), "preconditioner tables");
-  PC(rt->d_pc_wavg.alloc(sizeof(double) * rt->n), "preconditioner tables");
-  PC(rt->d_pc_work.alloc(sizeof(double) * (2 * rt->n_cells + 8)), "preconditioner work");
+  PC(rt->d_pc_nodal.alloc(sizeof(float) * kNodes * rt->n_cells), "preconditioner work");
+  PC(rt->d_pc_vert.alloc(sizeof(float) * cnn::n_vertices(pc_grid(rt))), "preconditioner work");
+  PC(rt->d_pc_work.alloc(sizeof(double) * (kPartials + 8)), "preconditioner work");
   PC(cudaMemcpyAsync(rt->d_pc_prop.p, prop.data(), sizeof(float2) * rt->n_cells, cudaMemcpyHostToDevice, rt->stream), "tables");
-  PC(cudaMemcpyAsync(rt->d_pc_wavg.p, w.data(), sizeof(double) * rt->n, cudaMemcpyHostToDevice, rt->stream), "tables");
   PC(cudaStreamSynchronize(rt->stream), "tables");
   rt->pc_group = rt->group;
+  return OURANOS_OK;
+}
+
+// normalisation of v into work[kPartials]
+int pc_scale(ouranos_rt* rt, const double* v) {
+  double* work = rt->d_pc_work.as<double>();
+  const long n0 = rt->n_cells * kNodes;
+  sumsq_partial_kernel<<<kPartials, 256, 0, rt->stream>>>(v, n0, work);
+  sumsq_final_kernel<<<1, 32, 0, rt->stream>>>(work, n0);
+  PC(cudaGetLastError(), "scale");
   return OURANOS_OK;
 }
 
 }  // namespace
 
 namespace ouranos {
-// features of v into feat ([cells][3] FP32, device); the normalisation stays
-// in the handle's work area (work[2*n_cells])
+// features of v into feat ([cells][OURANOS_CNN_FEATURES] FP32, device); the
+// normalisation stays in the handle's work area for rt_pc_correct
 int rt_pc_features(ouranos_rt* rt, const double* v, float* feat) {
   int rc = ensure_tables(rt);
   if (rc) return rc;
-  double* avg = rt->d_pc_work.as<double>();
-  double* sumsq = avg + 2 * rt->n_cells;
-  PC(cudaMemsetAsync(sumsq, 0, sizeof(double), rt->stream), "features");
-  cell_avg_kernel<<<blocks(rt->n_cells), 256, 0, rt->stream>>>(v, rt->d_pc_wavg.as<double>(), rt->n,
-                                                               rt->n_cells, avg, sumsq);
-  features_kernel<<<blocks(rt->n_cells), 256, 0, rt->stream>>>(avg, sumsq, rt->n_cells,
-                                                               rt->d_pc_prop.as<float2>(), feat);
+  if ((rc = pc_scale(rt, v))) return rc;
+  features_kernel<<<blocks(rt->n_cells * kFeat), 256, 0, rt->stream>>>(
+      v, rt->d_pc_work.as<double>() + kPartials, rt->n_cells, rt->d_pc_prop.as<float2>(), feat);
   PC(cudaGetLastError(), "features");
   return OURANOS_OK;
 }
 
-// z = v + s * expand(y) with the normalisation of the last rt_pc_features call
+// z = v + s * y with the normalisation of the last rt_pc_features call
 int rt_pc_correct(ouranos_rt* rt, const double* v, const float* y, double* z) {
-  const double* sumsq = rt->d_pc_work.as<double>() + 2 * rt->n_cells;
   const long len = (long)rt->n_mom * rt->n_dofs;
-  correct_kernel<<<blocks(len), 256, 0, rt->stream>>>(v, z, len, y, sumsq, rt->n, rt->n_cells);
+  correct_kernel<<<blocks(len), 256, 0, rt->stream>>>(v, z, len, y, rt->d_pc_work.as<double>() + kPartials,
+                                                      rt->n_cells * kNodes);
   PC(cudaGetLastError(), "correction");
   return OURANOS_OK;
 }
@@ -140,6 +171,18 @@ extern "C" {
 
 int ouranos_rt_set_preconditioner(ouranos_rt* rt, ouranos_cnn* cnn) {
   if (!rt) return OURANOS_ERR_BAD_INPUT;
+  if (cnn) {
+    int nx, ny, nz;
+    cnn_grid(cnn, &nx, &ny, &nz);
+    if (rt->dim != 3 || rt->n != kNodes) {
+      rt->err = "learned preconditioner: needs a 3-D DG Q1 mesh (8 nodes per cell)";
+      return OURANOS_ERR_UNSUPPORTED;
+    }
+    if (nx != rt->nx[0] || ny != rt->nx[1] || nz != rt->nx[2]) {
+      rt->err = "learned preconditioner: network grid differs from the mesh";
+      return OURANOS_ERR_BAD_INPUT;
+    }
+  }
   rt->cnn = cnn;
   return OURANOS_OK;
 }
@@ -149,13 +192,10 @@ int ouranos_rt_pc_features(ouranos_rt* rt, const double* v, float* features, dou
   cudaSetDevice(rt->device);
   int rc = rt_pc_features(rt, v, features);
   if (rc) return rc;
-  if (scale) {
-    double ss = 0.0;
-    PC(cudaMemcpyAsync(&ss, rt->d_pc_work.as<double>() + 2 * rt->n_cells, sizeof(double),
-                       cudaMemcpyDeviceToHost, rt->stream), "scale");
-    PC(cudaStreamSynchronize(rt->stream), "scale");
-    *scale = std::sqrt(ss / (double)rt->n_cells);
-  }
+  if (scale)
+    PC(cudaMemcpyAsync(scale, rt->d_pc_work.as<double>() + kPartials, sizeof(double), cudaMemcpyDeviceToHost,
+                       rt->stream),
+       "scale");
   PC(cudaStreamSynchronize(rt->stream), "features");
   return OURANOS_OK;
 }
@@ -165,15 +205,14 @@ int ouranos_rt_pc_target(ouranos_rt* rt, const double* v, const double* e, float
   cudaSetDevice(rt->device);
   int rc = ensure_tables(rt);
   if (rc) return rc;
-  double* avg = rt->d_pc_work.as<double>();
-  double* avg_e = avg + rt->n_cells;
-  double* sumsq = avg + 2 * rt->n_cells;
-  PC(cudaMemsetAsync(sumsq, 0, sizeof(double), rt->stream), "target");
-  cell_avg_kernel<<<blocks(rt->n_cells), 256, 0, rt->stream>>>(v, rt->d_pc_wavg.as<double>(), rt->n,
-                                                               rt->n_cells, avg, sumsq);
-  cell_avg_kernel<<<blocks(rt->n_cells), 256, 0, rt->stream>>>(e, rt->d_pc_wavg.as<double>(), rt->n,
-                                                               rt->n_cells, avg_e, nullptr);
-  target_kernel<<<blocks(rt->n_cells), 256, 0, rt->stream>>>(avg_e, avg, sumsq, rt->n_cells, target);
+  if ((rc = pc_scale(rt, v))) return rc;
+  const long n0 = rt->n_cells * kNodes;
+  float* d = rt->d_pc_nodal.as<float>();
+  float* vert = rt->d_pc_vert.as<float>();
+  const cnn::Grid g = pc_grid(rt);
+  target_kernel<<<blocks(n0), 256, 0, rt->stream>>>(v, e, rt->d_pc_work.as<double>() + kPartials, n0, d);
+  cnn::vertex_average_kernel<<<blocks(cnn::n_vertices(g)), 256, 0, rt->stream>>>(g, d, kNodes, 1.f, vert);
+  cnn::vertex_scatter_kernel<<<blocks(n0), 256, 0, rt->stream>>>(g, vert, target);
   PC(cudaGetLastError(), "target");
   PC(cudaStreamSynchronize(rt->stream), "target");
   return OURANOS_OK;
@@ -182,9 +221,9 @@ int ouranos_rt_pc_target(ouranos_rt* rt, const double* v, const double* e, float
 int ouranos_rt_pc_apply(ouranos_rt* rt, const double* v, double* z) {
   if (!rt || !v || !z || !rt->cnn) return OURANOS_ERR_BAD_INPUT;
   cudaSetDevice(rt->device);
-  PC(rt->d_pc_feat.alloc(sizeof(float) * 4 * rt->n_cells), "preconditioner");
+  PC(rt->d_pc_feat.alloc(sizeof(float) * (kFeat + kNodes) * rt->n_cells), "preconditioner");
   float* feat = rt->d_pc_feat.as<float>();
-  float* y = feat + 3 * rt->n_cells;
+  float* y = feat + (long)kFeat * rt->n_cells;
   int rc;
   if ((rc = rt_pc_features(rt, v, feat))) return rc;
   PC(cudaStreamSynchronize(rt->stream), "preconditioner");

@@ -199,6 +199,9 @@ int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double
   CUC(cudaMemsetAsync(x, 0, sizeof(double) * w.len, rt->stream), "gmres");
   int total = 0, cycles = 0;
   bool use_pc = learned && rt->cnn;
+  enum { kPcTrial, kPcCompare, kPcOn, kPcOff };
+  int pc_state = kPcTrial;
+  double pc_rate = 0.0, plain_rate = 0.0;
   double rel = bnorm > 0 ? 1.0 : 0.0;
   if (hist) hist[0] = rel;
   bool converged = bnorm == 0.0;
@@ -254,11 +257,27 @@ int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double
     }
     std::vector<double> y = gv.solve(k);
     RC(update(w, flexible ? Z0 : V0, y, x));
-    // fallback: a preconditioned cycle that used all m steps without halving
-    // its residual estimate counts as stagnation -> plain FGMRES from here on
-    if (use_pc && k == m && total < max_it) {
-      const double est = std::fabs(gv.g[k]) / bnorm;
-      if (est > 0.5 * rel) use_pc = false;
+    // Safeguard for the learned preconditioner (the plain method is its
+    // fallback).  A preconditioned cycle that needed all m steps is suspect:
+    // the next cycle runs unpreconditioned, and the solve keeps whichever of
+    // the two reduced the residual estimate more per iteration.  While the
+    // preconditioner stays on, every later full cycle is held to that plain
+    // rate; one that falls behind switches it off for the rest of the solve.
+    if (learned && rt->cnn && k > 0 && pc_state != kPcOff) {
+      const double est = std::max(std::fabs(gv.g[k]) / bnorm, 1e-300);
+      const double rate = std::log(est / rel) / k;  // < 0; more negative = faster
+      if (pc_state == kPcTrial && use_pc && k == m) {
+        pc_rate = rate;
+        pc_state = kPcCompare;
+        use_pc = false;
+      } else if (pc_state == kPcCompare) {
+        plain_rate = rate;
+        use_pc = pc_rate < plain_rate;
+        pc_state = use_pc ? kPcOn : kPcOff;
+      } else if (pc_state == kPcOn && k == m && rate > plain_rate) {
+        use_pc = false;
+        pc_state = kPcOff;
+      }
     }
   }
   // final FP64 true residual

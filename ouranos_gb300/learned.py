@@ -3,10 +3,12 @@ the GPU by the project's own forward/backward kernels, used as the right
 preconditioner of FGMRES (OURANOS_SOLVER_FGMRES_LEARNED).
 
 Training pairs come from the solver's own operator: for a seeded material map
-and a smooth random error field e, the residual is v = A e (one Apply), the
-network input is the per-cell feature set of v and the target the cell
-averages of (e - v) over the normalisation of v -- so z = v + correction
-approximates A^-1 v on the slowly converging, diffusive error modes.
+and an error field e, the residual is v = A e (one Apply), the network input is
+the per-cell feature set of v (its eight Q1 nodal scalar-flux values over the
+RMS s of v, log sigma_t, scattering ratio) and the target the nodal values of
+(e - v)/s -- so z = v + s*correction approximates A^-1 v.  The errors mix
+smooth random fields, power iterates T^j e0 of the transport iteration (what
+FGMRES's Krylov vectors are made of) and rough noise.
 """
 import ctypes as C
 import math
@@ -19,6 +21,8 @@ from .problem import thick_3d
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 WEIGHTS = os.path.join(HERE, "weights")
+FEATURES = 10  # OURANOS_CNN_FEATURES
+OUTPUTS = 8    # OURANOS_CNN_OUTPUTS
 
 
 def _lib():
@@ -89,7 +93,7 @@ class Network:
         self._check(_lib().ouranos_cnn_set_params(self._h, p.ctypes.data))
 
     def forward(self, feat, out):
-        """feat: CUDA float32 tensor [cells*3]; out: CUDA float32 tensor [cells]."""
+        """feat: CUDA float32 tensor [cells*FEATURES]; out: CUDA float32 tensor [cells*OUTPUTS]."""
         self._check(_lib().ouranos_cnn_forward(self._h, feat.data_ptr(), out.data_ptr()))
         return out
 
@@ -134,7 +138,7 @@ def nodal_error_field(problem, rng):
     on the vertex grid); higher moments zero."""
     nx, ny, nz = problem.n_cells
     p = problem.fe_order
-    corr = rng.uniform(2.0, 16.0)
+    corr = math.exp(rng.uniform(0.0, math.log(16.0)))  # 1 to 16 cells, log-uniform
     f = smooth_field((nz * p + 1, ny * p + 1, nx * p + 1), rng, corr * p)
     f += rng.uniform(-1.0, 1.0) * 0.5  # some mean component
     n = problem.dofs_per_cell
@@ -148,31 +152,67 @@ def nodal_error_field(problem, rng):
     return e
 
 
-def make_pairs(rt, problem, count, rng, torch, feat_out, target_out, offset):
+def _start_field(rt, problem, rng, torch, kind):
+    if kind == "smooth":
+        return torch.from_numpy(nodal_error_field(problem, rng)).cuda()
+    if kind == "rough":
+        return torch.from_numpy(rng.standard_normal(problem.vector_length)).cuda()
+    # the map's own right-hand side: the start of every Krylov space on it
+    b = torch.zeros(problem.vector_length, dtype=torch.float64, device="cuda")
+    rt.rhs(out=b)
+    return b
+
+
+def power_iterate(rt, e, steps, torch):
+    """e <- T^steps e with T = I - A (source iteration on the error, no
+    source), renormalised each step; T^j e is what the j-th Krylov vector is
+    made of, so pairs built on it look like FGMRES's own inputs."""
+    v = torch.empty_like(e)
+    for _ in range(steps):
+        rt.Apply(e, v)
+        e = e - v
+        e = e / (e.norm() / math.sqrt(e.numel()) + 1e-300)
+    return e
+
+
+def make_pairs(rt, problem, count, rng, torch, feat_out, target_out, offset, mix=(0.25, 0.5, 0.25)):
     """Fill feat_out[offset:offset+count] / target_out[...] (CUDA tensors) with
-    (features(A e), target(A e, e)) pairs for random smooth errors e."""
+    (features(A e), target(A e, e)) pairs.  A fraction mix[0] of the errors e
+    are smooth random fields, mix[1] power iterates T^j e0 (j log-uniform in
+    [1, 64], e0 smooth, rough or the map's right-hand side) and mix[2] rough
+    per-dof noise, so that the network sees the slow modes, the Krylov-like
+    differences A T^j e0 and inputs it must leave nearly alone."""
     L = _lib()
     n_cells = problem.total_cells
     for k in range(count):
-        e = torch.from_numpy(nodal_error_field(problem, rng)).cuda()
+        u = rng.uniform()
+        if u < mix[0]:
+            e = _start_field(rt, problem, rng, torch, "smooth")
+        elif u < mix[0] + mix[1]:
+            start = ("smooth", "rough", "rhs")[int(rng.integers(0, 3))]
+            steps = int(round(math.exp(rng.uniform(0.0, math.log(64.0)))))
+            e = power_iterate(rt, _start_field(rt, problem, rng, torch, start), steps, torch)
+        else:
+            e = _start_field(rt, problem, rng, torch, "rough")
+        e = e.contiguous()
         v = torch.empty_like(e)
         rt.Apply(e, v)
         f = feat_out[offset + k]
         t = target_out[offset + k]
         _capi.check(L.ouranos_rt_pc_features(rt._h, v.data_ptr(), f.data_ptr(), None), rt._h)
         _capi.check(L.ouranos_rt_pc_target(rt._h, v.data_ptr(), e.data_ptr(), t.data_ptr()), rt._h)
-        assert f.numel() == 3 * n_cells and t.numel() == n_cells
+        assert f.numel() == FEATURES * n_cells and t.numel() == OUTPUTS * n_cells
 
 
-def train(n=64, maps=128, fields_per_map=4, epochs=8, lr=2e-3, seed=7, map_seed0=2000,
+def train(n=64, maps=128, fields_per_map=4, epochs=8, lr=3e-4, seed=7, map_seed0=2000,
           sn=12, log=print):
     """Train the network on seeded 3-D thick-diffusive maps; returns (net, history)."""
     import torch
     from .transport import RadiativeTransfer
     rng = np.random.default_rng(seed)
     n_pairs = maps * fields_per_map
-    feats = torch.empty((n_pairs, n ** 3 * 3), dtype=torch.float32, device="cuda")
-    targets = torch.empty((n_pairs, n ** 3), dtype=torch.float32, device="cuda")
+    feats = torch.empty((n_pairs, n ** 3 * FEATURES), dtype=torch.float32, device="cuda")
+    targets = torch.empty((n_pairs, n ** 3 * OUTPUTS), dtype=torch.float32, device="cuda")
     for m in range(maps):
         prob = thick_3d(seed=map_seed0 + m, n=n, sn=sn)
         with RadiativeTransfer(prob, precision="fp32") as rt:

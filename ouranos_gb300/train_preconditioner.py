@@ -22,7 +22,7 @@ def main():
     ap.add_argument("--maps", type=int, default=128)
     ap.add_argument("--fields", type=int, default=4)
     ap.add_argument("--epochs", type=int, default=8)
-    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--lr", type=float, default=3e-4)
     ap.add_argument("--sn", type=int, default=12)
     ap.add_argument("--out", default=os.path.join(HERE, "weights", "precond_thick3d.npz"))
     args = ap.parse_args()

@@ -21,23 +21,25 @@ def test_network_forward_and_gradients_match_oracle(grid):
     net = Network(nx, ny, nz, seed=11)
     rng = np.random.default_rng(5)
     p = net.params()
-    nb = sum(c for _, c, _, _ in cnn_oracle.LAYERS)
-    p[-nb:] = rng.uniform(-0.05, 0.05, nb)  # nonzero biases
+    assert p.size == cnn_oracle.n_params()
+    ng = sum(3 * c for _, c, _ in cnn_oracle.LAYERS)
+    p[-ng:] += rng.uniform(-0.3, 0.3, ng)  # gates away from their (1, 0, 0) start
     net.set_params(p)
-    feat = rng.standard_normal((V, 3)).astype(np.float32)
-    target = rng.standard_normal(V).astype(np.float32)
+    feat = rng.standard_normal((V, cnn_oracle.FEATURES)).astype(np.float32)
+    feat[:, 8:] = rng.uniform(0, 1, (V, 2))  # material channels
+    target = rng.standard_normal((V, cnn_oracle.OUTPUTS)).astype(np.float32)
     fd = torch.from_numpy(feat.reshape(-1)).cuda()
-    td = torch.from_numpy(target).cuda()
-    out = torch.empty(V, dtype=torch.float32, device="cuda")
+    td = torch.from_numpy(target.reshape(-1)).cuda()
+    out = torch.empty(V * cnn_oracle.OUTPUTS, dtype=torch.float32, device="cuda")
     net.forward(fd, out)
     loss, grads = net.gradients(fd, td)
     loss_o, grads_o, out_o = cnn_oracle.gradients(p.astype(np.float64), feat.astype(np.float64),
                                                   target.astype(np.float64), grid)
     # BF16 activations/gradients: only FP32 vs FP64 accumulation order differs
-    assert _rel(out.cpu().numpy(), out_o) < 1e-2
+    assert _rel(out.cpu().numpy(), out_o.reshape(-1)) < 1e-2
     assert abs(loss - loss_o) / loss_o < 1e-2
     off = 0
-    for li, (cin, cout, _, _) in enumerate(cnn_oracle.LAYERS):
+    for li, (cin, cout, _) in enumerate(cnn_oracle.LAYERS):
         n = 27 * cin * cout
         assert _rel(grads[off:off + n], grads_o[off:off + n]) < 5e-2, ("weights", li)
         off += n
@@ -49,8 +51,10 @@ def test_training_reduces_loss():
     from ouranos_gb300.learned import Network
     net = Network(8, 8, 8, seed=3)
     rng = np.random.default_rng(9)
-    feat = torch.from_numpy(rng.standard_normal(8 ** 3 * 3).astype(np.float32)).cuda()
-    target = torch.from_numpy(np.tanh(rng.standard_normal(8 ** 3)).astype(np.float32)).cuda()
+    feat = torch.from_numpy(rng.standard_normal(8 ** 3 * cnn_oracle.FEATURES).astype(np.float32)).cuda()
+    # a continuous target: the network's output is continuous by construction
+    t = cnn_oracle.project(np.tanh(rng.standard_normal((8, 8, 8, cnn_oracle.OUTPUTS))))
+    target = torch.from_numpy(t.reshape(-1).astype(np.float32)).cuda()
     first = net.train_step(feat, target, 1e-3)
     for _ in range(200):
         last = net.train_step(feat, target, 1e-3)
@@ -58,27 +62,84 @@ def test_training_reduces_loss():
 
 
 def test_preconditioner_features_and_target():
-    """Features/targets of a known pair: e constant in space -> cell averages."""
+    """Features/targets of a known pair: e and v constant in space."""
     torch = pytest.importorskip("torch")
+    import ctypes as C
     import ouranos_gb300 as og
     from ouranos_gb300 import learned
     prob = og.thick_3d(seed=2100, n=8, sn=4, block=4, width=2.0)
     L = learned._lib()
+    nf, no = cnn_oracle.FEATURES, cnn_oracle.OUTPUTS
     with og.RadiativeTransfer(prob) as rt:
         e = torch.full((prob.vector_length,), 2.0, dtype=torch.float64, device="cuda")
         v = torch.full_like(e, 0.5)
-        feat = torch.empty(prob.total_cells * 3, dtype=torch.float32, device="cuda")
-        tgt = torch.empty(prob.total_cells, dtype=torch.float32, device="cuda")
-        import ctypes as C
+        feat = torch.empty(prob.total_cells * nf, dtype=torch.float32, device="cuda")
+        tgt = torch.empty(prob.total_cells * no, dtype=torch.float32, device="cuda")
         scale = C.c_double()
         assert L.ouranos_rt_pc_features(rt._h, v.data_ptr(), feat.data_ptr(), C.byref(scale)) == 0
         assert L.ouranos_rt_pc_target(rt._h, v.data_ptr(), e.data_ptr(), tgt.data_ptr()) == 0
-        f = feat.cpu().numpy().reshape(-1, 3)
+        f = feat.cpu().numpy().reshape(-1, nf)
         assert abs(scale.value - 0.5) < 1e-12
-        assert np.allclose(f[:, 0], 1.0, rtol=1e-6)
+        assert np.allclose(f[:, :8], 1.0, rtol=1e-6)
         st = prob.sigma_t[prob.material_id, 0]
-        assert np.allclose(f[:, 1], np.log(st) / np.log(100.0), rtol=1e-6)
-        assert np.allclose(tgt.cpu().numpy(), (2.0 - 0.5) / 0.5, rtol=1e-6)
+        ss = prob.sigma_s[prob.material_id, 0, 0, 0]
+        assert np.allclose(f[:, 8], np.log(st) / np.log(100.0), rtol=1e-6)
+        assert np.allclose(f[:, 9], ss / st, rtol=1e-6)
+        # K = 64; the projection leaves a constant field unchanged
+        assert np.allclose(tgt.cpu().numpy(), (2.0 - 0.5) / 0.5 / 64.0, rtol=1e-6)
+
+
+def test_preconditioner_nodal_features_follow_the_dofs():
+    """Each cell's eight feature channels are its eight scalar-moment dofs over
+    the RMS of the vector; the correction lands on the same dofs."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    import ouranos_gb300 as og
+    from ouranos_gb300 import learned
+    prob = og.thick_3d(seed=2102, n=8, sn=4, block=4, width=2.0)
+    L = learned._lib()
+    nf = cnn_oracle.FEATURES
+    rng = np.random.default_rng(4)
+    vh = rng.standard_normal(prob.vector_length)
+    with og.RadiativeTransfer(prob) as rt:
+        v = torch.from_numpy(vh).cuda()
+        feat = torch.empty(prob.total_cells * nf, dtype=torch.float32, device="cuda")
+        scale = C.c_double()
+        assert L.ouranos_rt_pc_features(rt._h, v.data_ptr(), feat.data_ptr(), C.byref(scale)) == 0
+        s = np.sqrt(np.mean(vh[:prob.total_cells * 8] ** 2))
+        assert abs(scale.value - s) < 1e-12 * s
+        f = feat.cpu().numpy().reshape(-1, nf)
+        assert np.allclose(f[:, :8], (vh[:prob.total_cells * 8] / s).reshape(-1, 8), rtol=1e-6, atol=1e-6)
+        # the target is the continuity projection of (e - v) / (s K)
+        eh = rng.standard_normal(prob.vector_length)
+        e = torch.from_numpy(eh).cuda()
+        tgt = torch.empty(prob.total_cells * 8, dtype=torch.float32, device="cuda")
+        assert L.ouranos_rt_pc_target(rt._h, v.data_ptr(), e.data_ptr(), tgt.data_ptr()) == 0
+        d = ((eh - vh)[:prob.total_cells * 8] / (s * 64.0)).reshape(8, 8, 8, 8)
+        want = cnn_oracle.project(d).reshape(-1)
+        assert _rel(tgt.cpu().numpy(), want) < 1e-6
+        # a zero network output leaves the vector unchanged
+        net = learned.Network(8, 8, 8, seed=9)
+        net.set_params(np.zeros(net.n_params, dtype=np.float32))
+        learned.install(rt, net)
+        z = torch.empty_like(v)
+        assert L.ouranos_rt_pc_apply(rt._h, v.data_ptr(), z.data_ptr()) == 0
+        assert torch.equal(z, v)
+
+
+def test_preconditioner_rejects_unsupported_meshes():
+    pytest.importorskip("torch")
+    import ouranos_gb300 as og
+    from ouranos_gb300 import _capi, learned
+    net = learned.Network(8, 8, 8, seed=2)
+    with og.RadiativeTransfer(og.heterogeneous_2d(seed=5, n=16, fe_order=1, sn=4, l_max=0)) as rt:
+        with pytest.raises(_capi.OuranosError) as ei:
+            learned.install(rt, net)
+        assert ei.value.code == _capi.ERR_UNSUPPORTED
+    with og.RadiativeTransfer(og.thick_3d(seed=2103, n=12, sn=4, block=4, width=2.0)) as rt:
+        with pytest.raises(_capi.OuranosError) as ei:
+            learned.install(rt, net)
+        assert ei.value.code == _capi.ERR_BAD_INPUT
 
 
 def test_learned_fgmres_converges_and_falls_back():

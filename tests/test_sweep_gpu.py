@@ -212,6 +212,30 @@ def test_device_pointers():
     assert rel_err(yd.cpu().numpy(), ref) < TOL64
 
 
+def test_device_input_written_just_before_the_call():
+    """A device vector whose last write is still queued on the default stream
+    (behind a long kernel) when Apply is called is read complete: the handle's
+    stream is ordered after the caller's earlier default-stream work."""
+    torch = pytest.importorskip("torch")
+    import ouranos_gb300 as og
+    prob = og.config_small(n=16, sn=4)
+    x = np.random.default_rng(3).standard_normal(prob.vector_length)
+    ref = po.OracleProblem(prob.arrays()).apply(x)
+    src = torch.from_numpy(x).cuda()
+    big = torch.randn(4096, 4096, device="cuda")
+    torch.cuda.synchronize()
+    with og.RadiativeTransfer(prob) as rt:
+        for _ in range(3):
+            xd = torch.zeros_like(src)
+            yd = torch.empty_like(src)
+            for _ in range(8):
+                big = big @ big
+                big = big / big.norm()
+            xd.copy_(src)  # queued behind the matmuls
+            rt.Apply(xd, yd)
+            assert rel_err(yd.cpu().numpy(), ref) < TOL64
+
+
 def test_wait_timeout_reports_error_and_recovers():
     """A dependency wait that cannot be satisfied (target biased past the end)
     runs out after the wait limit: the call returns OURANOS_ERR_TIMEOUT, no
