@@ -222,6 +222,38 @@ typedef struct ouranos_solve_info {
 int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it, double tol,
                   const double* group_flux, double* x, double* hist, ouranos_solve_info* info);
 
+/* ------------------------------------------------------- many problems
+ * No counterpart in the reference, which runs one problem per MPI job
+ * (src/ouranos.cc:43-209).  A batch holds `count` independent problems
+ * (descs is an array of count descriptions); its vectors are the problems'
+ * [mom][dof] vectors one after another (ouranos_batch_layout gives the
+ * offsets).  A batched Apply runs every problem's sweep in one persistent
+ * launch per (dimension, FE order, fused-moment form) class and is captured
+ * into a CUDA graph on its second use, replayed after (ouranos_batch_set_graphs
+ * switches that off).  Pointers may be host or device; calls return after the
+ * result is written.  One batch is not thread-safe, like a single handle. */
+typedef struct ouranos_batch ouranos_batch;
+int ouranos_batch_create(const ouranos_problem_desc* descs, int count, int device, ouranos_batch** out);
+int ouranos_batch_destroy(ouranos_batch* b);
+/* count, total vector length and offsets[count + 1] (each may be NULL) */
+int ouranos_batch_layout(const ouranos_batch* b, int* count, long* total_length, long* offsets);
+/* y = x - D L^-1 M2D S x for every problem, sweeps in `precision` */
+int ouranos_batch_apply(ouranos_batch* b, int precision, const double* x, double* y);
+/* rhs = D L^-1 (q + inflow) for every problem (FP64) */
+int ouranos_batch_rhs(ouranos_batch* b, double* rhs);
+/* restarted GMRES on every problem at once: inner = OURANOS_FP32 (FP32 Arnoldi
+ * sweeps, FP64 restarts) or OURANOS_FP64; info[count]; NOT_CONVERGED if any
+ * problem missed tol within max_it */
+int ouranos_batch_solve(ouranos_batch* b, int inner, int restart, int max_it, double tol, double* x,
+                        ouranos_solve_info* info);
+/* time the warp tilings of each problem's sweep in `precision` (reps timed
+ * runs each), keep the fastest; tiling (may be NULL) gets count x 3 ints */
+int ouranos_batch_autotune(ouranos_batch* b, int precision, int reps, int* tiling);
+int ouranos_batch_set_graphs(ouranos_batch* b, int enable);
+/* device time of the last batched sweep launches, graph launches so far */
+int ouranos_batch_stats(const ouranos_batch* b, double* last_sweep_ms, int* graph_launches);
+int ouranos_batch_last_error(const ouranos_batch* b, char* buf, size_t len);
+
 /* ------------------------------------------------- learned preconditioner
  * No counterpart in the reference (its Krylov solves use an identity
  * preconditioner, src/ouranos.cc:160-171).  A 3-D convolutional network on the

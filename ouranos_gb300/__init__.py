@@ -6,8 +6,9 @@ from . import _capi
 from .problem import (Problem, Quadrature, SplitMix64, batch_2d, build_quadrature, config_small,
                       heterogeneous_2d, thick_3d, time_dependent_3d, uniform_problem, zorder_cells)
 from .transport import RadiativeTransfer
+from .batch import Batch
 
-__all__ = ["Problem", "Quadrature", "SplitMix64", "RadiativeTransfer", "build_quadrature",
+__all__ = ["Problem", "Quadrature", "SplitMix64", "RadiativeTransfer", "Batch", "build_quadrature",
            "config_small", "heterogeneous_2d", "thick_3d", "batch_2d", "time_dependent_3d",
            "uniform_problem", "zorder_cells"]
 

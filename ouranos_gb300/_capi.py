@@ -39,6 +39,9 @@ EXPORTS = [
     "ouranos_cnn_set_params", "ouranos_cnn_forward", "ouranos_cnn_gradients",
     "ouranos_cnn_train_step", "ouranos_cnn_last_error", "ouranos_rt_set_preconditioner",
     "ouranos_rt_pc_features", "ouranos_rt_pc_target", "ouranos_rt_pc_apply",
+    "ouranos_batch_create", "ouranos_batch_destroy", "ouranos_batch_layout", "ouranos_batch_apply",
+    "ouranos_batch_rhs", "ouranos_batch_solve", "ouranos_batch_autotune", "ouranos_batch_set_graphs",
+    "ouranos_batch_stats", "ouranos_batch_last_error",
 ]
 
 
@@ -106,6 +109,16 @@ def lib():
         "ouranos_rt_debug_wait_bias": [vp, i],
         "ouranos_solve": [vp, i, i, i, d, vp, vp, vp, C.POINTER(SolveInfo)],
         "ouranos_rt_apply_noalloc": [vp, vp, vp],
+        "ouranos_batch_create": [C.POINTER(ProblemDesc), i, i, C.POINTER(vp)],
+        "ouranos_batch_destroy": [vp],
+        "ouranos_batch_layout": [vp, C.POINTER(i), C.POINTER(l), vp],
+        "ouranos_batch_apply": [vp, i, vp, vp],
+        "ouranos_batch_rhs": [vp, vp],
+        "ouranos_batch_solve": [vp, i, i, i, d, vp, vp],
+        "ouranos_batch_autotune": [vp, i, i, vp],
+        "ouranos_batch_set_graphs": [vp, i],
+        "ouranos_batch_stats": [vp, C.POINTER(d), C.POINTER(i)],
+        "ouranos_batch_last_error": [vp, C.c_char_p, sz],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -46,6 +47,20 @@ struct DevBuf {
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) {
+    o.p = nullptr;
+    o.bytes = 0;
+  }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p;
+      bytes = o.bytes;
+      o.p = nullptr;
+      o.bytes = 0;
+    }
+    return *this;
+  }
   ~DevBuf() { release(); }
   void release() {
     if (p) cudaFree(p);
@@ -103,6 +118,13 @@ struct SweepArgs {
 template <typename real>
 cudaError_t launch_sweep(int dim, int p1, int fused_moments, const SweepArgs<real>& a, int grid,
                          int block, cudaStream_t s);
+// Many problems in one persistent launch: args[p] per problem, tmap[t] =
+// (problem, task) for ticket t, epoch read from the device (all problems of
+// the launch share it), ticket reset to 0 by the caller.
+template <typename real>
+cudaError_t launch_sweep_batch(int dim, int p1, int fused_moments, const SweepArgs<real>* args,
+                               const int2* tmap, int n_total, int* ticket, const int* status,
+                               const unsigned* epoch, int grid, int block, cudaStream_t s);
 // q[d][e] = sum_m M2D[d][m] T[m][e] (+ iso[e])  -- moment -> direction expansion
 template <typename real>
 cudaError_t launch_expand_source(const real* T, const real* iso, const real* m2d, real* q,
@@ -133,10 +155,53 @@ cudaError_t launch_combine(const double* x, const real* phi, double* y, long len
 cudaError_t launch_permute(const double* in, double* out, const long* order, long n_cells,
                            int n, int n_vec, int to_internal, cudaStream_t s);
 cudaError_t launch_axpby(double a, const double* x, double b, double* y, long len, cudaStream_t s);
+// w += scale * sum_j coef[j] V[j] (coefficients on the device)
+cudaError_t launch_multi_axpy(const double* const* V, int k, const double* coef, double scale,
+                              double* w, long len, cudaStream_t s);
+cudaError_t launch_bump_epoch(unsigned* epoch, cudaStream_t s);
+cudaError_t launch_scale_inv_norm(const double* nrm2, double* v, long len, cudaStream_t s);
 constexpr int kDotGrid = 304;  // blocks of the dot-product kernel (2 per SM)
 cudaError_t launch_dots(const double* const* xs, const double* y, int k, long len, double* out,
                         double* partial, unsigned int* done, cudaStream_t s);
 
+}  // namespace ouranos
+namespace ouranos {
+// Least squares of restarted GMRES on the host: the (m+1) x m Hessenberg
+// matrix reduced by Givens rotations as columns arrive; g is the rotated
+// right-hand side beta e_1, |g[k+1]| the residual estimate after k+1 columns.
+struct Givens {
+  int m;
+  std::vector<double> H, cs, sn, g;
+  explicit Givens(int m_) : m(m_), H((m_ + 1) * m_, 0.0), cs(m_), sn(m_), g(m_ + 1, 0.0) {}
+  double& h(int i, int j) { return H[i * m + j]; }
+  // column k of H holds h[0..k+1]; returns |g_{k+1}|
+  double add_column(int k, const double* col) {
+    for (int i = 0; i <= k + 1; ++i) h(i, k) = col[i];
+    for (int j = 0; j < k; ++j) {
+      const double a = h(j, k), b = h(j + 1, k);
+      h(j, k) = cs[j] * a + sn[j] * b;
+      h(j + 1, k) = -sn[j] * a + cs[j] * b;
+    }
+    const double a = h(k, k), b = h(k + 1, k);
+    const double r = std::hypot(a, b);
+    cs[k] = r > 0 ? a / r : 1.0;
+    sn[k] = r > 0 ? b / r : 0.0;
+    h(k, k) = r;
+    h(k + 1, k) = 0.0;
+    g[k + 1] = -sn[k] * g[k];
+    g[k] = cs[k] * g[k];
+    return std::fabs(g[k + 1]);
+  }
+  std::vector<double> solve(int k) {
+    std::vector<double> y(k, 0.0);
+    for (int i = k - 1; i >= 0; --i) {
+      double s = g[i];
+      for (int j = i + 1; j < k; ++j) s -= h(i, j) * y[j];
+      y[i] = h(i, i) != 0.0 ? s / h(i, i) : 0.0;
+    }
+    return y;
+  }
+};
 }  // namespace ouranos
 struct ouranos_rt;
 struct ouranos_cnn;
@@ -150,6 +215,10 @@ void cnn_grid(const ouranos_cnn* net, int* nx, int* ny, int* nz);
 int rt_apply_device(ouranos_rt* rt, const double* x, double* y);
 int rt_rhs_device(ouranos_rt* rt, const double* gf, double* rhs);
 int rt_check_status(ouranos_rt* rt);
+// batched Apply pieces (see operator.cu)
+int rt_batch_prepare(ouranos_rt* rt, const double* x, SweepArgs<double>* a, int* fm, bool sources);
+int rt_batch_prepare(ouranos_rt* rt, const double* x, SweepArgs<float>* a, int* fm, bool sources);
+int rt_batch_finish(ouranos_rt* rt, const double* x, double* y, bool sources);
 int rt_clear_status(ouranos_rt* rt);
 int rt_stage_in(ouranos_rt* rt, const double* v, DevBuf& buf, int n_vec, const double** out);
 int rt_stage_out(ouranos_rt* rt, const double* dv, double* user);

@@ -204,9 +204,12 @@ int setup_group(ouranos_rt* rt) {
 // the moment axis that streams better than a per-step loop over moments).
 constexpr int kFusedMomentsMax = 2;
 
+// Sweep arguments for one problem (pointers into the handle's buffers) and,
+// when the source is expanded (fm = 0), the expansion launch.  Epoch, ticket
+// and status are left for the caller.
 template <typename real>
-int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd, real* phi) {
-  SweepArgs<real> a;
+int sweep_prepare(ouranos_rt* rt, const real* src, const real* iso, const real* bnd, SweepArgs<real>& a,
+                  int& fm, int& kernels) {
   const bool f64 = sizeof(real) == 8;
   const long len_dir = (long)rt->n_dir * rt->n_dofs;
   a.nx = rt->nx[0];
@@ -239,18 +242,14 @@ int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd,
   a.psi = rt->d_psi.as<real>();
   a.edge_x = rt->d_edge_x.as<unsigned long long>();
   a.edge_y = rt->d_edge_y.as<unsigned long long>();
-  // epochs cycle through [1, 0x7fff]; every sweep rewrites every edge word it
-  // reads, so a stale word carries the previous epoch and never matches
-  rt->epoch = rt->epoch % 0x7fffu + 1u;
-  a.epoch = rt->epoch;
-  int* ctrl = rt->d_ctrl.as<int>();
-  a.ticket = ctrl;
-  a.status = ctrl + 1;
   a.wait_limit_ns = rt->wait_limit_ns;
   a.wait_bias = rt->wait_bias;
-  int kernels = 0;
+  a.epoch = 0;
+  a.ticket = nullptr;
+  a.status = nullptr;
+  kernels = 0;
   // (the fused form holds (moments + 1) prefetched values per dof in registers)
-  const int fm = (rt->n_mom <= kFusedMomentsMax && rt->n * (rt->n_mom + 1) <= 32) ? rt->n_mom : 0;
+  fm = (rt->n_mom <= kFusedMomentsMax && rt->n * (rt->n_mom + 1) <= 32) ? rt->n_mom : 0;
   if (fm == 0) {
     CU(rt->d_q.alloc(sizeof(real) * len_dir), "expanded source");
     if (f64 && rt->fp64_contract == OURANOS_FP64_DF64)
@@ -265,6 +264,36 @@ int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd,
     kernels += (rt->n_mom + 15) / 16;
     a.q = rt->d_q.as<real>();
   }
+  return OURANOS_OK;
+}
+
+// phi = D2M psi (the moment reduction after a sweep)
+template <typename real>
+int sweep_reduce(ouranos_rt* rt, const real* psi, real* phi) {
+  const bool f64 = sizeof(real) == 8;
+  if (f64 && rt->fp64_contract == OURANOS_FP64_DF64)
+    CU(launch_reduce_moments_df64((const double*)psi, rt->d_d2m64.as<double>(), (double*)phi,
+                                  rt->n_dir, rt->n_mom, rt->n_dofs, rt->stream),
+       "moment reduction");
+  else
+    CU(launch_reduce_moments<real>(psi, (const real*)(f64 ? rt->d_d2m64.p : rt->d_d2m32.p), phi,
+                                   rt->n_dir, rt->n_mom, rt->n_dofs, rt->stream),
+       "moment reduction");
+  return OURANOS_OK;
+}
+
+template <typename real>
+int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd, real* phi) {
+  SweepArgs<real> a;
+  int fm = 0, kernels = 0;
+  OK_OR_RETURN(sweep_prepare<real>(rt, src, iso, bnd, a, fm, kernels));
+  // epochs cycle through [1, 0x7fff]; every sweep rewrites every edge word it
+  // reads, so a stale word carries the previous epoch and never matches
+  rt->epoch = rt->epoch % 0x7fffu + 1u;
+  a.epoch = rt->epoch;
+  int* ctrl = rt->d_ctrl.as<int>();
+  a.ticket = ctrl;
+  a.status = ctrl + 1;
   // ticket -> 0.  The status word [1] is sticky: it is cleared at the start of
   // each C-ABI call (clear_status), so a timeout inside a solve is seen at its
   // end and every later sweep of that call exits at once.  The dot counter at
@@ -280,14 +309,7 @@ int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd,
   CU(launch_sweep<real>(rt->dim, rt->p1, fm, a, grid, block, rt->stream), "sweep launch");
   CU(cudaEventRecord(rt->ev1, rt->stream), "event");
   ++kernels;
-  if (f64 && rt->fp64_contract == OURANOS_FP64_DF64)
-    CU(launch_reduce_moments_df64((const double*)a.psi, rt->d_d2m64.as<double>(), (double*)phi,
-                                  rt->n_dir, rt->n_mom, rt->n_dofs, rt->stream),
-       "moment reduction");
-  else
-    CU(launch_reduce_moments<real>(a.psi, (const real*)(f64 ? rt->d_d2m64.p : rt->d_d2m32.p), phi,
-                                   rt->n_dir, rt->n_mom, rt->n_dofs, rt->stream),
-       "moment reduction");
+  OK_OR_RETURN(sweep_reduce<real>(rt, a.psi, phi));
   kernels += (rt->n_mom + 15) / 16;
   rt->last_kernels = kernels;
   return OURANOS_OK;
@@ -445,6 +467,48 @@ int rt_rhs_device(ouranos_rt* rt, const double* gf, double* rhs) {
   OK_OR_RETURN(build_source(rt, nullptr, gf));
   OK_OR_RETURN(sweep_into_phi(rt, true));
   return phi_combine(rt, nullptr, rhs, 0.0, 1.0);
+}
+// Batched Apply pieces (batch.cu): the per-problem work before and after the
+// batched sweep launch.  prepare: the source terms in the sweep precision --
+// the scattering source of x, or with `sources` the fixed source and inflow
+// (no scattering) -- and the problem's sweep arguments (plus the source
+// expansion when the sweep reads expanded sources); finish: the moment
+// reduction and y = x - phi, or y = phi with `sources`.
+template <typename real>
+static int batch_prepare(ouranos_rt* rt, const double* x, SweepArgs<real>* a, int* fm, bool sources) {
+  const bool f64 = sizeof(real) == 8;
+  rt->precision = f64 ? OURANOS_FP64 : OURANOS_FP32;
+  OK_OR_RETURN(build_source(rt, sources ? nullptr : x, nullptr));
+  const long len = vec_len(rt);
+  if (f64) CU(rt->d_phi64.alloc(sizeof(double) * len), "flux");
+  else CU(rt->d_phi32.alloc(sizeof(float) * len), "flux");
+  const real* iso = nullptr;
+  const real* bnd = nullptr;
+  if (sources) {
+    DevBuf& ib = f64 ? rt->d_iso64 : rt->d_iso32;
+    CU(ib.alloc(sizeof(real) * rt->n_dofs), "iso");
+    CU(launch_iso_source<real>(ib.as<real>(), rt->d_qcell.as<double>(), rt->d_rowsum_mass.as<double>(),
+                               rt->d_source_id.as<int>(), rt->n_cells, rt->n, rt->stream),
+       "iso source");
+    iso = ib.as<real>();
+    bnd = (const real*)(f64 ? rt->d_bnd64.p : rt->d_bnd32.p);
+  }
+  int kernels = 0;
+  const real* src = (const real*)(f64 ? rt->d_src64.p : rt->d_src32.p);
+  return sweep_prepare<real>(rt, src, iso, bnd, *a, *fm, kernels);
+}
+int rt_batch_prepare(ouranos_rt* rt, const double* x, SweepArgs<double>* a, int* fm, bool sources) {
+  return batch_prepare<double>(rt, x, a, fm, sources);
+}
+int rt_batch_prepare(ouranos_rt* rt, const double* x, SweepArgs<float>* a, int* fm, bool sources) {
+  return batch_prepare<float>(rt, x, a, fm, sources);
+}
+int rt_batch_finish(ouranos_rt* rt, const double* x, double* y, bool sources) {
+  if (rt->precision == OURANOS_FP64)
+    OK_OR_RETURN(sweep_reduce<double>(rt, rt->d_psi.as<double>(), rt->d_phi64.as<double>()));
+  else
+    OK_OR_RETURN(sweep_reduce<float>(rt, rt->d_psi.as<float>(), rt->d_phi32.as<float>()));
+  return sources ? phi_combine(rt, nullptr, y, 0.0, 1.0) : phi_combine(rt, x, y, 1.0, -1.0);
 }
 int rt_check_status(ouranos_rt* rt) { return finish(rt); }
 int rt_clear_status(ouranos_rt* rt) { return clear_status(rt); }

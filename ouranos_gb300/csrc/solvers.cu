@@ -14,11 +14,6 @@
 
 using namespace ouranos;
 
-namespace ouranos {
-cudaError_t launch_multi_axpy(const double* const* V, int k, const double* coef, double scale,
-                              double* w, long len, cudaStream_t s);
-}
-
 namespace {
 
 #define RC(expr)                       \
@@ -128,40 +123,6 @@ int apply_prec(ouranos_rt* rt, int precision, const double* x, double* y) {
   rt->precision = saved;
   return rc;
 }
-
-struct Givens {
-  int m;
-  std::vector<double> H, cs, sn, g;
-  explicit Givens(int m_) : m(m_), H((m_ + 1) * m_, 0.0), cs(m_), sn(m_), g(m_ + 1, 0.0) {}
-  double& h(int i, int j) { return H[i * m + j]; }
-  // column k of H holds h[0..k+1]; returns |g_{k+1}|
-  double add_column(int k, const double* col) {
-    for (int i = 0; i <= k + 1; ++i) h(i, k) = col[i];
-    for (int j = 0; j < k; ++j) {
-      const double a = h(j, k), b = h(j + 1, k);
-      h(j, k) = cs[j] * a + sn[j] * b;
-      h(j + 1, k) = -sn[j] * a + cs[j] * b;
-    }
-    const double a = h(k, k), b = h(k + 1, k);
-    const double r = std::hypot(a, b);
-    cs[k] = r > 0 ? a / r : 1.0;
-    sn[k] = r > 0 ? b / r : 0.0;
-    h(k, k) = r;
-    h(k + 1, k) = 0.0;
-    g[k + 1] = -sn[k] * g[k];
-    g[k] = cs[k] * g[k];
-    return std::fabs(g[k + 1]);
-  }
-  std::vector<double> solve(int k) {
-    std::vector<double> y(k, 0.0);
-    for (int i = k - 1; i >= 0; --i) {
-      double s = g[i];
-      for (int j = i + 1; j < k; ++j) s -= h(i, j) * y[j];
-      y[i] = h(i, i) != 0.0 ? s / h(i, i) : 0.0;
-    }
-    return y;
-  }
-};
 
 // x += sum_j y_j Z_{first+j}
 int update(Work& w, int first, const std::vector<double>& y, double* x) {

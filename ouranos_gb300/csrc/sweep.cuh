@@ -172,15 +172,17 @@ struct Stream {
   static constexpr size_t warp_bytes = (size_t)kRing * 32 * (NV * sizeof(real) + sizeof(int));
 };
 
+// One task: a tile of wx x wy columns for kd directions, swept over the whole
+// sweep axis.  Shared by the single-problem and the batched kernels.
 template <typename real, int DIM, int P1, int FM>
-__global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
+__device__ __forceinline__ void sweep_task(const SweepArgs<real>& a, const int task,
+                                           unsigned char* smem_raw) {
   using C = Cell<DIM, P1>;
   constexpr int N = C::N;
   constexpr int FD = C::FD;
   constexpr int NV = Stream<real, FM, N>::NV;
   constexpr int W = Tagged<real>::W;
   constexpr unsigned FULL = 0xffffffffu;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   real* ring = reinterpret_cast<real*>(smem_raw + warp * Stream<real, FM, N>::warp_bytes);
@@ -197,17 +199,7 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
   const int nsteps = NS + (a.wx - 1) + (a.wy - 1);
   constexpr int AS = DIM - 1;  // physical axis of the sweep direction
   const unsigned want_epoch = a.epoch ^ (a.wait_bias ? 0x8000u : 0u);
-
-  for (;;) {
-    int task = 0, stop = 0;
-    if (lane == 0) {
-      task = atomicAdd(a.ticket, 1);
-      stop = *(volatile int*)a.status;
-    }
-    task = __shfl_sync(FULL, task, 0);
-    stop = __shfl_sync(FULL, stop, 0);
-    if (task >= a.n_tasks || stop) return;
-
+  {
     const int2 tk = a.tasks[task];
     const int grp = tk.x, tile = tk.y;
     const int tx = tile % a.tiles_x, ty = tile / a.tiles_x;
@@ -399,6 +391,65 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
   }
 }
 
+// Single problem: warps take tasks in ticket order (level-major), so every
+// task a warp waits on was taken earlier by a running warp -- any grid is
+// deadlock-free.
+template <typename real, int DIM, int P1, int FM>
+__global__ void __launch_bounds__(128) sweep_kernel(const __grid_constant__ SweepArgs<real> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr unsigned FULL = 0xffffffffu;
+  for (;;) {
+    int task = 0, stop = 0;
+    if ((threadIdx.x & 31) == 0) {
+      task = atomicAdd(a.ticket, 1);
+      stop = *(volatile int*)a.status;
+    }
+    task = __shfl_sync(FULL, task, 0);
+    stop = __shfl_sync(FULL, stop, 0);
+    if (task >= a.n_tasks || stop) return;
+    sweep_task<real, DIM, P1, FM>(a, task, smem_raw);
+  }
+}
+
+// Many problems in one persistent launch.  Ticket t names (problem, task) =
+// tmap[t]; the map lists each problem's tasks in its own order, interleaved
+// across problems, so the in-order argument above still holds.  A warp copies
+// its task's problem arguments into its shared slot before the task; the
+// edge-word epoch comes from device memory, so a captured launch replays with
+// the epoch of the moment.
+template <typename real, int DIM, int P1, int FM>
+__global__ void __launch_bounds__(128) sweep_batch_kernel(const SweepArgs<real>* __restrict__ args,
+                                                          const int2* __restrict__ tmap, int n_total,
+                                                          int* ticket, const int* status,
+                                                          const unsigned* epoch) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ SweepArgs<real> s_args[4];
+  static_assert(sizeof(SweepArgs<real>) % 4 == 0, "argument block is copied by words");
+  constexpr int WORDS = (int)(sizeof(SweepArgs<real>) / 4);
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  for (;;) {
+    int t = 0, stop = 0;
+    if (lane == 0) {
+      t = atomicAdd(ticket, 1);
+      stop = *(volatile const int*)status;
+    }
+    t = __shfl_sync(FULL, t, 0);
+    stop = __shfl_sync(FULL, stop, 0);
+    if (t >= n_total || stop) return;
+    const int2 pt = tmap[t];
+    const unsigned* src = reinterpret_cast<const unsigned*>(args + pt.x);
+    unsigned* dst = reinterpret_cast<unsigned*>(&s_args[warp]);
+    for (int i = lane; i < WORDS; i += 32) dst[i] = src[i];
+    __syncwarp();
+    if (lane == 0) s_args[warp].epoch = *epoch;  // set on the device before the launch
+    __syncwarp();
+    sweep_task<real, DIM, P1, FM>(s_args[warp], pt.y, smem_raw);
+    __syncwarp();  // the slot is rewritten by the next task
+  }
+}
+
 template <typename real, int DIM, int P1, int FM>
 cudaError_t launch_sweep_fm(const SweepArgs<real>& a, int grid, int block, cudaStream_t s) {
   constexpr int N = Cell<DIM, P1>::N;
@@ -412,6 +463,33 @@ cudaError_t launch_sweep_fm(const SweepArgs<real>& a, int grid, int block, cudaS
   }
   sweep_kernel<real, DIM, P1, FM><<<grid, block, smem, s>>>(a);
   return cudaGetLastError();
+}
+
+template <typename real, int DIM, int P1, int FM>
+cudaError_t launch_sweep_batch_fm(const SweepArgs<real>* args, const int2* tmap, int n_total, int* ticket,
+                                  const int* status, const unsigned* epoch, int grid, int block,
+                                  cudaStream_t s) {
+  constexpr int N = Cell<DIM, P1>::N;
+  const size_t smem = (size_t)(block / 32) * Stream<real, FM, N>::warp_bytes;
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(sweep_batch_kernel<real, DIM, P1, FM>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  sweep_batch_kernel<real, DIM, P1, FM><<<grid, block, smem, s>>>(args, tmap, n_total, ticket, status, epoch);
+  return cudaGetLastError();
+}
+
+template <typename real, int DIM, int P1>
+cudaError_t launch_sweep_batch_impl(int fm, const SweepArgs<real>* args, const int2* tmap, int n_total,
+                                    int* ticket, const int* status, const unsigned* epoch, int grid,
+                                    int block, cudaStream_t s) {
+  if (fm == 0) return launch_sweep_batch_fm<real, DIM, P1, 0>(args, tmap, n_total, ticket, status, epoch, grid, block, s);
+  if (fm == 1) return launch_sweep_batch_fm<real, DIM, P1, 1>(args, tmap, n_total, ticket, status, epoch, grid, block, s);
+  if (fm == 2) return launch_sweep_batch_fm<real, DIM, P1, 2>(args, tmap, n_total, ticket, status, epoch, grid, block, s);
+  return cudaErrorInvalidValue;
 }
 
 template <typename real, int DIM, int P1>

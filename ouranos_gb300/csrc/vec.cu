@@ -410,6 +410,28 @@ cudaError_t launch_multi_axpy(const double* const* V, int k, const double* coef,
   return cudaGetLastError();
 }
 
+namespace {
+// edge-word epochs cycle through [1, 0x7fff] (0 marks a never-written word)
+__global__ void bump_epoch_kernel(unsigned* e) { *e = *e % 0x7fffu + 1u; }
+// v *= 1/sqrt(*nrm2) (0 when the norm is 0)
+__global__ void scale_inv_norm_kernel(const double* nrm2, double* v, long len) {
+  const double n2 = *nrm2;
+  const double sc = n2 > 0.0 ? 1.0 / sqrt(n2) : 0.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < len; i += (long)gridDim.x * blockDim.x)
+    v[i] *= sc;
+}
+}  // namespace
+
+cudaError_t launch_bump_epoch(unsigned* epoch, cudaStream_t s) {
+  bump_epoch_kernel<<<1, 1, 0, s>>>(epoch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scale_inv_norm(const double* nrm2, double* v, long len, cudaStream_t s) {
+  scale_inv_norm_kernel<<<grid_for(len), kBlock, 0, s>>>(nrm2, v, len);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_axpby(double a, const double* x, double b, double* y, long len,
                          cudaStream_t s) {
   axpby_kernel<<<grid_for(len), kBlock, 0, s>>>(a, x, b, y, len);

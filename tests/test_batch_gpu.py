@@ -1,0 +1,118 @@
+"""Many problems in one persistent launch: the batched Apply against the
+single-problem operator (same task code: bit-identical) and the oracle, graph
+replays, the batched solve, the autotuner."""
+import numpy as np
+import pytest
+
+from helpers import rel_err
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+
+def _problems(count=6, seed=31):
+    import ouranos_gb300 as og
+    # small uneven mix: sides, DG orders, quadratures and P1 scattering vary
+    return og.batch_2d(seed=seed, count=count, sides=(8, 16, 24, 40), orders=(1, 2), sns=(4, 8))
+
+
+def _singles(problems, x_slices, precision="fp64"):
+    import ouranos_gb300 as og
+    out = []
+    for p, x in zip(problems, x_slices):
+        with og.RadiativeTransfer(p, precision=precision) as rt:
+            out.append(rt.apply(np.ascontiguousarray(x)))
+    return out
+
+
+def test_batched_apply_is_bit_identical_to_single_problems():
+    import ouranos_gb300 as og
+    probs = _problems()
+    with og.Batch(probs) as b:
+        x = np.random.default_rng(1).standard_normal(b.length)
+        y = b.apply(x)
+        for ys, yb in zip(_singles(probs, b.slices(x)), b.slices(y)):
+            assert np.array_equal(ys, yb)
+        y32 = b.apply(x, precision="fp32")
+        for ys, yb in zip(_singles(probs, b.slices(x), "fp32"), b.slices(y32)):
+            assert np.array_equal(ys, yb)
+
+
+def test_batched_apply_matches_the_oracle():
+    import ouranos_gb300 as og
+    probs = _problems(count=4, seed=33)
+    with og.Batch(probs) as b:
+        x = np.random.default_rng(2).standard_normal(b.length)
+        y = b.apply(x)
+        for p, xs, ys in zip(probs, b.slices(x), b.slices(y)):
+            ref = po.OracleProblem(p.arrays()).apply(np.ascontiguousarray(xs))
+            assert rel_err(ys, ref) < 1e-12
+
+
+def test_graph_replays_equal_eager_and_no_graph_runs():
+    import ouranos_gb300 as og
+    probs = _problems(count=5, seed=35)
+    with og.Batch(probs) as b:
+        x = np.random.default_rng(3).standard_normal(b.length)
+        runs = [b.apply(x) for _ in range(4)]  # eager, capture, replay, replay
+        _, launches = b.stats()
+        assert launches >= 3
+        for r in runs[1:]:
+            assert np.array_equal(r, runs[0])
+        b.set_graphs(False)
+        assert np.array_equal(b.apply(x), runs[0])
+
+
+def test_batched_rhs_matches_single_problems():
+    import ouranos_gb300 as og
+    probs = _problems(count=4, seed=37)
+    with og.Batch(probs) as b:
+        r = b.rhs()
+        for p, rb in zip(probs, b.slices(r)):
+            with og.RadiativeTransfer(p) as rt:
+                assert np.array_equal(rt.rhs(), rb)
+
+
+def test_batched_solve_matches_single_problem_gmres():
+    import ouranos_gb300 as og
+    probs = _problems(count=5, seed=39)
+    with og.Batch(probs) as b:
+        x, infos = b.solve(inner="fp32", tol=1e-8, max_it=1500)
+        x64, infos64 = b.solve(inner="fp64", tol=1e-8, max_it=1500)
+        for p, xs, info in zip(probs, b.slices(x), infos):
+            assert info["converged"] and info["residual"] < 1e-8
+            with og.RadiativeTransfer(p) as rt:
+                xr, ir, _ = rt.solve("gmres", tol=1e-10, max_it=3000)
+            assert rel_err(xs, xr) < 1e-6
+        for xs, xd in zip(b.slices(x), b.slices(x64)):
+            assert rel_err(xs, xd) < 1e-6
+        assert all(i["converged"] for i in infos64)
+
+
+def test_autotune_keeps_results_and_reports_tilings():
+    import ouranos_gb300 as og
+    probs = _problems(count=4, seed=41)
+    with og.Batch(probs) as b:
+        x = np.random.default_rng(4).standard_normal(b.length)
+        before = b.apply(x)
+        t = b.autotune(reps=2)
+        assert t.shape == (4, 3)
+        for cx, cy, kd in t:
+            assert cx * cy * kd == 32
+        after = b.apply(x)
+        for p, xs, ys in zip(probs, b.slices(x), b.slices(after)):
+            ref = po.OracleProblem(p.arrays()).apply(np.ascontiguousarray(xs))
+            assert rel_err(ys, ref) < 1e-12
+        assert rel_err(after, before) < 1e-13
+
+
+def test_device_vectors_through_the_batch():
+    torch = pytest.importorskip("torch")
+    import ouranos_gb300 as og
+    probs = _problems(count=3, seed=43)
+    with og.Batch(probs) as b:
+        xh = np.random.default_rng(5).standard_normal(b.length)
+        yh = b.apply(xh)
+        xd = torch.from_numpy(xh).cuda()
+        yd = b.apply(xd)
+        assert np.array_equal(yd.cpu().numpy(), yh)
