@@ -346,6 +346,76 @@ def run_solve(args):
     print(json.dumps({"solve": out}), flush=True)
 
 
+def run_batch(args):
+    """Batched uneven workload: `count` independent 2-D problems (side drawn
+    from {32, 64, 128, 256, 512}, DG Q1 or Q2, LS S4/S8/S12/S16, P1 scattering
+    with g ~ U[0, 0.8], seeded material maps) behind one batch handle.  Times
+    the batched FP32 Apply (one persistent sweep launch per class, replayed
+    from a CUDA graph) on device vectors and through host vectors, then solves
+    every problem to `tol` with FP32 Arnoldi sweeps and FP64 restarts and with
+    the plain FP64 method."""
+    import time
+    import numpy as np
+    import torch
+    import ouranos_gb300 as og
+    probs = og.batch_2d(seed=args.batch_seed, count=args.batch_count)
+    solves = int(sum(p.total_cells * p.quad.n_dir for p in probs))
+    t0 = time.perf_counter()
+    b = og.Batch(probs)
+    t_create = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    tiling = b.autotune(reps=2)
+    t_tune = time.perf_counter() - t0
+    x = torch.randn(b.length, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+
+    def timed(fn, steps):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        torch.cuda.synchronize()
+        t = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            fn()  # returns after its result is written
+            t.append(time.perf_counter() - t0)
+        return 1e3 * sum(t) / len(t)
+
+    ms_graph = timed(lambda: b.apply(x, "fp32", out=y), args.steps)
+    sweep_ms, graph_launches = b.stats()
+    b.set_graphs(False)
+    ms_eager = timed(lambda: b.apply(x, "fp32", out=y), max(3, args.steps // 4))
+    b.set_graphs(True)
+    xh = x.cpu().numpy()
+    yh = np.empty_like(xh)
+    ms_host = timed(lambda: b.apply(xh, "fp32", out=yh), max(3, args.steps // 4))
+    out = {
+        "metric": "batched FP32 Apply throughput, %d uneven 2-D problems" % len(probs),
+        "value": solves / (ms_graph * 1e-3), "unit": "cell-dir solves/s",
+        "ms_per_apply": ms_graph, "ms_per_apply_no_graph": ms_eager, "ms_per_apply_host_vectors": ms_host,
+        "sweep_ms_last": sweep_ms, "graph_launches": graph_launches,
+        "config": {"workload": "batch-2d-%d-seed%d" % (len(probs), args.batch_seed),
+                   "cell_dir_solves_per_apply": solves, "vector_length": int(b.length),
+                   "create_s": t_create, "autotune_s": t_tune,
+                   "tilings": {"%dx%d/%d" % tuple(t): int(c) for t, c in
+                               zip(*np.unique(tiling, axis=0, return_counts=True))}},
+    }
+    if args.batch_solve:
+        res = {}
+        for inner in ("fp32", "fp64"):
+            xs, infos = b.solve(inner=inner, tol=args.tol, max_it=args.max_it)
+            res[inner] = (xs, infos)
+            its = [i["iterations"] for i in infos]
+            out["solve_" + inner] = {"seconds": infos[0]["seconds"], "converged": sum(i["converged"] for i in infos),
+                                     "iterations_max": max(its), "iterations_mean": float(np.mean(its)),
+                                     "residual_max": max(i["residual"] for i in infos)}
+        x32, x64 = res["fp32"][0], res["fp64"][0]
+        out["solve_fp32"]["flux_rel_l2_vs_fp64_max"] = max(
+            float(np.linalg.norm(a - c) / max(np.linalg.norm(c), 1e-300)) for a, c in zip(b.slices(x32), b.slices(x64)))
+        out["solve_fp32"]["speedup_vs_fp64"] = out["solve_fp64"]["seconds"] / out["solve_fp32"]["seconds"]
+    b.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -361,7 +431,16 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--max-it", type=int, default=3000)
     ap.add_argument("--methods", default="gmres,fgmres_mixed,fgmres_learned")
+    ap.add_argument("--batch", action="store_true", help="batched uneven 2-D workload")
+    ap.add_argument("--batch-count", type=int, default=64)
+    ap.add_argument("--batch-seed", type=int, default=3000)
+    ap.add_argument("--batch-solve", action="store_true")
     args = ap.parse_args()
+    if args.batch:
+        import __graft_entry__
+        __graft_entry__.build()
+        run_batch(args)
+        return
     if args.solve:
         import __graft_entry__
         __graft_entry__.build()
