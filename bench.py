@@ -416,6 +416,51 @@ def run_batch(args):
     print(json.dumps(out), flush=True)
 
 
+def run_time(args):
+    """3-D time-dependent workload: [0,20]^3, 128^3 hexes, DG Q1, LS S8 (80
+    directions), implicit Euler with 1/(v dt) = 0.5, a Gaussian pulse
+    (peak 10 at step 20, width 5 steps) in a seeded 8^3-cell box, two-material
+    map.  Every step is solved to `tol` by FGMRES with FP32 sweeps and FP64
+    restarts, warm-started from the previous step; psi^n is kept in FP32.  The
+    first `time_compare` steps are repeated with plain FP64 GMRES."""
+    import time
+    import numpy as np
+    import ouranos_gb300 as og
+    prob = og.time_dependent_3d(seed=args.time_seed, n=args.time_n)
+    inv_vdt = prob.meta["inv_vdt"]
+    out = {"workload": "3d-td-%d^3-dgq1-ls8-%dsteps" % (args.time_n, args.time_steps), "tol": args.tol,
+           "inv_vdt": inv_vdt}
+
+    def run(method, steps):
+        with og.RadiativeTransfer(prob) as rt:
+            rt.set_time_step(inv_vdt)
+            phi = np.zeros(rt.length)
+            its, secs = [], []
+            t0 = time.perf_counter()
+            for n in range(steps):
+                rt.set_source([[0.0], [og.pulse_strength(n)]])
+                info = rt.time_advance(phi, method=method, tol=args.tol, max_it=args.max_it)
+                its.append(info["iterations"])
+                secs.append(info["seconds"])
+            wall = time.perf_counter() - t0
+            return phi, its, secs, wall
+
+    phi, its, secs, wall = run("fgmres_mixed", args.time_steps)
+    out["fgmres_mixed"] = {"wall_s": wall, "s_per_step": wall / args.time_steps,
+                           "iterations_total": int(sum(its)), "iterations_max": int(max(its)),
+                           "iterations_at_peak": int(its[min(20, len(its) - 1)]),
+                           "scalar_flux_max_final": float(phi.max())}
+    if args.time_compare:
+        k = min(args.time_compare, args.time_steps)
+        p32, i32, s32, w32 = run("fgmres_mixed", k)
+        p64, i64, s64, w64 = run("gmres", k)
+        out["compare_first_steps"] = {
+            "steps": k, "fgmres_mixed_s": w32, "gmres_fp64_s": w64, "speedup": w64 / w32,
+            "iterations_fp32": int(sum(i32)), "iterations_fp64": int(sum(i64)),
+            "flux_rel_l2_vs_fp64": float(np.linalg.norm(p32 - p64) / max(np.linalg.norm(p64), 1e-300))}
+    print(json.dumps({"time": out}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -435,7 +480,17 @@ def main():
     ap.add_argument("--batch-count", type=int, default=64)
     ap.add_argument("--batch-seed", type=int, default=3000)
     ap.add_argument("--batch-solve", action="store_true")
+    ap.add_argument("--time", action="store_true", help="time-dependent 3-D workload")
+    ap.add_argument("--time-n", type=int, default=128)
+    ap.add_argument("--time-steps", type=int, default=100)
+    ap.add_argument("--time-seed", type=int, default=4000)
+    ap.add_argument("--time-compare", type=int, default=5)
     args = ap.parse_args()
+    if args.time:
+        import __graft_entry__
+        __graft_entry__.build()
+        run_time(args)
+        return
     if args.batch:
         import __graft_entry__
         __graft_entry__.build()

@@ -207,6 +207,8 @@ int ouranos_rt_apply_noalloc(ouranos_rt* rt, const double* x, double* y);
  * ouranos_rt_set_preconditioner; falls back to the plain method for the rest of
  * the solve when a preconditioned restart cycle stagnates. */
 #define OURANOS_SOLVER_FGMRES_LEARNED 4
+/* OR into the solver: x holds the initial guess (not with BiCGSTAB) */
+#define OURANOS_SOLVER_WARM_START 0x100
 
 typedef struct ouranos_solve_info {
   int iterations;           /* operator applications in the Krylov/SI loop */
@@ -221,6 +223,25 @@ typedef struct ouranos_solve_info {
  * receives max_it+1 relative residuals. */
 int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it, double tol,
                   const double* group_flux, double* x, double* hist, ouranos_solve_info* info);
+
+/* ------------------------------------------------------- time dependence
+ * Implicit Euler in time.  No counterpart in the reference operator (its
+ * TimeDiscretization class, src/TimeDiscretization.cc:10-82, is never
+ * called).  With inv_vdt = 1/(v dt) > 0 each step solves
+ *   Omega.grad psi + (sigma_t + inv_vdt) psi = S phi + q/ws + inv_vdt psi^n
+ * and keeps psi^n (FP32, [dir][dof]) on the device, starting from 0; 0
+ * switches it off.  sigma_t in the description stays the physical one. */
+int ouranos_rt_set_time_step(ouranos_rt* rt, double inv_vdt);
+/* replace the fixed-source strengths ([n_sources][n_groups]), e.g. a pulse */
+int ouranos_rt_set_source(ouranos_rt* rt, const double* source);
+/* one step: phi in = initial guess (phi^n), out = phi^{n+1}; then psi^n
+ * advances by one FP64 source sweep of phi^{n+1}, stored in FP32 (only after
+ * convergence) */
+int ouranos_rt_time_advance(ouranos_rt* rt, int solver, int restart, int max_it, double tol, double* phi,
+                            ouranos_solve_info* info);
+/* psi^n as doubles, [dir][dof] with lexicographic cells: checkpoint / resume */
+int ouranos_rt_get_angular_flux(ouranos_rt* rt, double* psi);
+int ouranos_rt_set_angular_flux(ouranos_rt* rt, const double* psi);
 
 /* ------------------------------------------------------- many problems
  * No counterpart in the reference, which runs one problem per MPI job

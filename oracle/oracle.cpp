@@ -142,6 +142,10 @@ struct orc_problem {
   std::vector<long> last_order;
   /* state */
   std::vector<double> scat;                    // [mom][dof]
+  /* implicit Euler (an extension, see orc_set_time_step): sigma_t shift and psi^n */
+  double inv_vdt = 0.0;
+  std::vector<double> psi_prev;                // [dir][dof]
+  std::vector<double>* psi_capture = nullptr;  // receives the next sweep's psi
 
   long cell_index(int i, int j, int k) const { return i + (long)nx[0] * (j + (long)nx[1] * k); }
   void cell_ijk(long c, int* ijk) const {
@@ -159,7 +163,7 @@ struct orc_problem {
     if (ijk[a] < 0 || ijk[a] >= nx[a]) return -1;
     return cell_index(ijk[0], ijk[1], ijk[2]);
   }
-  double sig_t(int mat) const { return sigma_t[mat * G + group]; }
+  double sig_t(int mat) const { return sigma_t[mat * G + group] + inv_vdt; }
   double sig_s(int mat, int gf, int gt, int l) const {
     if (l > l_max) return 0.0;
     return sigma_s[l + gt * (l_max + 1) + gf * G * (l_max + 1) + (long)mat * G * G * (l_max + 1)];
@@ -351,6 +355,15 @@ void sweep_task(orc_problem* P, long t, SweepCtx& ctx, double* phi, int dir_base
       for (int j = 0; j < n; ++j) acc += P->M[i * n + j] * s;
       b[i] += acc;
     }
+    // implicit Euler: + inv_vdt M psi^n of this direction
+    if (!P->psi_prev.empty()) {
+      const double* pp = &P->psi_prev[(long)d * P->n_dofs + c * n];
+      for (int i = 0; i < n; ++i) {
+        double acc = 0.0;
+        for (int j = 0; j < n; ++j) acc += P->M[i * n + j] * pp[j];
+        b[i] += P->inv_vdt * acc;
+      }
+    }
     // other-group scattering, compute_outer_scattering_source :845-876
     for (int g = 0; g < P->G; ++g) {
       if (g == P->group) continue;
@@ -449,6 +462,9 @@ void run_sweep(orc_problem* P, double* phi, const double* group_flux, int schedu
       }
     }
   }
+  // the angular flux of directions [d0, d1) for orc_advance_angular
+  if (P->psi_capture)
+    std::copy(ctx.psi.begin(), ctx.psi.end(), P->psi_capture->begin() + (long)d0 * P->n_dofs);
 }
 
 double dot(const std::vector<double>& a, const std::vector<double>& b) {
@@ -503,6 +519,35 @@ orc_problem* orc_create(const orc_desc* D) {
 }
 
 void orc_destroy(orc_problem* p) { delete p; }
+
+/* Implicit Euler in time -- an extension: the reference operator is steady
+ * (its TimeDiscretization class, src/TimeDiscretization.cc:10-82, is never
+ * called).  inv_vdt = 1/(v dt) is added to sigma_t and source sweeps gain
+ * inv_vdt M psi^n per direction; psi^n starts at 0. */
+void orc_set_time_step(orc_problem* p, double inv_vdt) {
+  p->inv_vdt = inv_vdt;
+  if (inv_vdt > 0.0) p->psi_prev.assign((long)p->n_dir * p->n_dofs, 0.0);
+  else p->psi_prev.clear();
+}
+void orc_set_source(orc_problem* p, const double* source) {
+  p->source.assign(source, source + (long)p->n_src * p->G);
+}
+/* psi^n <- the angular flux of a source sweep of phi (the step's end) */
+void orc_advance_angular(orc_problem* p, const double* phi, int n_threads) {
+  std::vector<double> psi((long)p->n_dir * p->n_dofs, 0.0);
+  std::vector<double> gf((long)p->G * p->n_mom * p->n_dofs, 0.0), out((long)p->n_mom * p->n_dofs, 0.0);
+  orc_scattering_source(p, phi);
+  p->psi_capture = &psi;
+  orc_sweep(p, out.data(), gf.data(), 0, n_threads);
+  p->psi_capture = nullptr;
+  p->psi_prev.swap(psi);
+}
+void orc_get_angular(const orc_problem* p, double* psi) {
+  std::copy(p->psi_prev.begin(), p->psi_prev.end(), psi);
+}
+void orc_set_angular(orc_problem* p, const double* psi) {
+  std::copy(psi, psi + (long)p->n_dir * p->n_dofs, p->psi_prev.begin());
+}
 void orc_set_group(orc_problem* p, int g) { p->group = g; }
 long orc_n_dofs(const orc_problem* p) { return p->n_dofs; }
 long orc_n_tasks(const orc_problem* p) { return p->n_cells * p->n_dir; }

@@ -79,6 +79,12 @@ typedef struct orc_problem orc_problem;
 orc_problem* orc_create(const orc_desc* desc);
 void orc_destroy(orc_problem* p);
 void orc_set_group(orc_problem* p, int g);
+/* implicit Euler in time (an extension, not in the reference operator) */
+void orc_set_time_step(orc_problem* p, double inv_vdt);
+void orc_set_source(orc_problem* p, const double* source);   /* [n_sources][n_groups] */
+void orc_advance_angular(orc_problem* p, const double* phi, int n_threads);
+void orc_get_angular(const orc_problem* p, double* psi);     /* [dir][dof] */
+void orc_set_angular(orc_problem* p, const double* psi);
 
 long orc_n_dofs(const orc_problem* p);      /* cells * dofs per cell */
 long orc_n_tasks(const orc_problem* p);     /* cells * directions */

@@ -56,6 +56,11 @@ def lib():
         L.orc_create.argtypes = [C.POINTER(OrcDesc)]
         L.orc_destroy.argtypes = [vp]
         L.orc_set_group.argtypes = [vp, i]
+        L.orc_set_time_step.argtypes = [vp, C.c_double]
+        L.orc_set_source.argtypes = [vp, vp]
+        L.orc_advance_angular.argtypes = [vp, vp, i]
+        L.orc_get_angular.argtypes = [vp, vp]
+        L.orc_set_angular.argtypes = [vp, vp]
         L.orc_n_dofs.restype = l
         L.orc_n_dofs.argtypes = [vp]
         L.orc_n_tasks.restype = l
@@ -188,6 +193,28 @@ class OracleProblem:
 
     def set_group(self, g):
         lib().orc_set_group(self.h, g)
+
+    # implicit Euler in time (an extension: the reference operator is steady)
+    def set_time_step(self, inv_vdt):
+        lib().orc_set_time_step(self.h, float(inv_vdt))
+
+    def set_source(self, source):
+        src = np.ascontiguousarray(source, dtype=np.float64)
+        lib().orc_set_source(self.h, _ptr(src))
+
+    def advance_angular(self, phi, threads=1):
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        lib().orc_advance_angular(self.h, _ptr(phi), threads)
+
+    def angular_flux(self):
+        out = np.zeros(self.n_dir * self.n_dofs)
+        lib().orc_get_angular(self.h, _ptr(out))
+        return out
+
+    def set_angular_flux(self, psi):
+        psi = np.ascontiguousarray(psi, dtype=np.float64)
+        assert psi.size == self.n_dir * self.n_dofs
+        lib().orc_set_angular(self.h, _ptr(psi))
 
     def scattering_source(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)

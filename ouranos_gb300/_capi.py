@@ -23,6 +23,7 @@ HARM_ORTHONORMAL, HARM_REFERENCE = 0, 1
 FP64, FP32 = 0, 1
 FP64_NATIVE, FP64_DF64 = 0, 1
 SOLVER_SI, SOLVER_GMRES, SOLVER_BICGSTAB, SOLVER_FGMRES_MIXED, SOLVER_FGMRES_LEARNED = 0, 1, 2, 3, 4
+SOLVER_WARM_START = 0x100
 
 # every symbol include/ouranos_gb300.h declares
 EXPORTS = [
@@ -42,6 +43,8 @@ EXPORTS = [
     "ouranos_batch_create", "ouranos_batch_destroy", "ouranos_batch_layout", "ouranos_batch_apply",
     "ouranos_batch_rhs", "ouranos_batch_solve", "ouranos_batch_autotune", "ouranos_batch_set_graphs",
     "ouranos_batch_stats", "ouranos_batch_last_error",
+    "ouranos_rt_set_time_step", "ouranos_rt_set_source", "ouranos_rt_time_advance",
+    "ouranos_rt_get_angular_flux", "ouranos_rt_set_angular_flux",
 ]
 
 
@@ -119,6 +122,11 @@ def lib():
         "ouranos_batch_set_graphs": [vp, i],
         "ouranos_batch_stats": [vp, C.POINTER(d), C.POINTER(i)],
         "ouranos_batch_last_error": [vp, C.c_char_p, sz],
+        "ouranos_rt_set_time_step": [vp, d],
+        "ouranos_rt_set_source": [vp, vp],
+        "ouranos_rt_time_advance": [vp, i, i, i, d, vp, C.POINTER(SolveInfo)],
+        "ouranos_rt_get_angular_flux": [vp, vp],
+        "ouranos_rt_set_angular_flux": [vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

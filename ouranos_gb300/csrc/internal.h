@@ -159,6 +159,11 @@ cudaError_t launch_axpby(double a, const double* x, double b, double* y, long le
 cudaError_t launch_multi_axpy(const double* const* V, int k, const double* coef, double scale,
                               double* w, long len, cudaStream_t s);
 cudaError_t launch_bump_epoch(unsigned* epoch, cudaStream_t s);
+cudaError_t launch_to_f32(const double* in, float* out, long n, cudaStream_t s);
+// q[d][c n + i] += inv_vdt sum_j M_ij psi[d][c n + j]  (implicit Euler's psi^n term)
+template <typename real>
+cudaError_t launch_angular_source(real* q, const float* psi, const double* cell_mass, double inv_vdt,
+                                  int n, long n_cells, int n_dir, cudaStream_t s);
 cudaError_t launch_scale_inv_norm(const double* nrm2, double* v, long len, cudaStream_t s);
 constexpr int kDotGrid = 304;  // blocks of the dot-product kernel (2 per SM)
 cudaError_t launch_dots(const double* const* xs, const double* y, int k, long len, double* out,
@@ -271,6 +276,10 @@ struct ouranos_rt {
   ouranos::DevBuf d_x, d_y, d_gf, d_tmp, d_scatx;  // staging; d_scatx: scattering-source argument
   // solver workspace
   ouranos::DevBuf d_krylov;
+  // implicit Euler in time: 1/(v dt) added to sigma_t, inv_vdt M psi^n added to
+  // the source of source sweeps; psi^n (FP32, [dir][dof]) kept on the device
+  double inv_vdt = 0.0;
+  ouranos::DevBuf d_psi_prev;
   // learned preconditioner
   ouranos_cnn* cnn = nullptr;
   int pc_group = -1;

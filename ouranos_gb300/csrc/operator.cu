@@ -140,7 +140,7 @@ int setup_group(ouranos_rt* rt) {
   std::vector<double> cls_val;
   std::vector<int> mat_cls(rt->n_mat);
   for (int m = 0; m < rt->n_mat; ++m) {
-    const double st = rt->sigma_t[(size_t)m * G + g];
+    const double st = rt->sigma_t[(size_t)m * G + g] + rt->inv_vdt;  // implicit Euler shift
     auto it = std::find(cls_val.begin(), cls_val.end(), st);
     if (it == cls_val.end()) {
       mat_cls[m] = (int)cls_val.size();
@@ -250,6 +250,9 @@ int sweep_prepare(ouranos_rt* rt, const real* src, const real* iso, const real* 
   kernels = 0;
   // (the fused form holds (moments + 1) prefetched values per dof in registers)
   fm = (rt->n_mom <= kFusedMomentsMax && rt->n * (rt->n_mom + 1) <= 32) ? rt->n_mom : 0;
+  // a source sweep of a time step carries the per-direction psi^n term: expanded form
+  const bool angular = iso && rt->inv_vdt > 0.0 && rt->d_psi_prev.p;
+  if (angular) fm = 0;
   if (fm == 0) {
     CU(rt->d_q.alloc(sizeof(real) * len_dir), "expanded source");
     if (f64 && rt->fp64_contract == OURANOS_FP64_DF64)
@@ -263,6 +266,12 @@ int sweep_prepare(ouranos_rt* rt, const real* src, const real* iso, const real* 
          "source expansion");
     kernels += (rt->n_mom + 15) / 16;
     a.q = rt->d_q.as<real>();
+    if (angular) {
+      CU(launch_angular_source<real>(rt->d_q.as<real>(), rt->d_psi_prev.as<float>(), rt->d_cell_mass.as<double>(),
+                                     rt->inv_vdt, rt->n, rt->n_cells, rt->n_dir, rt->stream),
+         "time-step source");
+      ++kernels;
+    }
   }
   return OURANOS_OK;
 }
@@ -782,6 +791,93 @@ int ouranos_rt_sweep_rhs(ouranos_rt* rt, const double* group_flux, double* rhs) 
   OK_OR_RETURN(phi_combine(rt, drhs, rt->d_y.as<double>(), 1.0, 1.0));
   OK_OR_RETURN(stage_out(rt, rt->d_y.as<double>(), rhs));
   return finish(rt);
+}
+
+int ouranos_rt_set_time_step(ouranos_rt* rt, double inv_vdt) {
+  if (!rt) return OURANOS_ERR_BAD_INPUT;
+  if (!(inv_vdt >= 0.0) || !std::isfinite(inv_vdt)) return bad(rt, "1/(v dt) must be finite and >= 0");
+  cudaSetDevice(rt->device);
+  CU(cudaStreamSynchronize(rt->stream), "time step");
+  rt->inv_vdt = inv_vdt;
+  OK_OR_RETURN(setup_group(rt));  // sigma_t classes and cell inverses with the shift
+  if (inv_vdt > 0.0) {
+    const size_t bytes = sizeof(float) * (size_t)rt->n_dir * rt->n_dofs;
+    CU(rt->d_psi_prev.alloc(bytes), "angular flux of the previous step");
+    CU(cudaMemsetAsync(rt->d_psi_prev.p, 0, bytes, rt->stream), "angular flux of the previous step");
+  } else {
+    rt->d_psi_prev.release();
+  }
+  CU(cudaStreamSynchronize(rt->stream), "time step");
+  return OURANOS_OK;
+}
+
+int ouranos_rt_set_source(ouranos_rt* rt, const double* source) {
+  if (!rt || (!source && rt->n_src > 0)) return OURANOS_ERR_BAD_INPUT;
+  cudaSetDevice(rt->device);
+  CU(cudaStreamSynchronize(rt->stream), "source");
+  for (size_t k = 0; k < (size_t)rt->n_src * rt->G; ++k) {
+    if (!std::isfinite(source[k])) return bad(rt, "source strengths must be finite");
+    rt->source[k] = source[k];
+  }
+  // fixed source per source id: q/ws (src/RadiativeTransfer.cc:918-921)
+  std::vector<double> q(std::max(rt->n_src, 1), 0.0);
+  for (int s = 0; s < rt->n_src; ++s) q[s] = rt->source[(size_t)s * rt->G + rt->group] / rt->ws;
+  OK_OR_RETURN(upload(rt, rt->d_qcell, q, "sources"));
+  CU(cudaStreamSynchronize(rt->stream), "source");
+  return OURANOS_OK;
+}
+
+// One implicit Euler step: phi^{n+1} from (I - T) phi = D L^-1 (q + inflow +
+// inv_vdt M psi^n) with `solver` started from phi (e.g. phi^n), then psi^n <-
+// psi^{n+1} by one FP64 source sweep of phi^{n+1}, stored in FP32.  psi^n is
+// left as it was when the solve does not converge.
+int ouranos_rt_time_advance(ouranos_rt* rt, int solver, int restart, int max_it, double tol, double* phi,
+                            ouranos_solve_info* info) {
+  if (!rt || !phi) return OURANOS_ERR_BAD_INPUT;
+  if (!(rt->inv_vdt > 0.0) || !rt->d_psi_prev.p) return bad(rt, "no time step set (ouranos_rt_set_time_step)");
+  const int rc = ouranos_solve(rt, solver | OURANOS_SOLVER_WARM_START, restart, max_it, tol, nullptr, phi,
+                               nullptr, info);
+  if (rc != OURANOS_OK) return rc;
+  cudaSetDevice(rt->device);
+  OK_OR_RETURN(clear_status(rt));
+  const double* dphi = nullptr;
+  OK_OR_RETURN(stage_in(rt, phi, rt->d_x, 1, &dphi));
+  const int saved = rt->precision;
+  rt->precision = OURANOS_FP64;
+  int r2 = build_source(rt, dphi, nullptr);
+  if (r2 == OURANOS_OK) r2 = sweep_into_phi(rt, true);
+  rt->precision = saved;
+  OK_OR_RETURN(r2);
+  CU(launch_to_f32(rt->d_psi.as<double>(), rt->d_psi_prev.as<float>(), (long)rt->n_dir * rt->n_dofs, rt->stream),
+     "angular flux");
+  return finish(rt);
+}
+
+// psi^n as doubles ([dir][dof], lexicographic cells) -- a checkpoint's state
+int ouranos_rt_get_angular_flux(ouranos_rt* rt, double* psi) {
+  if (!rt || !psi) return OURANOS_ERR_BAD_INPUT;
+  if (!rt->d_psi_prev.p) return bad(rt, "no time step set (ouranos_rt_set_time_step)");
+  cudaSetDevice(rt->device);
+  const size_t n = (size_t)rt->n_dir * rt->n_dofs;
+  std::vector<float> h(n);
+  CU(cudaMemcpyAsync(h.data(), rt->d_psi_prev.p, sizeof(float) * n, cudaMemcpyDeviceToHost, rt->stream),
+     "angular flux");
+  CU(cudaStreamSynchronize(rt->stream), "angular flux");
+  for (size_t k = 0; k < n; ++k) psi[k] = h[k];
+  return OURANOS_OK;
+}
+
+int ouranos_rt_set_angular_flux(ouranos_rt* rt, const double* psi) {
+  if (!rt || !psi) return OURANOS_ERR_BAD_INPUT;
+  if (!rt->d_psi_prev.p) return bad(rt, "no time step set (ouranos_rt_set_time_step)");
+  cudaSetDevice(rt->device);
+  const size_t n = (size_t)rt->n_dir * rt->n_dofs;
+  std::vector<float> h(n);
+  for (size_t k = 0; k < n; ++k) h[k] = (float)psi[k];
+  CU(cudaMemcpyAsync(rt->d_psi_prev.p, h.data(), sizeof(float) * n, cudaMemcpyHostToDevice, rt->stream),
+     "angular flux");
+  CU(cudaStreamSynchronize(rt->stream), "angular flux");
+  return OURANOS_OK;
 }
 
 int ouranos_wavefront_levels(int dim, const int* nx, int n_dir, const double* omega, int* levels) {

@@ -146,7 +146,7 @@ int update(Work& w, int first, const std::vector<double>& y, double* x) {
 // restart refines the solution (iterative refinement).
 int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double* x,
           double* hist, ouranos_solve_info* info, int inner_prec, double inner_drop,
-          bool learned = false) {
+          bool learned = false, bool warm = false) {
   m = std::max(1, std::min(m, 32));  // dot kernel handles up to 32 basis vectors
   const bool flexible = inner_prec != OURANOS_FP64;
   // vectors: V[0..m], Z[0..m-1] (flexible), r
@@ -157,7 +157,7 @@ int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double
   int rc = 0;
   const double bnorm = nrm(w, b, &rc);
   RC(rc);
-  CUC(cudaMemsetAsync(x, 0, sizeof(double) * w.len, rt->stream), "gmres");
+  if (!warm) CUC(cudaMemsetAsync(x, 0, sizeof(double) * w.len, rt->stream), "gmres");
   int total = 0, cycles = 0;
   bool use_pc = learned && rt->cnn;
   enum { kPcTrial, kPcCompare, kPcOn, kPcOff };
@@ -168,7 +168,7 @@ int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double
   bool converged = bnorm == 0.0;
   while (!converged && total < max_it) {
     // true residual r = b - A x in FP64
-    if (cycles == 0) {
+    if (cycles == 0 && !warm) {  // x = 0: r = b
       CUC(cudaMemcpyAsync(w.v(R), b, sizeof(double) * w.len, cudaMemcpyDeviceToDevice, rt->stream),
           "gmres");
     } else {
@@ -316,12 +316,12 @@ int bicgstab(ouranos_rt* rt, int max_it, double tol, const double* b, double* x,
 // Source iteration phi <- D L^-1 (M2D S phi + q + inflow) (src/ouranos.cc:72-95,
 // written as intended: a fresh sweep each iteration), relative-change test.
 int source_iteration(ouranos_rt* rt, int max_it, double tol, const double* gf, const double* b,
-                     double* x, double* hist, ouranos_solve_info* info) {
+                     double* x, double* hist, ouranos_solve_info* info, bool warm) {
   Work w;
   RC(make_work(rt, 3, w));
   double *xn = w.v(0), *dlt = w.v(1), *rr = w.v(2);
   int rc = 0;
-  CUC(cudaMemsetAsync(x, 0, sizeof(double) * w.len, rt->stream), "si");
+  if (!warm) CUC(cudaMemsetAsync(x, 0, sizeof(double) * w.len, rt->stream), "si");
   int it = 0;
   double rel = 1.0;
   for (; it < max_it; ++it) {
@@ -364,6 +364,12 @@ extern "C" int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it
                              const double* group_flux, double* x, double* hist,
                              ouranos_solve_info* info) {
   if (!rt || !x || max_it < 1 || !(tol > 0)) return OURANOS_ERR_BAD_INPUT;
+  const bool warm = (solver & OURANOS_SOLVER_WARM_START) != 0;
+  solver &= ~OURANOS_SOLVER_WARM_START;
+  if (warm && solver == OURANOS_SOLVER_BICGSTAB) {
+    rt->err = "BiCGSTAB starts from zero";
+    return OURANOS_ERR_UNSUPPORTED;
+  }
   ouranos_solve_info local;
   if (!info) info = &local;
   std::memset(info, 0, sizeof *info);
@@ -379,22 +385,27 @@ extern "C" int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it
   CUC(rhs.alloc(sizeof(double) * len), "rhs");
   CUC(sol.alloc(sizeof(double) * len), "solution");
   RC(rt_rhs_device(rt, dgf, rhs.as<double>()));
+  if (warm) {
+    const double* dx = nullptr;
+    RC(rt_stage_in(rt, x, rt->d_x, 1, &dx));
+    CUC(cudaMemcpyAsync(sol.p, dx, sizeof(double) * len, cudaMemcpyDeviceToDevice, rt->stream), "guess");
+  }
   const int saved = rt->precision;
   int rc;
   switch (solver) {
     case OURANOS_SOLVER_SI:
-      rc = source_iteration(rt, max_it, tol, dgf, rhs.as<double>(), sol.as<double>(), hist, info);
+      rc = source_iteration(rt, max_it, tol, dgf, rhs.as<double>(), sol.as<double>(), hist, info, warm);
       break;
     case OURANOS_SOLVER_GMRES:
       rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info,
-                 OURANOS_FP64, 0.0);
+                 OURANOS_FP64, 0.0, false, warm);
       break;
     case OURANOS_SOLVER_BICGSTAB:
       rc = bicgstab(rt, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info);
       break;
     case OURANOS_SOLVER_FGMRES_MIXED:
       rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info,
-                 OURANOS_FP32, 1e-5);
+                 OURANOS_FP32, 1e-5, false, warm);
       break;
     case OURANOS_SOLVER_FGMRES_LEARNED:
       if (!rt->cnn) {
@@ -403,7 +414,7 @@ extern "C" int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it
         break;
       }
       rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info,
-                 OURANOS_FP32, 1e-5, true);
+                 OURANOS_FP32, 1e-5, true, warm);
       break;
     default:
       rt->err = "unknown solver";

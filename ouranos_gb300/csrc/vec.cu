@@ -422,6 +422,48 @@ __global__ void scale_inv_norm_kernel(const double* nrm2, double* v, long len) {
 }
 }  // namespace
 
+namespace {
+template <typename real>
+__global__ void angular_source_kernel(real* __restrict__ q, const float* __restrict__ psi,
+                                      const double* __restrict__ M, double inv_vdt, int n, long n_cells,
+                                      int n_dir) {
+  const long n_dofs = n_cells * n;
+  const long total = (long)n_dir * n_dofs;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n);
+    const float* pc = psi + (e - i);  // the cell's n values of this direction
+    const double* row = M + i * n;
+    double acc = 0.0;
+    for (int j = 0; j < n; ++j) acc += row[j] * (double)pc[j];
+    q[e] = (real)((double)q[e] + inv_vdt * acc);
+  }
+}
+}  // namespace
+
+template <typename real>
+cudaError_t launch_angular_source(real* q, const float* psi, const double* cell_mass, double inv_vdt,
+                                  int n, long n_cells, int n_dir, cudaStream_t s) {
+  angular_source_kernel<real><<<grid_for((long)n_dir * n_cells * n), kBlock, 0, s>>>(q, psi, cell_mass,
+                                                                                   inv_vdt, n, n_cells, n_dir);
+  return cudaGetLastError();
+}
+template cudaError_t launch_angular_source<double>(double*, const float*, const double*, double, int, long,
+                                                   int, cudaStream_t);
+template cudaError_t launch_angular_source<float>(float*, const float*, const double*, double, int, long,
+                                                  int, cudaStream_t);
+
+namespace {
+__global__ void to_f32_kernel(const double* in, float* out, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+}  // namespace
+
+cudaError_t launch_to_f32(const double* in, float* out, long n, cudaStream_t s) {
+  to_f32_kernel<<<grid_for(n), kBlock, 0, s>>>(in, out, n);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_bump_epoch(unsigned* epoch, cudaStream_t s) {
   bump_epoch_kernel<<<1, 1, 0, s>>>(epoch);
   return cudaGetLastError();

@@ -294,16 +294,17 @@ def batch_2d(seed=3000, count=64, sides=(32, 64, 128, 256, 512), orders=(1, 2),
 
 
 def time_dependent_3d(seed=4000, n=128, fe_order=1, sn=8, block=8, width=20.0, inv_vdt=0.5):
-    """3-D time-dependent case: [0,width]^3, n^3 hexes, LS S_sn (8 octants),
-    implicit Euler with 1/(v dt) added to sigma_t; two-material map on block^3
-    blocks, sigma_t in {0.5, 50}, c in {0.7, 0.99}; the pulse region is a
-    seeded block^3-cell box (the returned problem carries its cell mask)."""
+    """3-D time-dependent case: [0,width]^3, n^3 hexes, LS S_sn (8 octants);
+    two-material map on block^3 blocks, (physical) sigma_t in {0.5, 50}, c in
+    {0.7, 0.99}; source id 1 marks the pulse region, a seeded block^3-cell box
+    of unit strength (scaled per step with set_source).  1/(v dt) is in
+    meta["inv_vdt"], for RadiativeTransfer.set_time_step."""
     rng = SplitMix64(seed)
     quad = build_quadrature("LS", sn, 0, dim=3)
     blk, nb = _block_index((n, n, n), (block, block, block))
     kind = np.array([1 if rng.uniform() < 0.5 else 0 for _ in range(nb)], dtype=np.int32)
     mat = kind[blk].astype(np.int32)
-    st = np.array([[0.5 + inv_vdt], [50.0 + inv_vdt]])
+    st = np.array([[0.5], [50.0]])
     ss = np.array([[[[0.7 * 0.5]]], [[[0.99 * 50.0]]]])
     pulse_block = rng.integer(nb)
     sid = (blk == pulse_block).astype(np.int32)
@@ -311,6 +312,11 @@ def time_dependent_3d(seed=4000, n=128, fe_order=1, sn=8, block=8, width=20.0, i
                    np.array([[0.0], [1.0]]), (0,) * 6, None, None,
                    "3d-td-q%d-ls%d-%d^3-seed%d" % (fe_order, sn, n, seed),
                    {"seed": seed, "inv_vdt": inv_vdt})
+
+
+def pulse_strength(step, peak=10.0, center=20, width=5.0):
+    """Gaussian-in-time pulse: q = peak exp(-(step - center)^2 / (2 width^2))."""
+    return peak * math.exp(-0.5 * ((step - center) / width) ** 2)
 
 
 def zorder_cells(nx, ny):

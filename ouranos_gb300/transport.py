@@ -169,13 +169,49 @@ class RadiativeTransfer:
     def debug_wait_bias(self, extra):
         self._check(_capi.lib().ouranos_rt_debug_wait_bias(self._h, int(extra)))
 
-    def solve(self, method="gmres", tol=1e-8, max_it=1000, restart=30, group_flux=None, x=None):
-        """Drivers of src/ouranos.cc:43-209. Returns (x, info dict, residual history)."""
+    # ---- implicit Euler in time (an extension: the reference operator is steady)
+    def set_time_step(self, inv_vdt):
+        """1/(v dt) > 0 turns on implicit Euler (sigma_t + 1/(v dt), psi^n source,
+        psi^n = 0); 0 turns it off."""
+        self._check(_capi.lib().ouranos_rt_set_time_step(self._h, float(inv_vdt)))
+
+    def set_source(self, source):
+        """New fixed-source strengths, [n_sources][n_groups]."""
+        src = np.ascontiguousarray(source, dtype=np.float64)
+        self._check(_capi.lib().ouranos_rt_set_source(self._h, src.ctypes.data))
+
+    def time_advance(self, phi, method="fgmres_mixed", tol=1e-8, max_it=1000, restart=30):
+        """One implicit Euler step: phi (in: guess, e.g. phi^n; out: phi^{n+1})."""
+        kind = {"si": _capi.SOLVER_SI, "gmres": _capi.SOLVER_GMRES,
+                "fgmres_mixed": _capi.SOLVER_FGMRES_MIXED,
+                "fgmres_learned": _capi.SOLVER_FGMRES_LEARNED}[method]
+        info = _capi.SolveInfo()
+        self._check(_capi.lib().ouranos_rt_time_advance(self._h, kind, restart, max_it, tol, _ptr(phi),
+                                                        C.byref(info)))
+        return dict(iterations=info.iterations, restarts=info.restarts, residual=info.residual,
+                    seconds=info.seconds, converged=bool(info.converged))
+
+    def angular_flux(self):
+        """psi^n ([dir][dof], lexicographic cells) -- checkpoint state."""
+        out = np.zeros(self.problem.quad.n_dir * self.problem.total_cells * self.problem.dofs_per_cell)
+        self._check(_capi.lib().ouranos_rt_get_angular_flux(self._h, out.ctypes.data))
+        return out
+
+    def set_angular_flux(self, psi):
+        psi = np.ascontiguousarray(psi, dtype=np.float64)
+        self._check(_capi.lib().ouranos_rt_set_angular_flux(self._h, psi.ctypes.data))
+
+    def solve(self, method="gmres", tol=1e-8, max_it=1000, restart=30, group_flux=None, x=None,
+              warm=False):
+        """Drivers of src/ouranos.cc:43-209. Returns (x, info dict, residual history);
+        warm=True starts from the given x."""
         kind = {"si": _capi.SOLVER_SI, "gmres": _capi.SOLVER_GMRES,
                 "bicgstab": _capi.SOLVER_BICGSTAB, "fgmres_mixed": _capi.SOLVER_FGMRES_MIXED,
                 "fgmres_learned": _capi.SOLVER_FGMRES_LEARNED}[method]
         if x is None:
             x = np.zeros(self.length)
+        if warm:
+            kind |= _capi.SOLVER_WARM_START
         hist = np.zeros(max_it + 2)
         info = _capi.SolveInfo()
         rc = _capi.lib().ouranos_solve(self._h, kind, restart, max_it, tol, _ptr(group_flux),
