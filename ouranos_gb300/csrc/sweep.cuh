@@ -173,9 +173,12 @@ struct Stream {
 };
 
 // One task: a tile of wx x wy columns for kd directions, swept over the whole
-// sweep axis.  Shared by the single-problem and the batched kernels.
+// sweep axis.  Shared by the single-problem and the batched kernels.  The
+// arguments come by value: inlined into the single-problem kernel they stay
+// parameter reads the compiler can keep out of the inner loop (a reference
+// to the parameter block made them loads it had to repeat after every store).
 template <typename real, int DIM, int P1, int FM>
-__device__ __forceinline__ void sweep_task(const SweepArgs<real>& a, const int task,
+__device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int task,
                                            unsigned char* smem_raw) {
   using C = Cell<DIM, P1>;
   constexpr int N = C::N;
@@ -395,7 +398,7 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real>& a, const int t
 // task a warp waits on was taken earlier by a running warp -- any grid is
 // deadlock-free.
 template <typename real, int DIM, int P1, int FM>
-__global__ void __launch_bounds__(128) sweep_kernel(const __grid_constant__ SweepArgs<real> a) {
+__global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr unsigned FULL = 0xffffffffu;
   for (;;) {
