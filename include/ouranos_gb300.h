@@ -59,11 +59,17 @@ extern "C" {
 /* Arithmetic of the sweep. */
 #define OURANOS_FP64 0
 #define OURANOS_FP32 1
-/* How the FP64 path evaluates its moment <-> direction contractions: native
- * FP64 instructions, or double-float pairs on the FP32 pipes (about 48
- * significant bits, FP32 exponent range; the default). */
+/* How the FP64 path computes (double-float = pairs of FP32 numbers on the FP32
+ * pipes, about 48 significant bits and the FP32 exponent range; GB300 issues
+ * FP32 at 64x its FP64 rate):
+ *   NATIVE     native FP64 everywhere;
+ *   DF64       moment <-> direction contractions in double-float, sweep in FP64;
+ *   DF64_SWEEP contractions and the cell solves of the sweep in double-float,
+ *              sources and angular fluxes stored as pairs (the default).
+ * All three meet the 1e-12 parity bar against the FP64 oracle. */
 #define OURANOS_FP64_NATIVE 0
 #define OURANOS_FP64_DF64 1
+#define OURANOS_FP64_DF64_SWEEP 2
 
 /* Problem description: the data the reference spreads over Parameters,
  * Geometry, RTQuadrature and RTMaterialProperties (src/*.hh), restricted to a
@@ -124,8 +130,8 @@ int ouranos_rt_set_group(ouranos_rt* rt, int group);
 /* Sweep arithmetic: OURANOS_FP64 (default, parity path) or OURANOS_FP32. No
  * reference counterpart (the reference is FP64 only). */
 int ouranos_rt_set_precision(ouranos_rt* rt, int precision);
-/* Select OURANOS_FP64_NATIVE or OURANOS_FP64_DF64 for the FP64 path's moment
- * contractions.  No reference counterpart. */
+/* Select OURANOS_FP64_NATIVE, OURANOS_FP64_DF64 or OURANOS_FP64_DF64_SWEEP for
+ * the FP64 path.  No reference counterpart. */
 int ouranos_rt_set_fp64_contractions(ouranos_rt* rt, int mode);
 /* Length of a flux-moment vector, n_mom * n_dofs: the size of the Epetra_Map
  * returned by OperatorDomainMap/OperatorRangeMap (src/RadiativeTransfer.hh:240-249). */

@@ -14,6 +14,8 @@ namespace ouranos {
 
 struct df64 {
   float hi, lo;
+  df64() = default;
+  __host__ __device__ constexpr df64(float h, float l = 0.f) : hi(h), lo(l) {}
 };
 
 __device__ __forceinline__ df64 df64_from(double x) {
@@ -21,6 +23,25 @@ __device__ __forceinline__ df64 df64_from(double x) {
   return {hi, __double2float_rn(x - (double)hi)};
 }
 __device__ __forceinline__ double df64_to(df64 a) { return (double)a.hi + (double)a.lo; }
+// the same split on the host (tables)
+inline df64 df64_split(double x) {
+  const float hi = (float)x;
+  return df64(hi, (float)(x - (double)hi));
+}
+
+// storage conversions of the vector kernels: float/double by cast, df64 by split
+template <typename T>
+__device__ __forceinline__ T real_from_double(double x) { return (T)x; }
+template <>
+__device__ __forceinline__ df64 real_from_double<df64>(double x) { return df64_from(x); }
+template <typename T>
+__device__ __forceinline__ double real_to_double(T x) { return (double)x; }
+template <>
+__device__ __forceinline__ double real_to_double<df64>(df64 x) { return df64_to(x); }
+template <typename T>
+__device__ __forceinline__ df64 to_df64(T x) { return df64_from((double)x); }
+template <>
+__device__ __forceinline__ df64 to_df64<df64>(df64 x) { return x; }
 
 // compensated accumulator of a dot product
 struct df64_acc {

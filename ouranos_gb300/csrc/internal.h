@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/ouranos_gb300.h"
+#include "df64.cuh"
 
 namespace ouranos {
 
@@ -134,6 +135,12 @@ cudaError_t launch_expand_source_df64(const double* T, const double* iso, const 
                                       double* q, int n_dir, int n_mom, long n_dofs, cudaStream_t s);
 cudaError_t launch_reduce_moments_df64(const double* psi, const double* d2m_t, double* phi,
                                        int n_dir, int n_mom, long n_dofs, cudaStream_t s);
+// the same with T, iso, q (and psi) stored as double-float pairs (the
+// double-float sweep's storage)
+cudaError_t launch_expand_source_pairs(const df64* T, const df64* iso, const double* m2d, df64* q,
+                                       int n_dir, int n_mom, long n_dofs, cudaStream_t s);
+cudaError_t launch_reduce_moments_pairs(const df64* psi, const double* d2m_t, double* phi, int n_dir,
+                                        int n_mom, long n_dofs, cudaStream_t s);
 // phi[m][e] = sum_d D2M[m][d] psi[d][e]  -- direction -> moment reduction
 template <typename real>
 cudaError_t launch_reduce_moments(const real* psi, const real* d2m_t, real* phi, int n_dir,
@@ -160,6 +167,7 @@ cudaError_t launch_multi_axpy(const double* const* V, int k, const double* coef,
                               double* w, long len, cudaStream_t s);
 cudaError_t launch_bump_epoch(unsigned* epoch, cudaStream_t s);
 cudaError_t launch_to_f32(const double* in, float* out, long n, cudaStream_t s);
+cudaError_t launch_to_f32_pairs(const df64* in, float* out, long n, cudaStream_t s);
 // q[d][c n + i] += inv_vdt sum_j M_ij psi[d][c n + j]  (implicit Euler's psi^n term)
 template <typename real>
 cudaError_t launch_angular_source(real* q, const float* psi, const double* cell_mass, double inv_vdt,
@@ -248,7 +256,7 @@ struct ouranos_rt {
   std::vector<long> cell_order;
   ouranos::FETables fe;
   int precision = OURANOS_FP64;
-  int fp64_contract = OURANOS_FP64_DF64;  // arithmetic of the FP64 moment contractions
+  int fp64_contract = OURANOS_FP64_DF64_SWEEP;  // arithmetic of the FP64 path
   // schedule
   int wx = 0, wy = 1, kd = 0;          // 0 = not chosen yet
   int tiles_x = 0, tiles_y = 0, n_groups_dir = 0, n_tasks = 0;
@@ -269,6 +277,7 @@ struct ouranos_rt {
   ouranos::DevBuf d_cell_mass, d_rowsum_mass, d_sscale, d_oscale, d_qcell;
   ouranos::DevBuf d_dir_class, d_abs64, d_abs32, d_m2d64, d_m2d32, d_d2m64, d_d2m32;
   ouranos::DevBuf d_ainv64, d_ainv32, d_face64, d_face32, d_bnd64, d_bnd32;
+  ouranos::DevBuf d_absdf, d_m2ddf, d_ainvdf, d_facedf, d_bnddf;  // double-float sweep tables
   ouranos::DevBuf d_tasks, d_group_dirs, d_group_flip, d_progress, d_ctrl;
   ouranos::DevBuf d_edge_x, d_edge_y;
   // device: vectors

@@ -7,6 +7,7 @@
 #include <cstring>
 #include <map>
 #include <new>
+#include <type_traits>
 #include <vector>
 
 #include "internal.h"
@@ -50,6 +51,26 @@ int upload(ouranos_rt* rt, DevBuf& buf, const std::vector<T>& v, const char* wha
 template <class T>
 std::vector<float> to_f32(const std::vector<T>& v) {
   return std::vector<float>(v.begin(), v.end());
+}
+
+// tables of the double-float sweep: each value as its (hi, lo) float pair
+std::vector<df64> to_df(const std::vector<double>& v) {
+  std::vector<df64> out(v.size());
+  for (size_t k = 0; k < v.size(); ++k) out[k] = df64_split(v[k]);
+  return out;
+}
+
+// the sweep runs in double-float with pair storage
+bool df64_sweep(const ouranos_rt* rt) {
+  return rt->precision == OURANOS_FP64 && rt->fp64_contract == OURANOS_FP64_DF64_SWEEP;
+}
+
+// the table of the sweep's arithmetic type
+template <typename real>
+const real* table(const DevBuf& b64, const DevBuf& b32, const DevBuf& bdf) {
+  if (std::is_same<real, float>::value) return (const real*)b32.p;
+  if (std::is_same<real, df64>::value) return (const real*)bdf.p;
+  return (const real*)b64.p;
 }
 
 bool is_device_ptr(const void* p) {
@@ -162,6 +183,7 @@ int setup_group(ouranos_rt* rt) {
                         &ainv[(s * rt->n_dir_class + dc) * nn]);
   OK_OR_RETURN(upload(rt, rt->d_ainv64, ainv, "inverse tables"));
   OK_OR_RETURN(upload(rt, rt->d_ainv32, to_f32(ainv), "inverse tables"));
+  OK_OR_RETURN(upload(rt, rt->d_ainvdf, to_df(ainv), "inverse tables"));
   // scattering scales: sigma_s(mat, g'->g, l(m)) (by Legendre order)
   auto sig_s = [&](int mat, int gf, int gt, int l) {
     if (l > L) return 0.0;
@@ -195,6 +217,7 @@ int setup_group(ouranos_rt* rt) {
     }
   OK_OR_RETURN(upload(rt, rt->d_bnd64, bnd, "boundary"));
   OK_OR_RETURN(upload(rt, rt->d_bnd32, to_f32(bnd), "boundary"));
+  OK_OR_RETURN(upload(rt, rt->d_bnddf, to_df(bnd), "boundary"));
   return OURANOS_OK;
 }
 
@@ -229,11 +252,11 @@ int sweep_prepare(ouranos_rt* rt, const real* src, const real* iso, const real* 
   a.group_flip = rt->d_group_flip.as<int>();
   a.dir_class = rt->d_dir_class.as<int>();
   a.n_dir_class = rt->n_dir_class;
-  a.abs_omega = (const real*)(f64 ? rt->d_abs64.p : rt->d_abs32.p);
-  a.m2d = (const real*)(f64 ? rt->d_m2d64.p : rt->d_m2d32.p);
-  a.ainv = (const real*)(f64 ? rt->d_ainv64.p : rt->d_ainv32.p);
+  a.abs_omega = table<real>(rt->d_abs64, rt->d_abs32, rt->d_absdf);
+  a.m2d = table<real>(rt->d_m2d64, rt->d_m2d32, rt->d_m2ddf);
+  a.ainv = table<real>(rt->d_ainv64, rt->d_ainv32, rt->d_ainvdf);
   a.cell_class = rt->d_cell_class.as<int>();
-  a.face_mass = (const real*)(f64 ? rt->d_face64.p : rt->d_face32.p);
+  a.face_mass = table<real>(rt->d_face64, rt->d_face32, rt->d_facedf);
   a.src = src;
   a.iso = iso;
   a.q = nullptr;
@@ -255,8 +278,12 @@ int sweep_prepare(ouranos_rt* rt, const real* src, const real* iso, const real* 
   if (angular) fm = 0;
   if (fm == 0) {
     CU(rt->d_q.alloc(sizeof(real) * len_dir), "expanded source");
-    if (f64 && rt->fp64_contract == OURANOS_FP64_DF64)
-      CU(launch_expand_source_df64((const double*)src, (const double*)iso, (const double*)a.m2d,
+    if (std::is_same<real, df64>::value)  // pairs in, pairs out
+      CU(launch_expand_source_pairs((const df64*)src, (const df64*)iso, rt->d_m2d64.as<double>(),
+                                    rt->d_q.as<df64>(), rt->n_dir, rt->n_mom, rt->n_dofs, rt->stream),
+         "source expansion");
+    else if (std::is_same<real, double>::value && rt->fp64_contract != OURANOS_FP64_NATIVE)
+      CU(launch_expand_source_df64((const double*)src, (const double*)iso, rt->d_m2d64.as<double>(),
                                    rt->d_q.as<double>(), rt->n_dir, rt->n_mom, rt->n_dofs,
                                    rt->stream),
          "source expansion");
@@ -276,23 +303,31 @@ int sweep_prepare(ouranos_rt* rt, const real* src, const real* iso, const real* 
   return OURANOS_OK;
 }
 
-// phi = D2M psi (the moment reduction after a sweep)
+// phi = D2M psi (the moment reduction after a sweep); phi is float for the
+// FP32 sweep, double for the FP64 and double-float sweeps
 template <typename real>
-int sweep_reduce(ouranos_rt* rt, const real* psi, real* phi) {
-  const bool f64 = sizeof(real) == 8;
-  if (f64 && rt->fp64_contract == OURANOS_FP64_DF64)
+int sweep_reduce(ouranos_rt* rt, const real* psi, void* phi) {
+  if (std::is_same<real, df64>::value)
+    CU(launch_reduce_moments_pairs((const df64*)psi, rt->d_d2m64.as<double>(), (double*)phi, rt->n_dir,
+                                   rt->n_mom, rt->n_dofs, rt->stream),
+       "moment reduction");
+  else if (std::is_same<real, double>::value && rt->fp64_contract != OURANOS_FP64_NATIVE)
     CU(launch_reduce_moments_df64((const double*)psi, rt->d_d2m64.as<double>(), (double*)phi,
                                   rt->n_dir, rt->n_mom, rt->n_dofs, rt->stream),
        "moment reduction");
+  else if (std::is_same<real, double>::value)
+    CU(launch_reduce_moments<double>((const double*)psi, rt->d_d2m64.as<double>(), (double*)phi, rt->n_dir,
+                                     rt->n_mom, rt->n_dofs, rt->stream),
+       "moment reduction");
   else
-    CU(launch_reduce_moments<real>(psi, (const real*)(f64 ? rt->d_d2m64.p : rt->d_d2m32.p), phi,
-                                   rt->n_dir, rt->n_mom, rt->n_dofs, rt->stream),
+    CU(launch_reduce_moments<float>((const float*)psi, rt->d_d2m32.as<float>(), (float*)phi, rt->n_dir,
+                                    rt->n_mom, rt->n_dofs, rt->stream),
        "moment reduction");
   return OURANOS_OK;
 }
 
 template <typename real>
-int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd, real* phi) {
+int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd, void* phi) {
   SweepArgs<real> a;
   int fm = 0, kernels = 0;
   OK_OR_RETURN(sweep_prepare<real>(rt, src, iso, bnd, a, fm, kernels));
@@ -398,10 +433,18 @@ int stage_out(ouranos_rt* rt, const double* dv, double* user) {
 
 // Source moments T (precision of the sweep) from x (FP64, device) and the
 // other groups' fluxes gf (device or NULL).
-int build_source(ouranos_rt* rt, const double* x, const double* gf) {
+// (pairs: the double-float sweep's storage, in the same buffer as the FP64 source)
+int build_source(ouranos_rt* rt, const double* x, const double* gf, bool pairs) {
   const long len = vec_len(rt);
   const double* M = rt->d_cell_mass.as<double>();
-  if (rt->precision == OURANOS_FP64) {
+  if (rt->precision == OURANOS_FP64 && pairs) {
+    CU(rt->d_src64.alloc(sizeof(df64) * len), "source");
+    CU(launch_scatter_source<df64>(x, gf, rt->d_src64.as<df64>(), M, rt->d_sscale.as<double>(),
+                                   rt->d_oscale.as<double>(), rt->d_material.as<int>(), rt->n_mat,
+                                   rt->G, rt->group, rt->n_cells, rt->n, rt->n_mom, rt->n_dofs,
+                                   rt->stream),
+       "scattering source");
+  } else if (rt->precision == OURANOS_FP64) {
     CU(rt->d_src64.alloc(sizeof(double) * len), "source");
     CU(launch_scatter_source<double>(x, gf, rt->d_src64.as<double>(), M, rt->d_sscale.as<double>(),
                                      rt->d_oscale.as<double>(), rt->d_material.as<int>(), rt->n_mat,
@@ -422,6 +465,20 @@ int build_source(ouranos_rt* rt, const double* x, const double* gf) {
 // phi = D L^-1 (M2D T [+ iso + inflow]) into the precision's phi buffer.
 int sweep_into_phi(ouranos_rt* rt, bool sources) {
   const long len = vec_len(rt);
+  if (df64_sweep(rt)) {  // double-float sweep: sources as pairs
+    CU(rt->d_phi64.alloc(sizeof(double) * len), "flux");
+    const df64* iso = nullptr;
+    if (sources) {
+      CU(rt->d_iso64.alloc(sizeof(df64) * rt->n_dofs), "iso");
+      CU(launch_iso_source<df64>(rt->d_iso64.as<df64>(), rt->d_qcell.as<double>(),
+                                 rt->d_rowsum_mass.as<double>(), rt->d_source_id.as<int>(), rt->n_cells,
+                                 rt->n, rt->stream),
+         "iso source");
+      iso = rt->d_iso64.as<df64>();
+    }
+    return run_sweep<df64>(rt, rt->d_src64.as<df64>(), iso, sources ? rt->d_bnddf.as<df64>() : nullptr,
+                           rt->d_phi64.p);
+  }
   if (rt->precision == OURANOS_FP64) {
     CU(rt->d_phi64.alloc(sizeof(double) * len), "flux");
     const double* iso = nullptr;
@@ -434,7 +491,7 @@ int sweep_into_phi(ouranos_rt* rt, bool sources) {
       iso = rt->d_iso64.as<double>();
     }
     return run_sweep<double>(rt, rt->d_src64.as<double>(), iso,
-                             sources ? rt->d_bnd64.as<double>() : nullptr, rt->d_phi64.as<double>());
+                             sources ? rt->d_bnd64.as<double>() : nullptr, rt->d_phi64.p);
   }
   CU(rt->d_phi32.alloc(sizeof(float) * len), "flux");
   const float* iso = nullptr;
@@ -447,7 +504,7 @@ int sweep_into_phi(ouranos_rt* rt, bool sources) {
     iso = rt->d_iso32.as<float>();
   }
   return run_sweep<float>(rt, rt->d_src32.as<float>(), iso,
-                          sources ? rt->d_bnd32.as<float>() : nullptr, rt->d_phi32.as<float>());
+                          sources ? rt->d_bnd32.as<float>() : nullptr, rt->d_phi32.p);
 }
 
 // y = sx * x + sp * phi  (x may be NULL)
@@ -467,13 +524,13 @@ namespace ouranos {
 // Device-side Apply for the solvers: y = x - D L^-1 M2D S x, x and y device,
 // lexicographic numbering.  Does not synchronise.
 int rt_apply_device(ouranos_rt* rt, const double* x, double* y) {
-  OK_OR_RETURN(build_source(rt, x, nullptr));
+  OK_OR_RETURN(build_source(rt, x, nullptr, df64_sweep(rt)));
   OK_OR_RETURN(sweep_into_phi(rt, false));
   return phi_combine(rt, x, y, 1.0, -1.0);
 }
 // rhs = D L^-1 (q + outer + inflow) with zero in-group scattering (device).
 int rt_rhs_device(ouranos_rt* rt, const double* gf, double* rhs) {
-  OK_OR_RETURN(build_source(rt, nullptr, gf));
+  OK_OR_RETURN(build_source(rt, nullptr, gf, df64_sweep(rt)));
   OK_OR_RETURN(sweep_into_phi(rt, true));
   return phi_combine(rt, nullptr, rhs, 0.0, 1.0);
 }
@@ -487,7 +544,7 @@ template <typename real>
 static int batch_prepare(ouranos_rt* rt, const double* x, SweepArgs<real>* a, int* fm, bool sources) {
   const bool f64 = sizeof(real) == 8;
   rt->precision = f64 ? OURANOS_FP64 : OURANOS_FP32;
-  OK_OR_RETURN(build_source(rt, sources ? nullptr : x, nullptr));
+  OK_OR_RETURN(build_source(rt, sources ? nullptr : x, nullptr, false));  // batch: double sweep
   const long len = vec_len(rt);
   if (f64) CU(rt->d_phi64.alloc(sizeof(double) * len), "flux");
   else CU(rt->d_phi32.alloc(sizeof(float) * len), "flux");
@@ -514,9 +571,9 @@ int rt_batch_prepare(ouranos_rt* rt, const double* x, SweepArgs<float>* a, int* 
 }
 int rt_batch_finish(ouranos_rt* rt, const double* x, double* y, bool sources) {
   if (rt->precision == OURANOS_FP64)
-    OK_OR_RETURN(sweep_reduce<double>(rt, rt->d_psi.as<double>(), rt->d_phi64.as<double>()));
+    OK_OR_RETURN(sweep_reduce<double>(rt, rt->d_psi.as<double>(), rt->d_phi64.p));
   else
-    OK_OR_RETURN(sweep_reduce<float>(rt, rt->d_psi.as<float>(), rt->d_phi32.as<float>()));
+    OK_OR_RETURN(sweep_reduce<float>(rt, rt->d_psi.as<float>(), rt->d_phi32.p));
   return sources ? phi_combine(rt, nullptr, y, 0.0, 1.0) : phi_combine(rt, x, y, 1.0, -1.0);
 }
 int rt_check_status(ouranos_rt* rt) { return finish(rt); }
@@ -663,12 +720,15 @@ int ouranos_rt_create(const ouranos_problem_desc* D, int device, ouranos_rt** ou
   if ((rc = upload(rt, rt->d_dir_class, dcls, "dir classes")) ||
       (rc = upload(rt, rt->d_abs64, absw, "omega")) ||
       (rc = upload(rt, rt->d_abs32, to_f32(absw), "omega")) ||
+      (rc = upload(rt, rt->d_absdf, to_df(absw), "omega")) ||
       (rc = upload(rt, rt->d_m2d64, rt->m2d, "m2d")) ||
       (rc = upload(rt, rt->d_m2d32, to_f32(rt->m2d), "m2d")) ||
+      (rc = upload(rt, rt->d_m2ddf, to_df(rt->m2d), "m2d")) ||
       (rc = upload(rt, rt->d_d2m64, d2m_t, "d2m")) ||
       (rc = upload(rt, rt->d_d2m32, to_f32(d2m_t), "d2m")) ||
       (rc = upload(rt, rt->d_face64, rt->fe.face_mass, "face mass")) ||
       (rc = upload(rt, rt->d_face32, to_f32(rt->fe.face_mass), "face mass")) ||
+      (rc = upload(rt, rt->d_facedf, to_df(rt->fe.face_mass), "face mass")) ||
       (rc = upload(rt, rt->d_cell_mass, rt->fe.mass, "mass")) ||
       (rc = upload(rt, rt->d_rowsum_mass, rowsum, "mass")) ||
       (rc = upload(rt, rt->d_material, rt->material_id, "materials")) ||
@@ -716,7 +776,8 @@ int ouranos_rt_set_precision(ouranos_rt* rt, int precision) {
 
 int ouranos_rt_set_fp64_contractions(ouranos_rt* rt, int mode) {
   if (!rt) return OURANOS_ERR_BAD_INPUT;
-  if (mode != OURANOS_FP64_NATIVE && mode != OURANOS_FP64_DF64) return bad(rt, "unknown FP64 mode");
+  if (mode != OURANOS_FP64_NATIVE && mode != OURANOS_FP64_DF64 && mode != OURANOS_FP64_DF64_SWEEP)
+    return bad(rt, "unknown FP64 mode");
   rt->fp64_contract = mode;
   return OURANOS_OK;
 }
@@ -755,7 +816,7 @@ int ouranos_rt_sweep(ouranos_rt* rt, double* flux, const double* group_flux) {
   OK_OR_RETURN(clear_status(rt));
   const double* dgf = nullptr;
   if (group_flux) OK_OR_RETURN(stage_in(rt, group_flux, rt->d_gf, rt->G, &dgf));
-  OK_OR_RETURN(build_source(rt, rt->scat_valid ? rt->d_scatx.as<double>() : nullptr, dgf));
+  OK_OR_RETURN(build_source(rt, rt->scat_valid ? rt->d_scatx.as<double>() : nullptr, dgf, df64_sweep(rt)));
   OK_OR_RETURN(sweep_into_phi(rt, group_flux != nullptr));
   const double* dflux = nullptr;
   OK_OR_RETURN(stage_in(rt, flux, rt->d_x, 1, &dflux));
@@ -783,7 +844,7 @@ int ouranos_rt_sweep_rhs(ouranos_rt* rt, const double* group_flux, double* rhs) 
   OK_OR_RETURN(clear_status(rt));
   const double* dgf = nullptr;
   if (group_flux) OK_OR_RETURN(stage_in(rt, group_flux, rt->d_gf, rt->G, &dgf));
-  OK_OR_RETURN(build_source(rt, nullptr, dgf));
+  OK_OR_RETURN(build_source(rt, nullptr, dgf, df64_sweep(rt)));
   OK_OR_RETURN(sweep_into_phi(rt, true));
   const double* drhs = nullptr;
   OK_OR_RETURN(stage_in(rt, rhs, rt->d_x, 1, &drhs));
@@ -844,12 +905,21 @@ int ouranos_rt_time_advance(ouranos_rt* rt, int solver, int restart, int max_it,
   OK_OR_RETURN(stage_in(rt, phi, rt->d_x, 1, &dphi));
   const int saved = rt->precision;
   rt->precision = OURANOS_FP64;
-  int r2 = build_source(rt, dphi, nullptr);
+  int r2 = build_source(rt, dphi, nullptr, df64_sweep(rt));
   if (r2 == OURANOS_OK) r2 = sweep_into_phi(rt, true);
   rt->precision = saved;
   OK_OR_RETURN(r2);
-  CU(launch_to_f32(rt->d_psi.as<double>(), rt->d_psi_prev.as<float>(), (long)rt->n_dir * rt->n_dofs, rt->stream),
-     "angular flux");
+  rt->precision = OURANOS_FP64;
+  const bool pairs = df64_sweep(rt);
+  rt->precision = saved;
+  if (pairs)
+    CU(launch_to_f32_pairs(rt->d_psi.as<df64>(), rt->d_psi_prev.as<float>(), (long)rt->n_dir * rt->n_dofs,
+                           rt->stream),
+       "angular flux");
+  else
+    CU(launch_to_f32(rt->d_psi.as<double>(), rt->d_psi_prev.as<float>(), (long)rt->n_dir * rt->n_dofs,
+                     rt->stream),
+       "angular flux");
   return finish(rt);
 }
 

@@ -101,6 +101,49 @@ struct Tagged<double> {
   }
 };
 
+template <>
+struct Tagged<df64> {  // a double-float travels as its two tagged halves
+  static constexpr int W = 2;
+  static __device__ __forceinline__ void put(unsigned long long* w, df64 v, unsigned tag) {
+    st_relaxed_u64(w, ((unsigned long long)tag << 32) | __float_as_uint(v.hi));
+    st_relaxed_u64(w + 1, ((unsigned long long)tag << 32) | __float_as_uint(v.lo));
+  }
+  static __device__ __forceinline__ bool get(const unsigned long long* w, unsigned tag, df64& v) {
+    const unsigned long long a = ld_relaxed_u64(w), b = ld_relaxed_u64(w + 1);
+    v = df64(__uint_as_float((unsigned)a), __uint_as_float((unsigned)b));
+    return (unsigned)(a >> 32) == tag && (unsigned)(b >> 32) == tag;
+  }
+};
+
+// Arithmetic of the cell solve.  float / double: plain fused multiply-adds.
+// df64 (FP64 accuracy on the FP32 pipes): the products and sums of each dot
+// product go through the compensated accumulator of df64.cuh, renormalised once.
+template <typename real>
+struct Arith {
+  using acc = real;
+  static __device__ __forceinline__ acc zero() { return real(0); }
+  static __device__ __forceinline__ acc from(real v) { return v; }
+  static __device__ __forceinline__ void fma(acc& s, real a, real b) { s += a * b; }
+  static __device__ __forceinline__ real get(acc s) { return s; }
+  static __device__ __forceinline__ real ldg(const real* p) { return __ldg(p); }
+  static __device__ __forceinline__ real shfl_up(real v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
+};
+template <>
+struct Arith<df64> {
+  using acc = df64_acc;
+  static __device__ __forceinline__ acc zero() { return acc_zero(); }
+  static __device__ __forceinline__ acc from(df64 v) { return acc_from(v); }
+  static __device__ __forceinline__ void fma(acc& s, df64 a, df64 b) { acc_fma(s, a, b); }
+  static __device__ __forceinline__ df64 get(acc s) { return acc_result(s); }
+  static __device__ __forceinline__ df64 ldg(const df64* p) {
+    const float2 t = __ldg(reinterpret_cast<const float2*>(p));
+    return df64(t.x, t.y);
+  }
+  static __device__ __forceinline__ df64 shfl_up(df64 v, int d) {
+    return df64(__shfl_up_sync(0xffffffffu, v.hi, d), __shfl_up_sync(0xffffffffu, v.lo, d));
+  }
+};
+
 // Read FD tagged values; poll until every tag matches.  Returns false when the
 // wait ran out (and then records status 1) or when another warp has already
 // recorded an error.
@@ -186,6 +229,7 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
   constexpr int NV = Stream<real, FM, N>::NV;
   constexpr int W = Tagged<real>::W;
   constexpr unsigned FULL = 0xffffffffu;
+  using A = Arith<real>;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   real* ring = reinterpret_cast<real*>(smem_raw + warp * Stream<real, FM, N>::warp_bytes);
@@ -311,10 +355,10 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
       real upX[FD], upY[FD], upS[FD];
 #pragma unroll
       for (int t = 0; t < FD; ++t) {
-        const real sx = __shfl_up_sync(FULL, psiX[t], 1);
+        const real sx = A::shfl_up(psiX[t], 1);
         upX[t] = x_edge ? (tx == 0 ? bX : eX[t]) : sx;
         if (DIM == 3) {
-          const real sy = __shfl_up_sync(FULL, psiY[t], a.wx);
+          const real sy = A::shfl_up(psiY[t], a.wx);
           upY[t] = y_edge ? (ty == 0 ? bY : eY[t]) : sy;
         }
         upS[t] = sc == 0 ? bS : psiS[t];
@@ -327,9 +371,14 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
         real b[N];
 #pragma unroll
         for (int i = 0; i < N; ++i) {
-          if (FM == 0) b[i] = v[i];
-          else if (FM == 1) b[i] = w0 * v[i] + v[N + i];
-          else b[i] = w0 * v[i] + w1 * v[N + i] + v[2 * N + i];
+          if (FM == 0) {
+            b[i] = v[i];
+          } else {  // sum_m M2D(d, m) T_m + isotropic source
+            typename A::acc s = A::from(v[FM * N + i]);
+            A::fma(s, w0, v[i]);
+            if (FM >= 2) A::fma(s, w1, v[N + i]);
+            b[i] = A::get(s);
+          }
         }
         issue(sc + kPrefetch);  // refills the slot consumed one step ago
         // inflow faces: b_face += |Omega_a| F_a psi_up
@@ -337,23 +386,30 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
         const real* FS = a.face_mass + AS * FD * FD;
 #pragma unroll
         for (int t = 0; t < FD; ++t) {
-          real accx = 0, accs = 0;
+          typename A::acc accx = A::zero(), accs = A::zero();
 #pragma unroll
           for (int u = 0; u < FD; ++u) {
-            accx += __ldg(FX + t * FD + u) * upX[u];
-            accs += __ldg(FS + t * FD + u) * upS[u];
+            A::fma(accx, A::ldg(FX + t * FD + u), upX[u]);
+            A::fma(accs, A::ldg(FS + t * FD + u), upS[u]);
           }
-          b[C::x_in(t)] += wX * accx;
-          b[C::s_in(t)] += wS * accs;
+          // one after the other: the two inflow faces share the corner dof
+          typename A::acc bx = A::from(b[C::x_in(t)]);
+          A::fma(bx, wX, A::get(accx));
+          b[C::x_in(t)] = A::get(bx);
+          typename A::acc bs = A::from(b[C::s_in(t)]);
+          A::fma(bs, wS, A::get(accs));
+          b[C::s_in(t)] = A::get(bs);
         }
         if (DIM == 3) {
           const real* FY = a.face_mass + 1 * FD * FD;
 #pragma unroll
           for (int t = 0; t < FD; ++t) {
-            real acc = 0;
+            typename A::acc acc = A::zero();
 #pragma unroll
-            for (int u = 0; u < FD; ++u) acc += __ldg(FY + t * FD + u) * upY[u];
-            b[C::y_in(t)] += wY * acc;
+            for (int u = 0; u < FD; ++u) A::fma(acc, A::ldg(FY + t * FD + u), upY[u]);
+            typename A::acc by = A::from(b[C::y_in(t)]);
+            A::fma(by, wY, A::get(acc));
+            b[C::y_in(t)] = A::get(by);
           }
         }
         // x = A'^-1 b
@@ -361,10 +417,10 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
         real x[N];
 #pragma unroll
         for (int i = 0; i < N; ++i) {
-          real acc = 0;
+          typename A::acc acc = A::zero();
 #pragma unroll
-          for (int j = 0; j < N; ++j) acc += __ldg(Ai + i * N + j) * b[j];
-          x[i] = acc;
+          for (int j = 0; j < N; ++j) A::fma(acc, A::ldg(Ai + i * N + j), b[j]);
+          x[i] = A::get(acc);
         }
 #pragma unroll
         for (int t = 0; t < FD; ++t) {

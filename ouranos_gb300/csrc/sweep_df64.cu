@@ -1,0 +1,26 @@
+// Instantiations of the sweep kernel in double-float (FP64 accuracy on the
+// FP32 pipes): 2-D Q1..Q4, 3-D Q1..Q2.
+#include "sweep.cuh"
+
+namespace ouranos {
+
+template <>
+cudaError_t launch_sweep<df64>(int dim, int p1, int fm, const SweepArgs<df64>& a, int grid, int block,
+                               cudaStream_t s) {
+  if (dim == 2) {
+    switch (p1) {
+      case 2: return launch_sweep_impl<df64, 2, 2>(fm, a, grid, block, s);
+      case 3: return launch_sweep_impl<df64, 2, 3>(fm, a, grid, block, s);
+      case 4: return launch_sweep_impl<df64, 2, 4>(fm, a, grid, block, s);
+      case 5: return launch_sweep_impl<df64, 2, 5>(fm, a, grid, block, s);
+    }
+  } else if (dim == 3) {
+    switch (p1) {
+      case 2: return launch_sweep_impl<df64, 3, 2>(fm, a, grid, block, s);
+      case 3: return launch_sweep_impl<df64, 3, 3>(fm, a, grid, block, s);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace ouranos

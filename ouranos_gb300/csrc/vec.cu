@@ -50,7 +50,7 @@ __global__ void scatter_source_kernel(const double* __restrict__ x, const double
         acc += oscale[((size_t)mat * n_groups + g) * n_mom + m] * r;
       }
     }
-    src[(size_t)m * n_dofs + c * n + i] = (real)acc;
+    src[(size_t)m * n_dofs + c * n + i] = real_from_double<real>(acc);
   }
 }
 
@@ -65,7 +65,7 @@ __global__ void iso_source_kernel(real* iso, const double* qcell, const double* 
     const long c = e / n;
     const int i = e % n;
     const int sid = source_id ? source_id[c] : 0;
-    iso[e] = (real)(qcell[sid] * rowsum[i]);
+    iso[e] = real_from_double<real>(qcell[sid] * rowsum[i]);
   }
 }
 
@@ -213,9 +213,18 @@ __global__ void reduce_kernel(const real* __restrict__ psi, const real* __restri
 
 // FP64 contractions in double-float arithmetic on the FP32 pipes (see df64.cuh):
 // same inputs and outputs as expand_kernel<double> / reduce_kernel<double>.
-template <int NM>
-__global__ void expand_df64_kernel(const double* __restrict__ T, const double* __restrict__ iso,
-                                   const double* __restrict__ m2d, int ld, double* __restrict__ q,
+// result of a double-float contraction in the storage type: double (rounded)
+// or df64 (kept as the pair)
+template <typename S>
+__device__ __forceinline__ S store_df64(df64 v);
+template <>
+__device__ __forceinline__ double store_df64<double>(df64 v) { return df64_to(v); }
+template <>
+__device__ __forceinline__ df64 store_df64<df64>(df64 v) { return v; }
+
+template <int NM, typename S>
+__global__ void expand_df64_kernel(const S* __restrict__ T, const S* __restrict__ iso,
+                                   const double* __restrict__ m2d, int ld, S* __restrict__ q,
                                    int n_dir, int nm, long n_dofs, int accumulate) {
   extern __shared__ unsigned char smem_raw[];
   df64* sm = reinterpret_cast<df64*>(smem_raw);
@@ -225,20 +234,20 @@ __global__ void expand_df64_kernel(const double* __restrict__ T, const double* _
        e += (long)gridDim.x * blockDim.x) {
     df64 t[NM];
 #pragma unroll
-    for (int m = 0; m < NM; ++m) t[m] = df64_from(m < nm ? T[(size_t)m * n_dofs + e] : 0.0);
-    const df64 is = df64_from(iso ? iso[e] : 0.0);
+    for (int m = 0; m < NM; ++m) t[m] = m < nm ? to_df64(T[(size_t)m * n_dofs + e]) : df64(0.f);
+    const df64 is = iso ? to_df64(iso[e]) : df64(0.f);
     for (int d = 0; d < n_dir; ++d) {
-      df64_acc acc = acc_from(accumulate ? df64_from(q[(size_t)d * n_dofs + e]) : is);
+      df64_acc acc = acc_from(accumulate ? to_df64(q[(size_t)d * n_dofs + e]) : is);
 #pragma unroll
       for (int m = 0; m < NM; ++m)
         if (m < nm) acc_fma(acc, sm[d * nm + m], t[m]);
-      q[(size_t)d * n_dofs + e] = df64_to(acc_result(acc));
+      q[(size_t)d * n_dofs + e] = store_df64<S>(acc_result(acc));
     }
   }
 }
 
-template <int NM>
-__global__ void reduce_df64_kernel(const double* __restrict__ psi, const double* __restrict__ d2m_t,
+template <int NM, typename S>
+__global__ void reduce_df64_kernel(const S* __restrict__ psi, const double* __restrict__ d2m_t,
                                    int ld, double* __restrict__ phi, int n_dir, int nm, long n_dofs) {
   extern __shared__ unsigned char smem_raw[];
   df64* sm = reinterpret_cast<df64*>(smem_raw);
@@ -250,7 +259,7 @@ __global__ void reduce_df64_kernel(const double* __restrict__ psi, const double*
 #pragma unroll
     for (int m = 0; m < NM; ++m) acc[m] = acc_zero();
     for (int d = 0; d < n_dir; ++d) {
-      const df64 v = df64_from(psi[(size_t)d * n_dofs + e]);
+      const df64 v = to_df64(psi[(size_t)d * n_dofs + e]);
 #pragma unroll
       for (int m = 0; m < NM; ++m)
         if (m < nm) acc_fma(acc[m], sm[d * nm + m], v);
@@ -263,45 +272,64 @@ __global__ void reduce_df64_kernel(const double* __restrict__ psi, const double*
 
 }  // namespace
 
-cudaError_t launch_expand_source_df64(const double* T, const double* iso, const double* m2d,
-                                      double* q, int n_dir, int n_mom, long n_dofs,
-                                      cudaStream_t s) {
+template <typename S>
+static cudaError_t expand_df64_any(const S* T, const S* iso, const double* m2d, S* q, int n_dir, int n_mom,
+                                   long n_dofs, cudaStream_t s) {
   for (int m0 = 0; m0 < n_mom; m0 += 16) {
     const int nm = n_mom - m0 < 16 ? n_mom - m0 : 16;
     const size_t sh = sizeof(df64) * (size_t)n_dir * nm;
-    const double* Tm = T + (size_t)m0 * n_dofs;
+    const S* Tm = T + (size_t)m0 * n_dofs;
     const int acc = m0 > 0;
-    const double* is = m0 == 0 ? iso : nullptr;
+    const S* is = m0 == 0 ? iso : nullptr;
     if (nm <= 4)
-      expand_df64_kernel<4><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+      expand_df64_kernel<4, S><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
     else if (nm <= 10)
-      expand_df64_kernel<10><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+      expand_df64_kernel<10, S><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
     else
-      expand_df64_kernel<16><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+      expand_df64_kernel<16, S><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 
-cudaError_t launch_reduce_moments_df64(const double* psi, const double* d2m_t, double* phi,
-                                       int n_dir, int n_mom, long n_dofs, cudaStream_t s) {
+template <typename S>
+static cudaError_t reduce_df64_any(const S* psi, const double* d2m_t, double* phi, int n_dir, int n_mom,
+                                   long n_dofs, cudaStream_t s) {
   for (int m0 = 0; m0 < n_mom; m0 += 16) {
     const int nm = n_mom - m0 < 16 ? n_mom - m0 : 16;
     const size_t sh = sizeof(df64) * (size_t)n_dir * nm;
     double* ph = phi + (size_t)m0 * n_dofs;
     if (nm <= 1)
-      reduce_df64_kernel<1><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_df64_kernel<1, S><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
     else if (nm <= 4)
-      reduce_df64_kernel<4><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_df64_kernel<4, S><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
     else if (nm <= 10)
-      reduce_df64_kernel<10><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_df64_kernel<10, S><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
     else
-      reduce_df64_kernel<16><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_df64_kernel<16, S><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+cudaError_t launch_expand_source_df64(const double* T, const double* iso, const double* m2d,
+                                      double* q, int n_dir, int n_mom, long n_dofs,
+                                      cudaStream_t s) {
+  return expand_df64_any<double>(T, iso, m2d, q, n_dir, n_mom, n_dofs, s);
+}
+cudaError_t launch_reduce_moments_df64(const double* psi, const double* d2m_t, double* phi,
+                                       int n_dir, int n_mom, long n_dofs, cudaStream_t s) {
+  return reduce_df64_any<double>(psi, d2m_t, phi, n_dir, n_mom, n_dofs, s);
+}
+cudaError_t launch_expand_source_pairs(const df64* T, const df64* iso, const double* m2d, df64* q,
+                                       int n_dir, int n_mom, long n_dofs, cudaStream_t s) {
+  return expand_df64_any<df64>(T, iso, m2d, q, n_dir, n_mom, n_dofs, s);
+}
+cudaError_t launch_reduce_moments_pairs(const df64* psi, const double* d2m_t, double* phi, int n_dir,
+                                        int n_mom, long n_dofs, cudaStream_t s) {
+  return reduce_df64_any<df64>(psi, d2m_t, phi, n_dir, n_mom, n_dofs, s);
 }
 
 template <typename real>
@@ -373,6 +401,9 @@ template cudaError_t launch_scatter_source<float>(const double*, const double*, 
                                                   const double*, const double*, const double*,
                                                   const int*, int, int, int, long, int, int, long,
                                                   cudaStream_t);
+template cudaError_t launch_scatter_source<df64>(const double*, const double*, df64*, const double*,
+                                                 const double*, const double*, const int*, int, int, int,
+                                                 long, int, int, long, cudaStream_t);
 
 template <typename real>
 cudaError_t launch_iso_source(real* iso, const double* qcell, const double* rowsum,
@@ -385,6 +416,8 @@ template cudaError_t launch_iso_source<double>(double*, const double*, const dou
                                                long, int, cudaStream_t);
 template cudaError_t launch_iso_source<float>(float*, const double*, const double*, const int*,
                                               long, int, cudaStream_t);
+template cudaError_t launch_iso_source<df64>(df64*, const double*, const double*, const int*, long, int,
+                                             cudaStream_t);
 
 template <typename real>
 cudaError_t launch_combine(const double* x, const real* phi, double* y, long len, double sx,
@@ -435,7 +468,7 @@ __global__ void angular_source_kernel(real* __restrict__ q, const float* __restr
     const double* row = M + i * n;
     double acc = 0.0;
     for (int j = 0; j < n; ++j) acc += row[j] * (double)pc[j];
-    q[e] = (real)((double)q[e] + inv_vdt * acc);
+    q[e] = real_from_double<real>(real_to_double(q[e]) + inv_vdt * acc);
   }
 }
 }  // namespace
@@ -451,6 +484,8 @@ template cudaError_t launch_angular_source<double>(double*, const float*, const 
                                                    int, cudaStream_t);
 template cudaError_t launch_angular_source<float>(float*, const float*, const double*, double, int, long,
                                                   int, cudaStream_t);
+template cudaError_t launch_angular_source<df64>(df64*, const float*, const double*, double, int, long, int,
+                                                 cudaStream_t);
 
 namespace {
 __global__ void to_f32_kernel(const double* in, float* out, long n) {
@@ -458,6 +493,18 @@ __global__ void to_f32_kernel(const double* in, float* out, long n) {
     out[i] = (float)in[i];
 }
 }  // namespace
+
+namespace {
+__global__ void pairs_to_f32_kernel(const df64* in, float* out, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    out[i] = in[i].hi + in[i].lo;
+}
+}  // namespace
+
+cudaError_t launch_to_f32_pairs(const df64* in, float* out, long n, cudaStream_t s) {
+  pairs_to_f32_kernel<<<grid_for(n), kBlock, 0, s>>>(in, out, n);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_to_f32(const double* in, float* out, long n, cudaStream_t s) {
   to_f32_kernel<<<grid_for(n), kBlock, 0, s>>>(in, out, n);

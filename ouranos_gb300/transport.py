@@ -88,8 +88,11 @@ class RadiativeTransfer:
         self.precision = precision
 
     def set_fp64_contractions(self, mode):
-        """'df64' (double-float on the FP32 pipes, default) or 'native' FP64."""
-        m = {"native": _capi.FP64_NATIVE, "df64": _capi.FP64_DF64}[mode]
+        """FP64 path arithmetic: 'native' FP64; 'df64' (moment contractions in
+        double-float on the FP32 pipes, sweep in FP64); 'df64_sweep' (the sweep's
+        cell solves too; the default)."""
+        m = {"native": _capi.FP64_NATIVE, "df64": _capi.FP64_DF64,
+             "df64_sweep": _capi.FP64_DF64_SWEEP}[mode]
         self._check(_capi.lib().ouranos_rt_set_fp64_contractions(self._h, m))
 
     def get_n_tasks_to_execute(self):

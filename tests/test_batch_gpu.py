@@ -17,10 +17,13 @@ def _problems(count=6, seed=31):
 
 
 def _singles(problems, x_slices, precision="fp64"):
+    """Single-problem Applies with the batch's arithmetic: its FP64 sweep is the
+    FP64 kernel with double-float contractions (mode 'df64')."""
     import ouranos_gb300 as og
     out = []
     for p, x in zip(problems, x_slices):
         with og.RadiativeTransfer(p, precision=precision) as rt:
+            rt.set_fp64_contractions("df64")
             out.append(rt.apply(np.ascontiguousarray(x)))
     return out
 
@@ -70,6 +73,7 @@ def test_batched_rhs_matches_single_problems():
         r = b.rhs()
         for p, rb in zip(probs, b.slices(r)):
             with og.RadiativeTransfer(p) as rt:
+                rt.set_fp64_contractions("df64")
                 assert np.array_equal(rt.rhs(), rb)
 
 

@@ -258,16 +258,26 @@ def test_wait_timeout_reports_error_and_recovers():
     assert rel_err(y, ref) < TOL64
 
 
-@pytest.mark.parametrize("mode", ["native", "df64"])
+@pytest.mark.parametrize("mode", ["native", "df64", "df64_sweep"])
 def test_fp64_contraction_modes_match_oracle(mode):
-    """Both FP64 contraction arithmetics (native FP64, double-float on the FP32
-    pipes) keep the 1e-12 parity bar, on P3 (expanded source) and P0 (fused)."""
+    """Every FP64 arithmetic (native FP64; double-float contractions; double-float
+    contractions and cell solves) keeps the 1e-12 parity bar, on P3 (expanded
+    source), P0 (fused moments), 2-D Q1-Q4 and 3-D Q1-Q2, Apply and RHS sweeps."""
     import ouranos_gb300 as og
-    for prob in (og.heterogeneous_2d(seed=61, n=20, fe_order=2, sn=8, l_max=3, blocks=4),
-                 og.thick_3d(seed=2061, n=6, sn=4, block=2, width=2.0)):
+    probs = [og.heterogeneous_2d(seed=61, n=20, fe_order=2, sn=8, l_max=3, blocks=4),
+             og.heterogeneous_2d(seed=62, n=12, fe_order=4, sn=4, l_max=1, blocks=4),
+             og.heterogeneous_2d(seed=63, n=16, fe_order=1, sn=4, l_max=0, blocks=4),
+             og.thick_3d(seed=2061, n=6, sn=4, block=2, width=2.0),
+             og.uniform_problem(3, 2, (4, 5, 3), (0, 0, 0), (1.0, 1.0, 1.0),
+                                og.build_quadrature("LS", 4, 0, dim=3), 2.0, 1.5, 1.0)]
+    for prob in probs:
         x = np.random.default_rng(61).standard_normal(prob.vector_length)
-        ref = po.OracleProblem(prob.arrays()).apply(x)
+        O = po.OracleProblem(prob.arrays())
+        ref = O.apply(x)
+        ref_rhs = O.rhs()
         with og.RadiativeTransfer(prob) as rt:
             rt.set_fp64_contractions(mode)
             y = rt.apply(x)
-        assert rel_err(y, ref) < TOL64
+            r = rt.rhs()
+        assert rel_err(y, ref) < TOL64, prob.name
+        assert rel_err(r, ref_rhs) < TOL64, prob.name
