@@ -47,6 +47,13 @@ def workload_problem(seed=1001):
     return og.heterogeneous_2d(seed=seed, n=256, fe_order=2, sn=16, l_max=3, blocks=8)
 
 
+# DRAM traffic of one sweep launch on the default workload, from the ncu
+# capture summarised in profiles/sweep_kernel_2d-hetero-256x256-dgq2-ls16-p3.md
+# (dram__bytes_read.sum + dram__bytes_write.sum), per precision, default tiling
+# and FP64 arithmetic
+SWEEP_TRAFFIC_BYTES = {"fp64": 708.414208e6 + 660.699392e6, "fp32": 358.432e6 + 311.297792e6}
+
+
 def bytes_per_solve(prob, real_bytes=8):
     """Algorithmic HBM bytes per cell-direction solve: each outflow face value
     written once and read once downwind (2 * dim * fd values), the source and
@@ -261,6 +268,9 @@ def run_ours(args):
         raise RuntimeError("non-finite operator output")
 
     peak, peak_kind = measured_peaks()
+    # the captured configuration only: default seed, tiling and FP64 arithmetic
+    profiled = (rank == 0 and rt.tiling() == (32, 1, 1) and world == 1)
+    traffic = SWEEP_TRAFFIC_BYTES.get(args.precision) if profiled else None
     rb = 8 if args.precision == "fp64" else 4
     bps = bytes_per_solve(prob, rb)
     avg_sweep_s = sum(sweep_ms) / len(sweep_ms) / 1e3
@@ -291,7 +301,8 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * L,
                     "d2h_bytes_per_step": 8 * L},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak,
+                         "traffic": traffic,
                          "peak_kind": peak_kind, "bytes_per_solve": bps,
                          "sweep_ms": avg_sweep_s * 1e3,
                          "fp_flops_per_solve": fps,
