@@ -182,6 +182,71 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+// 16-byte cp.async (to shared memory through L2) and a cell's N contiguous
+// values copied in 16-byte pieces (N * sizeof(real) a multiple of 16, both
+// addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async_16(void* smem_dst, const void* gsrc) {
+  const unsigned dst = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(gsrc) : "memory");
+}
+template <typename real, int N>
+__device__ __forceinline__ void cp_async_cell(real* smem_dst, const real* gsrc) {
+#pragma unroll
+  for (int k = 0; k < (int)(N * sizeof(real) / 16); ++k)
+    cp_async_16(reinterpret_cast<char*>(smem_dst) + 16 * k, reinterpret_cast<const char*>(gsrc) + 16 * k);
+}
+
+// 32-bit words of a value (little endian), for 16-byte vector stores
+template <typename real>
+struct Bits;
+template <>
+struct Bits<float> {
+  static constexpr int W = 1;
+  static __device__ __forceinline__ unsigned word(float v, int) { return __float_as_uint(v); }
+};
+template <>
+struct Bits<double> {
+  static constexpr int W = 2;
+  static __device__ __forceinline__ unsigned word(double v, int w) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return w ? (unsigned)(b >> 32) : (unsigned)b;
+  }
+};
+template <>
+struct Bits<df64> {
+  static constexpr int W = 2;
+  static __device__ __forceinline__ unsigned word(df64 v, int w) {
+    return w ? __float_as_uint(v.lo) : __float_as_uint(v.hi);
+  }
+};
+// dst[0..N) = o[0..N) with 16-byte stores (dst 16-byte aligned)
+template <typename real, int N>
+__device__ __forceinline__ void store_cell(real* dst, const real (&o)[N]) {
+  constexpr int W = Bits<real>::W;
+#pragma unroll
+  for (int k = 0; k < (int)(N * sizeof(real) / 16); ++k) {
+    unsigned u[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) u[t] = Bits<real>::word(o[(4 * k + t) / W], (4 * k + t) % W);
+    *reinterpret_cast<uint4*>(reinterpret_cast<char*>(dst) + 16 * k) = make_uint4(u[0], u[1], u[2], u[3]);
+  }
+}
+// o[j] <- o[j ^ m] for every j (conditional swaps along each index bit)
+template <typename real, int N>
+__device__ __forceinline__ void xor_permute(real (&o)[N], int m) {
+#pragma unroll
+  for (int bit = 1; bit < N; bit <<= 1) {
+    const bool sw = (m & bit) != 0;
+#pragma unroll
+    for (int j = 0; j < N; ++j)
+      if (!(j & bit)) {
+        const real t0 = o[j], t1 = o[j | bit];
+        o[j] = sw ? t1 : t0;
+        o[j | bit] = sw ? t0 : t1;
+      }
+  }
+}
+
 // planes prefetched ahead of the one being solved; the ring has one more slot
 // so the slot being refilled was consumed a step earlier
 constexpr int kPrefetch = 3;
@@ -272,6 +337,11 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
     if (flip & 1) { base += (P1 - 1); st0 = -1; }
     if (flip & 2) { base += (P1 - 1) * P1; st1 = -P1; }
     if (DIM == 3 && (flip & 4)) { base += (P1 - 1) * P1 * P1; st2 = -P1 * P1; }
+    // Q1 cells: mirroring an axis flips one bit of the local index, so the
+    // physical position of canonical dof i is i ^ fmask and a cell's values
+    // move as whole 16-byte pieces
+    constexpr bool VEC = P1 == 2 && (N * sizeof(real)) % 16 == 0;
+    const int fmask = flip & (N - 1);
     auto off = [&](int i) {
       return C::comp(i, 0) * st0 + C::comp(i, 1) * st1 + (DIM == 3 ? C::comp(i, 2) * st2 : 0);
     };
@@ -298,7 +368,21 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
         const unsigned cdst = (unsigned)__cvta_generic_to_shared(cring + (pl % kRing) * 32 + lane);
         asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(cdst), "l"(a.cell_class + cell)
                      : "memory");
-        if (FM == 0) {
+        if (VEC) {  // the cell's values in physical order, 16 bytes at a time
+          const long c0 = cell * N;
+          if (FM == 0) {
+            cp_async_cell<real, N>(v, a.q + dirbase + c0);
+          } else {
+            cp_async_cell<real, N>(v, a.src + c0);
+            if (FM >= 2) cp_async_cell<real, N>(v + N, a.src + a.n_dofs + c0);
+            if (a.iso) {
+              cp_async_cell<real, N>(v + FM * N, a.iso + c0);
+            } else {
+#pragma unroll
+              for (int i = 0; i < N; ++i) v[FM * N + i] = real(0);
+            }
+          }
+        } else if (FM == 0) {
           const real* Q = a.q + dirbase + cb;
 #pragma unroll
           for (int i = 0; i < N; ++i) cp_async_elem(v + i, Q + off(i));
@@ -371,12 +455,13 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
         real b[N];
 #pragma unroll
         for (int i = 0; i < N; ++i) {
+          const int vi = VEC ? (i ^ fmask) : i;  // ring in physical order on the vector path
           if (FM == 0) {
-            b[i] = v[i];
+            b[i] = v[vi];
           } else {  // sum_m M2D(d, m) T_m + isotropic source
-            typename A::acc s = A::from(v[FM * N + i]);
-            A::fma(s, w0, v[i]);
-            if (FM >= 2) A::fma(s, w1, v[N + i]);
+            typename A::acc s = A::from(v[FM * N + vi]);
+            A::fma(s, w0, v[vi]);
+            if (FM >= 2) A::fma(s, w1, v[N + vi]);
             b[i] = A::get(s);
           }
         }
@@ -442,9 +527,17 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
 #pragma unroll
           for (int t = 0; t < FD; ++t) Tagged<real>::put(e + t * W, psiY[t], ptag);
         }
-        real* P = a.psi + dirbase + cell_of(sc) * N + base;
+        if (VEC) {  // physical order by swaps, then 16-byte stores
+          real o[N];
 #pragma unroll
-        for (int i = 0; i < N; ++i) P[off(i)] = x[i];
+          for (int i = 0; i < N; ++i) o[i] = x[i];
+          xor_permute<real, N>(o, fmask);
+          store_cell<real, N>(a.psi + dirbase + cell_of(sc) * N, o);
+        } else {
+          real* P = a.psi + dirbase + cell_of(sc) * N + base;
+#pragma unroll
+          for (int i = 0; i < N; ++i) P[off(i)] = x[i];
+        }
       }
     }
   }
