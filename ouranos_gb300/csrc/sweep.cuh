@@ -219,6 +219,38 @@ struct Bits<df64> {
     return w ? __float_as_uint(v.lo) : __float_as_uint(v.hi);
   }
 };
+// value from its 32-bit words (little endian)
+template <typename real>
+__device__ __forceinline__ real from_words(unsigned w0, unsigned w1);
+template <>
+__device__ __forceinline__ float from_words<float>(unsigned w0, unsigned) { return __uint_as_float(w0); }
+template <>
+__device__ __forceinline__ double from_words<double>(unsigned w0, unsigned w1) {
+  return __longlong_as_double((long long)(((unsigned long long)w1 << 32) | w0));
+}
+template <>
+__device__ __forceinline__ df64 from_words<df64>(unsigned w0, unsigned w1) {
+  return df64(__uint_as_float(w0), __uint_as_float(w1));
+}
+// o[0..N) = src[0..N) with 16-byte shared-memory loads (src 16-byte aligned)
+template <typename real, int N>
+__device__ __forceinline__ void load_cell(const real* src, real (&o)[N]) {
+  constexpr int W = Bits<real>::W;
+#pragma unroll
+  for (int k = 0; k < (int)(N * sizeof(real) / 16); ++k) {
+    const uint4 u = *reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(src) + 16 * k);
+    if (W == 1) {
+      o[4 * k + 0] = from_words<real>(u.x, 0);
+      o[4 * k + 1] = from_words<real>(u.y, 0);
+      o[4 * k + 2] = from_words<real>(u.z, 0);
+      o[4 * k + 3] = from_words<real>(u.w, 0);
+    } else {
+      o[2 * k + 0] = from_words<real>(u.x, u.y);
+      o[2 * k + 1] = from_words<real>(u.z, u.w);
+    }
+  }
+}
+
 // dst[0..N) = o[0..N) with 16-byte stores (dst 16-byte aligned)
 template <typename real, int N>
 __device__ __forceinline__ void store_cell(real* dst, const real (&o)[N]) {
@@ -277,7 +309,14 @@ struct Stream {
   // values streamed per plane and lane: the expanded source (FM = 0) or FM
   // moments plus the isotropic source
   static constexpr int NV = FM == 0 ? N : (FM + 1) * N;
-  static constexpr size_t warp_bytes = (size_t)kRing * 32 * (NV * sizeof(real) + sizeof(int));
+  // Q1 cells (N = 4 in 2-D, 8 in 3-D) move in 16-byte pieces; their ring slots
+  // are read back with 16-byte shared loads, so each lane's stride is padded to
+  // an odd number of 16-byte units: the 8 lanes of one access phase then fall
+  // on 8 different 4-bank groups
+  static constexpr bool VEC = (N == 4 || N == 8) && (N * sizeof(real)) % 16 == 0;
+  static constexpr int PAD = VEC && ((NV * sizeof(real) / 16) % 2 == 0) ? (int)(16 / sizeof(real)) : 0;
+  static constexpr int NVP = NV + PAD;  // per-lane stride of the ring, in values
+  static constexpr size_t warp_bytes = (size_t)kRing * 32 * (NVP * sizeof(real) + sizeof(int));
 };
 
 // One task: a tile of wx x wy columns for kd directions, swept over the whole
@@ -292,13 +331,14 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
   constexpr int N = C::N;
   constexpr int FD = C::FD;
   constexpr int NV = Stream<real, FM, N>::NV;
+  constexpr int NVP = Stream<real, FM, N>::NVP;
   constexpr int W = Tagged<real>::W;
   constexpr unsigned FULL = 0xffffffffu;
   using A = Arith<real>;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   real* ring = reinterpret_cast<real*>(smem_raw + warp * Stream<real, FM, N>::warp_bytes);
-  int* cring = reinterpret_cast<int*>(ring + kRing * 32 * NV);
+  int* cring = reinterpret_cast<int*>(ring + kRing * 32 * NVP);
   const int wc = a.wx * a.wy;
   const int kslot = lane / wc;
   const int cl = lane - kslot * wc;
@@ -340,7 +380,8 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
     // Q1 cells: mirroring an axis flips one bit of the local index, so the
     // physical position of canonical dof i is i ^ fmask and a cell's values
     // move as whole 16-byte pieces
-    constexpr bool VEC = P1 == 2 && (N * sizeof(real)) % 16 == 0;
+    constexpr bool VEC = Stream<real, FM, N>::VEC;
+    static_assert(!VEC || P1 == 2, "the 16-byte path relies on the XOR form of Q1 mirroring");
     const int fmask = flip & (N - 1);
     auto off = [&](int i) {
       return C::comp(i, 0) * st0 + C::comp(i, 1) * st1 + (DIM == 3 ? C::comp(i, 2) * st2 : 0);
@@ -362,7 +403,7 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
     // stream the source of plane pl into ring slot pl % kRing (one cp.async group per plane)
     auto issue = [&](int pl) {
       if (col_ok && pl < NS) {
-        real* v = ring + ((pl % kRing) * 32 + lane) * NV;
+        real* v = ring + ((pl % kRing) * 32 + lane) * NVP;
         const long cell = cell_of(pl);
         const long cb = cell * N + base;
         const unsigned cdst = (unsigned)__cvta_generic_to_shared(cring + (pl % kRing) * 32 + lane);
@@ -450,19 +491,43 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
 
       if (act) {
         cp_async_wait<kPrefetch - 1>();  // plane sc has landed
-        const real* v = ring + ((sc % kRing) * 32 + lane) * NV;
+        const real* v = ring + ((sc % kRing) * 32 + lane) * NVP;
         const int cls = cring[(sc % kRing) * 32 + lane];
         real b[N];
+        if (VEC) {  // 16-byte loads of the slot (physical order), then canonical order
+          real t0v[N], t1v[N], isv[N];
+          load_cell<real, N>(v, t0v);
+          xor_permute<real, N>(t0v, fmask);
+          if (FM >= 2) {
+            load_cell<real, N>(v + N, t1v);
+            xor_permute<real, N>(t1v, fmask);
+          }
+          if (FM >= 1) {
+            load_cell<real, N>(v + FM * N, isv);
+            xor_permute<real, N>(isv, fmask);
+          }
 #pragma unroll
-        for (int i = 0; i < N; ++i) {
-          const int vi = VEC ? (i ^ fmask) : i;  // ring in physical order on the vector path
-          if (FM == 0) {
-            b[i] = v[vi];
-          } else {  // sum_m M2D(d, m) T_m + isotropic source
-            typename A::acc s = A::from(v[FM * N + vi]);
-            A::fma(s, w0, v[vi]);
-            if (FM >= 2) A::fma(s, w1, v[N + vi]);
-            b[i] = A::get(s);
+          for (int i = 0; i < N; ++i) {
+            if (FM == 0) {
+              b[i] = t0v[i];
+            } else {  // sum_m M2D(d, m) T_m + isotropic source
+              typename A::acc s = A::from(isv[i]);
+              A::fma(s, w0, t0v[i]);
+              if (FM >= 2) A::fma(s, w1, t1v[i]);
+              b[i] = A::get(s);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            if (FM == 0) {
+              b[i] = v[i];
+            } else {  // sum_m M2D(d, m) T_m + isotropic source
+              typename A::acc s = A::from(v[FM * N + i]);
+              A::fma(s, w0, v[i]);
+              if (FM >= 2) A::fma(s, w1, v[N + i]);
+              b[i] = A::get(s);
+            }
           }
         }
         issue(sc + kPrefetch);  // refills the slot consumed one step ago
