@@ -4,6 +4,7 @@
 // out on device vectors).  Gram-Schmidt, norms and dot products are FP64
 // (classical Gram-Schmidt with one re-orthogonalisation pass); the small
 // Hessenberg least-squares problem is solved on the host.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -39,7 +40,8 @@ struct Work {
   long len;
   int nvec;
   double* base = nullptr;
-  double** dptrs = nullptr;   // device array of vector pointers
+  double** dptrs = nullptr;   // device array of vector pointers (scratch, 64)
+  double** vptrs = nullptr;   // device array of every basis vector's pointer (64)
   double* dres = nullptr;     // device results (64) + partials
   unsigned* done = nullptr;
   std::vector<double*> vec;   // host copy of vector pointers
@@ -51,7 +53,7 @@ int make_work(ouranos_rt* rt, int nvec, Work& w) {
   w.len = (long)rt->n_mom * rt->n_dofs;
   w.nvec = nvec;
   const size_t vbytes = sizeof(double) * (size_t)w.len;
-  const size_t ptr_bytes = sizeof(double*) * 64;
+  const size_t ptr_bytes = sizeof(double*) * 128;
   const size_t res_bytes = sizeof(double) * (64 + 64 * (size_t)kDotGrid);
   const size_t total = vbytes * nvec + ptr_bytes + res_bytes + 256;
   CUC(rt->d_krylov.alloc(total), "solver workspace");
@@ -61,23 +63,10 @@ int make_work(ouranos_rt* rt, int nvec, Work& w) {
   for (int i = 0; i < nvec; ++i) w.vec[i] = w.base + (size_t)i * w.len;
   p += vbytes * nvec;
   w.dptrs = (double**)p;
+  w.vptrs = w.dptrs + 64;
   p += ptr_bytes;
   w.dres = (double*)p;
   w.done = (unsigned*)(rt->d_ctrl.as<int>() + 2);
-  return OURANOS_OK;
-}
-
-// out[j] = <V_first+j, y>, j < k (host result)
-int dots(Work& w, int first, int k, const double* y, double* out) {
-  ouranos_rt* rt = w.rt;
-  CUC(cudaMemcpyAsync(w.dptrs, &w.vec[first], sizeof(double*) * k, cudaMemcpyHostToDevice,
-                      rt->stream),
-      "dots");
-  CUC(launch_dots((const double* const*)w.dptrs, y, k, w.len, w.dres, w.dres + 64, w.done,
-                  rt->stream),
-      "dots");
-  CUC(cudaMemcpyAsync(out, w.dres, sizeof(double) * k, cudaMemcpyDeviceToHost, rt->stream), "dots");
-  CUC(cudaStreamSynchronize(rt->stream), "dots");
   return OURANOS_OK;
 }
 
@@ -97,22 +86,6 @@ double nrm(Work& w, const double* a, int* rc) {
   double v = 0.0;
   *rc = dot_pair(w, a, a, &v);
   return std::sqrt(std::fmax(v, 0.0));
-}
-
-// w -= sum_j h_j V_{first+j} with h = V^T w, twice (CGS2); h accumulates into hout
-int orthogonalise(Work& w, int first, int k, double* target, double* hout) {
-  ouranos_rt* rt = w.rt;
-  std::vector<double> h(k);
-  for (int j = 0; j < k; ++j) hout[j] = 0.0;
-  for (int pass = 0; pass < 2; ++pass) {
-    RC(dots(w, first, k, target, h.data()));
-    // coefficients are already on the device in w.dres[0..k)
-    CUC(launch_multi_axpy((const double* const*)w.dptrs, k, w.dres, -1.0, target, w.len,
-                          rt->stream),
-        "orthogonalise");
-    for (int j = 0; j < k; ++j) hout[j] += h[j];
-  }
-  return OURANOS_OK;
 }
 
 // op(x) -> y : FP64 or FP32 sweep Apply
@@ -155,6 +128,17 @@ int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double
   RC(make_work(rt, nv, w));
   const int V0 = 0, Z0 = m + 1, R = nv - 1;
   int rc = 0;
+  // the basis pointers once, and a pinned block for each iteration's
+  // Gram-Schmidt coefficients ([0,32) pass 1, [32,64) pass 2, [64] |w|^2)
+  CUC(cudaMemcpyAsync(w.vptrs, &w.vec[V0], sizeof(double*) * (m + 1), cudaMemcpyHostToDevice, rt->stream),
+      "gmres");
+  struct Pinned {
+    double* p = nullptr;
+    ~Pinned() {
+      if (p) cudaFreeHost(p);
+    }
+  } hb;
+  CUC(cudaMallocHost((void**)&hb.p, sizeof(double) * 128), "gmres");
   const double bnorm = nrm(w, b, &rc);
   RC(rc);
   if (!warm) CUC(cudaMemsetAsync(x, 0, sizeof(double) * w.len, rt->stream), "gmres");
@@ -203,11 +187,27 @@ int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double
       }
       double* nxt = w.v(V0 + k + 1);
       RC(apply_prec(rt, inner_prec, vin, nxt));
-      RC(orthogonalise(w, V0, k + 1, nxt, col.data()));
-      const double hn = nrm(w, nxt, &rc);
-      RC(rc);
+      // CGS2 with the coefficients kept on the device, the norm and the
+      // normalisation too: one host synchronisation per iteration
+      for (int pass = 0; pass < 2; ++pass) {
+        CUC(launch_dots((const double* const*)w.vptrs, nxt, k + 1, w.len, w.dres, w.dres + 64, w.done,
+                        rt->stream),
+            "orthogonalise");
+        CUC(cudaMemcpyAsync(hb.p + 32 * pass, w.dres, sizeof(double) * (k + 1), cudaMemcpyDeviceToHost,
+                            rt->stream),
+            "orthogonalise");
+        CUC(launch_multi_axpy((const double* const*)w.vptrs, k + 1, w.dres, -1.0, nxt, w.len, rt->stream),
+            "orthogonalise");
+      }
+      CUC(launch_dots((const double* const*)(w.vptrs + k + 1), nxt, 1, w.len, w.dres, w.dres + 64, w.done,
+                      rt->stream),
+          "norm");
+      CUC(cudaMemcpyAsync(hb.p + 64, w.dres, sizeof(double), cudaMemcpyDeviceToHost, rt->stream), "norm");
+      CUC(launch_scale_inv_norm(w.dres, nxt, w.len, rt->stream), "normalise");
+      CUC(cudaStreamSynchronize(rt->stream), "gmres");
+      for (int j = 0; j <= k; ++j) col[j] = hb.p[j] + hb.p[32 + j];
+      const double hn = std::sqrt(std::max(hb.p[64], 0.0));
       col[k + 1] = hn;
-      if (hn > 0) CUC(launch_axpby(1.0 / hn, nxt, 0.0, nxt, w.len, rt->stream), "gmres");
       const double est = gv.add_column(k, col.data()) / bnorm;
       ++total;
       if (hist) hist[total] = est;
