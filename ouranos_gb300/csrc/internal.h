@@ -173,7 +173,7 @@ template <typename real>
 cudaError_t launch_angular_source(real* q, const float* psi, const double* cell_mass, double inv_vdt,
                                   int n, long n_cells, int n_dir, cudaStream_t s);
 cudaError_t launch_scale_inv_norm(const double* nrm2, double* v, long len, cudaStream_t s);
-constexpr int kDotGrid = 304;  // blocks of the dot-product kernel (2 per SM)
+constexpr int kDotGrid = 1216;  // blocks of the dot-product kernel (8 per SM: enough loads in flight)
 cudaError_t launch_dots(const double* const* xs, const double* y, int k, long len, double* out,
                         double* partial, unsigned int* done, cudaStream_t s);
 

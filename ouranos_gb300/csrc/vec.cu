@@ -97,13 +97,25 @@ __global__ void permute_kernel(const double* in, double* out, const long* order,
 }
 
 // w += scale * sum_j coef[j] V_j  (coef on the device)
+// w += scale * sum_j coef[j] V[j]; pointers and coefficients staged in shared
+// memory, the sum split over four accumulators so the k loads overlap
+template <int KMAX>
 __global__ void multi_axpy_kernel(const double* const* V, int k, const double* coef, double scale,
                                   double* w, long len) {
+  __shared__ const double* sv[KMAX];
+  __shared__ double sc[KMAX];
+  for (int j = threadIdx.x; j < KMAX; j += blockDim.x) {
+    sv[j] = j < k ? V[j] : nullptr;
+    sc[j] = j < k ? coef[j] * scale : 0.0;
+  }
+  __syncthreads();
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len;
        e += (long)gridDim.x * blockDim.x) {
-    double acc = 0.0;
-    for (int j = 0; j < k; ++j) acc += coef[j] * V[j][e];
-    w[e] += scale * acc;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int j = 0; j < KMAX; ++j)
+      if (j < k) acc[j & 3] += sc[j] * __ldg(sv[j] + e);
+    w[e] += (acc[0] + acc[1]) + (acc[2] + acc[3]);
   }
 }
 
@@ -113,48 +125,54 @@ __global__ void axpby_kernel(double a, const double* x, double b, double* y, lon
     y[e] = b == 0.0 ? a * x[e] : a * x[e] + b * y[e];  // y may be uninitialised when b == 0
 }
 
-// out[j] = sum_i xs[j][i] * y[i], j < k; one block per chunk writes partial
-// sums, the last block to finish reduces them in a fixed order (deterministic).
-template <int KMAX>
-__global__ void dots_kernel(const double* const* xs, const double* y, int k, long len,
-                            double* partial, double* out, unsigned int* done) {
-  __shared__ double red[KMAX][kBlock / 32];
-  __shared__ bool last;
-  double acc[KMAX];
-#pragma unroll
-  for (int j = 0; j < KMAX; ++j) acc[j] = 0.0;
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len;
-       e += (long)gridDim.x * blockDim.x) {
-    const double yv = y[e];
-#pragma unroll
-    for (int j = 0; j < KMAX; ++j)
-      if (j < k) acc[j] += xs[j][e] * yv;
-  }
+// out[j] = sum_i xs[j][i] * y[i], j < k, in two launches.  Block b reduces its
+// grid-stride slice into partial[j * gridDim.x + b], taking the vectors in
+// chunks of 8 (8 accumulators and 8 loads in flight per element; y is re-read
+// once per chunk); then one warp per output sums the partials in a fixed order
+// (deterministic, no atomics).
+constexpr int kDotChunk = 8;
+__global__ void __launch_bounds__(kBlock) dots_partial_kernel(const double* const* xs, const double* y, int k,
+                                                              long len, double* partial) {
+  __shared__ const double* sx[32];
+  __shared__ double red[kDotChunk][kBlock / 32];
+  for (int j = threadIdx.x; j < 32; j += blockDim.x) sx[j] = j < k ? xs[j] : nullptr;
+  __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int j0 = 0; j0 < k; j0 += kDotChunk) {
+    double acc[kDotChunk];
 #pragma unroll
-  for (int j = 0; j < KMAX; ++j) {
-    double v = acc[j];
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) red[j][warp] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < k) {
-    double v = 0.0;
-    for (int w = 0; w < kBlock / 32; ++w) v += red[threadIdx.x][w];
-    partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = v;
-  }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) last = (atomicAdd(done, 1u) == gridDim.x - 1);
-  __syncthreads();
-  if (last) {
-    __threadfence();
-    for (int j = threadIdx.x; j < k; j += blockDim.x) {
-      double v = 0.0;
-      for (unsigned b = 0; b < gridDim.x; ++b) v += partial[(size_t)j * gridDim.x + b];
-      out[j] = v;
+    for (int jj = 0; jj < kDotChunk; ++jj) acc[jj] = 0.0;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len;
+         e += (long)gridDim.x * blockDim.x) {
+      const double yv = __ldg(y + e);
+#pragma unroll
+      for (int jj = 0; jj < kDotChunk; ++jj)
+        if (j0 + jj < k) acc[jj] += __ldg(sx[j0 + jj] + e) * yv;
     }
-    if (threadIdx.x == 0) *done = 0;
+#pragma unroll
+    for (int jj = 0; jj < kDotChunk; ++jj) {
+      double v = acc[jj];
+      for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[jj][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kDotChunk && j0 + (int)threadIdx.x < k) {
+      double v = 0.0;
+      for (int w = 0; w < kBlock / 32; ++w) v += red[threadIdx.x][w];
+      partial[(size_t)(j0 + threadIdx.x) * gridDim.x + blockIdx.x] = v;
+    }
+    __syncthreads();
+  }
+}
+__global__ void __launch_bounds__(kBlock) dots_final_kernel(const double* partial, int k, int nblocks,
+                                                            double* out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int j = warp; j < k; j += kBlock / 32) {
+    const double* pj = partial + (size_t)j * nblocks;
+    double v = 0.0;
+    for (int b = lane; b < nblocks; b += 32) v += pj[b];
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) out[j] = v;
   }
 }
 
@@ -439,7 +457,12 @@ cudaError_t launch_permute(const double* in, double* out, const long* order, lon
 
 cudaError_t launch_multi_axpy(const double* const* V, int k, const double* coef, double scale,
                               double* w, long len, cudaStream_t s) {
-  multi_axpy_kernel<<<grid_for(len), kBlock, 0, s>>>(V, k, coef, scale, w, len);
+  if (k <= 8)
+    multi_axpy_kernel<8><<<grid_for(len), kBlock, 0, s>>>(V, k, coef, scale, w, len);
+  else if (k <= 32)
+    multi_axpy_kernel<32><<<grid_for(len), kBlock, 0, s>>>(V, k, coef, scale, w, len);
+  else
+    return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 
@@ -527,19 +550,14 @@ cudaError_t launch_axpby(double a, const double* x, double b, double* y, long le
   return cudaGetLastError();
 }
 
-// xs: device array of k device pointers; out: k doubles; partial: k * kDotGrid
-// doubles; done: a zeroed counter that the kernel leaves zeroed.
+// xs: device array of k (<= 32) device pointers; out: k doubles; partial:
+// k * kDotGrid doubles.  (`done` is not used by this two-launch form.)
 cudaError_t launch_dots(const double* const* xs, const double* y, int k, long len, double* out,
                         double* partial, unsigned int* done, cudaStream_t s) {
-  const int grid = kDotGrid;
-  if (k <= 1)
-    dots_kernel<1><<<grid, kBlock, 0, s>>>(xs, y, k, len, partial, out, done);
-  else if (k <= 8)
-    dots_kernel<8><<<grid, kBlock, 0, s>>>(xs, y, k, len, partial, out, done);
-  else if (k <= 32)
-    dots_kernel<32><<<grid, kBlock, 0, s>>>(xs, y, k, len, partial, out, done);
-  else
-    return cudaErrorInvalidValue;
+  (void)done;
+  if (k < 1 || k > 32) return cudaErrorInvalidValue;
+  dots_partial_kernel<<<kDotGrid, kBlock, 0, s>>>(xs, y, k, len, partial);
+  dots_final_kernel<<<1, kBlock, 0, s>>>(partial, k, kDotGrid, out);
   return cudaGetLastError();
 }
 
