@@ -281,8 +281,13 @@ __device__ __forceinline__ void xor_permute(real (&o)[N], int m) {
 
 // planes prefetched ahead of the one being solved; the ring has one more slot
 // so the slot being refilled was consumed a step earlier
-constexpr int kPrefetch = 3;
-constexpr int kRing = kPrefetch + 1;
+// (measured on GB300: 3 planes for FP32 values, 2 for 8-byte values, whose
+// smaller ring lets more blocks share an SM)
+template <typename real>
+struct Prefetch {
+  static constexpr int PF = sizeof(real) == 8 ? 2 : 3;
+  static constexpr int RING = PF + 1;
+};
 
 template <int DIM, int P1>
 struct Cell {
@@ -316,7 +321,7 @@ struct Stream {
   static constexpr bool VEC = (N == 4 || N == 8) && (N * sizeof(real)) % 16 == 0;
   static constexpr int PAD = VEC && ((NV * sizeof(real) / 16) % 2 == 0) ? (int)(16 / sizeof(real)) : 0;
   static constexpr int NVP = NV + PAD;  // per-lane stride of the ring, in values
-  static constexpr size_t warp_bytes = (size_t)kRing * 32 * (NVP * sizeof(real) + sizeof(int));
+  static constexpr size_t warp_bytes = (size_t)Prefetch<real>::RING * 32 * (NVP * sizeof(real) + sizeof(int));
 };
 
 // One task: a tile of wx x wy columns for kd directions, swept over the whole
@@ -338,6 +343,8 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   real* ring = reinterpret_cast<real*>(smem_raw + warp * Stream<real, FM, N>::warp_bytes);
+  constexpr int kPrefetch = Prefetch<real>::PF;
+  constexpr int kRing = Prefetch<real>::RING;
   int* cring = reinterpret_cast<int*>(ring + kRing * 32 * NVP);
   const int wc = a.wx * a.wy;
   const int kslot = lane / wc;
