@@ -322,7 +322,8 @@ def run_solve(args):
     """Time to a 1e-8 relative residual on the 3-D thick diffusive workload
     (64^3 hexes, DG Q1, GLC S12 = 168 directions, 4^3-cell blocks of
     (sigma_t, c) = (100, 0.999) or (1, 0.9)): plain FP64 GMRES(30) against
-    FGMRES(30) with FP32 sweeps and FP64 refinement.  Reports wall time,
+    FGMRES(30) with FP32 sweeps and FP64 refinement, each also with the
+    diffusion synthetic acceleration as right preconditioner ("+dsa").  Reports wall time,
     iterations, the FP64 true residual and the scalar-flux error of the mixed
     solve against the FP64 solve."""
     import numpy as np
@@ -342,8 +343,12 @@ def run_solve(args):
             else:
                 methods.remove("fgmres_learned")
                 out["learned_weights"] = None
+        if any(m.endswith("+dsa") for m in methods):
+            rt.set_dsa(args.dsa_cg)
+            out["dsa_cg_steps"] = args.dsa_cg
         for method in methods:
-            x, info, hist = rt.solve(method, tol=args.tol, max_it=args.max_it, restart=30)
+            base, dsa = (method[:-4], True) if method.endswith("+dsa") else (method, False)
+            x, info, hist = rt.solve(base, tol=args.tol, max_it=args.max_it, restart=30, dsa=dsa)
             res[method] = (x, info)
             out[method] = {k: info[k] for k in ("iterations", "restarts", "residual", "seconds",
                                                 "converged")}
@@ -442,33 +447,40 @@ def run_time(args):
     out = {"workload": "3d-td-%d^3-dgq1-ls8-%dsteps" % (args.time_n, args.time_steps), "tol": args.tol,
            "inv_vdt": inv_vdt}
 
-    def run(method, steps):
+    def run(method, steps, dsa=False):
         with og.RadiativeTransfer(prob) as rt:
             rt.set_time_step(inv_vdt)
+            if dsa:
+                rt.set_dsa(args.dsa_cg)
             phi = np.zeros(rt.length)
             its, secs = [], []
             t0 = time.perf_counter()
             for n in range(steps):
                 rt.set_source([[0.0], [og.pulse_strength(n)]])
-                info = rt.time_advance(phi, method=method, tol=args.tol, max_it=args.max_it)
+                info = rt.time_advance(phi, method=method, tol=args.tol, max_it=args.max_it, dsa=dsa)
                 its.append(info["iterations"])
                 secs.append(info["seconds"])
             wall = time.perf_counter() - t0
             return phi, its, secs, wall
 
-    phi, its, secs, wall = run("fgmres_mixed", args.time_steps)
-    out["fgmres_mixed"] = {"wall_s": wall, "s_per_step": wall / args.time_steps,
+    dsa = not args.time_no_dsa
+    main_name = "fgmres_mixed+dsa" if dsa else "fgmres_mixed"
+    phi, its, secs, wall = run("fgmres_mixed", args.time_steps, dsa)
+    out[main_name] = {"wall_s": wall, "s_per_step": wall / args.time_steps,
                            "iterations_total": int(sum(its)), "iterations_max": int(max(its)),
                            "iterations_at_peak": int(its[min(20, len(its) - 1)]),
                            "scalar_flux_max_final": float(phi.max())}
     if args.time_compare:
         k = min(args.time_compare, args.time_steps)
-        p32, i32, s32, w32 = run("fgmres_mixed", k)
+        p32, i32, s32, w32 = run("fgmres_mixed", k, dsa)
         p64, i64, s64, w64 = run("gmres", k)
         out["compare_first_steps"] = {
-            "steps": k, "fgmres_mixed_s": w32, "gmres_fp64_s": w64, "speedup": w64 / w32,
-            "iterations_fp32": int(sum(i32)), "iterations_fp64": int(sum(i64)),
+            "steps": k, main_name + "_s": w32, "gmres_fp64_s": w64, "speedup": w64 / w32,
+            "iterations_" + main_name: int(sum(i32)), "iterations_fp64": int(sum(i64)),
             "flux_rel_l2_vs_fp64": float(np.linalg.norm(p32 - p64) / max(np.linalg.norm(p64), 1e-300))}
+        if dsa:
+            pm, im_, sm, wm = run("fgmres_mixed", k)
+            out["compare_first_steps"].update({"fgmres_mixed_s": wm, "iterations_fgmres_mixed": int(sum(im_))})
     print(json.dumps({"time": out}), flush=True)
 
 
@@ -486,7 +498,8 @@ def main():
     ap.add_argument("--solve-seed", type=int, default=7000, help="evaluation map (training uses 2000+)")
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--max-it", type=int, default=3000)
-    ap.add_argument("--methods", default="gmres,fgmres_mixed,fgmres_learned")
+    ap.add_argument("--methods", default="gmres,fgmres_mixed,gmres+dsa,fgmres_mixed+dsa,fgmres_learned")
+    ap.add_argument("--dsa-cg", type=int, default=20, help="CG steps of the diffusion correction")
     ap.add_argument("--batch", action="store_true", help="batched uneven 2-D workload")
     ap.add_argument("--batch-count", type=int, default=64)
     ap.add_argument("--batch-seed", type=int, default=3000)
@@ -496,6 +509,7 @@ def main():
     ap.add_argument("--time-steps", type=int, default=100)
     ap.add_argument("--time-seed", type=int, default=4000)
     ap.add_argument("--time-compare", type=int, default=5)
+    ap.add_argument("--time-no-dsa", action="store_true", help="steps without the diffusion acceleration")
     args = ap.parse_args()
     if args.time:
         import __graft_entry__

@@ -215,6 +215,10 @@ int ouranos_rt_apply_noalloc(ouranos_rt* rt, const double* x, double* y);
 #define OURANOS_SOLVER_FGMRES_LEARNED 4
 /* OR into the solver: x holds the initial guess (not with BiCGSTAB) */
 #define OURANOS_SOLVER_WARM_START 0x100
+/* OR into SI, GMRES, FGMRES_MIXED or FGMRES_LEARNED: diffusion synthetic
+ * acceleration (ouranos_rt_set_dsa) as the right preconditioner (GMRES becomes
+ * FGMRES with FP64 sweeps), or as the acceleration step of SI */
+#define OURANOS_SOLVER_DSA 0x200
 
 typedef struct ouranos_solve_info {
   int iterations;           /* operator applications in the Krylov/SI loop */
@@ -321,6 +325,20 @@ int ouranos_rt_pc_features(ouranos_rt* rt, const double* v, float* features, dou
 int ouranos_rt_pc_target(ouranos_rt* rt, const double* v, const double* e, float* target);
 /* z = v + s g_c y, y the network output on v's features (device vectors) */
 int ouranos_rt_pc_apply(ouranos_rt* rt, const double* v, double* z);
+
+/* ------------------------------------- diffusion synthetic acceleration
+ * No counterpart in the reference (identity preconditioner, plain source
+ * iteration: src/ouranos.cc:72-95,160-171).  For a DG Q1 mesh (2-D or 3-D):
+ *   P v = v + f,  (-div D grad + sigma_a) f = sigma_s0 v_0,
+ * f continuous Q1 on the mesh vertices (Marshak condition on vacuum and inflow
+ * boundaries, zero current on reflective ones), D = 1/(3(sigma_t' - sigma_s1)),
+ * sigma_a = sigma_t' - sigma_s0, sigma_t' = sigma_t + 1/(v dt); f is added to
+ * the scalar moment's nodal values.  The diffusion system is solved by
+ * cg_iterations steps of Jacobi-preconditioned CG (FP32, FP64 scalars);
+ * 0 switches the acceleration off.  UNSUPPORTED unless the mesh is DG Q1. */
+int ouranos_rt_set_dsa(ouranos_rt* rt, int cg_iterations);
+/* z = P v ([mom][dof], host or device; z may equal v) */
+int ouranos_rt_dsa_apply(ouranos_rt* rt, const double* v, double* z);
 
 #ifdef __cplusplus
 }

@@ -24,6 +24,7 @@ FP64, FP32 = 0, 1
 FP64_NATIVE, FP64_DF64, FP64_DF64_SWEEP = 0, 1, 2
 SOLVER_SI, SOLVER_GMRES, SOLVER_BICGSTAB, SOLVER_FGMRES_MIXED, SOLVER_FGMRES_LEARNED = 0, 1, 2, 3, 4
 SOLVER_WARM_START = 0x100
+SOLVER_DSA = 0x200
 
 # every symbol include/ouranos_gb300.h declares
 EXPORTS = [
@@ -45,6 +46,7 @@ EXPORTS = [
     "ouranos_batch_stats", "ouranos_batch_last_error",
     "ouranos_rt_set_time_step", "ouranos_rt_set_source", "ouranos_rt_time_advance",
     "ouranos_rt_get_angular_flux", "ouranos_rt_set_angular_flux",
+    "ouranos_rt_set_dsa", "ouranos_rt_dsa_apply",
 ]
 
 
@@ -127,6 +129,8 @@ def lib():
         "ouranos_rt_time_advance": [vp, i, i, i, d, vp, C.POINTER(SolveInfo)],
         "ouranos_rt_get_angular_flux": [vp, vp],
         "ouranos_rt_set_angular_flux": [vp, vp],
+        "ouranos_rt_set_dsa": [vp, i],
+        "ouranos_rt_dsa_apply": [vp, vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

@@ -222,6 +222,9 @@ namespace ouranos {
 // learned preconditioner glue (precond.cu)
 int rt_pc_features(ouranos_rt* rt, const double* v, float* feat);
 int rt_pc_correct(ouranos_rt* rt, const double* v, const float* y, double* z);
+// diffusion synthetic acceleration (dsa.cu): out = v + f on the handle's stream
+int rt_dsa_apply(ouranos_rt* rt, const double* v, double* out);
+int rt_dsa_kernels(const ouranos_rt* rt);  // launches of one rt_dsa_apply
 // the network's cell grid
 void cnn_grid(const ouranos_cnn* net, int* nx, int* ny, int* nz);
 // Device-side pieces the solvers use (operator.cu).
@@ -293,4 +296,9 @@ struct ouranos_rt {
   ouranos_cnn* cnn = nullptr;
   int pc_group = -1;
   ouranos::DevBuf d_pc_prop, d_pc_work, d_pc_feat, d_pc_nodal, d_pc_vert;
+  // diffusion synthetic acceleration: CG steps (0 = off), cell coefficients,
+  // CG vectors and reductions; tables valid for (dsa_group, dsa_inv_vdt)
+  int dsa_iters = 0, dsa_group = -1;
+  double dsa_inv_vdt = -1.0;
+  ouranos::DevBuf d_dsa_cell, d_dsa_vec, d_dsa_red;
 };

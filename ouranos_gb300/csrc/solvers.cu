@@ -117,11 +117,13 @@ int update(Work& w, int first, const std::vector<double>& y, double* x) {
 // from the FP64 true residual.  mixed: the cycle stops once its own residual
 // estimate has dropped by `inner_drop` (FP32 operator accuracy), and the FP64
 // restart refines the solution (iterative refinement).
+// dsa: the diffusion synthetic acceleration is the right preconditioner (and
+// the learned one's fallback).
 int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double* x,
           double* hist, ouranos_solve_info* info, int inner_prec, double inner_drop,
-          bool learned = false, bool warm = false) {
+          bool learned = false, bool warm = false, bool dsa = false) {
   m = std::max(1, std::min(m, 32));  // dot kernel handles up to 32 basis vectors
-  const bool flexible = inner_prec != OURANOS_FP64;
+  const bool flexible = inner_prec != OURANOS_FP64 || dsa;
   // vectors: V[0..m], Z[0..m-1] (flexible), r
   Work w;
   const int nv = (m + 1) + (flexible ? m : 0) + 1;
@@ -175,9 +177,12 @@ int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double
     for (; k < m && total < max_it; ++k) {
       const double* vin = w.v(V0 + k);
       if (flexible) {
-        // right preconditioner: z_k = P(v_k), learned correction or identity
+        // right preconditioner: z_k = P(v_k), learned correction, diffusion
+        // correction or identity
         if (use_pc) {
           RC(ouranos_rt_pc_apply(rt, vin, w.v(Z0 + k)));
+        } else if (dsa) {
+          RC(rt_dsa_apply(rt, vin, w.v(Z0 + k)));
         } else {
           CUC(cudaMemcpyAsync(w.v(Z0 + k), vin, sizeof(double) * w.len, cudaMemcpyDeviceToDevice,
                               rt->stream),
@@ -315,8 +320,10 @@ int bicgstab(ouranos_rt* rt, int max_it, double tol, const double* b, double* x,
 
 // Source iteration phi <- D L^-1 (M2D S phi + q + inflow) (src/ouranos.cc:72-95,
 // written as intended: a fresh sweep each iteration), relative-change test.
+// With dsa, the change of each iteration is accelerated by the diffusion
+// correction of its scalar moment: phi <- phi + P (T phi + rhs - phi).
 int source_iteration(ouranos_rt* rt, int max_it, double tol, const double* gf, const double* b,
-                     double* x, double* hist, ouranos_solve_info* info, bool warm) {
+                     double* x, double* hist, ouranos_solve_info* info, bool warm, bool dsa) {
   Work w;
   RC(make_work(rt, 3, w));
   double *xn = w.v(0), *dlt = w.v(1), *rr = w.v(2);
@@ -331,6 +338,11 @@ int source_iteration(ouranos_rt* rt, int max_it, double tol, const double* gf, c
     CUC(launch_axpby(1.0, b, 1.0, xn, w.len, rt->stream), "si");   // xn = T x + rhs
     CUC(cudaMemcpyAsync(dlt, xn, sizeof(double) * w.len, cudaMemcpyDeviceToDevice, rt->stream), "si");
     CUC(launch_axpby(-1.0, x, 1.0, dlt, w.len, rt->stream), "si");
+    if (dsa) {
+      RC(rt_dsa_apply(rt, dlt, dlt));
+      CUC(cudaMemcpyAsync(xn, x, sizeof(double) * w.len, cudaMemcpyDeviceToDevice, rt->stream), "si");
+      CUC(launch_axpby(1.0, dlt, 1.0, xn, w.len, rt->stream), "si");
+    }
     const double num = nrm(w, dlt, &rc);
     RC(rc);
     const double den = nrm(w, xn, &rc);
@@ -365,7 +377,13 @@ extern "C" int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it
                              ouranos_solve_info* info) {
   if (!rt || !x || max_it < 1 || !(tol > 0)) return OURANOS_ERR_BAD_INPUT;
   const bool warm = (solver & OURANOS_SOLVER_WARM_START) != 0;
-  solver &= ~OURANOS_SOLVER_WARM_START;
+  const bool dsa = (solver & OURANOS_SOLVER_DSA) != 0;
+  solver &= ~(OURANOS_SOLVER_WARM_START | OURANOS_SOLVER_DSA);
+  if (dsa && (solver == OURANOS_SOLVER_BICGSTAB || rt->dsa_iters < 1)) {
+    rt->err = solver == OURANOS_SOLVER_BICGSTAB ? "BiCGSTAB runs unpreconditioned"
+                                                : "diffusion acceleration is off (ouranos_rt_set_dsa)";
+    return OURANOS_ERR_BAD_INPUT;
+  }
   if (warm && solver == OURANOS_SOLVER_BICGSTAB) {
     rt->err = "BiCGSTAB starts from zero";
     return OURANOS_ERR_UNSUPPORTED;
@@ -394,18 +412,18 @@ extern "C" int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it
   int rc;
   switch (solver) {
     case OURANOS_SOLVER_SI:
-      rc = source_iteration(rt, max_it, tol, dgf, rhs.as<double>(), sol.as<double>(), hist, info, warm);
+      rc = source_iteration(rt, max_it, tol, dgf, rhs.as<double>(), sol.as<double>(), hist, info, warm, dsa);
       break;
     case OURANOS_SOLVER_GMRES:
       rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info,
-                 OURANOS_FP64, 0.0, false, warm);
+                 OURANOS_FP64, 0.0, false, warm, dsa);
       break;
     case OURANOS_SOLVER_BICGSTAB:
       rc = bicgstab(rt, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info);
       break;
     case OURANOS_SOLVER_FGMRES_MIXED:
       rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info,
-                 OURANOS_FP32, 1e-5, false, warm);
+                 OURANOS_FP32, 1e-5, false, warm, dsa);
       break;
     case OURANOS_SOLVER_FGMRES_LEARNED:
       if (!rt->cnn) {
@@ -414,7 +432,7 @@ extern "C" int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it
         break;
       }
       rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info,
-                 OURANOS_FP32, 1e-5, true, warm);
+                 OURANOS_FP32, 1e-5, true, warm, dsa);
       break;
     default:
       rt->err = "unknown solver";

@@ -183,11 +183,13 @@ class RadiativeTransfer:
         src = np.ascontiguousarray(source, dtype=np.float64)
         self._check(_capi.lib().ouranos_rt_set_source(self._h, src.ctypes.data))
 
-    def time_advance(self, phi, method="fgmres_mixed", tol=1e-8, max_it=1000, restart=30):
+    def time_advance(self, phi, method="fgmres_mixed", tol=1e-8, max_it=1000, restart=30, dsa=False):
         """One implicit Euler step: phi (in: guess, e.g. phi^n; out: phi^{n+1})."""
         kind = {"si": _capi.SOLVER_SI, "gmres": _capi.SOLVER_GMRES,
                 "fgmres_mixed": _capi.SOLVER_FGMRES_MIXED,
                 "fgmres_learned": _capi.SOLVER_FGMRES_LEARNED}[method]
+        if dsa:
+            kind |= _capi.SOLVER_DSA
         info = _capi.SolveInfo()
         self._check(_capi.lib().ouranos_rt_time_advance(self._h, kind, restart, max_it, tol, _ptr(phi),
                                                         C.byref(info)))
@@ -204,10 +206,24 @@ class RadiativeTransfer:
         psi = np.ascontiguousarray(psi, dtype=np.float64)
         self._check(_capi.lib().ouranos_rt_set_angular_flux(self._h, psi.ctypes.data))
 
+    def set_dsa(self, cg_iterations):
+        """Diffusion synthetic acceleration of the scalar flux (DG Q1 meshes):
+        the diffusion correction is solved by `cg_iterations` Jacobi-CG steps;
+        0 switches it off.  Solves use it with solve(..., dsa=True)."""
+        self._check(_capi.lib().ouranos_rt_set_dsa(self._h, int(cg_iterations)))
+
+    def dsa_apply(self, v, out=None):
+        """out = v + f, f the diffusion correction of v's scalar moment."""
+        if out is None:
+            out = np.empty_like(v) if isinstance(v, np.ndarray) else v.new_empty(v.shape)
+        self._check(_capi.lib().ouranos_rt_dsa_apply(self._h, _ptr(v), _ptr(out)))
+        return out
+
     def solve(self, method="gmres", tol=1e-8, max_it=1000, restart=30, group_flux=None, x=None,
-              warm=False):
+              warm=False, dsa=False):
         """Drivers of src/ouranos.cc:43-209. Returns (x, info dict, residual history);
-        warm=True starts from the given x."""
+        warm=True starts from the given x; dsa=True preconditions with the
+        diffusion synthetic acceleration (set_dsa)."""
         kind = {"si": _capi.SOLVER_SI, "gmres": _capi.SOLVER_GMRES,
                 "bicgstab": _capi.SOLVER_BICGSTAB, "fgmres_mixed": _capi.SOLVER_FGMRES_MIXED,
                 "fgmres_learned": _capi.SOLVER_FGMRES_LEARNED}[method]
@@ -215,6 +231,8 @@ class RadiativeTransfer:
             x = np.zeros(self.length)
         if warm:
             kind |= _capi.SOLVER_WARM_START
+        if dsa:
+            kind |= _capi.SOLVER_DSA
         hist = np.zeros(max_it + 2)
         info = _capi.SolveInfo()
         rc = _capi.lib().ouranos_solve(self._h, kind, restart, max_it, tol, _ptr(group_flux),

@@ -1,0 +1,138 @@
+"""Diffusion synthetic acceleration on the GPU: the correction against the
+oracle's restatement (FP32 CG against FP64 CG with the same number of steps),
+and its use in the solvers."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from helpers import rel_err
+from oracle import dsa_oracle as do
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+TOL_CG = 1e-4  # FP32 vectors against the FP64 restatement, relative L2 of the correction
+
+
+def _thick(n=8, seed=7000):
+    import ouranos_gb300 as og
+    return og.thick_3d(seed=seed, n=n, sn=4, width=10.0 * n / 64)
+
+
+def _check_apply(prob, k, inv_vdt=0.0):
+    import ouranos_gb300 as og
+    d = do.Diffusion(prob, inv_vdt=inv_vdt)
+    rng = np.random.default_rng(11)
+    with og.RadiativeTransfer(prob) as rt:
+        if inv_vdt:
+            rt.set_time_step(inv_vdt)
+        rt.set_dsa(k)
+        v = rng.standard_normal(rt.length)
+        z = rt.dsa_apply(v)
+        ref = d.apply(v, k=k)
+        n0 = d.vid.shape[0] * d.nodes
+        assert rel_err(z[:n0] - v[:n0], ref[:n0] - v[:n0]) < TOL_CG
+        assert np.array_equal(z[n0:], v[n0:])  # higher moments pass unchanged
+
+
+@pytest.mark.parametrize("k", [1, 3, 20])
+def test_3d_correction_matches_oracle(k):
+    _check_apply(_thick(), k)
+
+
+def test_3d_correction_with_time_step_matches_oracle():
+    _check_apply(_thick(seed=7001), 10, inv_vdt=0.5)
+
+
+@pytest.mark.parametrize("k", [1, 10])
+def test_2d_anisotropic_reflective_correction_matches_oracle(k):
+    """2-D Q1, P1 scattering (D uses sigma_s1), reflective on the low x and y
+    sides (no Marshak term there)."""
+    import ouranos_gb300 as og
+    p = og.heterogeneous_2d(seed=1201, n=12, fe_order=1, sn=4, l_max=1, g_aniso=0.5, blocks=4)
+    p = dataclasses.replace(p, bc_type=(3, 0, 3, 0, 0, 0))
+    _check_apply(p, k)
+
+
+def test_in_place_and_device_vectors():
+    import torch
+
+    import ouranos_gb300 as og
+    prob = _thick(seed=7002)
+    with og.RadiativeTransfer(prob) as rt:
+        rt.set_dsa(5)
+        v = np.random.default_rng(5).standard_normal(rt.length)
+        ref = rt.dsa_apply(v)
+        t = torch.tensor(v, device="cuda")
+        rt.dsa_apply(t, out=t)
+        assert np.array_equal(t.cpu().numpy(), ref)
+
+
+def test_unsupported_and_missing_setup():
+    import ouranos_gb300 as og
+    from ouranos_gb300 import _capi
+    p2 = og.heterogeneous_2d(seed=1202, n=8, fe_order=2, sn=4, l_max=0, blocks=2)
+    with og.RadiativeTransfer(p2) as rt:
+        with pytest.raises(_capi.OuranosError) as e:
+            rt.set_dsa(5)
+        assert e.value.code == _capi.ERR_UNSUPPORTED
+    with og.RadiativeTransfer(_thick()) as rt:
+        with pytest.raises(_capi.OuranosError) as e:
+            rt.solve("fgmres_mixed", dsa=True)
+        assert e.value.code == _capi.ERR_BAD_INPUT
+
+
+def test_fgmres_with_dsa_converges_in_fewer_iterations():
+    """16^3 thick diffusive map: FGMRES(30) with FP32 sweeps and the diffusion
+    correction reaches 1e-8 in a fraction of the plain iterations, at the FP64
+    GMRES solution (scalar flux within 1e-6)."""
+    import ouranos_gb300 as og
+    prob = _thick(n=16)
+    with og.RadiativeTransfer(prob) as rt:
+        x64, i64, _ = rt.solve("gmres", tol=1e-8, max_it=2000)
+        rt.set_dsa(20)
+        xm, im, _ = rt.solve("fgmres_mixed", tol=1e-8, max_it=2000, dsa=True)
+        xd, idd, _ = rt.solve("gmres", tol=1e-8, max_it=2000, dsa=True)
+    assert i64["converged"] and im["converged"] and idd["converged"]
+    assert im["iterations"] * 4 < i64["iterations"]
+    assert idd["iterations"] * 4 < i64["iterations"]
+    n0 = prob.total_cells * 8
+    assert rel_err(xm[:n0], x64[:n0]) < 1e-6
+    assert rel_err(xd[:n0], x64[:n0]) < 1e-6
+
+
+def test_source_iteration_with_dsa():
+    """Accelerated source iteration converges in far fewer sweeps than plain
+    source iteration, to the GMRES solution."""
+    import ouranos_gb300 as og
+    prob = _thick(n=8, seed=7003)
+    with og.RadiativeTransfer(prob) as rt:
+        xg, _, _ = rt.solve("gmres", tol=1e-10, max_it=2000)
+        xs, isi, _ = rt.solve("si", tol=1e-9, max_it=20000)
+        rt.set_dsa(30)
+        xa, ia, _ = rt.solve("si", tol=1e-9, max_it=20000, dsa=True)
+    assert ia["converged"]
+    assert ia["iterations"] * 5 < isi["iterations"]
+    n0 = prob.total_cells * 8
+    assert rel_err(xa[:n0], xg[:n0]) < 1e-6
+
+
+def test_time_step_with_dsa_matches_plain():
+    import ouranos_gb300 as og
+    prob = og.time_dependent_3d(seed=4110, n=8, sn=4, block=4, width=2.5, inv_vdt=0.5)
+    out = []
+    for dsa in (False, True):
+        with og.RadiativeTransfer(prob, precision="fp32") as rt:
+            rt.set_time_step(0.5)
+            if dsa:
+                rt.set_dsa(10)
+            phi = np.zeros(rt.length)
+            its = 0
+            for step in range(3):
+                rt.set_source([[0.0], [og.pulse_strength(step, peak=10.0, center=1, width=1.0)]])
+                info = rt.time_advance(phi, method="fgmres_mixed", tol=1e-10, dsa=dsa)
+                assert info["converged"]
+                its += info["iterations"]
+            out.append((phi.copy(), its))
+    assert rel_err(out[1][0], out[0][0]) < 1e-8
+    assert out[1][1] < out[0][1]
