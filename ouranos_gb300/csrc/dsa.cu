@@ -19,15 +19,16 @@
 // the material discontinuities where the same correction used inside plain
 // source iteration can lose its efficiency.
 //
-// The diffusion system (one unknown per vertex, 27-point stencil in 3-D) is
-// assembled on the fly from per-cell coefficients and solved approximately by
+// The diffusion system (one unknown per vertex, 27-point stencil in 3-D, its
+// coefficients assembled once per table rebuild) is solved approximately by
 // a fixed number of Jacobi-preconditioned conjugate-gradient steps, in FP32
-// with FP64 scalars, each step two launches and no host synchronisation:
-//   update : x += alpha p, r -= alpha q, z = r / diag, rz' = r.z, beta = rz'/rz
+// with FP64 scalars, all in one cooperative launch (the vertex vectors of a
+// 64^3 mesh, 1.1 MB each, stay in L2) with two grid barriers per step:
 //   matvec : w = C z, p = z + beta p, q = w + beta q, pq = p.q, alpha = rz/pq
+//   update : x += alpha p, r -= alpha q, z = r / diag, rz' = r.z, beta = rz'/rz
 // (q = C p is carried by recurrence, so the matrix is applied once per step).
-// The dot products end in the last block of each launch, which sums the
-// per-block partials in a fixed order: the result is deterministic.
+// Every block sums the per-block partials of a dot product in block order, so
+// all blocks hold the same, deterministic scalars.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -39,35 +40,34 @@ using namespace ouranos;
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 256;     // setup kernels
+constexpr int kCgThreads = 1024;  // the CG kernel: one block per multiprocessor
 
 struct DsaGeom {
   int nx, ny, nz;      // cells per axis (nz = 1 in 2-D)
   int vx, vy, vz;      // vertices per axis (vz = 1 in 2-D)
-  long nv;             // vertices
+  int nv;              // vertices (< 2^31)
   float ks[3];         // stiffness scale of axis a: (measure of the cell) / h_a^2
   float vol;           // measure of a cell
   float face[3];       // (measure of a face normal to axis a) / 2
   int robin;           // bit 2a+s: Marshak term on side s (0 low, 1 high) of axis a
+  int off[27];         // index offset of stencil entry (dz*3 + dy)*3 + dx: vertex (I-1+dx, J-1+dy, K-1+dz)
 };
-
-// coefficients of CG's scalars, on the device
-struct DsaScalars {
-  double rz, alpha, beta, pq;
-  unsigned count;  // blocks done in the current launch
-};
+// stencil entries of a vertex row: 27 in 3-D, 9 in 2-D (dz = 1)
+template <int DIM>
+constexpr int kStencil = DIM == 3 ? 27 : 9;
 
 // 1-D Q1 factors between the basis functions of local corners u and w of a
 // cell of unit length: mass (1/3 on, 1/6 off the diagonal) and stiffness
 __device__ __forceinline__ float m1(int u, int w) { return u == w ? (1.f / 3.f) : (1.f / 6.f); }
 __device__ __forceinline__ float s1(int u, int w) { return u == w ? 1.f : -1.f; }
 
-// Row of the diffusion matrix at vertex (I, J, K) applied to the values that
-// ld(dx, dy, dz) returns for vertex (I-1+dx, J-1+dy, K-1+dz), dx..dz in 0..2
-// (2-D: dz = 1 always).  cell[c] = (D, sigma_a, sigma_s0, -).
-template <int DIM, class Load>
-__device__ __forceinline__ float row_apply(const DsaGeom& g, const float4* __restrict__ cell, int I, int J,
-                                           int K, Load ld) {
+// Row of the diffusion matrix at vertex (I, J, K) applied to the values
+// nb[dz][dy][dx] of vertices (I-1+dx, J-1+dy, K-1+dz), 0 outside the mesh
+// (2-D: only dz = 1 is read).  cell[c] = (D, sigma_a, sigma_s0, -).
+template <int DIM>
+__device__ __forceinline__ float row_apply(const DsaGeom& g, const float4* __restrict__ cell, int I, int J, int K,
+                                           const float (&nb)[3][3][3]) {
   constexpr int NC = DIM == 3 ? 2 : 1;
   float acc = 0.f;
 #pragma unroll
@@ -82,7 +82,7 @@ __device__ __forceinline__ float row_apply(const DsaGeom& g, const float4* __res
       for (int a = 0; a < 2; ++a) {
         const int kx = I - 1 + a;
         if (kx < 0 || kx >= g.nx) continue;
-        const float4 cp = cell[((long)kz * g.ny + ky) * g.nx + kx];
+        const float4 cp = __ldg(cell + (kz * g.ny + ky) * g.nx + kx);
         float sm = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
         for (int c2 = 0; c2 < NC; ++c2)
@@ -90,7 +90,7 @@ __device__ __forceinline__ float row_apply(const DsaGeom& g, const float4* __res
           for (int b2 = 0; b2 < 2; ++b2)
 #pragma unroll
             for (int a2 = 0; a2 < 2; ++a2) {
-              const float val = ld(a + a2, b + b2, DIM == 3 ? c + c2 : 1);
+              const float val = nb[DIM == 3 ? c + c2 : 1][b + b2][a + a2];
               const float mx = m1(1 - a, a2), my = m1(1 - b, b2);
               const float mz = DIM == 3 ? m1(1 - c, c2) : 1.f;
               sm += mx * my * mz * val;
@@ -117,7 +117,7 @@ __device__ __forceinline__ float row_apply(const DsaGeom& g, const float4* __res
 #pragma unroll
           for (int b2 = 0; b2 < 2; ++b2)
             acc += g.face[0] * m1(1 - b, b2) * (DIM == 3 ? m1(1 - c, c2) : 1.f) *
-                   ld(1, b + b2, DIM == 3 ? c + c2 : 1);
+                   nb[DIM == 3 ? c + c2 : 1][b + b2][1];
       }
     }
   }
@@ -135,7 +135,7 @@ __device__ __forceinline__ float row_apply(const DsaGeom& g, const float4* __res
 #pragma unroll
           for (int a2 = 0; a2 < 2; ++a2)
             acc += g.face[1] * m1(1 - a, a2) * (DIM == 3 ? m1(1 - c, c2) : 1.f) *
-                   ld(a + a2, 1, DIM == 3 ? c + c2 : 1);
+                   nb[DIM == 3 ? c + c2 : 1][1][a + a2];
       }
     }
   }
@@ -152,202 +152,255 @@ __device__ __forceinline__ float row_apply(const DsaGeom& g, const float4* __res
         for (int b2 = 0; b2 < 2; ++b2)
 #pragma unroll
           for (int a2 = 0; a2 < 2; ++a2)
-            acc += g.face[2] * m1(1 - a, a2) * m1(1 - b, b2) * ld(a + a2, b + b2, 1);
+            acc += g.face[2] * m1(1 - a, a2) * m1(1 - b, b2) * nb[1][b + b2][a + a2];
       }
     }
   }
   return acc;
 }
 
-__device__ __forceinline__ void vertex_ijk(const DsaGeom& g, long v, int& I, int& J, int& K) {
-  I = (int)(v % g.vx);
-  const long t = v / g.vx;
-  J = (int)(t % g.vy);
-  K = (int)(t / g.vy);
+__device__ __forceinline__ void vertex_ijk(const DsaGeom& g, int v, int& I, int& J, int& K) {
+  const int t = v / g.vx;
+  I = v - t * g.vx;
+  K = t / g.vy;
+  J = t - K * g.vy;
 }
 
-struct VecLoad {
-  const float* p;
-  const DsaGeom* g;
-  int I, J, K;
-  __device__ __forceinline__ float operator()(int dx, int dy, int dz) const {
-    const int i = I - 1 + dx, j = J - 1 + dy, k = K - 1 + dz;
-    if (i < 0 || i >= g->vx || j < 0 || j >= g->vy || k < 0 || k >= g->vz) return 0.f;
-    return p[((long)k * g->vy + j) * g->vx + i];
-  }
-};
-struct DeltaLoad {
-  __device__ __forceinline__ float operator()(int dx, int dy, int dz) const {
-    return (dx == 1 && dy == 1 && dz == 1) ? 1.f : 0.f;
-  }
-};
+__device__ __forceinline__ void delta_nb(float (&nb)[3][3][3], int ex, int ey, int ez) {
+#pragma unroll
+  for (int dz = 0; dz < 3; ++dz)
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+      for (int dx = 0; dx < 3; ++dx) nb[dz][dy][dx] = (dx == ex && dy == ey && dz == ez) ? 1.f : 0.f;
+}
 
-// Fixed-order block sum; thread 0 returns the block total.
+// Fixed-order sum over a block of kCgThreads; thread 0 returns the total.
 __device__ __forceinline__ double block_sum(double t) {
-  __shared__ double red[kThreads / 32];
+  __shared__ double red[kCgThreads / 32];
   for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
   __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x == 0)
-    for (int w = 0; w < kThreads / 32; ++w) s += red[w];
-  __syncthreads();
-  return s;
-}
-
-// Every block stores its partial; the last block to finish sums the partials
-// in block order and returns true in thread 0 with the total in *total.
-__device__ __forceinline__ bool grid_sum(double t, double* part, unsigned* count, double* total) {
-  __shared__ bool last;
-  const double s = block_sum(t);
-  if (threadIdx.x == 0) {
-    part[blockIdx.x] = s;
-    __threadfence();
-    last = atomicAdd(count, 1u) == gridDim.x - 1;
+  if (threadIdx.x < 32) {
+    double u = red[threadIdx.x];
+    for (int o = 16; o; o >>= 1) u += __shfl_xor_sync(0xffffffffu, u, o);
+    t = u;
   }
   __syncthreads();
-  if (!last) return false;
-  __threadfence();
+  return t;
+}
+
+// Sum of the per-block partials of a phase, in block order (every block gets
+// the same value).
+__device__ __forceinline__ double all_sum(const double* part) {
+  __shared__ double total;
   double u = 0.0;
-  for (unsigned i = threadIdx.x; i < gridDim.x; i += kThreads) u += __ldcg(part + i);
+  for (unsigned i = threadIdx.x; i < gridDim.x; i += kCgThreads) u += part[i];
   u = block_sum(u);
+  if (threadIdx.x == 0) total = u;
+  __syncthreads();
+  return total;
+}
+
+struct DsaSync {
+  unsigned count;  // blocks arrived at the current barrier
+  unsigned gen;    // barriers completed
+};
+constexpr int kStatusBarrier = 2;  // status bit: a barrier wait gave up
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
+// Grid-wide barrier of a cooperative launch (all blocks co-resident).
+// Thread 0 of each block arrives with a release (after the block's bar.sync)
+// and leaves with an acquire, so every write of any block before the barrier
+// is visible to every thread after it.  The wait is bounded by limit_ns: a
+// block that gives up sets the status bit and returns false, and blocks still
+// waiting elsewhere see the bit and give up too.
+__device__ __forceinline__ bool grid_barrier(DsaSync* s, int* status, long long limit_ns) {
+  __shared__ int ok;
+  __syncthreads();
   if (threadIdx.x == 0) {
-    *total = u;
-    *count = 0u;
-  }
-  return threadIdx.x == 0;
-}
-
-template <int DIM>
-__global__ void __launch_bounds__(kThreads) dsa_diag_kernel(DsaGeom g, const float4* __restrict__ cell,
-                                                            float* __restrict__ dinv) {
-  const long v = blockIdx.x * (long)kThreads + threadIdx.x;
-  if (v >= g.nv) return;
-  int I, J, K;
-  vertex_ijk(g, v, I, J, K);
-  const float d = row_apply<DIM>(g, cell, I, J, K, DeltaLoad{});
-  dinv[v] = d > 0.f ? 1.f / d : 0.f;
-}
-
-// r = assembled sigma_s0 M v_0, z = r / diag, x = 0, rz = r.z
-template <int DIM>
-__global__ void __launch_bounds__(kThreads) dsa_init_kernel(DsaGeom g, const float4* __restrict__ cell,
-                                                            const double* __restrict__ v,
-                                                            const float* __restrict__ dinv, float* r, float* z,
-                                                            float* x, double* part, DsaScalars* s) {
-  constexpr int NC = DIM == 3 ? 2 : 1;
-  constexpr int NODES = DIM == 3 ? 8 : 4;
-  const long vid = blockIdx.x * (long)kThreads + threadIdx.x;
-  double rz = 0.0;
-  if (vid < g.nv) {
-    int I, J, K;
-    vertex_ijk(g, vid, I, J, K);
-    float acc = 0.f;
-#pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      const int kz = DIM == 3 ? K - 1 + c : 0;
-      if (kz < 0 || kz >= g.nz) continue;
-#pragma unroll
-      for (int b = 0; b < 2; ++b) {
-        const int ky = J - 1 + b;
-        if (ky < 0 || ky >= g.ny) continue;
-#pragma unroll
-        for (int a = 0; a < 2; ++a) {
-          const int kx = I - 1 + a;
-          if (kx < 0 || kx >= g.nx) continue;
-          const long cid = ((long)kz * g.ny + ky) * g.nx + kx;
-          const double* vc = v + cid * NODES;
-          float sm = 0.f;
-#pragma unroll
-          for (int c2 = 0; c2 < NC; ++c2)
-#pragma unroll
-            for (int b2 = 0; b2 < 2; ++b2)
-#pragma unroll
-              for (int a2 = 0; a2 < 2; ++a2)
-                sm += m1(1 - a, a2) * m1(1 - b, b2) * (DIM == 3 ? m1(1 - c, c2) : 1.f) *
-                      (float)vc[a2 + 2 * b2 + 4 * c2];
-          acc += cell[cid].z * g.vol * sm;
+    ok = 1;
+    const unsigned g = ld_acquire(&s->gen);
+    if (atom_add_acq_rel(&s->count, 1u) == gridDim.x - 1) {
+      s->count = 0u;  // ordered before the release below; nobody arrives until it
+      atom_add_acq_rel(&s->gen, 1u);
+    } else {
+      const unsigned long long t0 = global_ns();
+      unsigned polls = 0;
+      while (ld_acquire(&s->gen) == g) {
+        if ((++polls & 255u) == 0 &&
+            ((long long)(global_ns() - t0) > limit_ns || (*(volatile int*)status & kStatusBarrier))) {
+          atomicOr(status, kStatusBarrier);
+          ok = 0;
+          break;
         }
       }
     }
-    const float zz = acc * dinv[vid];
-    r[vid] = acc;
-    z[vid] = zz;
-    x[vid] = 0.f;
-    rz = (double)acc * (double)zz;
   }
-  double tot;
-  if (grid_sum(rz, part, &s->count, &tot)) s->rz = tot;
+  __syncthreads();
+  return ok != 0;
 }
 
-// w = C z; p = z + beta p; q = w + beta q; alpha = rz / p.q
+// The matrix row of every vertex as stencil coefficients coef[s][vertex]
+// (entries that reach outside the mesh are 0), and 1 / diagonal.
 template <int DIM>
-__global__ void __launch_bounds__(kThreads) dsa_matvec_kernel(DsaGeom g, const float4* __restrict__ cell,
-                                                              const float* __restrict__ z, float* p, float* q,
-                                                              double* part, DsaScalars* s, int first) {
-  const long vid = blockIdx.x * (long)kThreads + threadIdx.x;
-  double pq = 0.0;
-  if (vid < g.nv) {
+__global__ void __launch_bounds__(kThreads) dsa_stencil_kernel(DsaGeom g, const float4* __restrict__ cell,
+                                                               float* __restrict__ coef, float* __restrict__ dinv) {
+  const int v = blockIdx.x * kThreads + threadIdx.x;
+  if (v >= g.nv) return;
+  int I, J, K;
+  vertex_ijk(g, v, I, J, K);
+  for (int s = 0; s < kStencil<DIM>; ++s) {
+    const int dx = s % 3, dy = (s / 3) % 3, dz = DIM == 3 ? s / 9 : 1;
+    float nb[3][3][3];
+    delta_nb(nb, dx, dy, dz);
+    const float c = row_apply<DIM>(g, cell, I, J, K, nb);
+    if (dx == 1 && dy == 1 && dz == 1) dinv[v] = c > 0.f ? 1.f / c : 0.f;
+    coef[(long)s * g.nv + v] = c;
+  }
+}
+
+// assembled sigma_s0 M v_0 at vertex (I, J, K)
+template <int DIM>
+__device__ __forceinline__ float assemble_rhs(const DsaGeom& g, const float4* __restrict__ cell,
+                                              const double* __restrict__ v, int I, int J, int K) {
+  constexpr int NC = DIM == 3 ? 2 : 1;
+  constexpr int NODES = DIM == 3 ? 8 : 4;
+  float acc = 0.f;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const int kz = DIM == 3 ? K - 1 + c : 0;
+    if (kz < 0 || kz >= g.nz) continue;
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      const int ky = J - 1 + b;
+      if (ky < 0 || ky >= g.ny) continue;
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        const int kx = I - 1 + a;
+        if (kx < 0 || kx >= g.nx) continue;
+        const int cid = (kz * g.ny + ky) * g.nx + kx;
+        const double* vc = v + (long)cid * NODES;
+        float sm = 0.f;
+#pragma unroll
+        for (int c2 = 0; c2 < NC; ++c2)
+#pragma unroll
+          for (int b2 = 0; b2 < 2; ++b2)
+#pragma unroll
+            for (int a2 = 0; a2 < 2; ++a2)
+              sm += m1(1 - a, a2) * m1(1 - b, b2) * (DIM == 3 ? m1(1 - c, c2) : 1.f) *
+                    (float)vc[a2 + 2 * b2 + 4 * c2];
+        acc += __ldg(&cell[cid].z) * g.vol * sm;
+      }
+    }
+  }
+  return acc;
+}
+
+// The whole preconditioner in one cooperative launch: assemble the right-hand
+// side, `iters` Jacobi-CG steps, and out = v + f on the scalar moment's nodes.
+// Each thread owns the same vertices (grid stride) in every phase, so its own
+// x, r, p, q need no synchronisation; z of the neighbours and the partials
+// cross blocks, and the barrier's release/acquire fences order them (plain
+// loads after it see every write made before it).  Dot products: FP32 per
+// thread, FP64 from the block sums on.
+template <int DIM>
+__global__ void __launch_bounds__(kCgThreads, 1) dsa_cg_kernel(DsaGeom g, const float4* __restrict__ cell,
+                                                          const float* __restrict__ coef, const double* v,
+                                                          double* out, long len, long n0,
+                                                          const float* __restrict__ dinv, float* x, float* r,
+                                                          float* z, float* p, float* q, double* part_a,
+                                                          double* part_b, DsaSync* sync, int* status,
+                                                          long long limit_ns, int iters) {
+  constexpr int NODES = DIM == 3 ? 8 : 4;
+  const int stride = gridDim.x * kCgThreads;
+  const int first = blockIdx.x * kCgThreads + threadIdx.x;
+  // r = rhs, z = r / diag, x = 0
+  float t = 0.f;
+  for (int vid = first; vid < g.nv; vid += stride) {
     int I, J, K;
     vertex_ijk(g, vid, I, J, K);
-    const float w = row_apply<DIM>(g, cell, I, J, K, VecLoad{z, &g, I, J, K});
-    const float beta = first ? 0.f : (float)s->beta;
-    const float pn = z[vid] + beta * (first ? 0.f : p[vid]);
-    const float qn = w + beta * (first ? 0.f : q[vid]);
-    p[vid] = pn;
-    q[vid] = qn;
-    pq = (double)pn * (double)qn;
+    const float rr = assemble_rhs<DIM>(g, cell, v, I, J, K);
+    const float zz = rr * dinv[vid];
+    r[vid] = rr;
+    z[vid] = zz;
+    x[vid] = 0.f;
+    t += rr * zz;
   }
-  double tot;
-  if (grid_sum(pq, part, &s->count, &tot)) {
-    s->pq = tot;
-    s->alpha = tot > 0.0 ? s->rz / tot : 0.0;
+  double bt = block_sum(t);
+  if (threadIdx.x == 0) part_b[blockIdx.x] = bt;
+  if (!grid_barrier(sync, status, limit_ns)) return;
+  double rz = all_sum(part_b), beta = 0.0, alpha = 0.0;
+  for (int it = 0; it < iters; ++it) {
+    // w = C z; p = z + beta p; q = w + beta q
+    const float fb = (float)beta;
+    t = 0.f;
+    for (int vid = first; vid < g.nv; vid += stride) {
+      // z has a zero halo: every stencil offset stays inside the buffer, and
+      // entries that wrap to another row have coefficient 0
+      float w = 0.f;
+#pragma unroll
+      for (int s = 0; s < kStencil<DIM>; ++s) w += coef[(long)s * g.nv + vid] * z[vid + g.off[s]];
+      const float zz = z[vid];
+      const float pn = it ? zz + fb * p[vid] : zz;
+      const float qn = it ? w + fb * q[vid] : w;
+      p[vid] = pn;
+      q[vid] = qn;
+      t += pn * qn;
+    }
+    bt = block_sum(t);
+    if (threadIdx.x == 0) part_a[blockIdx.x] = bt;
+    if (!grid_barrier(sync, status, limit_ns)) return;
+    const double pq = all_sum(part_a);
+    alpha = pq > 0.0 ? rz / pq : 0.0;
+    if (it == iters - 1) break;  // the last update folds into the output
+    // x += alpha p; r -= alpha q; z = r / diag
+    const float fa = (float)alpha;
+    t = 0.f;
+    for (int vid = first; vid < g.nv; vid += stride) {
+      x[vid] += fa * p[vid];
+      const float rn = r[vid] - fa * q[vid];
+      const float zn = rn * dinv[vid];
+      r[vid] = rn;
+      z[vid] = zn;
+      t += rn * zn;
+    }
+    bt = block_sum(t);
+    if (threadIdx.x == 0) part_b[blockIdx.x] = bt;
+    if (!grid_barrier(sync, status, limit_ns)) return;
+    const double rzn = all_sum(part_b);
+    beta = rz > 0.0 ? rzn / rz : 0.0;
+    rz = rzn;
   }
-}
-
-// x += alpha p; r -= alpha q; z = r / diag; beta = r.z / rz
-__global__ void __launch_bounds__(kThreads) dsa_update_kernel(long nv, const float* __restrict__ p,
-                                                              const float* __restrict__ q,
-                                                              const float* __restrict__ dinv, float* x, float* r,
-                                                              float* z, double* part, DsaScalars* s) {
-  const long vid = blockIdx.x * (long)kThreads + threadIdx.x;
-  double rz = 0.0;
-  if (vid < nv) {
-    const float alpha = (float)s->alpha;
-    x[vid] += alpha * p[vid];
-    const float rn = r[vid] - alpha * q[vid];
-    const float zn = rn * dinv[vid];
-    r[vid] = rn;
-    z[vid] = zn;
-    rz = (double)rn * (double)zn;
-  }
-  double tot;
-  if (grid_sum(rz, part, &s->count, &tot)) {
-    const double old = s->rz;
-    s->beta = old > 0.0 ? tot / old : 0.0;
-    s->rz = tot;
-  }
-}
-
-// out = v, plus f = x + alpha p at the vertices of each cell on the scalar
-// moment's nodes (the last CG step's update folded in)
-template <int DIM>
-__global__ void dsa_correct_kernel(DsaGeom g, const double* v, double* out, long len, long n0,
-                                   const float* __restrict__ x, const float* __restrict__ p,
-                                   const DsaScalars* __restrict__ s) {
-  constexpr int NODES = DIM == 3 ? 8 : 4;
-  const float alpha = (float)s->alpha;
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len; e += (long)gridDim.x * blockDim.x) {
+  // out = v + f, f = x + alpha p at the vertex of each scalar-moment node (x
+  // and p of other blocks' vertices: complete at the last barrier)
+  const float fa = (float)alpha;
+  for (long e = first; e < len; e += stride) {
     double val = v[e];
     if (e < n0) {
       const long cid = e / NODES;
       const int k = (int)(e % NODES);
       const int kx = (int)(cid % g.nx);
-      const long t = cid / g.nx;
-      const int ky = (int)(t % g.ny), kz = (int)(t / g.ny);
+      const long tt = cid / g.nx;
+      const int ky = (int)(tt % g.ny), kz = (int)(tt / g.ny);
       const long vid = ((long)(kz + (DIM == 3 ? (k >> 2) : 0)) * g.vy + (ky + ((k >> 1) & 1))) * g.vx +
                        (kx + (k & 1));
-      val += (double)(x[vid] + alpha * p[vid]);
+      val += (double)(x[vid] + fa * p[vid]);
     }
     out[e] = val;
   }
@@ -373,7 +426,7 @@ DsaGeom geom(const ouranos_rt* rt) {
   g.vx = g.nx + 1;
   g.vy = g.ny + 1;
   g.vz = rt->dim == 3 ? g.nz + 1 : 1;
-  g.nv = (long)g.vx * g.vy * g.vz;
+  g.nv = (int)((long)g.vx * g.vy * g.vz);
   const double hx = rt->h[0], hy = rt->h[1], hz = rt->dim == 3 ? rt->h[2] : 1.0;
   const double vol = hx * hy * hz;
   g.vol = (float)vol;
@@ -386,8 +439,15 @@ DsaGeom geom(const ouranos_rt* rt) {
   g.robin = 0;
   for (int f = 0; f < 2 * rt->dim; ++f)
     if (rt->bc[f] != OURANOS_BC_REFLECTIVE) g.robin |= 1 << f;
+  for (int s = 0; s < 27; ++s) {
+    const int dx = s % 3 - 1, dy = (s / 3) % 3 - 1, dz = rt->dim == 3 ? s / 9 - 1 : 0;
+    g.off[s] = (dz * g.vy + dy) * g.vx + dx;
+  }
   return g;
 }
+
+// zero halo on each side of the z vector: the largest stencil offset
+long halo(const DsaGeom& g) { return (long)g.vx * g.vy + g.vx + 1; }
 
 inline int nblocks(long n) { return (int)((n + kThreads - 1) / kThreads); }
 
@@ -396,6 +456,10 @@ inline int nblocks(long n) { return (int)((n + kThreads - 1) / kThreads); }
 int ensure_tables(ouranos_rt* rt) {
   if (rt->n != (rt->dim == 3 ? 8 : 4) || rt->p != 1) {
     rt->err = "diffusion acceleration needs a DG Q1 mesh";
+    return OURANOS_ERR_UNSUPPORTED;
+  }
+  if ((long)(rt->nx[0] + 1) * (rt->nx[1] + 1) * (rt->dim == 3 ? rt->nx[2] + 1 : 1) >= (1L << 31)) {
+    rt->err = "diffusion acceleration: at most 2^31 - 1 mesh vertices";
     return OURANOS_ERR_UNSUPPORTED;
   }
   if (rt->dsa_group == rt->group && rt->dsa_inv_vdt == rt->inv_vdt && rt->d_dsa_cell.p) return OURANOS_OK;
@@ -416,19 +480,36 @@ int ensure_tables(ouranos_rt* rt) {
   const long nv = g.nv;
   const int nb = nblocks(nv);
   DC(rt->d_dsa_cell.alloc(sizeof(float4) * rt->n_cells), "tables");
-  DC(rt->d_dsa_vec.alloc(sizeof(float) * 6 * nv), "vectors");
-  DC(rt->d_dsa_red.alloc(sizeof(double) * (nb + 8)), "reductions");
+  const int ns = rt->dim == 3 ? kStencil<3> : kStencil<2>;
+  DC(rt->d_dsa_vec.alloc(sizeof(float) * (6 * nv + 2 * halo(g))), "vectors");
+  DC(rt->d_dsa_coef.alloc(sizeof(float) * ns * nv), "stencil");
+  DC(cudaMemsetAsync(rt->d_dsa_vec.p, 0, sizeof(float) * (6 * nv + 2 * halo(g)), rt->stream), "vectors");
+  // partials of the two phases (one per block of the cooperative grid) and the barrier
+  int per_sm = 0, sms = 0;
+  DC(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, rt->device), "device");
+  DC(rt->dim == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dsa_cg_kernel<3>, kCgThreads, 0)
+                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dsa_cg_kernel<2>, kCgThreads, 0),
+     "occupancy");
+  if (per_sm < 1) {
+    rt->err = "diffusion acceleration: the CG kernel does not fit on a multiprocessor";
+    return OURANOS_ERR_CUDA;
+  }
+  // one block per multiprocessor keeps the grid barrier to a few participants
+  rt->dsa_grid = (int)std::min<long>(sms, (nv + kCgThreads - 1) / kCgThreads);
+  DC(rt->d_dsa_red.alloc(sizeof(double) * (2 * rt->dsa_grid + 2)), "reductions");
   DC(cudaMemcpyAsync(rt->d_dsa_cell.p, cell.data(), sizeof(float4) * rt->n_cells, cudaMemcpyHostToDevice,
                      rt->stream),
      "tables");
-  DsaScalars* s = reinterpret_cast<DsaScalars*>(rt->d_dsa_red.as<double>() + nb);
-  DC(cudaMemsetAsync(s, 0, sizeof(DsaScalars), rt->stream), "reductions");
-  float* dinv = rt->d_dsa_vec.as<float>() + 5 * nv;
+  DC(cudaMemsetAsync(rt->d_dsa_red.as<double>() + 2 * rt->dsa_grid, 0, sizeof(DsaSync), rt->stream),
+     "barrier");
+  float* dinv = rt->d_dsa_vec.as<float>() + 4 * nv;
   if (rt->dim == 3)
-    dsa_diag_kernel<3><<<nb, kThreads, 0, rt->stream>>>(g, rt->d_dsa_cell.as<float4>(), dinv);
+    dsa_stencil_kernel<3><<<nb, kThreads, 0, rt->stream>>>(g, rt->d_dsa_cell.as<float4>(),
+                                                           rt->d_dsa_coef.as<float>(), dinv);
   else
-    dsa_diag_kernel<2><<<nb, kThreads, 0, rt->stream>>>(g, rt->d_dsa_cell.as<float4>(), dinv);
-  DC(cudaGetLastError(), "diagonal");
+    dsa_stencil_kernel<2><<<nb, kThreads, 0, rt->stream>>>(g, rt->d_dsa_cell.as<float4>(),
+                                                           rt->d_dsa_coef.as<float>(), dinv);
+  DC(cudaGetLastError(), "stencil");
   DC(cudaStreamSynchronize(rt->stream), "tables");
   rt->dsa_group = rt->group;
   rt->dsa_inv_vdt = rt->inv_vdt;
@@ -437,26 +518,28 @@ int ensure_tables(ouranos_rt* rt) {
 
 template <int DIM>
 int dsa_run(ouranos_rt* rt, const double* v, double* out, int iters) {
-  const DsaGeom g = geom(rt);
+  DsaGeom g = geom(rt);
   const long nv = g.nv;
-  const int nb = nblocks(nv);
+  // x, r, p, q, 1/diag, then z with its halo
   float* base = rt->d_dsa_vec.as<float>();
-  float *x = base, *r = base + nv, *z = base + 2 * nv, *p = base + 3 * nv, *q = base + 4 * nv,
-        *dinv = base + 5 * nv;
-  double* part = rt->d_dsa_red.as<double>();
-  DsaScalars* s = reinterpret_cast<DsaScalars*>(part + nb);
+  float *x = base, *r = base + nv, *p = base + 2 * nv, *q = base + 3 * nv;
+  const float* dinv = base + 4 * nv;
+  float* z = base + 5 * nv + halo(g);
+  const float* coef = rt->d_dsa_coef.as<float>();
+  double* part_a = rt->d_dsa_red.as<double>();
+  double* part_b = part_a + rt->dsa_grid;
+  DsaSync* sync = reinterpret_cast<DsaSync*>(part_b + rt->dsa_grid);
+  int* status = rt->d_ctrl.as<int>() + 1;
   const float4* cell = rt->d_dsa_cell.as<float4>();
-  cudaStream_t st = rt->stream;
-  dsa_init_kernel<DIM><<<nb, kThreads, 0, st>>>(g, cell, v, dinv, r, z, x, part, s);
-  dsa_matvec_kernel<DIM><<<nb, kThreads, 0, st>>>(g, cell, z, p, q, part, s, 1);
-  for (int it = 1; it < iters; ++it) {
-    dsa_update_kernel<<<nb, kThreads, 0, st>>>(nv, p, q, dinv, x, r, z, part, s);
-    dsa_matvec_kernel<DIM><<<nb, kThreads, 0, st>>>(g, cell, z, p, q, part, s, 0);
-  }
-  const long len = (long)rt->n_mom * rt->n_dofs;
-  const long blocks = std::min<long>((len + kThreads - 1) / kThreads, 152L * 16);
-  dsa_correct_kernel<DIM><<<(int)blocks, kThreads, 0, st>>>(g, v, out, len, rt->n_cells * (long)rt->n, x, p, s);
-  DC(cudaGetLastError(), "solve");
+  long len = (long)rt->n_mom * rt->n_dofs, n0 = rt->n_cells * (long)rt->n;
+  // a barrier that gave up in an earlier call leaves its counters behind
+  DC(cudaMemsetAsync(sync, 0, sizeof(DsaSync), rt->stream), "barrier");
+  long long limit = rt->wait_limit_ns;
+  void* args[] = {&g, &cell, &coef, &v, &out, &len, &n0, &dinv, &x, &r, &z, &p, &q, &part_a, &part_b, &sync, &status,
+                  &limit, &iters};
+  DC(cudaLaunchCooperativeKernel((const void*)dsa_cg_kernel<DIM>, dim3(rt->dsa_grid), dim3(kCgThreads), args, 0,
+                                 rt->stream),
+     "solve");
   return OURANOS_OK;
 }
 
@@ -474,7 +557,7 @@ int rt_dsa_apply(ouranos_rt* rt, const double* v, double* out) {
   if (rc) return rc;
   return rt->dim == 3 ? dsa_run<3>(rt, v, out, rt->dsa_iters) : dsa_run<2>(rt, v, out, rt->dsa_iters);
 }
-int rt_dsa_kernels(const ouranos_rt* rt) { return rt->dsa_iters > 0 ? 2 * rt->dsa_iters + 1 : 0; }
+int rt_dsa_kernels(const ouranos_rt* rt) { return rt->dsa_iters > 0 ? 1 : 0; }
 }  // namespace ouranos
 
 extern "C" {
@@ -497,14 +580,15 @@ int ouranos_rt_set_dsa(ouranos_rt* rt, int cg_iterations) {
 int ouranos_rt_dsa_apply(ouranos_rt* rt, const double* v, double* z) {
   if (!rt || !v || !z) return OURANOS_ERR_BAD_INPUT;
   cudaSetDevice(rt->device);
+  int rc = rt_clear_status(rt);
+  if (rc) return rc;
   const double* dv = nullptr;
-  int rc = rt_stage_in(rt, v, rt->d_x, 1, &dv);
+  rc = rt_stage_in(rt, v, rt->d_x, 1, &dv);
   if (rc) return rc;
   DC(rt->d_y.alloc(sizeof(double) * (long)rt->n_mom * rt->n_dofs), "output");
   if ((rc = rt_dsa_apply(rt, dv, rt->d_y.as<double>()))) return rc;
   if ((rc = rt_stage_out(rt, rt->d_y.as<double>(), z))) return rc;
-  DC(cudaStreamSynchronize(rt->stream), "apply");
-  return OURANOS_OK;
+  return rt_check_status(rt);
 }
 
 }  // extern "C"

@@ -298,7 +298,7 @@ struct ouranos_rt {
   ouranos::DevBuf d_pc_prop, d_pc_work, d_pc_feat, d_pc_nodal, d_pc_vert;
   // diffusion synthetic acceleration: CG steps (0 = off), cell coefficients,
   // CG vectors and reductions; tables valid for (dsa_group, dsa_inv_vdt)
-  int dsa_iters = 0, dsa_group = -1;
+  int dsa_iters = 0, dsa_group = -1, dsa_grid = 0;
   double dsa_inv_vdt = -1.0;
-  ouranos::DevBuf d_dsa_cell, d_dsa_vec, d_dsa_red;
+  ouranos::DevBuf d_dsa_cell, d_dsa_coef, d_dsa_vec, d_dsa_red;
 };

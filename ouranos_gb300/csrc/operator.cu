@@ -369,9 +369,12 @@ int finish(ouranos_rt* rt) {
   int st = 0;
   CU(cudaMemcpy(&st, rt->d_ctrl.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost), "status");
   float ms = 0.f;
-  if (cudaEventElapsedTime(&ms, rt->ev0, rt->ev1) == cudaSuccess) rt->last_ms = ms;
+  if (cudaEventElapsedTime(&ms, rt->ev0, rt->ev1) == cudaSuccess)
+    rt->last_ms = ms;
+  else
+    (void)cudaGetLastError();  // no sweep recorded the events: not an error of this call
   if (st) {
-    rt->err = "sweep dependency wait timed out";
+    rt->err = (st & 2) ? "diffusion acceleration: grid barrier wait timed out" : "sweep dependency wait timed out";
     return OURANOS_ERR_TIMEOUT;
   }
   return OURANOS_OK;

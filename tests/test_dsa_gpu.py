@@ -134,5 +134,6 @@ def test_time_step_with_dsa_matches_plain():
                 assert info["converged"]
                 its += info["iterations"]
             out.append((phi.copy(), its))
-    assert rel_err(out[1][0], out[0][0]) < 1e-8
+    # psi^n is stored in FP32 after every step: the two runs differ at its rounding
+    assert rel_err(out[1][0], out[0][0]) < 1e-6
     assert out[1][1] < out[0][1]
