@@ -285,6 +285,9 @@ def run_ours(args):
                "sample": "%d full sweep(s) of the workload (%.1f s of CPU work) with the oracle/ C++ "
                          "restatement of the reference sweep, directions split over threads"
                          % (len(times), sum(times))}
+    tts = None
+    if rank == 0 and world == 1 and not args.no_solve:
+        tts = time_to_solution(args.solve_seed, args.solve_n, args.tol, args.dsa_cg, args.max_it)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -312,10 +315,37 @@ def run_ours(args):
         }
         if cpu:
             line["cpu_baseline"] = cpu
+        if tts:
+            line["time_to_solution"] = tts
         print(json.dumps(line), flush=True)
     rt.close()
     if dist:
         dist.destroy_process_group()
+
+
+def time_to_solution(seed, n, tol, dsa_cg, max_it):
+    """Time to a `tol` relative residual on the 3-D thick diffusive map (n^3
+    hexes, DG Q1, GLC S12): plain FP64 GMRES(30) against FGMRES(30) with FP32
+    sweeps, FP64 restarts and the diffusion synthetic acceleration (dsa_cg CG
+    steps).  Wall time of each ouranos_solve call (right-hand side, solve and
+    final FP64 residual on the device), iterations, the final FP64 residual
+    and the scalar-flux difference between the two solutions."""
+    import numpy as np
+    import ouranos_gb300 as og
+    prob = og.thick_3d(seed=seed, n=n, sn=12)
+    out = {"workload": "3d-thick-%d^3-dgq1-glc12-seed%d" % (n, seed), "tol": tol, "dsa_cg_steps": dsa_cg,
+           "cell_dir_solves_per_sweep": prob.total_cells * prob.quad.n_dir}
+    with og.RadiativeTransfer(prob) as rt:
+        rt.set_dsa(dsa_cg)
+        x64, i64, _ = rt.solve("gmres", tol=tol, max_it=max_it, restart=30)
+        xd, idsa, _ = rt.solve("fgmres_mixed", tol=tol, max_it=max_it, restart=30, dsa=True)
+    n0 = prob.total_cells * prob.dofs_per_cell
+    for name, info in (("fp64_gmres", i64), ("fp32_fgmres_dsa", idsa)):
+        out[name] = {k: info[k] for k in ("seconds", "iterations", "restarts", "residual", "converged")}
+    out["speedup"] = i64["seconds"] / idsa["seconds"]
+    out["flux_rel_l2_vs_fp64"] = float(np.linalg.norm(xd[:n0] - x64[:n0]) / np.linalg.norm(x64[:n0]))
+    out["flux_max_abs_vs_fp64"] = float(np.abs(xd[:n0] - x64[:n0]).max())
+    return out
 
 
 def run_solve(args):
@@ -492,7 +522,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-reps", type=int, default=2)
+    ap.add_argument("--cpu-reps", type=int, default=14, help="full CPU sweeps timed (~10 s on 16 cores)")
+    ap.add_argument("--no-solve", action="store_true",
+                    help="skip the time-to-solution comparison of the default line")
     ap.add_argument("--solve", action="store_true", help="time-to-solution mode")
     ap.add_argument("--solve-n", type=int, default=64)
     ap.add_argument("--solve-seed", type=int, default=7000, help="evaluation map (training uses 2000+)")

@@ -152,6 +152,7 @@ int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double
   double rel = bnorm > 0 ? 1.0 : 0.0;
   if (hist) hist[0] = rel;
   bool converged = bnorm == 0.0;
+  if (converged && warm) CUC(cudaMemsetAsync(x, 0, sizeof(double) * w.len, rt->stream), "gmres");  // b = 0: x = 0
   while (!converged && total < max_it) {
     // true residual r = b - A x in FP64
     if (cycles == 0 && !warm) {  // x = 0: r = b
@@ -246,11 +247,14 @@ int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double
       }
     }
   }
-  // final FP64 true residual
-  RC(apply_prec(rt, OURANOS_FP64, x, w.v(R)));
-  CUC(launch_axpby(1.0, b, -1.0, w.v(R), w.len, rt->stream), "gmres");
-  const double fin = nrm(w, w.v(R), &rc) / (bnorm > 0 ? bnorm : 1.0);
-  RC(rc);
+  // final FP64 true residual (already in hand when the loop ended on it)
+  double fin = rel;
+  if (!converged) {
+    RC(apply_prec(rt, OURANOS_FP64, x, w.v(R)));
+    CUC(launch_axpby(1.0, b, -1.0, w.v(R), w.len, rt->stream), "gmres");
+    fin = nrm(w, w.v(R), &rc) / (bnorm > 0 ? bnorm : 1.0);
+    RC(rc);
+  }
   RC(rt_check_status(rt));
   info->iterations = total;
   info->restarts = cycles;
