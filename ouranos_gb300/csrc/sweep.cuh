@@ -674,16 +674,45 @@ __global__ void __launch_bounds__(128) sweep_batch_kernel(const SweepArgs<real>*
   }
 }
 
+// Shared-memory carveout for a launch: as much as the blocks that can be
+// resident at once need, the rest of the SM's on-chip memory stays L1, where
+// the cell-solve tables of the running directions live.
+inline int carveout_percent(int grid, size_t smem_per_block, int max_blocks_per_sm) {
+  static int sms = 0, smem_sm = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (sms < 1 || smem_sm < 1) return -1;  // leave the driver's choice
+  }
+  int per_sm = (grid + sms - 1) / sms;
+  if (per_sm > max_blocks_per_sm) per_sm = max_blocks_per_sm;
+  const size_t need = (size_t)per_sm * (smem_per_block + 1024);  // + the runtime's reserve per block
+  const int pct = (int)((need * 100 + smem_sm - 1) / smem_sm);
+  return pct < 100 ? pct : 100;
+}
+
 template <typename real, int DIM, int P1, int FM>
 cudaError_t launch_sweep_fm(const SweepArgs<real>& a, int grid, int block, cudaStream_t s) {
   constexpr int N = Cell<DIM, P1>::N;
   const size_t smem = (size_t)(block / 32) * Stream<real, FM, N>::warp_bytes;
   static bool configured = false;  // opt in to > 48 KB once per instantiation
+  static int max_per_sm = 0, carve = -2;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(sweep_kernel<real, DIM, P1, FM>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, sweep_kernel<real, DIM, P1, FM>, block, smem);
+    if (e != cudaSuccess) return e;
     configured = true;
+  }
+  const int pct = carveout_percent(grid, smem, max_per_sm > 0 ? max_per_sm : 1);
+  if (pct >= 0 && pct != carve) {
+    cudaError_t e = cudaFuncSetAttribute(sweep_kernel<real, DIM, P1, FM>,
+                                         cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+    if (e != cudaSuccess) return e;
+    carve = pct;
   }
   sweep_kernel<real, DIM, P1, FM><<<grid, block, smem, s>>>(a);
   return cudaGetLastError();
@@ -696,11 +725,23 @@ cudaError_t launch_sweep_batch_fm(const SweepArgs<real>* args, const int2* tmap,
   constexpr int N = Cell<DIM, P1>::N;
   const size_t smem = (size_t)(block / 32) * Stream<real, FM, N>::warp_bytes;
   static bool configured = false;
+  static int max_per_sm = 0, carve = -2;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(sweep_batch_kernel<real, DIM, P1, FM>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, sweep_batch_kernel<real, DIM, P1, FM>, block,
+                                                      smem);
+    if (e != cudaSuccess) return e;
     configured = true;
+  }
+  // static shared memory (the argument slots) counts too
+  const int pct = carveout_percent(grid, smem + 4 * sizeof(SweepArgs<real>), max_per_sm > 0 ? max_per_sm : 1);
+  if (pct >= 0 && pct != carve) {
+    cudaError_t e = cudaFuncSetAttribute(sweep_batch_kernel<real, DIM, P1, FM>,
+                                         cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+    if (e != cudaSuccess) return e;
+    carve = pct;
   }
   sweep_batch_kernel<real, DIM, P1, FM><<<grid, block, smem, s>>>(args, tmap, n_total, ticket, status, epoch);
   return cudaGetLastError();
