@@ -171,7 +171,10 @@ int ouranos_rt_last_error(const ouranos_rt* rt, char* buf, size_t len);
  * on the handle's stream; and the number of kernels that sweep launched. */
 int ouranos_rt_last_sweep_ms(const ouranos_rt* rt, double* ms, int* kernels);
 /* Tiling of the sweep kernel: cells per warp along x (and y in 3-D) and
- * directions per warp, with cells_x * cells_y * dirs == 32.  0s = autotuned. */
+ * directions per warp, with cells_x * cells_y * dirs == 32 (one lane per cell),
+ * or == 16 for cells of 9 or more dofs (2-D Q2+, 3-D Q2): two lanes share each
+ * cell solve.  0s = the default (one direction per warp; 2-D 32 x 1, 3-D
+ * 8 x 4; two lanes per cell and 16 cells where allowed). */
 int ouranos_rt_set_tiling(ouranos_rt* rt, int cells_x, int cells_y, int dirs_per_warp);
 int ouranos_rt_get_tiling(const ouranos_rt* rt, int* cells_x, int* cells_y, int* dirs_per_warp);
 /* Spin limit of the in-kernel dependency waits, in nanoseconds (default 2 s).

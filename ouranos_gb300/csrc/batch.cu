@@ -40,7 +40,7 @@ constexpr size_t kMaxTicketMaps = 256;
 
 struct TicketMap {
   // classes present in the set: (dim, p1, fm), first ticket-map entry, count
-  struct Cls { int dim, p1, fm; long first, count; };
+  struct Cls { int dim, p1, fm, lpc; long first, count; };
   std::vector<Cls> cls;
   DevBuf d;  // int2 (problem, task) entries of all classes
 };
@@ -134,12 +134,12 @@ int ticket_map(ouranos_batch* b, const std::vector<char>& mask, TicketMap** out)
   for (size_t p = 0; p < b->rt.size(); ++p) {
     if (!mask[p] || done[p]) continue;
     const ouranos_rt* r = b->rt[p];
-    const int dim = r->dim, p1 = r->p1, fm = b->fm[p];
+    const int dim = r->dim, p1 = r->p1, fm = b->fm[p], lpc = r->lpc;
     struct Key { double f; int p, t; };
     std::vector<Key> keys;
     for (size_t q = p; q < b->rt.size(); ++q) {
       const ouranos_rt* s = b->rt[q];
-      if (!mask[q] || done[q] || s->dim != dim || s->p1 != p1 || b->fm[q] != fm) continue;
+      if (!mask[q] || done[q] || s->dim != dim || s->p1 != p1 || b->fm[q] != fm || s->lpc != lpc) continue;
       done[q] = 1;
       for (int t = 0; t < s->n_tasks; ++t) keys.push_back({(double)t / s->n_tasks, (int)q, t});
     }
@@ -147,7 +147,7 @@ int ticket_map(ouranos_batch* b, const std::vector<char>& mask, TicketMap** out)
       return x.f != y.f ? x.f < y.f : (x.p != y.p ? x.p < y.p : x.t < y.t);
     });
     if ((int)tm.cls.size() == kMaxClasses) return bbad(b, "too many problem classes in one batch");
-    tm.cls.push_back({dim, p1, fm, (long)all.size(), (long)keys.size()});
+    tm.cls.push_back({dim, p1, fm, lpc, (long)all.size(), (long)keys.size()});
     for (const Key& k : keys) all.push_back(make_int2(k.p, k.t));
   }
   BC(tm.d.alloc(sizeof(int2) * std::max<size_t>(all.size(), 1)), "ticket map");
@@ -190,7 +190,7 @@ int apply_body(ouranos_batch* b, const std::vector<char>& mask, bool sources, Ti
   for (size_t c = 0; c < tm->cls.size(); ++c) {
     const TicketMap::Cls& k = tm->cls[c];
     const int grid = (int)std::min<long>((k.count + 3) / 4, (long)std::max(1, b->sms * 8));
-    BC(launch_sweep_batch<real>(k.dim, k.p1, k.fm, d_args.as<SweepArgs<real>>(),
+    BC(launch_sweep_batch<real>(k.dim, k.p1, k.fm, k.lpc, d_args.as<SweepArgs<real>>(),
                                 tm->d.as<int2>() + k.first, (int)k.count, ctrl + c, ctrl + kStatus,
                                 (const unsigned*)(ctrl + kEpoch), grid, 128, b->stream),
        "batched sweep");
@@ -459,7 +459,8 @@ int ouranos_batch_last_error(const ouranos_batch* b, char* buf, size_t len) {
 }
 
 // Per problem, time each tiling whose lanes cover one warp (2-D: 32x1 cells
-// by 1 direction down to 4x1 by 8; 3-D: 8x4 x 1 down to 2x2 x 8) on its own
+// by 1 direction down to 4x1 by 8; 3-D: 8x4 x 1 down to 2x2 x 8; for cells of
+// 9 or more dofs also two lanes per cell, 16 cells per warp) on its own
 // sweep kernel in `precision`, keep the fastest.  Results are cached per
 // (dim, order, directions, cells, precision) for the process.  tiling_out
 // (may be NULL) receives count x 3 ints.
@@ -485,6 +486,10 @@ int ouranos_batch_autotune(ouranos_batch* b, int precision, int reps, int* tilin
       std::vector<std::vector<int>> cand;
       if (r->dim == 2) cand = {{32, 1, 1}, {16, 1, 2}, {8, 1, 4}, {4, 1, 8}};
       else cand = {{8, 4, 1}, {4, 4, 2}, {4, 2, 4}, {2, 2, 8}};
+      if (r->n >= 9) {  // two lanes per cell
+        if (r->dim == 2) cand.insert(cand.end(), {{16, 1, 1}, {8, 1, 2}, {4, 1, 4}});
+        else cand.insert(cand.end(), {{4, 4, 1}, {4, 2, 2}, {2, 2, 4}});
+      }
       const long len = (long)r->n_mom * r->n_dofs;
       BC(tx.alloc(sizeof(double) * len), "autotune");
       BC(ty.alloc(sizeof(double) * len), "autotune");

@@ -86,7 +86,7 @@ struct SweepArgs {
   int n_sweep;                 // cells along the sweep axis (y in 2-D, z in 3-D)
   long n_dofs;                 // cells * n
   int n_mom;
-  int wx, wy, kd;              // warp tiling: wx*wy cells x kd directions = 32 lanes
+  int wx, wy, kd;              // warp tiling: wx*wy cells x kd directions x lpc = 32 lanes
   int tiles_x, tiles_y;
   int n_tasks;
   const int2* tasks;           // (dir group, tile) in dependency order
@@ -112,6 +112,7 @@ struct SweepArgs {
   int* status;                 // 0 ok, 1 wait timeout
   long long wait_limit_ns;
   int wait_bias;
+  int lpc;                     // lanes per cell: 1, or 2 (cells of 9 or more dofs)
 };
 
 // fused_moments: 0 = read the expanded per-direction source q; 1 or 2 = apply
@@ -123,9 +124,9 @@ cudaError_t launch_sweep(int dim, int p1, int fused_moments, const SweepArgs<rea
 // (problem, task) for ticket t, epoch read from the device (all problems of
 // the launch share it), ticket reset to 0 by the caller.
 template <typename real>
-cudaError_t launch_sweep_batch(int dim, int p1, int fused_moments, const SweepArgs<real>* args,
-                               const int2* tmap, int n_total, int* ticket, const int* status,
-                               const unsigned* epoch, int grid, int block, cudaStream_t s);
+cudaError_t launch_sweep_batch(int dim, int p1, int fused_moments, int lanes_per_cell,
+                               const SweepArgs<real>* args, const int2* tmap, int n_total, int* ticket,
+                               const int* status, const unsigned* epoch, int grid, int block, cudaStream_t s);
 // q[d][e] = sum_m M2D[d][m] T[m][e] (+ iso[e])  -- moment -> direction expansion
 template <typename real>
 cudaError_t launch_expand_source(const real* T, const real* iso, const real* m2d, real* q,
@@ -262,6 +263,7 @@ struct ouranos_rt {
   int fp64_contract = OURANOS_FP64_DF64_SWEEP;  // arithmetic of the FP64 path
   // schedule
   int wx = 0, wy = 1, kd = 0;          // 0 = not chosen yet
+  int lpc = 1;                         // lanes per cell (2 only for cells of >= 9 dofs)
   int tiles_x = 0, tiles_y = 0, n_groups_dir = 0, n_tasks = 0;
   std::vector<int> dir_class_h;
   std::vector<double> class_abs_omega;  // [n_dir_class][3]

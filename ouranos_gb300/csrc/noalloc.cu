@@ -140,6 +140,7 @@ int apply_noalloc(ouranos_rt* rt, unsigned char* base, const Layout& L, bool exp
   a.wx = rt->wx;
   a.wy = rt->wy;
   a.kd = rt->kd;
+  a.lpc = rt->lpc;
   a.tiles_x = rt->tiles_x;
   a.tiles_y = rt->tiles_y;
   a.n_tasks = rt->n_tasks;

@@ -141,13 +141,15 @@ int build_schedule(ouranos_rt* rt) {
 
 int default_tiling(ouranos_rt* rt) {
   // one direction per warp: every lane of a warp reads the same inverse table
-  // (broadcast loads); 32 cells per warp (2-D: 32 x 1, 3-D: 8 x 4)
+  // (broadcast loads); 32 cells per warp (2-D: 32 x 1, 3-D: 8 x 4), or 16
+  // cells solved by two lanes each for cells of 9 or more dofs
   rt->kd = 1;
+  rt->lpc = rt->n >= 9 ? 2 : 1;
   if (rt->dim == 2) {
-    rt->wx = 32;
+    rt->wx = 32 / rt->lpc;
     rt->wy = 1;
   } else {
-    rt->wx = 8;
+    rt->wx = rt->lpc == 2 ? 4 : 8;
     rt->wy = 4;
   }
   return OURANOS_OK;
@@ -244,6 +246,7 @@ int sweep_prepare(ouranos_rt* rt, const real* src, const real* iso, const real* 
   a.wx = rt->wx;
   a.wy = rt->wy;
   a.kd = rt->kd;
+  a.lpc = rt->lpc;
   a.tiles_x = rt->tiles_x;
   a.tiles_y = rt->tiles_y;
   a.n_tasks = rt->n_tasks;
@@ -1012,11 +1015,14 @@ int ouranos_rt_set_tiling(ouranos_rt* rt, int cells_x, int cells_y, int dirs) {
   } else {
     if (rt->dim == 2) cells_y = 1;
     const int lanes = cells_x * cells_y * dirs;
-    if (cells_x < 1 || cells_y < 1 || dirs < 1 || lanes != 32 || (dirs & (dirs - 1)))
-      return bad(rt, "tiling must satisfy cells_x*cells_y*dirs == 32 with dirs a power of two");
+    const bool two = lanes == 16 && rt->n >= 9;  // two lanes per cell
+    if (cells_x < 1 || cells_y < 1 || dirs < 1 || (lanes != 32 && !two) || (dirs & (dirs - 1)))
+      return bad(rt, "tiling must satisfy cells_x*cells_y*dirs == 32 (or 16, two lanes per cell, for cells "
+                     "of 9 or more dofs) with dirs a power of two");
     rt->wx = cells_x;
     rt->wy = cells_y;
     rt->kd = dirs;
+    rt->lpc = two ? 2 : 1;
   }
   OK_OR_RETURN(build_schedule(rt));
   CU(cudaStreamSynchronize(rt->stream), "tiling");

@@ -80,10 +80,14 @@ struct Tagged<float> {
   static __device__ __forceinline__ void put(unsigned long long* w, float v, unsigned tag) {
     st_relaxed_u64(w, ((unsigned long long)tag << 32) | __float_as_uint(v));
   }
-  static __device__ __forceinline__ bool get(const unsigned long long* w, unsigned tag, float& v) {
-    const unsigned long long a = ld_relaxed_u64(w);
+  static __device__ __forceinline__ bool decode(const unsigned long long* raw, unsigned tag, float& v) {
+    const unsigned long long a = raw[0];
     v = __uint_as_float((unsigned)a);
     return (unsigned)(a >> 32) == tag;
+  }
+  static __device__ __forceinline__ bool get(const unsigned long long* w, unsigned tag, float& v) {
+    const unsigned long long a = ld_relaxed_u64(w);
+    return decode(&a, tag, v);
   }
 };
 template <>
@@ -94,10 +98,14 @@ struct Tagged<double> {
     st_relaxed_u64(w, ((unsigned long long)tag << 32) | (b & 0xffffffffull));
     st_relaxed_u64(w + 1, ((unsigned long long)tag << 32) | (b >> 32));
   }
-  static __device__ __forceinline__ bool get(const unsigned long long* w, unsigned tag, double& v) {
-    const unsigned long long lo = ld_relaxed_u64(w), hi = ld_relaxed_u64(w + 1);
+  static __device__ __forceinline__ bool decode(const unsigned long long* raw, unsigned tag, double& v) {
+    const unsigned long long lo = raw[0], hi = raw[1];
     v = __longlong_as_double((long long)((hi << 32) | (lo & 0xffffffffull)));
     return (unsigned)(lo >> 32) == tag && (unsigned)(hi >> 32) == tag;
+  }
+  static __device__ __forceinline__ bool get(const unsigned long long* w, unsigned tag, double& v) {
+    const unsigned long long raw[2] = {ld_relaxed_u64(w), ld_relaxed_u64(w + 1)};
+    return decode(raw, tag, v);
   }
 };
 
@@ -108,10 +116,14 @@ struct Tagged<df64> {  // a double-float travels as its two tagged halves
     st_relaxed_u64(w, ((unsigned long long)tag << 32) | __float_as_uint(v.hi));
     st_relaxed_u64(w + 1, ((unsigned long long)tag << 32) | __float_as_uint(v.lo));
   }
-  static __device__ __forceinline__ bool get(const unsigned long long* w, unsigned tag, df64& v) {
-    const unsigned long long a = ld_relaxed_u64(w), b = ld_relaxed_u64(w + 1);
+  static __device__ __forceinline__ bool decode(const unsigned long long* raw, unsigned tag, df64& v) {
+    const unsigned long long a = raw[0], b = raw[1];
     v = df64(__uint_as_float((unsigned)a), __uint_as_float((unsigned)b));
     return (unsigned)(a >> 32) == tag && (unsigned)(b >> 32) == tag;
+  }
+  static __device__ __forceinline__ bool get(const unsigned long long* w, unsigned tag, df64& v) {
+    const unsigned long long raw[2] = {ld_relaxed_u64(w), ld_relaxed_u64(w + 1)};
+    return decode(raw, tag, v);
   }
 };
 
@@ -127,6 +139,7 @@ struct Arith {
   static __device__ __forceinline__ real get(acc s) { return s; }
   static __device__ __forceinline__ real ldg(const real* p) { return __ldg(p); }
   static __device__ __forceinline__ real shfl_up(real v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
+  static __device__ __forceinline__ real shfl_xor(real v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
 };
 template <>
 struct Arith<df64> {
@@ -141,6 +154,9 @@ struct Arith<df64> {
   }
   static __device__ __forceinline__ df64 shfl_up(df64 v, int d) {
     return df64(__shfl_up_sync(0xffffffffu, v.hi, d), __shfl_up_sync(0xffffffffu, v.lo, d));
+  }
+  static __device__ __forceinline__ df64 shfl_xor(df64 v, int m) {
+    return df64(__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m));
   }
 };
 
@@ -158,8 +174,10 @@ static __device__ __forceinline__ bool fetch_edge(const unsigned long long* w, u
   const long long t0 = global_ns();
   unsigned sleep_ns = 16;
   for (unsigned it = 0; it < (1u << 26); ++it) {
-    __nanosleep(sleep_ns);
-    if (sleep_ns < 256) sleep_ns <<= 1;
+    if (it >= 8) {  // the first re-polls go straight back (a value in flight lands within them)
+      __nanosleep(sleep_ns);
+      if (sleep_ns < 256) sleep_ns <<= 1;
+    }
     ok = true;
 #pragma unroll
     for (int t = 0; t < FD; ++t) ok &= Tagged<real>::get(w + t * W, tag, out[t]);
@@ -324,12 +342,27 @@ struct Stream {
   static constexpr size_t warp_bytes = (size_t)Prefetch<real>::RING * 32 * (NVP * sizeof(real) + sizeof(int));
 };
 
+// Row r of a cell solve split over H lanes: lane `half` of the pair holds rows
+// k H + half in xr[k]; both lanes return row r (a converged shuffle).
+template <typename real, int H, int NR>
+__device__ __forceinline__ real cell_row(const real (&xr)[NR], int r, int half) {
+  if (H == 1) return xr[r];
+  const real mine = xr[r / 2];
+  const real other = Arith<real>::shfl_xor(mine, 1);
+  return (r & 1) == half ? mine : other;
+}
+
 // One task: a tile of wx x wy columns for kd directions, swept over the whole
 // sweep axis.  Shared by the single-problem and the batched kernels.  The
 // arguments come by value: inlined into the single-problem kernel they stay
 // parameter reads the compiler can keep out of the inner loop (a reference
 // to the parameter block made them loads it had to repeat after every store).
-template <typename real, int DIM, int P1, int FM>
+// H lanes solve one cell (H = 2 for cells of 9 or more dofs may be chosen by
+// the tiling): both assemble the right-hand side, each computes half of the
+// rows of A'^-1 b, and the outflow values they pass on are exchanged; a warp
+// then covers 32 / H cells, so twice as many warps share the wavefront and
+// each does half the cell-solve arithmetic per step.
+template <typename real, int DIM, int P1, int FM, int H>
 __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int task,
                                            unsigned char* smem_raw) {
   using C = Cell<DIM, P1>;
@@ -346,9 +379,14 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
   constexpr int kPrefetch = Prefetch<real>::PF;
   constexpr int kRing = Prefetch<real>::RING;
   int* cring = reinterpret_cast<int*>(ring + kRing * 32 * NVP);
+  static_assert(H == 1 || H == 2, "one or two lanes per cell");
+  static_assert(H == 1 || !Stream<real, FM, N>::VEC, "16-byte cells are solved by one lane");
+  constexpr int NR = (N + H - 1) / H;  // rows of the cell solve per lane
+  const int cell_lane = lane / H;
+  const int half = H == 2 ? (lane & 1) : 0;
   const int wc = a.wx * a.wy;
-  const int kslot = lane / wc;
-  const int cl = lane - kslot * wc;
+  const int kslot = cell_lane / wc;
+  const int cl = cell_lane - kslot * wc;
   const int lx = cl % a.wx;
   const int ly = cl / a.wx;
   const int tiles = a.tiles_x * a.tiles_y;
@@ -455,6 +493,22 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
     real psiS[FD], psiX[FD], psiY[FD];
 #pragma unroll
     for (int t = 0; t < FD; ++t) psiS[t] = psiX[t] = psiY[t] = real(0);
+    // Edge words of the upwind tile are loaded one step ahead (the load
+    // overlaps a step's work); their tags are checked when they are used, and
+    // words that were not yet published are polled for as before
+    // (8-byte values only: for FP32 the extra registers cost more than the
+    // hidden load latency saves)
+    constexpr bool kAhead = sizeof(real) == 8;
+    const bool recv_x = col_ok && lx == 0 && tx > 0;
+    const bool recv_y = DIM == 3 && col_ok && ly == 0 && ty > 0;
+    auto edge_x_at = [&](int r) {
+      return a.edge_x + ((((size_t)d * tiles + tile - 1) * NS + r) * a.wy + ly) * (FD * W);
+    };
+    auto edge_y_at = [&](int r) {
+      return a.edge_y + ((((size_t)d * tiles + tile - a.tiles_x) * NS + r) * a.wx + lx) * (FD * W);
+    };
+    unsigned long long rX[FD * W], rY[FD * W];
+    bool hX = false, hY = false;  // rX / rY hold the words of this step's row
 
     for (int s = 0; s < nsteps; ++s) {
       const int sc = s - lx - ly;
@@ -468,15 +522,30 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
       for (int t = 0; t < FD; ++t) eX[t] = eY[t] = real(0);
       bool failed = false;
       const unsigned tag = (want_epoch << 16) | ((unsigned)sc & 0xffffu);
-      if (act && lx == 0 && tx > 0) {
-        const unsigned long long* e =
-            a.edge_x + ((((size_t)d * tiles + tile - 1) * NS + sc) * a.wy + ly) * (FD * W);
-        failed |= !fetch_edge<real, FD>(e, tag, eX, a.status, a.wait_limit_ns);
+      if (act && recv_x) {
+        bool ok = hX;
+#pragma unroll
+        for (int t = 0; t < FD; ++t) ok &= Tagged<real>::decode(rX + t * W, tag, eX[t]);
+        if (!ok) failed |= !fetch_edge<real, FD>(edge_x_at(sc), tag, eX, a.status, a.wait_limit_ns);
       }
-      if (DIM == 3 && act && ly == 0 && ty > 0) {
-        const unsigned long long* e =
-            a.edge_y + ((((size_t)d * tiles + tile - a.tiles_x) * NS + sc) * a.wx + lx) * (FD * W);
-        failed |= !fetch_edge<real, FD>(e, tag, eY, a.status, a.wait_limit_ns);
+      if (DIM == 3 && act && recv_y) {
+        bool ok = hY;
+#pragma unroll
+        for (int t = 0; t < FD; ++t) ok &= Tagged<real>::decode(rY + t * W, tag, eY[t]);
+        if (!ok) failed |= !fetch_edge<real, FD>(edge_y_at(sc), tag, eY, a.status, a.wait_limit_ns);
+      }
+      // the next step's row (sc + 1): load its words now
+      hX = kAhead && recv_x && sc + 1 >= 0 && sc + 1 < NS;
+      if (hX) {
+        const unsigned long long* e = edge_x_at(sc + 1);
+#pragma unroll
+        for (int k = 0; k < FD * W; ++k) rX[k] = ld_relaxed_u64(e + k);
+      }
+      hY = kAhead && recv_y && sc + 1 >= 0 && sc + 1 < NS;
+      if (DIM == 3 && hY) {
+        const unsigned long long* e = edge_y_at(sc + 1);
+#pragma unroll
+        for (int k = 0; k < FD * W; ++k) rY[k] = ld_relaxed_u64(e + k);
       }
       if (__any_sync(FULL, failed)) {  // status is set; drain own copies, leave
         cp_async_wait<0>();
@@ -487,15 +556,18 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
       real upX[FD], upY[FD], upS[FD];
 #pragma unroll
       for (int t = 0; t < FD; ++t) {
-        const real sx = A::shfl_up(psiX[t], 1);
+        const real sx = A::shfl_up(psiX[t], H);
         upX[t] = x_edge ? (tx == 0 ? bX : eX[t]) : sx;
         if (DIM == 3) {
-          const real sy = A::shfl_up(psiY[t], a.wx);
+          const real sy = A::shfl_up(psiY[t], a.wx * H);
           upY[t] = y_edge ? (ty == 0 ? bY : eY[t]) : sy;
         }
         upS[t] = sc == 0 ? bS : psiS[t];
       }
 
+      real xr[NR];
+#pragma unroll
+      for (int k = 0; k < NR; ++k) xr[k] = real(0);
       if (act) {
         cp_async_wait<kPrefetch - 1>();  // plane sc has landed
         const real* v = ring + ((sc % kRing) * 32 + lane) * NVP;
@@ -538,6 +610,20 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
           }
         }
         issue(sc + kPrefetch);  // refills the slot consumed one step ago
+        // FP32: this lane's rows of A'^-1 into registers now, so their loads
+        // overlap the right-hand side below (for 8-byte values the longer
+        // arithmetic hides them and the registers are better spent elsewhere)
+        constexpr bool kHoist = sizeof(real) == 4;
+        const real* Ai = a.ainv + ((size_t)cls * a.n_dir_class + dcls) * (N * N);
+        real arow[kHoist ? NR : 1][kHoist ? N : 1];
+        if constexpr (kHoist) {
+#pragma unroll
+          for (int k = 0; k < NR; ++k) {
+            const int i = k * H + half;
+#pragma unroll
+            for (int j = 0; j < N; ++j) arow[k][j] = (H == 1 || i < N) ? A::ldg(Ai + i * N + j) : real(0);
+          }
+        }
         // inflow faces: b_face += |Omega_a| F_a psi_up
         const real* FX = a.face_mass + 0 * FD * FD;
         const real* FS = a.face_mass + AS * FD * FD;
@@ -569,46 +655,64 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
             b[C::y_in(t)] = A::get(by);
           }
         }
-        // x = A'^-1 b
-        const real* Ai = a.ainv + ((size_t)cls * a.n_dir_class + dcls) * (N * N);
-        real x[N];
+        // x = A'^-1 b: this lane's rows i = k H + half
 #pragma unroll
-        for (int i = 0; i < N; ++i) {
+        for (int k = 0; k < NR; ++k) {
+          const int i = k * H + half;
           typename A::acc acc = A::zero();
+          if (H == 1 || i < N) {
 #pragma unroll
-          for (int j = 0; j < N; ++j) A::fma(acc, A::ldg(Ai + i * N + j), b[j]);
-          x[i] = A::get(acc);
+            for (int j = 0; j < N; ++j) {
+              if constexpr (kHoist)
+                A::fma(acc, arow[k][j], b[j]);
+              else
+                A::fma(acc, A::ldg(Ai + i * N + j), b[j]);
+            }
+          }
+          xr[k] = A::get(acc);
         }
+      }
+      // outflow values (converged: with H = 2 the partner lane holds half the rows)
 #pragma unroll
-        for (int t = 0; t < FD; ++t) {
-          psiX[t] = x[C::x_out(t)];
-          psiS[t] = x[C::s_out(t)];
-          if (DIM == 3) psiY[t] = x[C::y_out(t)];
+      for (int t = 0; t < FD; ++t) {
+        const real vx = cell_row<real, H>(xr, C::x_out(t), half);
+        const real vs = cell_row<real, H>(xr, C::s_out(t), half);
+        real vy = real(0);
+        if (DIM == 3) vy = cell_row<real, H>(xr, C::y_out(t), half);
+        if (act) {
+          psiX[t] = vx;
+          psiS[t] = vs;
+          if (DIM == 3) psiY[t] = vy;
         }
+      }
+      if (act) {
         // edge values first, so the downwind tile can start; then the angular flux
         const unsigned ptag = (a.epoch << 16) | ((unsigned)sc & 0xffffu);
-        if (pub_x) {
+        if (pub_x && half == 0) {
           unsigned long long* e =
               a.edge_x + ((((size_t)d * tiles + tile) * NS + sc) * a.wy + ly) * (FD * W);
 #pragma unroll
           for (int t = 0; t < FD; ++t) Tagged<real>::put(e + t * W, psiX[t], ptag);
         }
-        if (pub_y) {
+        if (pub_y && half == 0) {
           unsigned long long* e =
               a.edge_y + ((((size_t)d * tiles + tile) * NS + sc) * a.wx + lx) * (FD * W);
 #pragma unroll
           for (int t = 0; t < FD; ++t) Tagged<real>::put(e + t * W, psiY[t], ptag);
         }
-        if (VEC) {  // physical order by swaps, then 16-byte stores
+        if constexpr (VEC) {  // physical order by swaps, then 16-byte stores (H = 1: xr holds the cell)
           real o[N];
 #pragma unroll
-          for (int i = 0; i < N; ++i) o[i] = x[i];
+          for (int i = 0; i < N; ++i) o[i] = xr[i];
           xor_permute<real, N>(o, fmask);
           store_cell<real, N>(a.psi + dirbase + cell_of(sc) * N, o);
         } else {
           real* P = a.psi + dirbase + cell_of(sc) * N + base;
 #pragma unroll
-          for (int i = 0; i < N; ++i) P[off(i)] = x[i];
+          for (int k = 0; k < NR; ++k) {
+            const int i = k * H + half;
+            if (H == 1 || i < N) P[off(i)] = xr[k];
+          }
         }
       }
     }
@@ -618,7 +722,7 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
 // Single problem: warps take tasks in ticket order (level-major), so every
 // task a warp waits on was taken earlier by a running warp -- any grid is
 // deadlock-free.
-template <typename real, int DIM, int P1, int FM>
+template <typename real, int DIM, int P1, int FM, int H>
 __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr unsigned FULL = 0xffffffffu;
@@ -631,7 +735,7 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
     task = __shfl_sync(FULL, task, 0);
     stop = __shfl_sync(FULL, stop, 0);
     if (task >= a.n_tasks || stop) return;
-    sweep_task<real, DIM, P1, FM>(a, task, smem_raw);
+    sweep_task<real, DIM, P1, FM, H>(a, task, smem_raw);
   }
 }
 
@@ -641,7 +745,7 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<real> a) {
 // its task's problem arguments into its shared slot before the task; the
 // edge-word epoch comes from device memory, so a captured launch replays with
 // the epoch of the moment.
-template <typename real, int DIM, int P1, int FM>
+template <typename real, int DIM, int P1, int FM, int H>
 __global__ void __launch_bounds__(128) sweep_batch_kernel(const SweepArgs<real>* __restrict__ args,
                                                           const int2* __restrict__ tmap, int n_total,
                                                           int* ticket, const int* status,
@@ -669,7 +773,7 @@ __global__ void __launch_bounds__(128) sweep_batch_kernel(const SweepArgs<real>*
     __syncwarp();
     if (lane == 0) s_args[warp].epoch = *epoch;  // set on the device before the launch
     __syncwarp();
-    sweep_task<real, DIM, P1, FM>(s_args[warp], pt.y, smem_raw);
+    sweep_task<real, DIM, P1, FM, H>(s_args[warp], pt.y, smem_raw);
     __syncwarp();  // the slot is rewritten by the next task
   }
 }
@@ -693,32 +797,32 @@ inline int carveout_percent(int grid, size_t smem_per_block, int max_blocks_per_
   return pct < 100 ? pct : 100;
 }
 
-template <typename real, int DIM, int P1, int FM>
+template <typename real, int DIM, int P1, int FM, int H>
 cudaError_t launch_sweep_fm(const SweepArgs<real>& a, int grid, int block, cudaStream_t s) {
   constexpr int N = Cell<DIM, P1>::N;
   const size_t smem = (size_t)(block / 32) * Stream<real, FM, N>::warp_bytes;
   static bool configured = false;  // opt in to > 48 KB once per instantiation
   static int max_per_sm = 0, carve = -2;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(sweep_kernel<real, DIM, P1, FM>,
+    cudaError_t e = cudaFuncSetAttribute(sweep_kernel<real, DIM, P1, FM, H>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, sweep_kernel<real, DIM, P1, FM>, block, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, sweep_kernel<real, DIM, P1, FM, H>, block, smem);
     if (e != cudaSuccess) return e;
     configured = true;
   }
   const int pct = carveout_percent(grid, smem, max_per_sm > 0 ? max_per_sm : 1);
   if (pct >= 0 && pct != carve) {
-    cudaError_t e = cudaFuncSetAttribute(sweep_kernel<real, DIM, P1, FM>,
+    cudaError_t e = cudaFuncSetAttribute(sweep_kernel<real, DIM, P1, FM, H>,
                                          cudaFuncAttributePreferredSharedMemoryCarveout, pct);
     if (e != cudaSuccess) return e;
     carve = pct;
   }
-  sweep_kernel<real, DIM, P1, FM><<<grid, block, smem, s>>>(a);
+  sweep_kernel<real, DIM, P1, FM, H><<<grid, block, smem, s>>>(a);
   return cudaGetLastError();
 }
 
-template <typename real, int DIM, int P1, int FM>
+template <typename real, int DIM, int P1, int FM, int H>
 cudaError_t launch_sweep_batch_fm(const SweepArgs<real>* args, const int2* tmap, int n_total, int* ticket,
                                   const int* status, const unsigned* epoch, int grid, int block,
                                   cudaStream_t s) {
@@ -727,10 +831,10 @@ cudaError_t launch_sweep_batch_fm(const SweepArgs<real>* args, const int2* tmap,
   static bool configured = false;
   static int max_per_sm = 0, carve = -2;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(sweep_batch_kernel<real, DIM, P1, FM>,
+    cudaError_t e = cudaFuncSetAttribute(sweep_batch_kernel<real, DIM, P1, FM, H>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, sweep_batch_kernel<real, DIM, P1, FM>, block,
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, sweep_batch_kernel<real, DIM, P1, FM, H>, block,
                                                       smem);
     if (e != cudaSuccess) return e;
     configured = true;
@@ -738,32 +842,56 @@ cudaError_t launch_sweep_batch_fm(const SweepArgs<real>* args, const int2* tmap,
   // static shared memory (the argument slots) counts too
   const int pct = carveout_percent(grid, smem + 4 * sizeof(SweepArgs<real>), max_per_sm > 0 ? max_per_sm : 1);
   if (pct >= 0 && pct != carve) {
-    cudaError_t e = cudaFuncSetAttribute(sweep_batch_kernel<real, DIM, P1, FM>,
+    cudaError_t e = cudaFuncSetAttribute(sweep_batch_kernel<real, DIM, P1, FM, H>,
                                          cudaFuncAttributePreferredSharedMemoryCarveout, pct);
     if (e != cudaSuccess) return e;
     carve = pct;
   }
-  sweep_batch_kernel<real, DIM, P1, FM><<<grid, block, smem, s>>>(args, tmap, n_total, ticket, status, epoch);
+  sweep_batch_kernel<real, DIM, P1, FM, H><<<grid, block, smem, s>>>(args, tmap, n_total, ticket, status, epoch);
   return cudaGetLastError();
 }
 
-template <typename real, int DIM, int P1>
-cudaError_t launch_sweep_batch_impl(int fm, const SweepArgs<real>* args, const int2* tmap, int n_total,
-                                    int* ticket, const int* status, const unsigned* epoch, int grid,
-                                    int block, cudaStream_t s) {
-  if (fm == 0) return launch_sweep_batch_fm<real, DIM, P1, 0>(args, tmap, n_total, ticket, status, epoch, grid, block, s);
-  if (fm == 1) return launch_sweep_batch_fm<real, DIM, P1, 1>(args, tmap, n_total, ticket, status, epoch, grid, block, s);
-  if (fm == 2) return launch_sweep_batch_fm<real, DIM, P1, 2>(args, tmap, n_total, ticket, status, epoch, grid, block, s);
+template <typename real, int DIM, int P1, int H>
+cudaError_t launch_sweep_batch_h(int fm, const SweepArgs<real>* args, const int2* tmap, int n_total, int* ticket,
+                                 const int* status, const unsigned* epoch, int grid, int block, cudaStream_t s) {
+  if (fm == 0) return launch_sweep_batch_fm<real, DIM, P1, 0, H>(args, tmap, n_total, ticket, status, epoch, grid, block, s);
+  if (fm == 1) return launch_sweep_batch_fm<real, DIM, P1, 1, H>(args, tmap, n_total, ticket, status, epoch, grid, block, s);
+  if (fm == 2) return launch_sweep_batch_fm<real, DIM, P1, 2, H>(args, tmap, n_total, ticket, status, epoch, grid, block, s);
   return cudaErrorInvalidValue;
 }
 
+// lanes per cell: 1, or 2 for cells of 9 or more dofs
+template <typename real, int DIM, int P1>
+cudaError_t launch_sweep_batch_impl(int fm, int lpc, const SweepArgs<real>* args, const int2* tmap, int n_total,
+                                    int* ticket, const int* status, const unsigned* epoch, int grid,
+                                    int block, cudaStream_t s) {
+  if (lpc == 2) {
+    if constexpr (Cell<DIM, P1>::N >= 9)
+      return launch_sweep_batch_h<real, DIM, P1, 2>(fm, args, tmap, n_total, ticket, status, epoch, grid, block, s);
+    return cudaErrorInvalidValue;
+  }
+  if (lpc != 1) return cudaErrorInvalidValue;
+  return launch_sweep_batch_h<real, DIM, P1, 1>(fm, args, tmap, n_total, ticket, status, epoch, grid, block, s);
+}
+
+template <typename real, int DIM, int P1, int H>
+cudaError_t launch_sweep_h(int fm, const SweepArgs<real>& a, int grid, int block, cudaStream_t s) {
+  if (fm == 0) return launch_sweep_fm<real, DIM, P1, 0, H>(a, grid, block, s);
+  if (fm == 1) return launch_sweep_fm<real, DIM, P1, 1, H>(a, grid, block, s);
+  if (fm == 2) return launch_sweep_fm<real, DIM, P1, 2, H>(a, grid, block, s);
+  return cudaErrorInvalidValue;
+}
+
+// a.lpc lanes per cell: 1, or 2 for cells of 9 or more dofs
 template <typename real, int DIM, int P1>
 cudaError_t launch_sweep_impl(int fm, const SweepArgs<real>& a, int grid, int block,
                               cudaStream_t s) {
-  if (fm == 0) return launch_sweep_fm<real, DIM, P1, 0>(a, grid, block, s);
-  if (fm == 1) return launch_sweep_fm<real, DIM, P1, 1>(a, grid, block, s);
-  if (fm == 2) return launch_sweep_fm<real, DIM, P1, 2>(a, grid, block, s);
-  return cudaErrorInvalidValue;
+  if (a.lpc == 2) {
+    if constexpr (Cell<DIM, P1>::N >= 9) return launch_sweep_h<real, DIM, P1, 2>(fm, a, grid, block, s);
+    return cudaErrorInvalidValue;
+  }
+  if (a.lpc != 1) return cudaErrorInvalidValue;
+  return launch_sweep_h<real, DIM, P1, 1>(fm, a, grid, block, s);
 }
 
 }  // namespace ouranos

@@ -4,10 +4,10 @@
 namespace ouranos {
 
 template <>
-cudaError_t launch_sweep_batch<double>(int dim, int p1, int fm, const SweepArgs<double>* args, const int2* tmap,
+cudaError_t launch_sweep_batch<double>(int dim, int p1, int fm, int lpc, const SweepArgs<double>* args, const int2* tmap,
                                    int n_total, int* ticket, const int* status, const unsigned* epoch,
                                    int grid, int block, cudaStream_t s) {
-#define ARGS fm, args, tmap, n_total, ticket, status, epoch, grid, block, s
+#define ARGS fm, lpc, args, tmap, n_total, ticket, status, epoch, grid, block, s
   if (dim == 2) {
     switch (p1) {
       case 2: return launch_sweep_batch_impl<double, 2, 2>(ARGS);

@@ -68,6 +68,50 @@ def test_tilings_2d(tiling):
     assert rel_err(y, ref) < TOL64
 
 
+@pytest.mark.parametrize("tiling", [(16, 1, 1), (8, 1, 2), (4, 1, 4), (2, 1, 8), (1, 1, 16)])
+@pytest.mark.parametrize("order", [2, 3, 4])
+def test_two_lanes_per_cell_2d(tiling, order):
+    """Cells of 9 or more dofs may be solved by two lanes each (16 cells per
+    warp): every 16-lane tiling matches the oracle, in FP64 and FP32."""
+    import ouranos_gb300 as og
+    prob = og.heterogeneous_2d(seed=6, n=21, fe_order=order, sn=6, l_max=1, blocks=3)
+    x = np.random.default_rng(5).standard_normal(prob.vector_length)
+    ref = po.OracleProblem(prob.arrays()).apply(x)
+    with og.RadiativeTransfer(prob) as rt:
+        rt.set_tiling(*tiling)
+        assert rt.tiling() == tiling
+        assert rel_err(rt.apply(x), ref) < TOL64
+        rt.set_precision("fp32")
+        assert rel_err(rt.apply(x), ref) < 2e-6
+
+
+@pytest.mark.parametrize("tiling", [(4, 4, 1), (4, 2, 2), (2, 2, 4), (16, 1, 1)])
+def test_two_lanes_per_cell_3d(tiling):
+    import ouranos_gb300 as og
+    prob = og.thick_3d(seed=2003, n=9, fe_order=2, sn=4, block=3, width=3.0)
+    x = np.random.default_rng(6).standard_normal(prob.vector_length)
+    ref = po.OracleProblem(prob.arrays()).apply(x)
+    with og.RadiativeTransfer(prob) as rt:
+        rt.set_tiling(*tiling)
+        assert rel_err(rt.apply(x), ref) < TOL64
+
+
+def test_default_tiling_and_lane_rules():
+    """Q2+ cells default to two lanes per cell (16 cells per warp); Q1 cells
+    keep one lane per cell and reject 16-lane tilings."""
+    import ouranos_gb300 as og
+    from ouranos_gb300 import _capi
+    with og.RadiativeTransfer(og.heterogeneous_2d(seed=7, n=16, fe_order=2, sn=4, l_max=0, blocks=2)) as rt:
+        assert rt.tiling() == (16, 1, 1)
+    with og.RadiativeTransfer(og.thick_3d(seed=2004, n=8, fe_order=2, sn=4, block=4, width=2.0)) as rt:
+        assert rt.tiling() == (4, 4, 1)
+    with og.RadiativeTransfer(og.config_small(n=16, sn=4)) as rt:
+        assert rt.tiling() == (32, 1, 1)
+        with pytest.raises(_capi.OuranosError) as e:
+            rt.set_tiling(16, 1, 1)
+        assert e.value.code == _capi.ERR_BAD_INPUT
+
+
 @pytest.mark.parametrize("tiling", [(4, 4, 2), (8, 4, 1), (4, 2, 4), (2, 2, 8), (2, 4, 4)])
 def test_tilings_3d(tiling):
     import ouranos_gb300 as og
