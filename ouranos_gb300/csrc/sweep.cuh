@@ -779,9 +779,15 @@ __global__ void __launch_bounds__(128) sweep_batch_kernel(const SweepArgs<real>*
 }
 
 // Shared-memory carveout for a launch: as much as the blocks that can be
-// resident at once need, the rest of the SM's on-chip memory stays L1, where
-// the cell-solve tables of the running directions live.
-inline int carveout_percent(int grid, size_t smem_per_block, int max_blocks_per_sm) {
+// resident need, but at most what leaves keep_kb of the SM's on-chip memory
+// to L1, where the cell-solve tables of the running directions live.  The
+// kernels that stream their sources element by element (cp.async.ca, which
+// allocates in L1) keep 144 KB: fewer resident warps with their tables in L1
+// beat more warps missing it (2-D Q2 S16 double-float sweep: 4 blocks per SM
+// 1.63 ms, 3 blocks 1.40 ms, 2 blocks 1.35 ms); the 16-byte kernels (Q1 cells,
+// cp.async.cg past L1) keep 32 KB (3-D Q1 GLC S12 FP32: 5 blocks 2.30 ms,
+// 3 or 4 blocks 2.10 ms).
+inline int carveout_percent(int grid, size_t smem_per_block, int max_blocks_per_sm, int keep_kb) {
   static int sms = 0, smem_sm = 0;
   if (!sms) {
     int dev = 0;
@@ -790,12 +796,18 @@ inline int carveout_percent(int grid, size_t smem_per_block, int max_blocks_per_
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     if (sms < 1 || smem_sm < 1) return -1;  // leave the driver's choice
   }
+  const size_t per_block = smem_per_block + 1024;  // + the runtime's reserve per block
   int per_sm = (grid + sms - 1) / sms;
   if (per_sm > max_blocks_per_sm) per_sm = max_blocks_per_sm;
-  const size_t need = (size_t)per_sm * (smem_per_block + 1024);  // + the runtime's reserve per block
+  const long room = (long)smem_sm - (long)keep_kb * 1024;
+  const int fit = room >= (long)per_block ? (int)(room / (long)per_block) : 1;
+  if (per_sm > fit) per_sm = fit;
+  const size_t need = (size_t)per_sm * per_block;
   const int pct = (int)((need * 100 + smem_sm - 1) / smem_sm);
   return pct < 100 ? pct : 100;
 }
+template <typename real, int FM, int N>
+constexpr int l1_keep_kb() { return Stream<real, FM, N>::VEC ? 32 : 144; }
 
 template <typename real, int DIM, int P1, int FM, int H>
 cudaError_t launch_sweep_fm(const SweepArgs<real>& a, int grid, int block, cudaStream_t s) {
@@ -811,7 +823,7 @@ cudaError_t launch_sweep_fm(const SweepArgs<real>& a, int grid, int block, cudaS
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  const int pct = carveout_percent(grid, smem, max_per_sm > 0 ? max_per_sm : 1);
+  const int pct = carveout_percent(grid, smem, max_per_sm > 0 ? max_per_sm : 1, l1_keep_kb<real, FM, N>());
   if (pct >= 0 && pct != carve) {
     cudaError_t e = cudaFuncSetAttribute(sweep_kernel<real, DIM, P1, FM, H>,
                                          cudaFuncAttributePreferredSharedMemoryCarveout, pct);
@@ -840,7 +852,8 @@ cudaError_t launch_sweep_batch_fm(const SweepArgs<real>* args, const int2* tmap,
     configured = true;
   }
   // static shared memory (the argument slots) counts too
-  const int pct = carveout_percent(grid, smem + 4 * sizeof(SweepArgs<real>), max_per_sm > 0 ? max_per_sm : 1);
+  const int pct = carveout_percent(grid, smem + 4 * sizeof(SweepArgs<real>), max_per_sm > 0 ? max_per_sm : 1,
+                                   l1_keep_kb<real, FM, N>());
   if (pct >= 0 && pct != carve) {
     cudaError_t e = cudaFuncSetAttribute(sweep_batch_kernel<real, DIM, P1, FM, H>,
                                          cudaFuncAttributePreferredSharedMemoryCarveout, pct);
