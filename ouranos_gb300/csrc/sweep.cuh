@@ -269,7 +269,16 @@ __device__ __forceinline__ void load_cell(const real* src, real (&o)[N]) {
   }
 }
 
-// dst[0..N) = o[0..N) with 16-byte stores (dst 16-byte aligned)
+// Streaming (evict-first) stores of the angular flux: written once per sweep
+// and read back once by the reduction, it should not push the cell tables and
+// the sources out of the caches.
+__device__ __forceinline__ void store_stream(float* p, float v) { __stcs(p, v); }
+__device__ __forceinline__ void store_stream(double* p, double v) { __stcs(p, v); }
+__device__ __forceinline__ void store_stream(df64* p, df64 v) {
+  __stcs(reinterpret_cast<float2*>(p), make_float2(v.hi, v.lo));
+}
+
+// dst[0..N) = o[0..N) with 16-byte streaming stores (dst 16-byte aligned)
 template <typename real, int N>
 __device__ __forceinline__ void store_cell(real* dst, const real (&o)[N]) {
   constexpr int W = Bits<real>::W;
@@ -278,7 +287,7 @@ __device__ __forceinline__ void store_cell(real* dst, const real (&o)[N]) {
     unsigned u[4];
 #pragma unroll
     for (int t = 0; t < 4; ++t) u[t] = Bits<real>::word(o[(4 * k + t) / W], (4 * k + t) % W);
-    *reinterpret_cast<uint4*>(reinterpret_cast<char*>(dst) + 16 * k) = make_uint4(u[0], u[1], u[2], u[3]);
+    __stcs(reinterpret_cast<uint4*>(reinterpret_cast<char*>(dst) + 16 * k), make_uint4(u[0], u[1], u[2], u[3]));
   }
 }
 // o[j] <- o[j ^ m] for every j (conditional swaps along each index bit)
@@ -711,7 +720,7 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
 #pragma unroll
           for (int k = 0; k < NR; ++k) {
             const int i = k * H + half;
-            if (H == 1 || i < N) P[off(i)] = xr[k];
+            if (H == 1 || i < N) store_stream(P + off(i), xr[k]);
           }
         }
       }
