@@ -468,8 +468,10 @@ def run_time(args):
     directions), implicit Euler with 1/(v dt) = 0.5, a Gaussian pulse
     (peak 10 at step 20, width 5 steps) in a seeded 8^3-cell box, two-material
     map.  Every step is solved to `tol` by FGMRES with FP32 sweeps and FP64
-    restarts, warm-started from the previous step; psi^n is kept in FP32.  The
-    first `time_compare` steps are repeated with plain FP64 GMRES."""
+    restarts (and the diffusion acceleration unless --time-no-dsa),
+    warm-started from the previous step; phi and psi^n (FP32) stay on the
+    device.  The first `time_compare` steps are repeated with plain FP64
+    GMRES."""
     import time
     import numpy as np
     import ouranos_gb300 as og
@@ -478,12 +480,15 @@ def run_time(args):
     out = {"workload": "3d-td-%d^3-dgq1-ls8-%dsteps" % (args.time_n, args.time_steps), "tol": args.tol,
            "inv_vdt": inv_vdt}
 
+    import torch
+
     def run(method, steps, dsa=False):
         with og.RadiativeTransfer(prob) as rt:
             rt.set_time_step(inv_vdt)
             if dsa:
                 rt.set_dsa(args.dsa_cg)
-            phi = np.zeros(rt.length)
+            # phi stays on the device between steps (each call takes and returns device vectors)
+            phi = torch.zeros(rt.length, dtype=torch.float64, device="cuda")
             its, secs = [], []
             t0 = time.perf_counter()
             for n in range(steps):
@@ -492,7 +497,7 @@ def run_time(args):
                 its.append(info["iterations"])
                 secs.append(info["seconds"])
             wall = time.perf_counter() - t0
-            return phi, its, secs, wall
+            return phi.cpu().numpy(), its, secs, wall
 
     dsa = not args.time_no_dsa
     main_name = "fgmres_mixed+dsa" if dsa else "fgmres_mixed"

@@ -479,19 +479,55 @@ __global__ void scale_inv_norm_kernel(const double* nrm2, double* v, long len) {
 }  // namespace
 
 namespace {
-template <typename real>
-__global__ void angular_source_kernel(real* __restrict__ q, const float* __restrict__ psi,
-                                      const double* __restrict__ M, double inv_vdt, int n, long n_cells,
-                                      int n_dir) {
-  const long n_dofs = n_cells * n;
-  const long total = (long)n_dir * n_dofs;
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(e % n);
-    const float* pc = psi + (e - i);  // the cell's n values of this direction
-    const double* row = M + i * n;
-    double acc = 0.0;
-    for (int j = 0; j < n; ++j) acc += row[j] * (double)pc[j];
-    q[e] = real_from_double<real>(real_to_double(q[e]) + inv_vdt * acc);
+// One thread per (direction, cell): the cell's n values of psi^n are read
+// once and q[d][c n + i] += sum_j (inv_vdt M)_ij psi^n_j is formed in
+// double-float (FP64 storage) or FP32 -- no FP64 instruction, whose rate on
+// GB300 is 1/64 of FP32.
+template <typename real, int N>
+__global__ void __launch_bounds__(256) angular_source_kernel(real* __restrict__ q, const float* __restrict__ psi,
+                                                             const double* __restrict__ M, double inv_vdt,
+                                                             long n_cells, int n_dir) {
+  constexpr bool F32 = sizeof(real) == 4;
+  __shared__ df64 sd[N * N];
+  __shared__ float sf[N * N];
+  for (int k = threadIdx.x; k < N * N; k += blockDim.x) {
+    const double m = inv_vdt * M[k];
+    sd[k] = df64_from(m);
+    sf[k] = (float)m;
+  }
+  __syncthreads();
+  const long total = (long)n_dir * n_cells;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    const float* pc = psi + t * N;  // [dir][cell][N]: (direction, cell) t is contiguous
+    float p[N];
+    if constexpr (N % 4 == 0) {
+#pragma unroll
+      for (int k = 0; k < N / 4; ++k) {
+        const float4 v = reinterpret_cast<const float4*>(pc)[k];
+        p[4 * k] = v.x;
+        p[4 * k + 1] = v.y;
+        p[4 * k + 2] = v.z;
+        p[4 * k + 3] = v.w;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < N; ++j) p[j] = pc[j];
+    }
+    real* qc = q + t * N;
+#pragma unroll 1
+    for (int i = 0; i < N; ++i) {
+      if constexpr (F32) {
+        float acc = (float)real_to_double(qc[i]);
+#pragma unroll
+        for (int j = 0; j < N; ++j) acc = __fmaf_rn(sf[i * N + j], p[j], acc);
+        qc[i] = (real)acc;
+      } else {
+        df64_acc acc = acc_from(to_df64(qc[i]));
+#pragma unroll
+        for (int j = 0; j < N; ++j) acc_fma(acc, sd[i * N + j], df64(p[j]));
+        qc[i] = store_df64<real>(acc_result(acc));
+      }
+    }
   }
 }
 }  // namespace
@@ -499,8 +535,18 @@ __global__ void angular_source_kernel(real* __restrict__ q, const float* __restr
 template <typename real>
 cudaError_t launch_angular_source(real* q, const float* psi, const double* cell_mass, double inv_vdt,
                                   int n, long n_cells, int n_dir, cudaStream_t s) {
-  angular_source_kernel<real><<<grid_for((long)n_dir * n_cells * n), kBlock, 0, s>>>(q, psi, cell_mass,
-                                                                                   inv_vdt, n, n_cells, n_dir);
+  const long total = (long)n_dir * n_cells;
+  const int grid = grid_for(total);
+  switch (n) {
+#define CASE(NN)                                                                                             \
+  case NN:                                                                                                   \
+    angular_source_kernel<real, NN><<<grid, 256, 0, s>>>(q, psi, cell_mass, inv_vdt, n_cells, n_dir);         \
+    break;
+    CASE(4) CASE(8) CASE(9) CASE(16) CASE(25) CASE(27)
+#undef CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 template cudaError_t launch_angular_source<double>(double*, const float*, const double*, double, int, long,
