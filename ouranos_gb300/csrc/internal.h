@@ -142,6 +142,26 @@ cudaError_t launch_expand_source_pairs(const df64* T, const df64* iso, const dou
                                        int n_dir, int n_mom, long n_dofs, cudaStream_t s);
 cudaError_t launch_reduce_moments_pairs(const df64* psi, const double* d2m_t, double* phi, int n_dir,
                                         int n_mom, long n_dofs, cudaStream_t s);
+// Octant symmetry of a quadrature: the directions form classes of P = 2^dim
+// members with the same |Omega|, member f having Omega_a < 0 exactly for the
+// bits a of f; every moment m belongs to a parity group g whose M2D (and D2M)
+// entries on member f are those of member 0 times -1 where bit f of sign[g]
+// is set.  Built on the host (operator.cu) when the quadrature has it.
+struct SymTables {
+  int n_class = 0, P = 0, G = 0;
+  const int* cls_dir = nullptr;       // [n_class][P] direction of member f
+  const int* mom_group = nullptr;     // [n_mom] parity group
+  const unsigned* sign = nullptr;     // [G] bit f set: negative on member f
+  const double* m2d_rep = nullptr;    // [n_class][n_mom] M2D of member 0
+  const double* d2m_rep = nullptr;    // [n_class][n_mom] D2M of member 0
+};
+// the double-float pair contractions through the symmetry: each class forms
+// its products once per parity group (expansion) or its signed sums of psi
+// once per group (reduction), about half the arithmetic of the direct form
+cudaError_t launch_expand_sym_pairs(const df64* T, const df64* iso, const SymTables& st, df64* q, int n_mom,
+                                    long n_dofs, cudaStream_t s);
+cudaError_t launch_reduce_sym_pairs(const df64* psi, const SymTables& st, double* phi, int n_mom, long n_dofs,
+                                    cudaStream_t s);
 // phi[m][e] = sum_d D2M[m][d] psi[d][e]  -- direction -> moment reduction
 template <typename real>
 cudaError_t launch_reduce_moments(const real* psi, const real* d2m_t, real* phi, int n_dir,
@@ -294,6 +314,9 @@ struct ouranos_rt {
   // the source of source sweeps; psi^n (FP32, [dir][dof]) kept on the device
   double inv_vdt = 0.0;
   ouranos::DevBuf d_psi_prev;
+  // octant symmetry of the quadrature (empty: contractions take the direct form)
+  ouranos::SymTables sym;
+  ouranos::DevBuf d_sym_dir, d_sym_group, d_sym_sign, d_sym_m2d, d_sym_d2m;
   // learned preconditioner
   ouranos_cnn* cnn = nullptr;
   int pc_group = -1;

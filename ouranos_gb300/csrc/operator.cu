@@ -85,6 +85,88 @@ bool is_device_ptr(const void* p) {
 
 long vec_len(const ouranos_rt* rt) { return (long)rt->n_mom * rt->n_dofs; }
 
+// --------------------------------------------------------- octant symmetry
+// Classes of P = 2^dim directions with equal |Omega| (member f: Omega_a < 0
+// for the bits a of f), and for every moment the sign pattern of its M2D and
+// D2M entries over the members, which must be the same in every class (the
+// parity of a real spherical harmonic under the axis reflections).  Entries
+// count as equal or opposite within 32 ulps of the moment's largest entry
+// (harmonics evaluated at reflected angles differ by a few ulps);
+// anything else (a quadrature without full octant symmetry, directions on an
+// axis plane) leaves the symmetric contractions off.
+int build_symmetry(ouranos_rt* rt) {
+  rt->sym = SymTables{};
+  const int P = 1 << rt->dim, nd = rt->n_dir, nm = rt->n_mom, nc = rt->n_dir_class;
+  if (nm > 16 || nd != nc * P) return OURANOS_OK;
+  std::vector<int> cls(nc * P, -1);
+  for (int d = 0; d < nd; ++d) {
+    int f = 0;
+    for (int a = 0; a < rt->dim; ++a) {
+      if (rt->omega[3 * d + a] == 0.0) return OURANOS_OK;
+      if (rt->omega[3 * d + a] < 0.0) f |= 1 << a;
+    }
+    int& slot = cls[rt->dir_class_h[d] * P + f];
+    if (slot >= 0) return OURANOS_OK;
+    slot = d;
+  }
+  for (int v : cls)
+    if (v < 0) return OURANOS_OK;
+  const double tol = 32.0 * 2.220446049250313e-16;
+  auto m2d = [&](int d, int m) { return rt->m2d[(size_t)d * nm + m]; };
+  auto d2m = [&](int d, int m) { return rt->d2m[(size_t)m * nd + d]; };
+  std::vector<unsigned> group_sign;
+  std::vector<int> mom_group(nm, 0);
+  for (int m = 0; m < nm; ++m) {
+    // bits whose sign some entry pins down (equal or opposite to member 0's
+    // within the tolerance), and their values
+    unsigned known = 0, value = 0;
+    for (int which = 0; which < 2; ++which) {
+      auto val = [&](int d) { return which ? d2m(d, m) : m2d(d, m); };
+      double scale = 0.0;
+      for (int d = 0; d < nd; ++d) scale = std::max(scale, std::fabs(val(d)));
+      const double t = tol * scale;
+      for (int c = 0; c < nc; ++c) {
+        const double a = val(cls[c * P]);
+        for (int f = 0; f < P; ++f) {
+          const double b = val(cls[c * P + f]);
+          const bool eq = std::fabs(b - a) <= t, opp = std::fabs(b + a) <= t;
+          if (!eq && !opp) return OURANOS_OK;
+          if (eq == opp) continue;  // |a|, |b| below the tolerance: either sign
+          const unsigned bit = 1u << f;
+          if ((known & bit) && ((value & bit) != 0) != opp) return OURANOS_OK;
+          known |= bit;
+          if (opp) value |= bit;
+        }
+      }
+    }
+    int g = 0;
+    while (g < (int)group_sign.size() && group_sign[g] != value) ++g;
+    if (g == (int)group_sign.size()) group_sign.push_back(value);
+    mom_group[m] = g;
+  }
+  if ((int)group_sign.size() > P) return OURANOS_OK;
+  std::vector<double> m2d_rep((size_t)nc * nm), d2m_rep((size_t)nc * nm);
+  for (int c = 0; c < nc; ++c)
+    for (int m = 0; m < nm; ++m) {
+      m2d_rep[(size_t)c * nm + m] = m2d(cls[c * P], m);
+      d2m_rep[(size_t)c * nm + m] = d2m(cls[c * P], m);
+    }
+  int rc;
+  if ((rc = upload(rt, rt->d_sym_dir, cls, "symmetry")) || (rc = upload(rt, rt->d_sym_group, mom_group, "symmetry")) ||
+      (rc = upload(rt, rt->d_sym_sign, group_sign, "symmetry")) ||
+      (rc = upload(rt, rt->d_sym_m2d, m2d_rep, "symmetry")) || (rc = upload(rt, rt->d_sym_d2m, d2m_rep, "symmetry")))
+    return rc;
+  rt->sym.n_class = nc;
+  rt->sym.P = P;
+  rt->sym.G = (int)group_sign.size();
+  rt->sym.cls_dir = rt->d_sym_dir.as<int>();
+  rt->sym.mom_group = rt->d_sym_group.as<int>();
+  rt->sym.sign = rt->d_sym_sign.as<unsigned>();
+  rt->sym.m2d_rep = rt->d_sym_m2d.as<double>();
+  rt->sym.d2m_rep = rt->d_sym_d2m.as<double>();
+  return OURANOS_OK;
+}
+
 // ------------------------------------------------------------------ schedule
 // Directions of one octant (same sign pattern) are grouped kd at a time; each
 // group crosses the transverse tiles in dependency order.
@@ -281,7 +363,11 @@ int sweep_prepare(ouranos_rt* rt, const real* src, const real* iso, const real* 
   if (angular) fm = 0;
   if (fm == 0) {
     CU(rt->d_q.alloc(sizeof(real) * len_dir), "expanded source");
-    if (std::is_same<real, df64>::value)  // pairs in, pairs out
+    if (std::is_same<real, df64>::value && rt->sym.n_class)  // pairs, through the octant symmetry
+      CU(launch_expand_sym_pairs((const df64*)src, (const df64*)iso, rt->sym, rt->d_q.as<df64>(), rt->n_mom,
+                                 rt->n_dofs, rt->stream),
+         "source expansion");
+    else if (std::is_same<real, df64>::value)  // pairs in, pairs out
       CU(launch_expand_source_pairs((const df64*)src, (const df64*)iso, rt->d_m2d64.as<double>(),
                                     rt->d_q.as<df64>(), rt->n_dir, rt->n_mom, rt->n_dofs, rt->stream),
          "source expansion");
@@ -310,7 +396,10 @@ int sweep_prepare(ouranos_rt* rt, const real* src, const real* iso, const real* 
 // FP32 sweep, double for the FP64 and double-float sweeps
 template <typename real>
 int sweep_reduce(ouranos_rt* rt, const real* psi, void* phi) {
-  if (std::is_same<real, df64>::value)
+  if (std::is_same<real, df64>::value && rt->sym.n_class)
+    CU(launch_reduce_sym_pairs((const df64*)psi, rt->sym, (double*)phi, rt->n_mom, rt->n_dofs, rt->stream),
+       "moment reduction");
+  else if (std::is_same<real, df64>::value)
     CU(launch_reduce_moments_pairs((const df64*)psi, rt->d_d2m64.as<double>(), (double*)phi, rt->n_dir,
                                    rt->n_mom, rt->n_dofs, rt->stream),
        "moment reduction");
@@ -742,6 +831,7 @@ int ouranos_rt_create(const ouranos_problem_desc* D, int device, ouranos_rt** ou
     return fail(rc);
   if (!rt->cell_order.empty() && (rc = upload(rt, rt->d_cell_order, rt->cell_order, "cell order")))
     return fail(rc);
+  if ((rc = build_symmetry(rt))) return fail(rc);
   if ((rc = default_tiling(rt)) || (rc = build_schedule(rt)) || (rc = setup_group(rt)))
     return fail(rc);
   if (cudaStreamSynchronize(rt->stream) != cudaSuccess)

@@ -1,6 +1,10 @@
 // Vector kernels around the sweep: scattering source, fixed source, the
 // residual form of Apply, layout permutations and the FP64 BLAS-1 pieces of
 // the Krylov drivers.  All are HBM-streaming, one grid-stride loop each.
+#include <algorithm>
+#include <mutex>
+#include <unordered_map>
+
 #include "df64.cuh"
 #include "internal.h"
 
@@ -12,6 +16,40 @@ constexpr int kBlock = 256;
 inline int grid_for(long n) {
   long g = (n + kBlock - 1) / kBlock;
   if (g > 152L * 32) g = 152L * 32;  // 152 SMs x 32 resident blocks of 256 threads at most
+  return g < 1 ? 1 : (int)g;
+}
+
+// Grid of the direction-axis contractions: no more blocks than can be
+// resident at once, so the grid-stride loop runs in balanced rounds (one
+// thread per dof left a nearly empty last wave: 2304 blocks over 760-912
+// resident slots).  Resident blocks per SM are queried once per kernel.
+template <typename K>
+int resident_grid(K kernel, long n, size_t smem) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, int> per_sm_cache;
+  static int sms = 0;
+  int per_sm = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!sms) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (sms < 1) sms = 152;
+    }
+    auto it = per_sm_cache.find((const void*)kernel);
+    if (it != per_sm_cache.end()) {
+      per_sm = it->second;
+    } else {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, smem) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+      }
+      per_sm_cache[(const void*)kernel] = per_sm;
+    }
+  }
+  const long need = (n + kBlock - 1) / kBlock;
+  const long g = std::min(need, (long)per_sm * sms);
   return g < 1 ? 1 : (int)g;
 }
 
@@ -276,6 +314,7 @@ __global__ void reduce_df64_kernel(const S* __restrict__ psi, const double* __re
     df64_acc acc[NM];
 #pragma unroll
     for (int m = 0; m < NM; ++m) acc[m] = acc_zero();
+#pragma unroll 4  // several directions' loads in flight
     for (int d = 0; d < n_dir; ++d) {
       const df64 v = to_df64(psi[(size_t)d * n_dofs + e]);
 #pragma unroll
@@ -300,11 +339,11 @@ static cudaError_t expand_df64_any(const S* T, const S* iso, const double* m2d, 
     const int acc = m0 > 0;
     const S* is = m0 == 0 ? iso : nullptr;
     if (nm <= 4)
-      expand_df64_kernel<4, S><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+      expand_df64_kernel<4, S><<<resident_grid(expand_df64_kernel<4, S>, n_dofs, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
     else if (nm <= 10)
-      expand_df64_kernel<10, S><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+      expand_df64_kernel<10, S><<<resident_grid(expand_df64_kernel<10, S>, n_dofs, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
     else
-      expand_df64_kernel<16, S><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+      expand_df64_kernel<16, S><<<resident_grid(expand_df64_kernel<16, S>, n_dofs, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -319,17 +358,170 @@ static cudaError_t reduce_df64_any(const S* psi, const double* d2m_t, double* ph
     const size_t sh = sizeof(df64) * (size_t)n_dir * nm;
     double* ph = phi + (size_t)m0 * n_dofs;
     if (nm <= 1)
-      reduce_df64_kernel<1, S><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_df64_kernel<1, S><<<resident_grid(reduce_df64_kernel<1, S>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
     else if (nm <= 4)
-      reduce_df64_kernel<4, S><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_df64_kernel<4, S><<<resident_grid(reduce_df64_kernel<4, S>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
     else if (nm <= 10)
-      reduce_df64_kernel<10, S><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_df64_kernel<10, S><<<resident_grid(reduce_df64_kernel<10, S>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
     else
-      reduce_df64_kernel<16, S><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_df64_kernel<16, S><<<resident_grid(reduce_df64_kernel<16, S>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+namespace {
+// Shared-memory images of the symmetry tables: representative M2D or D2M rows
+// as double-float [class][nm], members [class][P], groups [nm], signs [G].
+template <int P>
+__device__ __forceinline__ void load_sym(const SymTables& st, const double* rep, int nm, df64* srep, int* sdir,
+                                         int* sgrp, unsigned* ssign) {
+  for (int k = threadIdx.x; k < st.n_class * nm; k += blockDim.x) srep[k] = df64_from(rep[k]);
+  for (int k = threadIdx.x; k < st.n_class * P; k += blockDim.x) sdir[k] = st.cls_dir[k];
+  for (int k = threadIdx.x; k < nm; k += blockDim.x) sgrp[k] = st.mom_group[k];
+  for (int k = threadIdx.x; k < st.G; k += blockDim.x) ssign[k] = st.sign[k];
+  __syncthreads();
+}
+__device__ __forceinline__ df64 neg_if(df64 v, bool neg) { return neg ? df64(-v.hi, -v.lo) : v; }
+
+// q[d][e] for the P members d of each class: the class's products
+// M2D_rep[m] T_m are summed per parity group once, then each member adds the
+// group sums with its signs (+ iso)
+template <int NM, int P>
+__global__ void __launch_bounds__(256) expand_sym_kernel(const df64* __restrict__ T, const df64* __restrict__ iso,
+                                                         SymTables st, df64* __restrict__ q, int nm, long n_dofs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  df64* srep = reinterpret_cast<df64*>(smem_raw);
+  int* sdir = reinterpret_cast<int*>(srep + st.n_class * nm);
+  int* sgrp = sdir + st.n_class * P;
+  unsigned* ssign = reinterpret_cast<unsigned*>(sgrp + 16);
+  load_sym<P>(st, st.m2d_rep, nm, srep, sdir, sgrp, ssign);
+  const int G = st.G;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n_dofs; e += (long)gridDim.x * blockDim.x) {
+    df64 t[NM];
+#pragma unroll
+    for (int m = 0; m < NM; ++m) t[m] = m < nm ? T[(size_t)m * n_dofs + e] : df64(0.f);
+    const df64 is = iso ? iso[e] : df64(0.f);
+    for (int c = 0; c < st.n_class; ++c) {
+      df64_acc S[P];
+#pragma unroll
+      for (int g = 0; g < P; ++g) S[g] = acc_zero();
+      const df64* rep = srep + c * nm;
+#pragma unroll
+      for (int m = 0; m < NM; ++m) {
+        if (m >= nm) break;
+        const df64 r = rep[m];
+        const int grp = sgrp[m];  // the same for every thread: uniform branches
+#pragma unroll
+        for (int g = 0; g < P; ++g)
+          if (grp == g) acc_fma(S[g], r, t[m]);
+      }
+      df64 sg[P];
+#pragma unroll
+      for (int g = 0; g < P; ++g) sg[g] = acc_result(S[g]);
+#pragma unroll
+      for (int f = 0; f < P; ++f) {
+        df64_acc o = acc_from(is);
+#pragma unroll
+        for (int g = 0; g < P; ++g)
+          if (g < G) acc_add(o, neg_if(sg[g], (ssign[g] >> f) & 1u));
+        q[(size_t)sdir[c * P + f] * n_dofs + e] = acc_result(o);
+      }
+    }
+  }
+}
+
+// phi[m][e]: each class's P values of psi are combined into one signed sum
+// per parity group, then every moment takes D2M_rep[m] times its group's sum
+template <int NM, int P>
+__global__ void __launch_bounds__(256) reduce_sym_kernel(const df64* __restrict__ psi, SymTables st,
+                                                         double* __restrict__ phi, int nm, long n_dofs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  df64* srep = reinterpret_cast<df64*>(smem_raw);
+  int* sdir = reinterpret_cast<int*>(srep + st.n_class * nm);
+  int* sgrp = sdir + st.n_class * P;
+  unsigned* ssign = reinterpret_cast<unsigned*>(sgrp + 16);
+  load_sym<P>(st, st.d2m_rep, nm, srep, sdir, sgrp, ssign);
+  const int G = st.G;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n_dofs; e += (long)gridDim.x * blockDim.x) {
+    df64_acc acc[NM];
+#pragma unroll
+    for (int m = 0; m < NM; ++m) acc[m] = acc_zero();
+    for (int c = 0; c < st.n_class; ++c) {
+      df64 ps[P];
+#pragma unroll
+      for (int f = 0; f < P; ++f) ps[f] = psi[(size_t)sdir[c * P + f] * n_dofs + e];
+      df64 C[P];
+#pragma unroll
+      for (int g = 0; g < P; ++g) {
+        C[g] = df64(0.f);
+        if (g < G) {
+          const unsigned sg = ssign[g];
+          df64_acc o = acc_from(neg_if(ps[0], sg & 1u));
+#pragma unroll
+          for (int f = 1; f < P; ++f) acc_add(o, neg_if(ps[f], (sg >> f) & 1u));
+          C[g] = acc_result(o);
+        }
+      }
+      const df64* rep = srep + c * nm;
+#pragma unroll
+      for (int m = 0; m < NM; ++m) {
+        if (m >= nm) break;
+        const int grp = sgrp[m];
+        df64 cg = C[0];
+#pragma unroll
+        for (int g = 1; g < P; ++g)
+          if (grp == g) cg = C[g];
+        acc_fma(acc[m], rep[m], cg);
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < NM; ++m)
+      if (m < nm) phi[(size_t)m * n_dofs + e] = df64_to(acc_result(acc[m]));
+  }
+}
+
+template <int P>
+cudaError_t expand_sym_any(const df64* T, const df64* iso, const SymTables& st, df64* q, int nm, long n_dofs,
+                           cudaStream_t s) {
+  const size_t sh = sizeof(df64) * st.n_class * nm + sizeof(int) * (st.n_class * P + 16) + sizeof(unsigned) * 8;
+  if (nm <= 4)
+    expand_sym_kernel<4, P><<<resident_grid(expand_sym_kernel<4, P>, n_dofs, sh), kBlock, sh, s>>>(T, iso, st, q, nm, n_dofs);
+  else if (nm <= 10)
+    expand_sym_kernel<10, P><<<resident_grid(expand_sym_kernel<10, P>, n_dofs, sh), kBlock, sh, s>>>(T, iso, st, q, nm, n_dofs);
+  else
+    expand_sym_kernel<16, P><<<resident_grid(expand_sym_kernel<16, P>, n_dofs, sh), kBlock, sh, s>>>(T, iso, st, q, nm, n_dofs);
+  return cudaGetLastError();
+}
+template <int P>
+cudaError_t reduce_sym_any(const df64* psi, const SymTables& st, double* phi, int nm, long n_dofs, cudaStream_t s) {
+  const size_t sh = sizeof(df64) * st.n_class * nm + sizeof(int) * (st.n_class * P + 16) + sizeof(unsigned) * 8;
+  if (nm <= 1)
+    reduce_sym_kernel<1, P><<<resident_grid(reduce_sym_kernel<1, P>, n_dofs, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs);
+  else if (nm <= 4)
+    reduce_sym_kernel<4, P><<<resident_grid(reduce_sym_kernel<4, P>, n_dofs, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs);
+  else if (nm <= 10)
+    reduce_sym_kernel<10, P><<<resident_grid(reduce_sym_kernel<10, P>, n_dofs, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs);
+  else
+    reduce_sym_kernel<16, P><<<resident_grid(reduce_sym_kernel<16, P>, n_dofs, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs);
+  return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_expand_sym_pairs(const df64* T, const df64* iso, const SymTables& st, df64* q, int n_mom,
+                                    long n_dofs, cudaStream_t s) {
+  if (n_mom > 16 || st.G > st.P) return cudaErrorInvalidValue;
+  if (st.P == 4) return expand_sym_any<4>(T, iso, st, q, n_mom, n_dofs, s);
+  if (st.P == 8) return expand_sym_any<8>(T, iso, st, q, n_mom, n_dofs, s);
+  return cudaErrorInvalidValue;
+}
+cudaError_t launch_reduce_sym_pairs(const df64* psi, const SymTables& st, double* phi, int n_mom, long n_dofs,
+                                    cudaStream_t s) {
+  if (n_mom > 16 || st.G > st.P) return cudaErrorInvalidValue;
+  if (st.P == 4) return reduce_sym_any<4>(psi, st, phi, n_mom, n_dofs, s);
+  if (st.P == 8) return reduce_sym_any<8>(psi, st, phi, n_mom, n_dofs, s);
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_expand_source_df64(const double* T, const double* iso, const double* m2d,
@@ -361,11 +553,11 @@ cudaError_t launch_expand_source(const real* T, const real* iso, const real* m2d
     const int acc = m0 > 0;
     const real* is = m0 == 0 ? iso : nullptr;
     if (nm <= 4)
-      expand_kernel<real, 4><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+      expand_kernel<real, 4><<<resident_grid(expand_kernel<real, 4>, n_dofs, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
     else if (nm <= 10)
-      expand_kernel<real, 10><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+      expand_kernel<real, 10><<<resident_grid(expand_kernel<real, 10>, n_dofs, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
     else
-      expand_kernel<real, 16><<<grid_for(n_dofs), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+      expand_kernel<real, 16><<<resident_grid(expand_kernel<real, 16>, n_dofs, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -384,13 +576,13 @@ cudaError_t launch_reduce_moments(const real* psi, const real* d2m_t, real* phi,
     const size_t sh = sizeof(real) * (size_t)n_dir * nm;
     real* ph = phi + (size_t)m0 * n_dofs;
     if (nm <= 1)
-      reduce_kernel<real, 1><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_kernel<real, 1><<<resident_grid(reduce_kernel<real, 1>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
     else if (nm <= 4)
-      reduce_kernel<real, 4><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_kernel<real, 4><<<resident_grid(reduce_kernel<real, 4>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
     else if (nm <= 10)
-      reduce_kernel<real, 10><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_kernel<real, 10><<<resident_grid(reduce_kernel<real, 10>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
     else
-      reduce_kernel<real, 16><<<grid_for(n_dofs), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_kernel<real, 16><<<resident_grid(reduce_kernel<real, 16>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
