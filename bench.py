@@ -52,7 +52,7 @@ def workload_problem(seed=1001):
 # (dram__bytes_read.sum + dram__bytes_write.sum), per precision, default tiling
 # and FP64 arithmetic
 PROFILED_TILING = (16, 1, 1)  # the default for Q2 cells: two lanes per cell
-SWEEP_TRAFFIC_BYTES = {"fp64": 702.409472e6 + 663.693312e6, "fp32": 361.859328e6 + 316.292352e6}
+SWEEP_TRAFFIC_BYTES = {"fp64": 702.409472e6 + 663.693312e6, "fp32": 361.657088e6 + 316.145664e6}
 
 
 def bytes_per_solve(prob, real_bytes=8):
