@@ -96,9 +96,9 @@ struct SweepArgs {
   int n_dir_class;
   const real* abs_omega;       // [n_dir][3]
   const real* m2d;             // [n_dir][n_mom]      (moment-fused form)
-  const real* ainv;            // [n_sigma_class][n_dir_class][n][n]
+  const real* ainv;            // [n_sigma_class][n_dir_class][n][pad4(n)]
   const int* cell_class;       // [cells] sigma_t class
-  const real* face_mass;       // [3][fd][fd]
+  const real* face_mass;       // [3][fd][pad4(fd)]
   const real* src;             // [n_mom][n_dofs] source moments T (moment-fused form)
   const real* iso;             // [n_dofs] isotropic fixed source or NULL (moment-fused form)
   const real* q;               // [n_dir][n_dofs] per-direction source (expanded form)

@@ -60,6 +60,16 @@ std::vector<df64> to_df(const std::vector<double>& v) {
   return out;
 }
 
+// rows x cols -> rows x pad4(cols), zero padding: the sweep's cell tables are
+// read a row at a time in 16-byte pieces
+std::vector<double> pad_rows(const std::vector<double>& v, long rows, int cols) {
+  const int pc = (cols + 3) & ~3;
+  std::vector<double> out((size_t)rows * pc, 0.0);
+  for (long r = 0; r < rows; ++r)
+    for (int c = 0; c < cols; ++c) out[(size_t)r * pc + c] = v[(size_t)r * cols + c];
+  return out;
+}
+
 // the sweep runs in double-float with pair storage
 bool df64_sweep(const ouranos_rt* rt) {
   return rt->precision == OURANOS_FP64 && rt->fp64_contract == OURANOS_FP64_DF64_SWEEP;
@@ -265,9 +275,11 @@ int setup_group(ouranos_rt* rt) {
     for (int dc = 0; dc < rt->n_dir_class; ++dc)
       canonical_inverse(rt->fe, cls_val[s], &rt->class_abs_omega[3 * dc],
                         &ainv[(s * rt->n_dir_class + dc) * nn]);
-  OK_OR_RETURN(upload(rt, rt->d_ainv64, ainv, "inverse tables"));
-  OK_OR_RETURN(upload(rt, rt->d_ainv32, to_f32(ainv), "inverse tables"));
-  OK_OR_RETURN(upload(rt, rt->d_ainvdf, to_df(ainv), "inverse tables"));
+  // rows padded to whole 16-byte pieces in every precision (the sweep loads them as vectors)
+  const std::vector<double> ainv_p = pad_rows(ainv, (long)cls_val.size() * rt->n_dir_class * n, n);
+  OK_OR_RETURN(upload(rt, rt->d_ainv64, ainv_p, "inverse tables"));
+  OK_OR_RETURN(upload(rt, rt->d_ainv32, to_f32(ainv_p), "inverse tables"));
+  OK_OR_RETURN(upload(rt, rt->d_ainvdf, to_df(ainv_p), "inverse tables"));
   // scattering scales: sigma_s(mat, g'->g, l(m)) (by Legendre order)
   auto sig_s = [&](int mat, int gf, int gt, int l) {
     if (l > L) return 0.0;
@@ -821,9 +833,9 @@ int ouranos_rt_create(const ouranos_problem_desc* D, int device, ouranos_rt** ou
       (rc = upload(rt, rt->d_m2ddf, to_df(rt->m2d), "m2d")) ||
       (rc = upload(rt, rt->d_d2m64, d2m_t, "d2m")) ||
       (rc = upload(rt, rt->d_d2m32, to_f32(d2m_t), "d2m")) ||
-      (rc = upload(rt, rt->d_face64, rt->fe.face_mass, "face mass")) ||
-      (rc = upload(rt, rt->d_face32, to_f32(rt->fe.face_mass), "face mass")) ||
-      (rc = upload(rt, rt->d_facedf, to_df(rt->fe.face_mass), "face mass")) ||
+      (rc = upload(rt, rt->d_face64, pad_rows(rt->fe.face_mass, 3L * rt->fd, rt->fd), "face mass")) ||
+      (rc = upload(rt, rt->d_face32, to_f32(pad_rows(rt->fe.face_mass, 3L * rt->fd, rt->fd)), "face mass")) ||
+      (rc = upload(rt, rt->d_facedf, to_df(pad_rows(rt->fe.face_mass, 3L * rt->fd, rt->fd)), "face mass")) ||
       (rc = upload(rt, rt->d_cell_mass, rt->fe.mass, "mass")) ||
       (rc = upload(rt, rt->d_rowsum_mass, rowsum, "mass")) ||
       (rc = upload(rt, rt->d_material, rt->material_id, "materials")) ||

@@ -250,6 +250,23 @@ template <>
 __device__ __forceinline__ df64 from_words<df64>(unsigned w0, unsigned w1) {
   return df64(__uint_as_float(w0), __uint_as_float(w1));
 }
+// A table row of NV values stored padded to whole 16-byte pieces (p 16-byte
+// aligned): read through the read-only path in 16-byte loads
+template <typename real, int NV>
+__device__ __forceinline__ void load_row(const real* p, real (&o)[NV]) {
+  constexpr int PER = 16 / (int)sizeof(real);  // values per piece: 4 floats, 2 doubles or pairs
+  constexpr int W = Bits<real>::W;
+#pragma unroll
+  for (int k = 0; k < (NV + PER - 1) / PER; ++k) {
+    const uint4 u = __ldg(reinterpret_cast<const uint4*>(p) + k);
+    const unsigned w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int t = 0; t < PER; ++t)
+      if (k * PER + t < NV) o[k * PER + t] = from_words<real>(w[t * W], W == 2 ? w[t * W + 1] : 0u);
+  }
+}
+__host__ __device__ constexpr int pad4(int n) { return (n + 3) & ~3; }
+
 // o[0..N) = src[0..N) with 16-byte shared-memory loads (src 16-byte aligned)
 template <typename real, int N>
 __device__ __forceinline__ void load_cell(const real* src, real (&o)[N]) {
@@ -623,26 +640,34 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
         // overlap the right-hand side below (for 8-byte values the longer
         // arithmetic hides them and the registers are better spent elsewhere)
         constexpr bool kHoist = sizeof(real) == 4;
-        const real* Ai = a.ainv + ((size_t)cls * a.n_dir_class + dcls) * (N * N);
+        constexpr int NP = pad4(N), FDP = pad4(FD);  // padded row strides of the tables
+        const real* Ai = a.ainv + ((size_t)cls * a.n_dir_class + dcls) * (N * NP);
         real arow[kHoist ? NR : 1][kHoist ? N : 1];
         if constexpr (kHoist) {
 #pragma unroll
           for (int k = 0; k < NR; ++k) {
             const int i = k * H + half;
+            if (H == 1 || i < N) {
+              load_row<real, N>(Ai + i * NP, arow[k]);
+            } else {
 #pragma unroll
-            for (int j = 0; j < N; ++j) arow[k][j] = (H == 1 || i < N) ? A::ldg(Ai + i * N + j) : real(0);
+              for (int j = 0; j < N; ++j) arow[k][j] = real(0);
+            }
           }
         }
         // inflow faces: b_face += |Omega_a| F_a psi_up
-        const real* FX = a.face_mass + 0 * FD * FD;
-        const real* FS = a.face_mass + AS * FD * FD;
+        const real* FX = a.face_mass + 0 * FD * FDP;
+        const real* FS = a.face_mass + AS * FD * FDP;
 #pragma unroll
         for (int t = 0; t < FD; ++t) {
           typename A::acc accx = A::zero(), accs = A::zero();
+          real fx[FD], fs[FD];
+          load_row<real, FD>(FX + t * FDP, fx);
+          load_row<real, FD>(FS + t * FDP, fs);
 #pragma unroll
           for (int u = 0; u < FD; ++u) {
-            A::fma(accx, A::ldg(FX + t * FD + u), upX[u]);
-            A::fma(accs, A::ldg(FS + t * FD + u), upS[u]);
+            A::fma(accx, fx[u], upX[u]);
+            A::fma(accs, fs[u], upS[u]);
           }
           // one after the other: the two inflow faces share the corner dof
           typename A::acc bx = A::from(b[C::x_in(t)]);
@@ -653,12 +678,14 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
           b[C::s_in(t)] = A::get(bs);
         }
         if (DIM == 3) {
-          const real* FY = a.face_mass + 1 * FD * FD;
+          const real* FY = a.face_mass + 1 * FD * FDP;
 #pragma unroll
           for (int t = 0; t < FD; ++t) {
             typename A::acc acc = A::zero();
+            real fy[FD];
+            load_row<real, FD>(FY + t * FDP, fy);
 #pragma unroll
-            for (int u = 0; u < FD; ++u) A::fma(acc, A::ldg(FY + t * FD + u), upY[u]);
+            for (int u = 0; u < FD; ++u) A::fma(acc, fy[u], upY[u]);
             typename A::acc by = A::from(b[C::y_in(t)]);
             A::fma(by, wY, A::get(acc));
             b[C::y_in(t)] = A::get(by);
@@ -670,12 +697,14 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
           const int i = k * H + half;
           typename A::acc acc = A::zero();
           if (H == 1 || i < N) {
+            if constexpr (kHoist) {
 #pragma unroll
-            for (int j = 0; j < N; ++j) {
-              if constexpr (kHoist)
-                A::fma(acc, arow[k][j], b[j]);
-              else
-                A::fma(acc, A::ldg(Ai + i * N + j), b[j]);
+              for (int j = 0; j < N; ++j) A::fma(acc, arow[k][j], b[j]);
+            } else {
+              real row[N];
+              load_row<real, N>(Ai + i * NP, row);
+#pragma unroll
+              for (int j = 0; j < N; ++j) A::fma(acc, row[j], b[j]);
             }
           }
           xr[k] = A::get(acc);
