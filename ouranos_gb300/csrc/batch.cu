@@ -539,7 +539,6 @@ struct Solve {
   DevBuf mem;
   double *B = nullptr, *Xs = nullptr, *dres = nullptr, *partial = nullptr, *ycoef = nullptr;
   double** dptrs = nullptr;
-  unsigned* done = nullptr;
   std::vector<double*> V;
   double* hb = nullptr;  // pinned: [0,32) pass 1, [32,64) pass 2, [64] |w|^2, [65] |r|^2, [66,98) y
   Givens gv{1};
@@ -563,8 +562,6 @@ int solve_setup(ouranos_batch* b, Solve& S, long len, int m) {
   S.dres = (double*)p;
   S.partial = S.dres + 64;
   S.ycoef = S.partial + 64 * (size_t)kDotGrid;
-  S.done = (unsigned*)(S.ycoef + 64);
-  BC(cudaMemsetAsync(S.done, 0, sizeof(unsigned), b->stream), "solver workspace");
   BC(cudaMemcpyAsync(S.dptrs, S.V.data(), sizeof(double*) * (m + 1), cudaMemcpyHostToDevice, b->stream),
      "solver workspace");
   BC(cudaMemsetAsync(S.Xs, 0, vb, b->stream), "solver workspace");
@@ -574,7 +571,7 @@ int solve_setup(ouranos_batch* b, Solve& S, long len, int m) {
 
 // |v|^2 of S.V[j] into dres[0] and host slot hb[slot]; then v /= |v| on the device
 int norm_and_scale(ouranos_batch* b, Solve& S, int j, int slot) {
-  BC(launch_dots((const double* const*)(S.dptrs + j), S.V[j], 1, S.len, S.dres, S.partial, S.done, b->stream),
+  BC(launch_dots((const double* const*)(S.dptrs + j), S.V[j], 1, S.len, S.dres, S.partial, b->stream),
      "norm");
   BC(cudaMemcpyAsync(S.hb + slot, S.dres, sizeof(double), cudaMemcpyDeviceToHost, b->stream), "norm");
   BC(launch_scale_inv_norm(S.dres, S.V[j], S.len, b->stream), "normalise");
@@ -585,7 +582,7 @@ int norm_and_scale(ouranos_batch* b, Solve& S, int j, int slot) {
 int gram_schmidt(ouranos_batch* b, Solve& S) {
   const int n = S.k + 1;
   for (int pass = 0; pass < 2; ++pass) {
-    BC(launch_dots((const double* const*)S.dptrs, S.V[S.k + 1], n, S.len, S.dres, S.partial, S.done, b->stream),
+    BC(launch_dots((const double* const*)S.dptrs, S.V[S.k + 1], n, S.len, S.dres, S.partial, b->stream),
        "orthogonalise");
     BC(cudaMemcpyAsync(S.hb + 32 * pass, S.dres, sizeof(double) * n, cudaMemcpyDeviceToHost, b->stream),
        "orthogonalise");

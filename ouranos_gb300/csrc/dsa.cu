@@ -557,7 +557,6 @@ int rt_dsa_apply(ouranos_rt* rt, const double* v, double* out) {
   if (rc) return rc;
   return rt->dim == 3 ? dsa_run<3>(rt, v, out, rt->dsa_iters) : dsa_run<2>(rt, v, out, rt->dsa_iters);
 }
-int rt_dsa_kernels(const ouranos_rt* rt) { return rt->dsa_iters > 0 ? 1 : 0; }
 }  // namespace ouranos
 
 extern "C" {

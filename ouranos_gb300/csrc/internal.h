@@ -195,8 +195,11 @@ cudaError_t launch_angular_source(real* q, const float* psi, const double* cell_
                                   int n, long n_cells, int n_dir, cudaStream_t s);
 cudaError_t launch_scale_inv_norm(const double* nrm2, double* v, long len, cudaStream_t s);
 constexpr int kDotGrid = 1216;  // blocks of the dot-product kernel (8 per SM: enough loads in flight)
+// out[j] = xs[j] . y for j < k (k <= 32), FP64: per-block partials in chunks
+// of 8 vectors into partial[k * kDotGrid], then one warp per output sums them
+// in a fixed order (deterministic, no atomics)
 cudaError_t launch_dots(const double* const* xs, const double* y, int k, long len, double* out,
-                        double* partial, unsigned int* done, cudaStream_t s);
+                        double* partial, cudaStream_t s);
 
 }  // namespace ouranos
 namespace ouranos {
@@ -245,7 +248,6 @@ int rt_pc_features(ouranos_rt* rt, const double* v, float* feat);
 int rt_pc_correct(ouranos_rt* rt, const double* v, const float* y, double* z);
 // diffusion synthetic acceleration (dsa.cu): out = v + f on the handle's stream
 int rt_dsa_apply(ouranos_rt* rt, const double* v, double* out);
-int rt_dsa_kernels(const ouranos_rt* rt);  // launches of one rt_dsa_apply
 // the network's cell grid
 void cnn_grid(const ouranos_cnn* net, int* nx, int* ny, int* nz);
 // Device-side pieces the solvers use (operator.cu).

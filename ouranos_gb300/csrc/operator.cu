@@ -216,7 +216,7 @@ int build_schedule(ouranos_rt* rt) {
   OK_OR_RETURN(upload(rt, rt->d_tasks, tasks, "tasks"));
   OK_OR_RETURN(upload(rt, rt->d_group_dirs, gdirs, "group dirs"));
   OK_OR_RETURN(upload(rt, rt->d_group_flip, gflip, "group flips"));
-  // control block: [0] ticket, [1] status, [2..] dot counter, [64..] progress
+  // control block: [0] ticket, [1] status (the rest is spare)
   CU(rt->d_ctrl.alloc(sizeof(int) * (64 + (size_t)n_groups * tiles)), "control block");
   CU(cudaMemsetAsync(rt->d_ctrl.p, 0, rt->d_ctrl.bytes, rt->stream), "control block");
   const size_t ex = (size_t)rt->n_dir * tiles * NS * rt->wy * rt->fd;
@@ -443,9 +443,9 @@ int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd,
   a.ticket = ctrl;
   a.status = ctrl + 1;
   // ticket -> 0.  The status word [1] is sticky: it is cleared at the start of
-  // each C-ABI call (clear_status), so a timeout inside a solve is seen at its
-  // end and every later sweep of that call exits at once.  The dot counter at
-  // [2] is 0 whenever no dot kernel is in flight on this stream.
+  // each C-ABI call (clear_status), so a timeout inside a solve (a sweep's
+  // dependency wait, bit 1; a diffusion-solve barrier, bit 2) is seen at its
+  // end and every later sweep of that call exits at once.
   CU(cudaMemsetAsync(ctrl, 0, sizeof(int), rt->stream), "reset sweep control");
   int sms = 0;
   CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, rt->device), "device query");

@@ -43,7 +43,6 @@ struct Work {
   double** dptrs = nullptr;   // device array of vector pointers (scratch, 64)
   double** vptrs = nullptr;   // device array of every basis vector's pointer (64)
   double* dres = nullptr;     // device results (64) + partials
-  unsigned* done = nullptr;
   std::vector<double*> vec;   // host copy of vector pointers
   double* v(int i) const { return vec[i]; }
 };
@@ -66,7 +65,6 @@ int make_work(ouranos_rt* rt, int nvec, Work& w) {
   w.vptrs = w.dptrs + 64;
   p += ptr_bytes;
   w.dres = (double*)p;
-  w.done = (unsigned*)(rt->d_ctrl.as<int>() + 2);
   return OURANOS_OK;
 }
 
@@ -74,7 +72,7 @@ int dot_pair(Work& w, const double* a, const double* b, double* out) {
   ouranos_rt* rt = w.rt;
   const double* ptrs[1] = {a};
   CUC(cudaMemcpyAsync(w.dptrs, ptrs, sizeof(double*), cudaMemcpyHostToDevice, rt->stream), "dot");
-  CUC(launch_dots((const double* const*)w.dptrs, b, 1, w.len, w.dres, w.dres + 64, w.done,
+  CUC(launch_dots((const double* const*)w.dptrs, b, 1, w.len, w.dres, w.dres + 64,
                   rt->stream),
       "dot");
   CUC(cudaMemcpyAsync(out, w.dres, sizeof(double), cudaMemcpyDeviceToHost, rt->stream), "dot");
@@ -196,7 +194,7 @@ int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double
       // CGS2 with the coefficients kept on the device, the norm and the
       // normalisation too: one host synchronisation per iteration
       for (int pass = 0; pass < 2; ++pass) {
-        CUC(launch_dots((const double* const*)w.vptrs, nxt, k + 1, w.len, w.dres, w.dres + 64, w.done,
+        CUC(launch_dots((const double* const*)w.vptrs, nxt, k + 1, w.len, w.dres, w.dres + 64,
                         rt->stream),
             "orthogonalise");
         CUC(cudaMemcpyAsync(hb.p + 32 * pass, w.dres, sizeof(double) * (k + 1), cudaMemcpyDeviceToHost,
@@ -205,7 +203,7 @@ int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double
         CUC(launch_multi_axpy((const double* const*)w.vptrs, k + 1, w.dres, -1.0, nxt, w.len, rt->stream),
             "orthogonalise");
       }
-      CUC(launch_dots((const double* const*)(w.vptrs + k + 1), nxt, 1, w.len, w.dres, w.dres + 64, w.done,
+      CUC(launch_dots((const double* const*)(w.vptrs + k + 1), nxt, 1, w.len, w.dres, w.dres + 64,
                       rt->stream),
           "norm");
       CUC(cudaMemcpyAsync(hb.p + 64, w.dres, sizeof(double), cudaMemcpyDeviceToHost, rt->stream), "norm");

@@ -791,8 +791,7 @@ cudaError_t launch_axpby(double a, const double* x, double b, double* y, long le
 // xs: device array of k (<= 32) device pointers; out: k doubles; partial:
 // k * kDotGrid doubles.  (`done` is not used by this two-launch form.)
 cudaError_t launch_dots(const double* const* xs, const double* y, int k, long len, double* out,
-                        double* partial, unsigned int* done, cudaStream_t s) {
-  (void)done;
+                        double* partial, cudaStream_t s) {
   if (k < 1 || k > 32) return cudaErrorInvalidValue;
   dots_partial_kernel<<<kDotGrid, kBlock, 0, s>>>(xs, y, k, len, partial);
   dots_final_kernel<<<1, kBlock, 0, s>>>(partial, k, kDotGrid, out);
