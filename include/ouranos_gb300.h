@@ -237,6 +237,26 @@ typedef struct ouranos_solve_info {
 int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it, double tol,
                   const double* group_flux, double* x, double* hist, ouranos_solve_info* info);
 
+/* Multigroup outer iteration (src/ouranos.cc:62-128 for SI, 141-207 for the
+ * Krylov solvers): Gauss-Seidel over the groups -- each outer iteration
+ * solves every group g in turn, (I - T_g) phi_g = rhs_g(phi of the other
+ * groups), with `solver` (flags allowed; warm-started from the group's last
+ * flux except with BiCGSTAB) to inner_tol within max_inner_it, until the
+ * relative L2 change of all group fluxes falls below outer_tol (the
+ * reference's sqrt(num/denom) test) or max_outer_it iterations have run.
+ * group_flux: [n_groups][n_mom][n_dofs], host or device; in: initial fluxes,
+ * out: the solution.  Leaves the handle on the last group. */
+typedef struct ouranos_multigroup_info {
+  int outer_iterations;
+  int inner_iterations;     /* operator applications summed over all group solves */
+  double change;            /* last relative change of the group fluxes */
+  double seconds;
+  int converged;
+} ouranos_multigroup_info;
+int ouranos_solve_multigroup(ouranos_rt* rt, int solver, int restart, int max_inner_it, double inner_tol,
+                             int max_outer_it, double outer_tol, double* group_flux,
+                             ouranos_multigroup_info* info);
+
 /* ------------------------------------------------------- time dependence
  * Implicit Euler in time.  No counterpart in the reference operator (its
  * TimeDiscretization class, src/TimeDiscretization.cc:10-82, is never

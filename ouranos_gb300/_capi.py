@@ -46,7 +46,7 @@ EXPORTS = [
     "ouranos_batch_stats", "ouranos_batch_last_error",
     "ouranos_rt_set_time_step", "ouranos_rt_set_source", "ouranos_rt_time_advance",
     "ouranos_rt_get_angular_flux", "ouranos_rt_set_angular_flux",
-    "ouranos_rt_set_dsa", "ouranos_rt_dsa_apply",
+    "ouranos_rt_set_dsa", "ouranos_rt_dsa_apply", "ouranos_solve_multigroup",
 ]
 
 
@@ -67,6 +67,11 @@ class ProblemDesc(C.Structure):
 
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", C.c_int), ("restarts", C.c_int), ("residual", C.c_double),
+                ("seconds", C.c_double), ("converged", C.c_int)]
+
+
+class MultigroupInfo(C.Structure):
+    _fields_ = [("outer_iterations", C.c_int), ("inner_iterations", C.c_int), ("change", C.c_double),
                 ("seconds", C.c_double), ("converged", C.c_int)]
 
 
@@ -131,6 +136,7 @@ def lib():
         "ouranos_rt_set_angular_flux": [vp, vp],
         "ouranos_rt_set_dsa": [vp, i],
         "ouranos_rt_dsa_apply": [vp, vp, vp],
+        "ouranos_solve_multigroup": [vp, i, i, i, d, i, d, vp, C.POINTER(MultigroupInfo)],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

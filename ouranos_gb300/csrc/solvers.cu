@@ -372,12 +372,12 @@ int source_iteration(ouranos_rt* rt, int max_it, double tol, const double* gf, c
   return OURANOS_OK;
 }
 
-}  // namespace
 
-extern "C" int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it, double tol,
-                             const double* group_flux, double* x, double* hist,
-                             ouranos_solve_info* info) {
-  if (!rt || !x || max_it < 1 || !(tol > 0)) return OURANOS_ERR_BAD_INPUT;
+// One group's solve on device vectors in the handle's numbering: dgf (may be
+// NULL) the group fluxes of the other groups, sol the initial guess (with
+// OURANOS_SOLVER_WARM_START) and the solution.  Flags as in ouranos_solve.
+int solve_device(ouranos_rt* rt, int solver, int restart, int max_it, double tol, const double* dgf, double* sol,
+                 double* hist, ouranos_solve_info* info) {
   const bool warm = (solver & OURANOS_SOLVER_WARM_START) != 0;
   const bool dsa = (solver & OURANOS_SOLVER_DSA) != 0;
   solver &= ~(OURANOS_SOLVER_WARM_START | OURANOS_SOLVER_DSA);
@@ -390,41 +390,30 @@ extern "C" int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it
     rt->err = "BiCGSTAB starts from zero";
     return OURANOS_ERR_UNSUPPORTED;
   }
-  ouranos_solve_info local;
-  if (!info) info = &local;
   std::memset(info, 0, sizeof *info);
-  cudaSetDevice(rt->device);
-  RC(rt_clear_status(rt));
-  const auto t0 = std::chrono::steady_clock::now();
-  const double* dgf = nullptr;
-  if (group_flux) RC(rt_stage_in(rt, group_flux, rt->d_gf, rt->G, &dgf));
-  // rhs and solution live in the handle's staging buffers while the solver
-  // workspace holds the Krylov vectors
+  // rhs and solution live in their own buffers while the solver workspace
+  // holds the Krylov vectors
   const long len = (long)rt->n_mom * rt->n_dofs;
-  DevBuf rhs, sol;
+  DevBuf rhs, x;
   CUC(rhs.alloc(sizeof(double) * len), "rhs");
-  CUC(sol.alloc(sizeof(double) * len), "solution");
+  CUC(x.alloc(sizeof(double) * len), "solution");
   RC(rt_rhs_device(rt, dgf, rhs.as<double>()));
-  if (warm) {
-    const double* dx = nullptr;
-    RC(rt_stage_in(rt, x, rt->d_x, 1, &dx));
-    CUC(cudaMemcpyAsync(sol.p, dx, sizeof(double) * len, cudaMemcpyDeviceToDevice, rt->stream), "guess");
-  }
+  if (warm) CUC(cudaMemcpyAsync(x.p, sol, sizeof(double) * len, cudaMemcpyDeviceToDevice, rt->stream), "guess");
   const int saved = rt->precision;
   int rc;
   switch (solver) {
     case OURANOS_SOLVER_SI:
-      rc = source_iteration(rt, max_it, tol, dgf, rhs.as<double>(), sol.as<double>(), hist, info, warm, dsa);
+      rc = source_iteration(rt, max_it, tol, dgf, rhs.as<double>(), x.as<double>(), hist, info, warm, dsa);
       break;
     case OURANOS_SOLVER_GMRES:
-      rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info,
+      rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), x.as<double>(), hist, info,
                  OURANOS_FP64, 0.0, false, warm, dsa);
       break;
     case OURANOS_SOLVER_BICGSTAB:
-      rc = bicgstab(rt, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info);
+      rc = bicgstab(rt, max_it, tol, rhs.as<double>(), x.as<double>(), hist, info);
       break;
     case OURANOS_SOLVER_FGMRES_MIXED:
-      rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info,
+      rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), x.as<double>(), hist, info,
                  OURANOS_FP32, 1e-5, false, warm, dsa);
       break;
     case OURANOS_SOLVER_FGMRES_LEARNED:
@@ -433,7 +422,7 @@ extern "C" int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it
         rc = OURANOS_ERR_BAD_INPUT;
         break;
       }
-      rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), sol.as<double>(), hist, info,
+      rc = gmres(rt, restart, max_it, tol, rhs.as<double>(), x.as<double>(), hist, info,
                  OURANOS_FP32, 1e-5, true, warm, dsa);
       break;
     default:
@@ -442,8 +431,104 @@ extern "C" int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it
   }
   rt->precision = saved;
   if (rc) return rc;
+  CUC(cudaMemcpyAsync(sol, x.p, sizeof(double) * len, cudaMemcpyDeviceToDevice, rt->stream), "solution");
+  return OURANOS_OK;
+}
+
+}  // namespace
+
+extern "C" int ouranos_solve(ouranos_rt* rt, int solver, int restart, int max_it, double tol,
+                             const double* group_flux, double* x, double* hist,
+                             ouranos_solve_info* info) {
+  if (!rt || !x || max_it < 1 || !(tol > 0)) return OURANOS_ERR_BAD_INPUT;
+  ouranos_solve_info local;
+  if (!info) info = &local;
+  std::memset(info, 0, sizeof *info);
+  cudaSetDevice(rt->device);
+  RC(rt_clear_status(rt));
+  const auto t0 = std::chrono::steady_clock::now();
+  const double* dgf = nullptr;
+  if (group_flux) RC(rt_stage_in(rt, group_flux, rt->d_gf, rt->G, &dgf));
+  const long len = (long)rt->n_mom * rt->n_dofs;
+  DevBuf sol;
+  CUC(sol.alloc(sizeof(double) * len), "solution");
+  if (solver & OURANOS_SOLVER_WARM_START) {
+    const double* dx = nullptr;
+    RC(rt_stage_in(rt, x, rt->d_x, 1, &dx));
+    CUC(cudaMemcpyAsync(sol.p, dx, sizeof(double) * len, cudaMemcpyDeviceToDevice, rt->stream), "guess");
+  }
+  RC(solve_device(rt, solver, restart, max_it, tol, dgf, sol.as<double>(), hist, info));
   RC(rt_stage_out(rt, sol.as<double>(), x));
   CUC(cudaStreamSynchronize(rt->stream), "solve");
+  info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return info->converged ? OURANOS_OK : OURANOS_ERR_NOT_CONVERGED;
+}
+
+// Gauss-Seidel over the groups (src/ouranos.cc:62-128, 141-207): each outer
+// iteration solves every group in turn against the latest fluxes of the
+// others, warm-started from its own last flux (BiCGSTAB from zero), and
+// stops once the relative L2 change of all group fluxes is below outer_tol.
+extern "C" int ouranos_solve_multigroup(ouranos_rt* rt, int solver, int restart, int max_inner_it,
+                                        double inner_tol, int max_outer_it, double outer_tol,
+                                        double* group_flux, ouranos_multigroup_info* info) {
+  if (!rt || !group_flux || max_inner_it < 1 || max_outer_it < 1 || !(inner_tol > 0) || !(outer_tol > 0))
+    return OURANOS_ERR_BAD_INPUT;
+  ouranos_multigroup_info local;
+  if (!info) info = &local;
+  std::memset(info, 0, sizeof *info);
+  cudaSetDevice(rt->device);
+  RC(rt_clear_status(rt));
+  const auto t0 = std::chrono::steady_clock::now();
+  const int G = rt->G;
+  const long len = (long)rt->n_mom * rt->n_dofs;
+  const long all = (long)G * len;
+  DevBuf cur, old, red;
+  CUC(cur.alloc(sizeof(double) * all), "group fluxes");
+  CUC(old.alloc(sizeof(double) * all), "group fluxes");
+  CUC(red.alloc(sizeof(double) * (64 + 64 * (size_t)kDotGrid) + sizeof(double*) * 2), "reductions");
+  {
+    const double* in = nullptr;
+    RC(rt_stage_in(rt, group_flux, cur, G, &in));
+    if (in != cur.as<double>())
+      CUC(cudaMemcpyAsync(cur.p, in, sizeof(double) * all, cudaMemcpyDeviceToDevice, rt->stream), "group fluxes");
+  }
+  const int kind = solver & ~OURANOS_SOLVER_WARM_START;
+  const int inner = (kind & ~OURANOS_SOLVER_DSA) == OURANOS_SOLVER_BICGSTAB ? kind : kind | OURANOS_SOLVER_WARM_START;
+  double* d_out = red.as<double>();
+  double* partial = d_out + 64;
+  const double** ptrs = reinterpret_cast<const double**>(partial + 64 * (size_t)kDotGrid);
+  const double* host_ptrs[2] = {old.as<double>(), cur.as<double>()};
+  CUC(cudaMemcpyAsync(ptrs, host_ptrs, sizeof host_ptrs, cudaMemcpyHostToDevice, rt->stream), "reductions");
+  double change = 0.0;
+  for (int out = 0; out < max_outer_it; ++out) {
+    CUC(cudaMemcpyAsync(old.p, cur.p, sizeof(double) * all, cudaMemcpyDeviceToDevice, rt->stream), "group fluxes");
+    for (int g = 0; g < G; ++g) {
+      RC(ouranos_rt_set_group(rt, g));
+      ouranos_solve_info gi;
+      const int rc = solve_device(rt, inner, restart, max_inner_it, inner_tol, cur.as<double>(),
+                                  cur.as<double>() + (size_t)g * len, nullptr, &gi);
+      if (rc && rc != OURANOS_ERR_NOT_CONVERGED) return rc;
+      info->inner_iterations += gi.iterations;
+    }
+    // change = |cur - old| / |cur| over all groups
+    CUC(launch_axpby(1.0, cur.as<double>(), -1.0, old.as<double>(), all, rt->stream), "change");
+    CUC(launch_dots(ptrs, old.as<double>(), 1, all, d_out, partial, rt->stream), "change");
+    CUC(launch_dots(ptrs + 1, cur.as<double>(), 1, all, d_out + 1, partial, rt->stream), "change");
+    double h[2] = {0.0, 0.0};
+    CUC(cudaMemcpyAsync(h, d_out, sizeof h, cudaMemcpyDeviceToHost, rt->stream), "change");
+    CUC(cudaStreamSynchronize(rt->stream), "change");
+    change = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : std::sqrt(h[0]);
+    info->outer_iterations = out + 1;
+    info->change = change;
+    if (change < outer_tol) {
+      info->converged = 1;
+      break;
+    }
+  }
+  for (int g = 0; g < G; ++g)
+    RC(rt_stage_out(rt, cur.as<double>() + (size_t)g * len, group_flux + (size_t)g * len));
+  CUC(cudaStreamSynchronize(rt->stream), "multigroup");
+  RC(rt_check_status(rt));
   info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   return info->converged ? OURANOS_OK : OURANOS_ERR_NOT_CONVERGED;
 }

@@ -219,6 +219,27 @@ class RadiativeTransfer:
         self._check(_capi.lib().ouranos_rt_dsa_apply(self._h, _ptr(v), _ptr(out)))
         return out
 
+    def solve_multigroup(self, method="gmres", inner_tol=1e-8, max_inner_it=1000, outer_tol=1e-8,
+                         max_outer_it=100, restart=30, group_flux=None, dsa=False):
+        """Gauss-Seidel outer iteration over the groups (src/ouranos.cc:62-207):
+        returns (group_flux [n_groups * length], info dict); group_flux (host
+        or device, [group][mom][dof]) is the initial guess and is updated in
+        place."""
+        kind = {"si": _capi.SOLVER_SI, "gmres": _capi.SOLVER_GMRES,
+                "bicgstab": _capi.SOLVER_BICGSTAB, "fgmres_mixed": _capi.SOLVER_FGMRES_MIXED,
+                "fgmres_learned": _capi.SOLVER_FGMRES_LEARNED}[method]
+        if dsa:
+            kind |= _capi.SOLVER_DSA
+        if group_flux is None:
+            group_flux = np.zeros(self.problem.n_groups * self.length)
+        info = _capi.MultigroupInfo()
+        rc = _capi.lib().ouranos_solve_multigroup(self._h, kind, restart, max_inner_it, inner_tol, max_outer_it,
+                                                  outer_tol, _ptr(group_flux), C.byref(info))
+        if rc not in (_capi.OK, _capi.ERR_NOT_CONVERGED):
+            self._check(rc)
+        return group_flux, dict(outer_iterations=info.outer_iterations, inner_iterations=info.inner_iterations,
+                                change=info.change, seconds=info.seconds, converged=bool(info.converged))
+
     def solve(self, method="gmres", tol=1e-8, max_it=1000, restart=30, group_flux=None, x=None,
               warm=False, dsa=False):
         """Drivers of src/ouranos.cc:43-209. Returns (x, info dict, residual history);

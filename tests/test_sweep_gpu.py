@@ -325,3 +325,56 @@ def test_fp64_contraction_modes_match_oracle(mode):
             r = rt.rhs()
         assert rel_err(y, ref) < TOL64, prob.name
         assert rel_err(r, ref_rhs) < TOL64, prob.name
+
+
+def _three_group_problem(og, dim):
+    """Three groups with down- and up-scatter (P1), sources, inflow and
+    reflective sides."""
+    if dim == 2:
+        q = og.build_quadrature("LS", 4, 1, dim=2)
+        n, lo, hi, bc = (6, 7), (0, 0), (1.2, 1.4), (1, 3, 0, 2, 0, 0)
+    else:
+        q = og.build_quadrature("LS", 4, 1, dim=3)
+        n, lo, hi, bc = (4, 3, 5), (0, 0, 0), (1.0, 0.8, 1.2), (1, 0, 3, 0, 2, 0)
+    G = 3
+    nc = int(np.prod(n))
+    rng = np.random.default_rng(29)
+    st = rng.uniform(1.0, 5.0, (2, G))
+    ss = np.zeros((2, G, G, 2))
+    for m in range(2):
+        for gf in range(G):
+            for gt in range(G):
+                ss[m, gf, gt, 0] = rng.uniform(0.05, 0.25) * st[m, gt]
+            ss[m, gf, gf, 0] = rng.uniform(0.3, 0.6) * st[m, gf]
+            ss[m, gf, gf, 1] = 0.3 * ss[m, gf, gf, 0]
+    mat = rng.integers(0, 2, nc).astype(np.int32)
+    sid = rng.integers(0, 2, nc).astype(np.int32)
+    src = rng.uniform(0.0, 2.0, (2, G))
+    inc = rng.uniform(0.5, 1.5, (2 * dim, G))
+    return og.Problem(dim, 1, n, lo, hi, q, st, ss, mat, sid, src, bc, inc)
+
+
+@pytest.mark.parametrize("dim,method,dsa", [(2, "gmres", False), (2, "si", False), (3, "bicgstab", False),
+                                            (2, "fgmres_mixed", True), (3, "gmres", True)])
+def test_multigroup_outer_iteration_matches_oracle(dim, method, dsa):
+    """Gauss-Seidel over the groups (src/ouranos.cc:62-207) against the same
+    outer loop driven through the oracle's single-group solves."""
+    import ouranos_gb300 as og
+    prob = _three_group_problem(og, dim)
+    O = po.OracleProblem(prob.arrays())
+    G, L = prob.n_groups, O.length
+    ref = np.zeros(G * L)
+    for _ in range(200):
+        old = ref.copy()
+        for g in range(G):
+            O.set_group(g)
+            ref[g * L:(g + 1) * L] = O.solve("gmres", tol=1e-13, max_it=800, group_flux=ref)[0]
+        if np.linalg.norm(ref - old) < 1e-12 * np.linalg.norm(ref):
+            break
+    with og.RadiativeTransfer(prob) as rt:
+        if dsa:
+            rt.set_dsa(10)
+        gf, info = rt.solve_multigroup(method, inner_tol=1e-12, outer_tol=1e-11, max_outer_it=200, dsa=dsa)
+    assert info["converged"] and info["outer_iterations"] > 1
+    tol = 1e-6 if method == "fgmres_mixed" else 1e-8
+    assert rel_err(gf, ref) < tol
