@@ -138,6 +138,33 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def faithful_scheduler_fit(target_tasks):
+    """The reference's own task scheduler (src/RadiativeTransfer.cc:605-692:
+    every get_next_task/send_angular_flux scans the task list, O(T^2) per
+    sweep), restated in the oracle, timed single-threaded on small 2-D Q1 LS
+    S8 meshes; the power law t = a T^k fitted to them is reported with the
+    time it predicts for `target_tasks` -- a fitted figure, not a
+    measurement."""
+    import numpy as np
+    import ouranos_gb300 as og
+    from oracle import pyoracle
+    pts = []
+    for n in (8, 12, 16, 24):
+        p = og.config_small(n=n, sn=8)
+        O = pyoracle.OracleProblem(p.arrays())
+        O.scattering_source(np.random.default_rng(n).standard_normal(O.length))
+        t0 = time.perf_counter()
+        O.sweep(scheduler=1, threads=1)
+        pts.append((n * n * p.quad.n_dir, time.perf_counter() - t0))
+    T = np.log([t for t, _ in pts])
+    S = np.log([s for _, s in pts])
+    k, loga = np.polyfit(T, S, 1)
+    return {"tasks": [int(t) for t, _ in pts], "seconds": [round(s, 4) for _, s in pts],
+            "fit": "t = a T^k", "k": round(float(k), 3),
+            "predicted_seconds_per_sweep_of_this_workload": float(np.exp(loga) * target_tasks ** k),
+            "note": "fitted to the small meshes, not measured at this size"}
+
+
 def cpu_reference_rate(prob, threads, reps=1):
     """The reference's sweep restated on the CPU (oracle/), all threads."""
     import numpy as np
@@ -285,7 +312,8 @@ def run_ours(args):
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": "%d full sweep(s) of the workload (%.1f s of CPU work) with the oracle/ C++ "
                          "restatement of the reference sweep, directions split over threads"
-                         % (len(times), sum(times))}
+                         % (len(times), sum(times)),
+               "faithful_scheduler": faithful_scheduler_fit(solves)}
     tts = None
     if rank == 0 and world == 1 and not args.no_solve:
         tts = time_to_solution(args.solve_seed, args.solve_n, args.tol, args.dsa_cg, args.max_it)
