@@ -165,6 +165,17 @@ def faithful_scheduler_fit(target_tasks):
             "note": "fitted to the small meshes, not measured at this size"}
 
 
+def single_core_rate():
+    """The linear-scheduler port on one core: one Apply of the bench
+    workload's physics on a 64 x 64 mesh (590 k solves) -- the per-solve
+    rate, whose mesh dependence is only the scheduler's linear bookkeeping."""
+    import ouranos_gb300 as og
+    p = og.heterogeneous_2d(seed=1001, n=64, fe_order=2, sn=16, l_max=3, blocks=8)
+    rate, times = cpu_reference_rate(p, 1, reps=1)
+    return {"value": rate, "unit": UNIT, "cores": 1,
+            "sample": "one Apply of the same physics on 64 x 64 cells (%.2f s)" % times[0]}
+
+
 def cpu_reference_rate(prob, threads, reps=1):
     """The reference's sweep restated on the CPU (oracle/), all threads."""
     import numpy as np
@@ -313,7 +324,8 @@ def run_ours(args):
                "sample": "%d full sweep(s) of the workload (%.1f s of CPU work) with the oracle/ C++ "
                          "restatement of the reference sweep, directions split over threads"
                          % (len(times), sum(times)),
-               "faithful_scheduler": faithful_scheduler_fit(solves)}
+               "faithful_scheduler": faithful_scheduler_fit(solves),
+               "single_core": single_core_rate()}
     tts = None
     if rank == 0 and world == 1 and not args.no_solve:
         tts = time_to_solution(args.solve_seed, args.solve_n, args.tol, args.dsa_cg, args.max_it)
