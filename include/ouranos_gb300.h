@@ -351,14 +351,16 @@ int ouranos_rt_pc_apply(ouranos_rt* rt, const double* v, double* z);
 
 /* ------------------------------------- diffusion synthetic acceleration
  * No counterpart in the reference (identity preconditioner, plain source
- * iteration: src/ouranos.cc:72-95,160-171).  For a DG Q1 mesh (2-D or 3-D):
+ * iteration: src/ouranos.cc:72-95,160-171).  For a DG Q_p mesh (2-D or 3-D):
  *   P v = v + f,  (-div D grad + sigma_a) f = sigma_s0 v_0,
  * f continuous Q1 on the mesh vertices (Marshak condition on vacuum and inflow
  * boundaries, zero current on reflective ones), D = 1/(3(sigma_t' - sigma_s1)),
- * sigma_a = sigma_t' - sigma_s0, sigma_t' = sigma_t + 1/(v dt); f is added to
- * the scalar moment's nodal values.  The diffusion system is solved by
- * cg_iterations steps of Jacobi-preconditioned CG (FP32, FP64 scalars);
- * 0 switches the acceleration off.  UNSUPPORTED unless the mesh is DG Q1. */
+ * sigma_a = sigma_t' - sigma_s0, sigma_t' = sigma_t + 1/(v dt); v_0 enters
+ * through the mixed mass matrix of the vertex hat functions and the Q_p basis,
+ * and f, interpolated at the Q_p nodes, is added to the scalar moment's nodal
+ * values.  The diffusion system is solved by cg_iterations steps of
+ * Jacobi-preconditioned CG (FP32, FP64 scalars); 0 switches the acceleration
+ * off. */
 int ouranos_rt_set_dsa(ouranos_rt* rt, int cg_iterations);
 /* z = P v ([mom][dof], host or device; z may equal v) */
 int ouranos_rt_dsa_apply(ouranos_rt* rt, const double* v, double* z);

@@ -11,12 +11,16 @@ with f continuous Q1 on the mesh vertices (Galerkin, exact element
 integrals), the Marshak term (1/2) integral f w on the faces of vacuum and
 inflow boundaries and none on reflective ones, D = 1/(3 (sigma_t' -
 sigma_s1)), sigma_a = sigma_t' - sigma_s0, sigma_t' = sigma_t + 1/(v dt), and
-f added to the scalar moment's nodal values.  `apply` solves the diffusion
+f (interpolated at the cell's DG Q_p nodes) added to the scalar moment's
+nodal values; for Q_p cells the right-hand side takes the residual through
+the mixed mass matrix of the vertex hat functions and the Q_p basis.  `apply`
+solves the diffusion
 system by k steps of Jacobi-preconditioned conjugate gradients (k = None: a
 direct solve), in FP64.
 
-Layout conventions: cells lexicographic (x fastest), DG Q1 nodes of a cell at
-its corners, local index a + 2 b (+ 4 c) for the corner offsets (a, b, c);
+Layout conventions: cells lexicographic (x fastest), DG Q_p nodes of a cell
+on the equidistant points j/p, x fastest; corner index a + 2 b (+ 4 c) for
+the corner offsets (a, b, c);
 vertices lexicographic on the (nx+1) x (ny+1) (x (nz+1)) grid.
 """
 import numpy as np
@@ -39,19 +43,55 @@ def cell_coefficients(problem, group=0, inv_vdt=0.0):
     return 1.0 / (3.0 * tr), sa, s0
 
 
+def q1_qp_tables(p, dim, vol):
+    """Mixed mass matrix [corner][node] (vertex hat functions against the DG
+    Q_p basis on the equidistant nodes j/p, cell measure vol) and the hat
+    functions' values at the nodes [node][corner]; tensor products of 1-D
+    factors, x fastest."""
+    gx, gw = np.polynomial.legendre.leggauss(p + 2)
+    gx, gw = 0.5 * (gx + 1.0), 0.5 * gw
+    nodes1 = np.arange(p + 1) / p
+
+    def lag(k, x):
+        v = np.ones_like(x)
+        for j in range(p + 1):
+            if j != k:
+                v = v * (x - nodes1[j]) / (nodes1[k] - nodes1[j])
+        return v
+
+    hat = [lambda x: 1.0 - x, lambda x: x]
+    m1 = np.array([[np.sum(gw * hat[a](gx) * lag(k, gx)) for k in range(p + 1)] for a in range(2)])
+    i1 = np.array([[hat[a](nodes1[k]) for a in range(2)] for k in range(p + 1)])
+    nc, p1 = 2 ** dim, p + 1
+    n = p1 ** dim
+    mix = np.zeros((nc, n))
+    ipl = np.zeros((n, nc))
+    for cr in range(nc):
+        for j in range(n):
+            mm, ip = vol, 1.0
+            for ax in range(dim):
+                bit = (cr >> ax) & 1
+                comp = (j // p1 ** ax) % p1
+                mm *= m1[bit, comp]
+                ip *= i1[comp, bit]
+            mix[cr, j] = mm
+            ipl[j, cr] = ip
+    return mix, ipl
+
+
 class Diffusion:
     """The assembled vertex system of one problem."""
 
     def __init__(self, problem, group=0, inv_vdt=0.0):
         dim = problem.dim
-        assert problem.fe_order == 1
         n = list(problem.n_cells)
         h = [(problem.upper[a] - problem.lower[a]) / n[a] for a in range(dim)]
         self.dim, self.n = dim, n
         nv = [k + 1 for k in n]
         self.nv = nv
-        nodes = 2 ** dim
-        self.nodes = nodes
+        nodes = 2 ** dim  # corners of a cell
+        self.corners = nodes
+        self.nodes = (problem.fe_order + 1) ** dim  # DG nodes of a cell
         D, sa, s0 = cell_coefficients(problem, group, inv_vdt)
         self.s0 = s0
         vol = float(np.prod(h))
@@ -65,6 +105,7 @@ class Diffusion:
             return out
 
         self.Mref = vol * kron([m1] * dim)
+        self.mix, self.ipl = q1_qp_tables(problem.fe_order, dim, vol)
         Kref = np.zeros((nodes, nodes))
         for a in range(dim):
             fac = [m1] * dim
@@ -119,9 +160,10 @@ class Diffusion:
         self.diag = self.C.diagonal()
 
     def rhs(self, v0):
-        """Assembled sigma_s0 M v0 (v0: the DG scalar-moment values, [cell][node])."""
+        """Assembled sigma_s0 M v0 (v0: the DG scalar-moment values, [cell][node]),
+        through the mixed mass matrix of the vertex hat functions."""
         ve = np.asarray(v0, dtype=np.float64).reshape(-1, self.nodes)
-        r = self.s0[:, None] * (ve @ self.Mref.T)
+        r = self.s0[:, None] * (ve @ self.mix.T)
         return np.bincount(self.vid.ravel(), weights=r.ravel(), minlength=self.NV)
 
     def solve(self, b, k=None):
@@ -152,5 +194,5 @@ class Diffusion:
         n0 = self.vid.shape[0] * self.nodes
         f = self.solve(self.rhs(v[:n0]), k)
         out = v.copy()
-        out[:n0] += f[self.vid].ravel()
+        out[:n0] += (f[self.vid] @ self.ipl.T).ravel()  # the vertex field at each cell's nodes
         return out

@@ -1,6 +1,6 @@
-// Diffusion synthetic acceleration (DSA) of the scalar flux for DG Q1 meshes,
-// used as the right preconditioner of FGMRES and as the acceleration step of
-// source iteration.
+// Diffusion synthetic acceleration (DSA) of the scalar flux for DG Q_p
+// meshes, used as the right preconditioner of FGMRES and as the acceleration
+// step of source iteration.
 //
 // The reference's Krylov solves run unpreconditioned (src/ouranos.cc:160-171),
 // and its source iteration (src/ouranos.cc:72-95) is plain.  In optically
@@ -8,12 +8,14 @@
 // the transport iteration are continuous scalar-flux fields that obey a
 // diffusion equation.  For a residual v ([mom][dof]) the preconditioner is
 //   P v = v + f,   (-div D grad + sigma_a) f = sigma_s0 v_0,
-// f continuous trilinear (bilinear in 2-D) on the mesh vertices, with the
+// f continuous trilinear (bilinear in 2-D) on the mesh vertices (for every
+// DG order: the right-hand side takes the Q_p residual through the mixed
+// mass matrix, the correction is f interpolated at the Q_p nodes), with the
 // Marshak condition D df/dn + f/2 = 0 on vacuum and inflow boundaries and a
 // zero current on reflective ones; D = 1 / (3 (sigma_t' - sigma_s1)),
 // sigma_a = sigma_t' - sigma_s0, sigma_t' = sigma_t + 1/(v dt) in time steps.
-// f is added to the scalar moment's nodal values of every cell (the DG Q1
-// space contains the continuous one), the higher moments pass unchanged.
+// f is added to the scalar moment's nodal values of every cell (the DG Q_p
+// space contains the continuous Q1 one), the higher moments pass unchanged.
 // This is the continuous-finite-element DSA of the source-iteration error
 // equation; as a right preconditioner of a Krylov method it stays effective at
 // the material discontinuities where the same correction used inside plain
@@ -42,6 +44,7 @@ namespace {
 
 constexpr int kThreads = 256;     // setup kernels
 constexpr int kCgThreads = 1024;  // the CG kernel: one block per multiprocessor
+constexpr int kMaxNodes = 27;     // DG Q_p nodes per cell the tables hold (3-D Q2, 2-D Q4: 25)
 
 struct DsaGeom {
   int nx, ny, nz;      // cells per axis (nz = 1 in 2-D)
@@ -275,12 +278,15 @@ __global__ void __launch_bounds__(kThreads) dsa_stencil_kernel(DsaGeom g, const 
   }
 }
 
-// assembled sigma_s0 M v_0 at vertex (I, J, K)
+// assembled sigma_s0 M v_0 at vertex (I, J, K): for each cell around the
+// vertex, the cell's nodal values times the row of the mixed mass matrix
+// (vertex hat function x the cell's DG Q_p basis, cell measure folded in) of
+// the corner the vertex is for that cell
 template <int DIM>
 __device__ __forceinline__ float assemble_rhs(const DsaGeom& g, const float4* __restrict__ cell,
-                                              const double* __restrict__ v, int I, int J, int K) {
+                                              const double* __restrict__ v, int I, int J, int K,
+                                              const float* __restrict__ smix, int n) {
   constexpr int NC = DIM == 3 ? 2 : 1;
-  constexpr int NODES = DIM == 3 ? 8 : 4;
   float acc = 0.f;
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
@@ -295,17 +301,11 @@ __device__ __forceinline__ float assemble_rhs(const DsaGeom& g, const float4* __
         const int kx = I - 1 + a;
         if (kx < 0 || kx >= g.nx) continue;
         const int cid = (kz * g.ny + ky) * g.nx + kx;
-        const double* vc = v + (long)cid * NODES;
+        const double* vc = v + (long)cid * n;
+        const float* row = smix + ((1 - a) + 2 * (1 - b) + (DIM == 3 ? 4 * (1 - c) : 0)) * n;
         float sm = 0.f;
-#pragma unroll
-        for (int c2 = 0; c2 < NC; ++c2)
-#pragma unroll
-          for (int b2 = 0; b2 < 2; ++b2)
-#pragma unroll
-            for (int a2 = 0; a2 < 2; ++a2)
-              sm += m1(1 - a, a2) * m1(1 - b, b2) * (DIM == 3 ? m1(1 - c, c2) : 1.f) *
-                    (float)vc[a2 + 2 * b2 + 4 * c2];
-        acc += __ldg(&cell[cid].z) * g.vol * sm;
+        for (int j = 0; j < n; ++j) sm += row[j] * (float)vc[j];
+        acc += __ldg(&cell[cid].z) * sm;
       }
     }
   }
@@ -326,8 +326,17 @@ __global__ void __launch_bounds__(kCgThreads, 1) dsa_cg_kernel(DsaGeom g, const 
                                                           const float* __restrict__ dinv, float* x, float* r,
                                                           float* z, float* p, float* q, double* part_a,
                                                           double* part_b, DsaSync* sync, int* status,
-                                                          long long limit_ns, int iters) {
-  constexpr int NODES = DIM == 3 ? 8 : 4;
+                                                          long long limit_ns, int iters,
+                                                          const float* __restrict__ fe, int n) {
+  constexpr int NCORNER = DIM == 3 ? 8 : 4;
+  // the cell tables: mixed mass [corner][n] (measure folded in), then the
+  // interpolation of the vertex values at the nodes [n][corner]
+  __shared__ float smix[NCORNER * kMaxNodes], sipl[kMaxNodes * NCORNER];
+  for (int k = threadIdx.x; k < NCORNER * n; k += kCgThreads) {
+    smix[k] = fe[k];
+    sipl[k] = fe[NCORNER * n + k];
+  }
+  __syncthreads();
   const int stride = gridDim.x * kCgThreads;
   const int first = blockIdx.x * kCgThreads + threadIdx.x;
   // r = rhs, z = r / diag, x = 0
@@ -335,7 +344,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) dsa_cg_kernel(DsaGeom g, const 
   for (int vid = first; vid < g.nv; vid += stride) {
     int I, J, K;
     vertex_ijk(g, vid, I, J, K);
-    const float rr = assemble_rhs<DIM>(g, cell, v, I, J, K);
+    const float rr = assemble_rhs<DIM>(g, cell, v, I, J, K, smix, n);
     const float zz = rr * dinv[vid];
     r[vid] = rr;
     z[vid] = zz;
@@ -387,20 +396,31 @@ __global__ void __launch_bounds__(kCgThreads, 1) dsa_cg_kernel(DsaGeom g, const 
     beta = rz > 0.0 ? rzn / rz : 0.0;
     rz = rzn;
   }
-  // out = v + f, f = x + alpha p at the vertex of each scalar-moment node (x
-  // and p of other blocks' vertices: complete at the last barrier)
+  // out = v + f, f = x + alpha p interpolated from the cell's corner vertices
+  // at each scalar-moment node (Q1: the node is the vertex); x and p of other
+  // blocks' vertices are complete at the last barrier
   const float fa = (float)alpha;
   for (long e = first; e < len; e += stride) {
     double val = v[e];
     if (e < n0) {
-      const long cid = e / NODES;
-      const int k = (int)(e % NODES);
+      const long cid = e / n;
+      const int k = (int)(e % n);
       const int kx = (int)(cid % g.nx);
       const long tt = cid / g.nx;
       const int ky = (int)(tt % g.ny), kz = (int)(tt / g.ny);
-      const long vid = ((long)(kz + (DIM == 3 ? (k >> 2) : 0)) * g.vy + (ky + ((k >> 1) & 1))) * g.vx +
-                       (kx + (k & 1));
-      val += (double)(x[vid] + fa * p[vid]);
+      const long v0 = ((long)kz * g.vy + ky) * g.vx + kx;  // the cell's corner (0, 0, 0)
+      float f = 0.f;
+      if (n == NCORNER) {
+        const long vid = v0 + (DIM == 3 ? (long)(k >> 2) * g.vy * g.vx : 0) + ((k >> 1) & 1) * g.vx + (k & 1);
+        f = x[vid] + fa * p[vid];
+      } else {
+#pragma unroll
+        for (int cr = 0; cr < NCORNER; ++cr) {
+          const long vid = v0 + (DIM == 3 ? (long)(cr >> 2) * g.vy * g.vx : 0) + ((cr >> 1) & 1) * g.vx + (cr & 1);
+          f += sipl[k * NCORNER + cr] * (x[vid] + fa * p[vid]);
+        }
+      }
+      val += (double)f;
     }
     out[e] = val;
   }
@@ -453,9 +473,73 @@ inline int nblocks(long n) { return (int)((n + kThreads - 1) / kThreads); }
 
 // per-cell coefficients and the Jacobi diagonal, rebuilt when the group or
 // the time step changes
+// Gauss-Legendre rule with m points on [0, 1] (Newton on P_m from the
+// Chebyshev-like initial guesses)
+void gauss01(int m, std::vector<double>& x, std::vector<double>& w) {
+  x.assign(m, 0.0);
+  w.assign(m, 0.0);
+  for (int i = 0; i < m; ++i) {
+    double t = std::cos(3.14159265358979323846 * (i + 0.75) / (m + 0.5)), dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = t;
+      for (int k = 2; k <= m; ++k) {
+        const double p2 = ((2.0 * k - 1.0) * t * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = m * (t * p1 - p0) / (t * t - 1.0);
+      const double dt = p1 / dp;
+      t -= dt;
+      if (std::fabs(dt) < 1e-16) break;
+    }
+    x[i] = 0.5 * (1.0 - t);
+    w[i] = 1.0 / ((1.0 - t * t) * dp * dp);  // (2 / ((1-t^2) P'^2)) / 2
+  }
+}
+
+// The cell tables for DG Q_p nodes on the equidistant points j/p: the mixed
+// mass matrix of the vertex hat functions against the Q_p basis, [corner][n]
+// with the cell measure folded in, then the values of the hat functions at
+// the nodes, [n][corner].  Both are tensor products of 1-D factors.  Q1: the
+// Q1 mass matrix and the identity.
+std::vector<float> fe_tables(const ouranos_rt* rt, double vol) {
+  const int p = rt->p, p1 = p + 1, dim = rt->dim, nc = 1 << dim, n = rt->n;
+  std::vector<double> gx, gw;
+  gauss01(p + 2, gx, gw);
+  auto lag = [&](int k, double x) {
+    double v = 1.0;
+    for (int j = 0; j <= p; ++j)
+      if (j != k) v *= (x - (double)j / p) / ((double)(k - j) / p);
+    return v;
+  };
+  auto hat = [](int a, double x) { return a ? x : 1.0 - x; };
+  std::vector<double> m1(2 * p1), i1(p1 * 2);
+  for (int a = 0; a < 2; ++a)
+    for (int k = 0; k < p1; ++k) {
+      double s = 0.0;
+      for (size_t q = 0; q < gx.size(); ++q) s += gw[q] * hat(a, gx[q]) * lag(k, gx[q]);
+      m1[a * p1 + k] = s;
+      i1[k * 2 + a] = hat(a, (double)k / p);
+    }
+  std::vector<float> out(2 * (size_t)nc * n);
+  for (int cr = 0; cr < nc; ++cr)
+    for (int j = 0; j < n; ++j) {
+      double mm = vol, ip = 1.0;
+      for (int ax = 0; ax < dim; ++ax) {
+        const int bit = (cr >> ax) & 1;
+        const int comp = ax == 0 ? j % p1 : (ax == 1 ? (j / p1) % p1 : j / (p1 * p1));
+        mm *= m1[bit * p1 + comp];
+        ip *= i1[comp * 2 + bit];
+      }
+      out[(size_t)cr * n + j] = (float)mm;
+      out[(size_t)nc * n + (size_t)j * nc + cr] = (float)ip;
+    }
+  return out;
+}
+
 int ensure_tables(ouranos_rt* rt) {
-  if (rt->n != (rt->dim == 3 ? 8 : 4) || rt->p != 1) {
-    rt->err = "diffusion acceleration needs a DG Q1 mesh";
+  if (rt->n > kMaxNodes) {
+    rt->err = "diffusion acceleration: cells of at most 27 dofs";
     return OURANOS_ERR_UNSUPPORTED;
   }
   if ((long)(rt->nx[0] + 1) * (rt->nx[1] + 1) * (rt->dim == 3 ? rt->nx[2] + 1 : 1) >= (1L << 31)) {
@@ -500,6 +584,10 @@ int ensure_tables(ouranos_rt* rt) {
   DC(cudaMemcpyAsync(rt->d_dsa_cell.p, cell.data(), sizeof(float4) * rt->n_cells, cudaMemcpyHostToDevice,
                      rt->stream),
      "tables");
+  const std::vector<float> fe = fe_tables(rt, (double)g.vol);
+  DC(rt->d_dsa_fe.alloc(sizeof(float) * fe.size()), "tables");
+  DC(cudaMemcpyAsync(rt->d_dsa_fe.p, fe.data(), sizeof(float) * fe.size(), cudaMemcpyHostToDevice, rt->stream),
+     "tables");
   DC(cudaMemsetAsync(rt->d_dsa_red.as<double>() + 2 * rt->dsa_grid, 0, sizeof(DsaSync), rt->stream),
      "barrier");
   float* dinv = rt->d_dsa_vec.as<float>() + 4 * nv;
@@ -535,8 +623,10 @@ int dsa_run(ouranos_rt* rt, const double* v, double* out, int iters) {
   // a barrier that gave up in an earlier call leaves its counters behind
   DC(cudaMemsetAsync(sync, 0, sizeof(DsaSync), rt->stream), "barrier");
   long long limit = rt->wait_limit_ns;
+  const float* fe = rt->d_dsa_fe.as<float>();
+  int n = rt->n;
   void* args[] = {&g, &cell, &coef, &v, &out, &len, &n0, &dinv, &x, &r, &z, &p, &q, &part_a, &part_b, &sync, &status,
-                  &limit, &iters};
+                  &limit, &iters, &fe, &n};
   DC(cudaLaunchCooperativeKernel((const void*)dsa_cg_kernel<DIM>, dim3(rt->dsa_grid), dim3(kCgThreads), args, 0,
                                  rt->stream),
      "solve");

@@ -327,5 +327,5 @@ struct ouranos_rt {
   // CG vectors and reductions; tables valid for (dsa_group, dsa_inv_vdt)
   int dsa_iters = 0, dsa_group = -1, dsa_grid = 0;
   double dsa_inv_vdt = -1.0;
-  ouranos::DevBuf d_dsa_cell, d_dsa_coef, d_dsa_vec, d_dsa_red;
+  ouranos::DevBuf d_dsa_cell, d_dsa_coef, d_dsa_vec, d_dsa_red, d_dsa_fe;
 };

@@ -207,7 +207,7 @@ class RadiativeTransfer:
         self._check(_capi.lib().ouranos_rt_set_angular_flux(self._h, psi.ctypes.data))
 
     def set_dsa(self, cg_iterations):
-        """Diffusion synthetic acceleration of the scalar flux (DG Q1 meshes):
+        """Diffusion synthetic acceleration of the scalar flux (DG Q_p meshes):
         the diffusion correction is solved by `cg_iterations` Jacobi-CG steps;
         0 switches it off.  Solves use it with solve(..., dsa=True)."""
         self._check(_capi.lib().ouranos_rt_set_dsa(self._h, int(cg_iterations)))

@@ -8,24 +8,43 @@ from oracle import dsa_oracle as do
 from oracle import pyoracle as po
 
 
-def homogeneous(dim, n, sigma_t, sigma_s, bc, sn=4, l_max=0, width=2.0):
+def homogeneous(dim, n, sigma_t, sigma_s, bc, sn=4, l_max=0, width=2.0, fe_order=1):
     quad = og.build_quadrature("GLC" if dim == 3 else "LS", sn, l_max, dim=dim)
-    p = og.uniform_problem(dim, 1, (n,) * dim, (0.0,) * dim, (width,) * dim, quad, sigma_t, sigma_s, 1.0,
-                           bc=bc)
+    p = og.uniform_problem(dim, fe_order, (n,) * dim, (0.0,) * dim, (width,) * dim, quad, sigma_t, sigma_s,
+                           1.0, bc=bc)
     return p
 
 
-@pytest.mark.parametrize("dim", [2, 3])
-def test_flat_residual_in_an_infinite_medium(dim):
+@pytest.mark.parametrize("p,dim", [(1, 2), (2, 2), (3, 2), (1, 3), (2, 3)])
+def test_cell_tables(p, dim):
+    """The mixed mass matrix and the nodal interpolation of the vertex hat
+    functions: Q1 gives the Q1 mass matrix and the identity; the hat
+    functions sum to one at every node and each integrates to vol / 2^dim."""
+    vol = 0.37
+    mix, ipl = do.q1_qp_tables(p, dim, vol)
+    nc, n = 2 ** dim, (p + 1) ** dim
+    assert mix.shape == (nc, n) and ipl.shape == (n, nc)
+    assert np.allclose(ipl.sum(axis=1), 1.0, atol=1e-14)
+    assert np.allclose(mix.sum(axis=1), vol / nc, rtol=1e-13)
+    if p == 1:
+        m1 = np.array([[1 / 3, 1 / 6], [1 / 6, 1 / 3]])
+        ref = m1 if dim == 1 else np.kron(m1, m1) if dim == 2 else np.kron(np.kron(m1, m1), m1)
+        assert np.allclose(mix, vol * ref, atol=1e-15)
+        assert np.allclose(ipl, np.eye(nc))
+
+
+@pytest.mark.parametrize("dim,order", [(2, 1), (3, 1), (2, 2), (3, 2), (2, 4)])
+def test_flat_residual_in_an_infinite_medium(dim, order):
     """Reflective on every side, homogeneous: a flat scalar-moment residual v has
     the flat correction sigma_s/sigma_a v, so P v = v / (1 - c) -- the exact
-    inverse of source iteration's error operator for that mode.  The
-    time-step term adds 1/(v dt) to sigma_t (so to sigma_a)."""
+    inverse of source iteration's error operator for that mode -- for every
+    DG order (the hat functions sum to one).  The time-step term adds 1/(v dt)
+    to sigma_t (so to sigma_a)."""
     n = 5
     for inv_vdt in (0.0, 0.5):
-        p = homogeneous(dim, n, 1.0, 0.9, (3,) * 6)
+        p = homogeneous(dim, n, 1.0, 0.9, (3,) * 6, fe_order=order)
         d = do.Diffusion(p, inv_vdt=inv_vdt)
-        nodes = 2 ** dim
+        nodes = (order + 1) ** dim
         v = np.zeros(p.quad.n_mom * n ** dim * nodes)
         v[: n ** dim * nodes] = 1.0
         expect = 1.0 + 0.9 / (0.1 + inv_vdt)
