@@ -488,17 +488,20 @@ def run_batch(args):
     }
     if args.batch_solve:
         res = {}
-        for inner in ("fp32", "fp64"):
-            xs, infos = b.solve(inner=inner, tol=args.tol, max_it=args.max_it)
-            res[inner] = (xs, infos)
+        b.set_dsa(args.dsa_cg)
+        for name, inner, dsa in (("fp32", "fp32", False), ("fp64", "fp64", False), ("fp32+dsa", "fp32", True)):
+            xs, infos = b.solve(inner=inner, tol=args.tol, max_it=args.max_it, dsa=dsa)
+            res[name] = (xs.copy(), infos)
             its = [i["iterations"] for i in infos]
-            out["solve_" + inner] = {"seconds": infos[0]["seconds"], "converged": sum(i["converged"] for i in infos),
-                                     "iterations_max": max(its), "iterations_mean": float(np.mean(its)),
-                                     "residual_max": max(i["residual"] for i in infos)}
-        x32, x64 = res["fp32"][0], res["fp64"][0]
-        out["solve_fp32"]["flux_rel_l2_vs_fp64_max"] = max(
-            float(np.linalg.norm(a - c) / max(np.linalg.norm(c), 1e-300)) for a, c in zip(b.slices(x32), b.slices(x64)))
-        out["solve_fp32"]["speedup_vs_fp64"] = out["solve_fp64"]["seconds"] / out["solve_fp32"]["seconds"]
+            out["solve_" + name] = {"seconds": infos[0]["seconds"], "converged": sum(i["converged"] for i in infos),
+                                    "iterations_max": max(its), "iterations_mean": float(np.mean(its)),
+                                    "residual_max": max(i["residual"] for i in infos)}
+        x64 = res["fp64"][0]
+        for name in ("fp32", "fp32+dsa"):
+            out["solve_" + name]["flux_rel_l2_vs_fp64_max"] = max(
+                float(np.linalg.norm(a - c) / max(np.linalg.norm(c), 1e-300))
+                for a, c in zip(b.slices(res[name][0]), b.slices(x64)))
+            out["solve_" + name]["speedup_vs_fp64"] = out["solve_fp64"]["seconds"] / out["solve_" + name]["seconds"]
     b.close()
     print(json.dumps(out), flush=True)
 

@@ -304,6 +304,10 @@ int ouranos_batch_solve(ouranos_batch* b, int inner, int restart, int max_it, do
  * runs each), keep the fastest; tiling (may be NULL) gets count x 3 ints */
 int ouranos_batch_autotune(ouranos_batch* b, int precision, int reps, int* tiling);
 int ouranos_batch_set_graphs(ouranos_batch* b, int enable);
+/* diffusion synthetic acceleration on every problem (ouranos_rt_set_dsa);
+ * ouranos_batch_solve uses it when OURANOS_SOLVER_DSA is OR'ed into `inner`
+ * (FGMRES with each problem's diffusion correction as right preconditioner) */
+int ouranos_batch_set_dsa(ouranos_batch* b, int cg_iterations);
 /* device time of the last batched sweep launches, graph launches so far */
 int ouranos_batch_stats(const ouranos_batch* b, double* last_sweep_ms, int* graph_launches);
 int ouranos_batch_last_error(const ouranos_batch* b, char* buf, size_t len);

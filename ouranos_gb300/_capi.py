@@ -46,7 +46,7 @@ EXPORTS = [
     "ouranos_batch_stats", "ouranos_batch_last_error",
     "ouranos_rt_set_time_step", "ouranos_rt_set_source", "ouranos_rt_time_advance",
     "ouranos_rt_get_angular_flux", "ouranos_rt_set_angular_flux",
-    "ouranos_rt_set_dsa", "ouranos_rt_dsa_apply", "ouranos_solve_multigroup",
+    "ouranos_rt_set_dsa", "ouranos_rt_dsa_apply", "ouranos_solve_multigroup", "ouranos_batch_set_dsa",
 ]
 
 
@@ -137,6 +137,7 @@ def lib():
         "ouranos_rt_set_dsa": [vp, i],
         "ouranos_rt_dsa_apply": [vp, vp, vp],
         "ouranos_solve_multigroup": [vp, i, i, i, d, i, d, vp, C.POINTER(MultigroupInfo)],
+        "ouranos_batch_set_dsa": [vp, i],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

@@ -89,8 +89,16 @@ class Batch:
         self._check(_capi.lib().ouranos_batch_rhs(self._h, _ptr(y)))
         return y
 
-    def solve(self, inner="fp32", tol=1e-8, max_it=2000, restart=30, out=None):
+    def set_dsa(self, cg_iterations):
+        """Diffusion synthetic acceleration on every problem (0 switches it off)."""
+        self._check(_capi.lib().ouranos_batch_set_dsa(self._h, int(cg_iterations)))
+
+    def solve(self, inner="fp32", tol=1e-8, max_it=2000, restart=30, out=None, dsa=False):
+        """Restarted GMRES on all problems at once; dsa=True: FGMRES with each
+        problem's diffusion correction (set_dsa) as right preconditioner."""
         prec = {"fp64": _capi.FP64, "fp32": _capi.FP32}[inner]
+        if dsa:
+            prec |= _capi.SOLVER_DSA
         x = np.empty(self.length) if out is None else out
         infos = (_capi.SolveInfo * self.count)()
         self._check(_capi.lib().ouranos_batch_solve(self._h, prec, restart, max_it, tol, _ptr(x), infos),

@@ -538,17 +538,19 @@ struct Solve {
   bool converged = false;
   DevBuf mem;
   double *B = nullptr, *Xs = nullptr, *dres = nullptr, *partial = nullptr, *ycoef = nullptr;
-  double** dptrs = nullptr;
-  std::vector<double*> V;
+  double** dptrs = nullptr;  // [0, m] basis V, [32, 32 + m) the preconditioned Z (flexible form)
+  std::vector<double*> V, Z;
+  bool flexible = false;
   double* hb = nullptr;  // pinned: [0,32) pass 1, [32,64) pass 2, [64] |w|^2, [65] |r|^2, [66,98) y
   Givens gv{1};
 };
 
-int solve_setup(ouranos_batch* b, Solve& S, long len, int m) {
+int solve_setup(ouranos_batch* b, Solve& S, long len, int m, bool flexible) {
   S.len = len;
   S.m = m;
+  S.flexible = flexible;
   const size_t vb = sizeof(double) * (size_t)len;
-  const size_t nvec = (size_t)m + 3;  // V[0..m], B, Xs
+  const size_t nvec = (size_t)m + 3 + (flexible ? (size_t)m : 0);  // V[0..m], B, Xs (, Z[0..m))
   const size_t extra = sizeof(double*) * 64 + sizeof(double) * (64 + 64 * (size_t)kDotGrid + 64) + 256;
   BC(S.mem.alloc(vb * nvec + extra), "solver workspace");
   char* p = (char*)S.mem.p;
@@ -556,6 +558,8 @@ int solve_setup(ouranos_batch* b, Solve& S, long len, int m) {
   for (int j = 0; j <= m; ++j) S.V[j] = (double*)(p + vb * j);
   S.B = (double*)(p + vb * (m + 1));
   S.Xs = (double*)(p + vb * (m + 2));
+  S.Z.assign(flexible ? m : 0, nullptr);
+  for (int j = 0; j < (int)S.Z.size(); ++j) S.Z[j] = (double*)(p + vb * (m + 3 + j));
   p += vb * nvec;
   S.dptrs = (double**)p;
   p += sizeof(double*) * 64;
@@ -564,6 +568,9 @@ int solve_setup(ouranos_batch* b, Solve& S, long len, int m) {
   S.ycoef = S.partial + 64 * (size_t)kDotGrid;
   BC(cudaMemcpyAsync(S.dptrs, S.V.data(), sizeof(double*) * (m + 1), cudaMemcpyHostToDevice, b->stream),
      "solver workspace");
+  if (flexible)
+    BC(cudaMemcpyAsync(S.dptrs + 32, S.Z.data(), sizeof(double*) * m, cudaMemcpyHostToDevice, b->stream),
+       "solver workspace");
   BC(cudaMemsetAsync(S.Xs, 0, vb, b->stream), "solver workspace");
   BC(cudaMallocHost((void**)&S.hb, sizeof(double) * 128), "pinned solver block");
   return OURANOS_OK;
@@ -592,7 +599,7 @@ int gram_schmidt(ouranos_batch* b, Solve& S) {
   return norm_and_scale(b, S, S.k + 1, 64);
 }
 
-int batch_solve(ouranos_batch* b, int inner, int m, int max_it, double tol, std::vector<Solve>& S) {
+int batch_solve(ouranos_batch* b, int inner, bool dsa, int m, int max_it, double tol, std::vector<Solve>& S) {
   const int P = (int)b->rt.size();
   const double drop = inner == OURANOS_FP32 ? 1e-5 : 0.0;  // FP32 operator accuracy
   double* X = b->d_X.as<double>();
@@ -600,7 +607,7 @@ int batch_solve(ouranos_batch* b, int inner, int m, int max_it, double tol, std:
   // right-hand sides (FP64) and their norms; x = 0 so r = b
   BR(batched_apply(b, OURANOS_FP64, all_of(b), true));
   for (int p = 0; p < P; ++p) {
-    BR(solve_setup(b, S[p], b->off[p + 1] - b->off[p], m));
+    BR(solve_setup(b, S[p], b->off[p + 1] - b->off[p], m, dsa));
     BC(cudaMemcpyAsync(S[p].B, Y + b->off[p], sizeof(double) * S[p].len, cudaMemcpyDeviceToDevice, b->stream),
        "rhs");
     BC(cudaMemcpyAsync(S[p].V[0], S[p].B, sizeof(double) * S[p].len, cudaMemcpyDeviceToDevice, b->stream),
@@ -629,12 +636,17 @@ int batch_solve(ouranos_batch* b, int inner, int m, int max_it, double tol, std:
       any_r |= mr[p] != 0;
     }
     if (!any_i && !any_r) break;
-    if (any_i) {  // one Arnoldi step: w = A v_k in the inner precision, orthogonalised
+    if (any_i) {  // one Arnoldi step: w = A v_k (or A P v_k) in the inner precision, orthogonalised
       for (int p = 0; p < P; ++p)
-        if (mi[p])
-          BC(cudaMemcpyAsync(X + b->off[p], S[p].V[S[p].k], sizeof(double) * S[p].len, cudaMemcpyDeviceToDevice,
-                             b->stream),
+        if (mi[p]) {
+          const double* in = S[p].V[S[p].k];
+          if (dsa) {  // z_k = P v_k: the member's diffusion correction (on the batch stream)
+            BR(member(b, p, rt_dsa_apply(b->rt[p], in, S[p].Z[S[p].k])));
+            in = S[p].Z[S[p].k];
+          }
+          BC(cudaMemcpyAsync(X + b->off[p], in, sizeof(double) * S[p].len, cudaMemcpyDeviceToDevice, b->stream),
              "arnoldi");
+        }
       BR(batched_apply(b, inner, mi, false));
       for (int p = 0; p < P; ++p)
         if (mi[p]) {
@@ -676,7 +688,8 @@ int batch_solve(ouranos_batch* b, int inner, int m, int max_it, double tol, std:
           std::memcpy(s.hb + 66, y.data(), sizeof(double) * s.k);
           BC(cudaMemcpyAsync(s.ycoef, s.hb + 66, sizeof(double) * s.k, cudaMemcpyHostToDevice, b->stream),
              "update");
-          BC(launch_multi_axpy((const double* const*)s.dptrs, s.k, s.ycoef, 1.0, s.Xs, s.len, b->stream),
+          BC(launch_multi_axpy((const double* const*)(s.flexible ? s.dptrs + 32 : s.dptrs), s.k, s.ycoef, 1.0,
+                               s.Xs, s.len, b->stream),
              "update");
           s.phase = Solve::kRestart;
         }
@@ -706,22 +719,39 @@ int batch_solve(ouranos_batch* b, int inner, int m, int max_it, double tol, std:
 
 extern "C" {
 
+// Diffusion synthetic acceleration for every problem of the batch (the
+// members' ouranos_rt_set_dsa): used by ouranos_batch_solve with
+// OURANOS_SOLVER_DSA OR'ed into `inner`.
+int ouranos_batch_set_dsa(ouranos_batch* b, int cg_iterations) {
+  if (!b) return OURANOS_ERR_BAD_INPUT;
+  cudaSetDevice(b->device);
+  for (size_t p = 0; p < b->rt.size(); ++p) BR(member(b, (int)p, ouranos_rt_set_dsa(b->rt[p], cg_iterations)));
+  return OURANOS_OK;
+}
+
 // Restarted GMRES on every problem of the batch at once (right-hand side from
 // each problem's fixed source and inflow): inner = OURANOS_FP32 for FP32
 // Arnoldi sweeps with FP64 restarts (a cycle also ends once its estimate has
-// dropped 1e-5 below the cycle's start), OURANOS_FP64 for the plain method.
+// dropped 1e-5 below the cycle's start), OURANOS_FP64 for the plain method;
+// with OURANOS_SOLVER_DSA OR'ed in, FGMRES with each problem's diffusion
+// correction as the right preconditioner (x += Z y).
 // x (concatenated, host or device) receives the solutions, info[count] the
 // per-problem results; seconds is the batch's wall time.
 int ouranos_batch_solve(ouranos_batch* b, int inner, int restart, int max_it, double tol, double* x,
                         ouranos_solve_info* info) {
   if (!b || !x || !info || max_it < 1 || !(tol > 0)) return OURANOS_ERR_BAD_INPUT;
+  const bool dsa = (inner & OURANOS_SOLVER_DSA) != 0;
+  inner &= ~OURANOS_SOLVER_DSA;
   if (inner != OURANOS_FP64 && inner != OURANOS_FP32) return bbad(b, "unknown inner precision");
+  if (dsa)
+    for (ouranos_rt* r : b->rt)
+      if (r->dsa_iters < 1) return bbad(b, "diffusion acceleration is off (ouranos_batch_set_dsa)");
   cudaSetDevice(b->device);
   const auto t0 = std::chrono::steady_clock::now();
   BR(order_after_caller(b));
   const int m = std::max(1, std::min(restart, 30));
   std::vector<Solve> S(b->rt.size());
-  int rc = batch_solve(b, inner, m, max_it, tol, S);
+  int rc = batch_solve(b, inner, dsa, m, max_it, tol, S);
   if (rc == OURANOS_OK) rc = copy_out(b, x);
   if (rc == OURANOS_OK) rc = check_status(b);
   const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

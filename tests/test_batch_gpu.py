@@ -93,6 +93,25 @@ def test_batched_solve_matches_single_problem_gmres():
         assert all(i["converged"] for i in infos64)
 
 
+def test_batched_solve_with_dsa():
+    """FGMRES with every problem's diffusion correction (Q1 and Q2 problems,
+    P1 scattering): the same solutions as single-problem FP64 GMRES, in no
+    more iterations than the plain batched solve for any problem and far
+    fewer in total."""
+    import ouranos_gb300 as og
+    probs = _problems(count=5, seed=39)
+    with og.Batch(probs) as b:
+        x0, i0 = b.solve(inner="fp32", tol=1e-8, max_it=1500)
+        b.set_dsa(15)
+        x, infos = b.solve(inner="fp32", tol=1e-8, max_it=1500, dsa=True)
+        for p, xs, info in zip(probs, b.slices(x), infos):
+            assert info["converged"] and info["residual"] < 1e-8
+            with og.RadiativeTransfer(p) as rt:
+                xr, _, _ = rt.solve("gmres", tol=1e-10, max_it=3000)
+            assert rel_err(xs, xr) < 1e-6
+        assert sum(i["iterations"] for i in infos) < sum(i["iterations"] for i in i0)
+
+
 def test_autotune_keeps_results_and_reports_tilings():
     import ouranos_gb300 as og
     probs = _problems(count=4, seed=41)
