@@ -174,7 +174,8 @@ int ouranos_rt_last_sweep_ms(const ouranos_rt* rt, double* ms, int* kernels);
  * directions per warp, with cells_x * cells_y * dirs == 32 (one lane per cell),
  * or == 16 for cells of 9 or more dofs (2-D Q2+, 3-D Q2): two lanes share each
  * cell solve.  0s = the default (one direction per warp; 2-D 32 x 1, 3-D
- * 8 x 4; two lanes per cell and 16 cells where allowed). */
+ * 4 x 8; two lanes per cell and 16 cells where allowed: 2-D 16 x 1, 3-D
+ * 4 x 4). */
 int ouranos_rt_set_tiling(ouranos_rt* rt, int cells_x, int cells_y, int dirs_per_warp);
 int ouranos_rt_get_tiling(const ouranos_rt* rt, int* cells_x, int* cells_y, int* dirs_per_warp);
 /* Spin limit of the in-kernel dependency waits, in nanoseconds (default 2 s).

@@ -9,6 +9,12 @@ RMS s of v, log sigma_t, scattering ratio) and the target the nodal values of
 (e - v)/s -- so z = v + s*correction approximates A^-1 v.  The errors mix
 smooth random fields, power iterates T^j e0 of the transport iteration (what
 FGMRES's Krylov vectors are made of) and rough noise.
+
+`train_on_solver_pairs` trains instead on the vectors FGMRES itself meets:
+the inputs of its right preconditioner in a diffusion-accelerated solve (and
+then in the learned-preconditioned one), each with its diffusion correction
+as the target; `fgmres_pairs` exposes every Arnoldi step's exact pair
+(w = A z, z).
 """
 import ctypes as C
 import math
@@ -202,6 +208,168 @@ def make_pairs(rt, problem, count, rng, torch, feat_out, target_out, offset, mix
         _capi.check(L.ouranos_rt_pc_features(rt._h, v.data_ptr(), f.data_ptr(), None), rt._h)
         _capi.check(L.ouranos_rt_pc_target(rt._h, v.data_ptr(), e.data_ptr(), t.data_ptr()), rt._h)
         assert f.numel() == FEATURES * n_cells and t.numel() == OUTPUTS * n_cells
+
+
+def fgmres_pairs(rt, b, precondition, record, m=30, max_it=60, tol=1e-8):
+    """Restarted FGMRES(m) on A = rt's operator (CUDA float64 vectors), that
+    hands every Arnoldi step's exact pair to record(w, z): z = P(v_j) is the
+    preconditioned basis vector and w = A z the operator's image of it, taken
+    before the orthogonalisation.  So z is the true error of the residual w,
+    and the pairs are the ones the solver itself meets, with the distribution
+    of its own Krylov vectors.  Classical Gram-Schmidt with one
+    re-orthogonalisation, like csrc/solvers.cu.  Returns (x, iterations)."""
+    import torch
+    x = torch.zeros_like(b)
+    nb = float(b.norm())
+    it, res = 0, float("inf")
+    while it < max_it:
+        r = b - rt.apply(x) if it else b.clone()
+        beta = float(r.norm())
+        if beta <= tol * nb:
+            break
+        V = [r / beta]
+        Z = []
+        H = torch.zeros((m + 1, m), dtype=torch.float64)
+        y = None
+        for j in range(m):
+            z = precondition(V[j])
+            w = rt.apply(z)
+            record(w, z)
+            Z.append(z)
+            it += 1
+            Vs = torch.stack(V)
+            for _ in range(2):
+                h = Vs @ w
+                w = w - Vs.T @ h
+                H[: j + 1, j] += h.cpu()
+            H[j + 1, j] = float(w.norm())
+            V.append(w / max(float(H[j + 1, j]), 1e-300))
+            e1 = torch.zeros(j + 2, dtype=torch.float64)
+            e1[0] = beta
+            y = torch.linalg.lstsq(H[: j + 2, : j + 1], e1[:, None]).solution[:, 0]
+            res = float((H[: j + 2, : j + 1] @ y - e1).norm())
+            if res <= tol * nb or it >= max_it:
+                break
+        x = x + torch.stack(Z).T @ y.to(x.device)
+        if res <= tol * nb:
+            break
+    return x, it
+
+
+def solver_pairs(rt, count, feat_out, target_out, offset, precondition=None, base=None, m=30):
+    """Fill feat_out/target_out[offset:offset+count] with the pairs of the first
+    `count` Arnoldi steps of FGMRES(m) on rt's own right-hand side: features of
+    w = A z and the target (z - base(w)) / (s K) -- the part of the true error z
+    that the network has to add to base(w) (base=None: w itself, the plain
+    network; the diffusion correction when the network refines it).
+    precondition=None is the identity, else a function v -> z.  Returns how
+    many pairs were written (fewer if the solve converged first)."""
+    import torch
+    L = _lib()
+    b = torch.zeros(rt.length, dtype=torch.float64, device="cuda")
+    rt.rhs(out=b)
+    done = [0]
+
+    def record(w, z):
+        if done[0] >= count:
+            return
+        k = offset + done[0]
+        w = w.contiguous()
+        e = z if base is None else z - base(w) + w
+        e = e.contiguous()
+        _capi.check(L.ouranos_rt_pc_features(rt._h, w.data_ptr(), feat_out[k].data_ptr(), None), rt._h)
+        _capi.check(L.ouranos_rt_pc_target(rt._h, w.data_ptr(), e.data_ptr(), target_out[k].data_ptr()),
+                    rt._h)
+        done[0] += 1
+
+    fgmres_pairs(rt, b, precondition or (lambda v: v), record, m=m, max_it=count)
+    return done[0]
+
+
+def learned_precondition(rt, dsa=False):
+    """v -> P v through the network installed on rt (ouranos_rt_pc_apply);
+    dsa=True: the network's correction added to the diffusion correction,
+    P v = DSA(v) + (network part)."""
+    L = _lib()
+
+    def pc(v):
+        v = v.contiguous()
+        z = v.new_empty(v.shape)
+        _capi.check(L.ouranos_rt_pc_apply(rt._h, v.data_ptr(), z.data_ptr()), rt._h)
+        if dsa:
+            z = z - v + rt.dsa_apply(v)
+        return z
+    return pc
+
+
+def train_on_solver_pairs(n=32, maps=32, steps_per_map=60, rounds=2, epochs=6, lr=3e-4, seed=7,
+                          map_seed0=2000, sn=12, dsa=100, log=print):
+    """Train the network to predict the diffusion correction of the residuals
+    FGMRES meets on seeded thick maps.
+
+    The pairs are (v, DSA(v)) for the solver's own Krylov vectors v -- the
+    inputs of its right preconditioner -- with the diffusion correction
+    solved to convergence (`dsa` CG steps): the correction is a linear,
+    material-dependent, local-scale map of the scalar flux (its range is the
+    diffusion length: ~12 cells in the scattering cells, ~1 in the thick
+    ones), which the gated-linear network can represent.  Round 0 collects
+    the vectors of FGMRES(30) preconditioned by that correction; every later
+    round installs the network trained so far and collects the vectors of the
+    learned-preconditioned FGMRES, which are the ones the network meets in
+    use, and trains on all pairs so far.  Returns (net, loss history per
+    epoch)."""
+    import torch
+    from .transport import RadiativeTransfer
+    rng = np.random.default_rng(seed)
+    L = _lib()
+    cap = maps * steps_per_map * rounds
+    cells = n ** 3
+    feats = torch.empty((cap, cells * FEATURES), dtype=torch.float32, device="cuda")
+    targets = torch.empty((cap, cells * OUTPUTS), dtype=torch.float32, device="cuda")
+    net = Network(n, n, n, seed=seed)
+    rts = [RadiativeTransfer(thick_3d(seed=map_seed0 + k, n=n, sn=sn, width=10.0 * n / 64), precision="fp32")
+           for k in range(maps)]
+    hist = []
+    filled = 0
+    try:
+        for rt in rts:
+            rt.set_dsa(dsa)
+        for rnd in range(rounds):
+            for rt in rts:
+                if rnd:
+                    install(rt, net)
+                inner = learned_precondition(rt) if rnd else rt.dsa_apply
+                b = torch.zeros(rt.length, dtype=torch.float64, device="cuda")
+                rt.rhs(out=b)
+                start = filled
+
+                def pc(v, rt=rt, inner=inner, start=start):
+                    nonlocal filled
+                    if filled - start < steps_per_map:
+                        v = v.contiguous()
+                        e = rt.dsa_apply(v)
+                        _capi.check(L.ouranos_rt_pc_features(rt._h, v.data_ptr(), feats[filled].data_ptr(),
+                                                             None), rt._h)
+                        _capi.check(L.ouranos_rt_pc_target(rt._h, v.data_ptr(), e.data_ptr(),
+                                                           targets[filled].data_ptr()), rt._h)
+                        filled += 1
+                    return inner(v)
+
+                fgmres_pairs(rt, b, pc, lambda w, z: None, max_it=steps_per_map)
+                if rnd:
+                    install(rt, None)
+            for ep in range(epochs):
+                order = rng.permutation(filled)
+                rate = lr * (0.5 * (1 + math.cos(math.pi * ep / epochs))) / (1 + rnd)
+                tot = 0.0
+                for i in order:
+                    tot += net.train_step(feats[i], targets[i], rate)
+                hist.append(tot / filled)
+                log("round %d epoch %d pairs %d loss %.4e" % (rnd, ep, filled, hist[-1]))
+    finally:
+        for rt in rts:
+            rt.close()
+    return net, hist
 
 
 def train(n=64, maps=128, fields_per_map=4, epochs=8, lr=3e-4, seed=7, map_seed0=2000,

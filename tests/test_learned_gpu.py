@@ -156,3 +156,29 @@ def test_learned_fgmres_converges_and_falls_back():
         xl, il, _ = rt.solve("fgmres_learned", tol=1e-8, max_it=800)
     assert il["converged"] and il["residual"] < 1e-8
     assert _rel(xl, xg) < 1e-6
+
+
+def test_solver_pairs_are_exact_and_the_trainer_runs():
+    """The Arnoldi pairs of fgmres_pairs satisfy w = A z to the operator's
+    accuracy (z is the exact error of the residual w), its FGMRES converges
+    like the device solver's, and the trainer on solver-generated pairs runs
+    end to end (both rounds) on a small grid with a finite loss."""
+    torch = pytest.importorskip("torch")
+    import ouranos_gb300 as og
+    from ouranos_gb300 import learned
+    prob = og.thick_3d(seed=2102, n=8, sn=4, block=2, width=2.0)
+    with og.RadiativeTransfer(prob) as rt:
+        b = torch.zeros(rt.length, dtype=torch.float64, device="cuda")
+        rt.rhs(out=b)
+        seen = []
+        x, it = learned.fgmres_pairs(rt, b, lambda v: v, lambda w, z: seen.append((w.clone(), z.clone())),
+                                     max_it=400)
+        assert len(seen) == it > 5
+        for w, z in seen[:5]:
+            assert _rel(w.cpu().numpy(), rt.apply(z).cpu().numpy()) < 1e-13
+        xg, info, _ = rt.solve("gmres", tol=1e-8, max_it=800)
+        assert float((b - rt.apply(x)).norm() / b.norm()) < 1e-7
+        assert _rel(x.cpu().numpy(), xg) < 1e-6
+    net, hist = learned.train_on_solver_pairs(n=8, maps=2, steps_per_map=6, rounds=2, epochs=3, lr=1e-3,
+                                              sn=4, dsa=40, log=lambda s: None)
+    assert len(hist) == 6 and all(np.isfinite(hist))

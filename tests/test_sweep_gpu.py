@@ -105,6 +105,8 @@ def test_default_tiling_and_lane_rules():
         assert rt.tiling() == (16, 1, 1)
     with og.RadiativeTransfer(og.thick_3d(seed=2004, n=8, fe_order=2, sn=4, block=4, width=2.0)) as rt:
         assert rt.tiling() == (4, 4, 1)
+    with og.RadiativeTransfer(og.thick_3d(seed=2004, n=8, sn=4, block=4, width=2.0)) as rt:
+        assert rt.tiling() == (4, 8, 1)
     with og.RadiativeTransfer(og.config_small(n=16, sn=4)) as rt:
         assert rt.tiling() == (32, 1, 1)
         with pytest.raises(_capi.OuranosError) as e:
@@ -112,7 +114,7 @@ def test_default_tiling_and_lane_rules():
         assert e.value.code == _capi.ERR_BAD_INPUT
 
 
-@pytest.mark.parametrize("tiling", [(4, 4, 2), (8, 4, 1), (4, 2, 4), (2, 2, 8), (2, 4, 4)])
+@pytest.mark.parametrize("tiling", [(4, 4, 2), (8, 4, 1), (4, 8, 1), (4, 2, 4), (2, 2, 8), (2, 4, 4)])
 def test_tilings_3d(tiling):
     import ouranos_gb300 as og
     prob = og.thick_3d(seed=2002, n=9, sn=4, block=3, width=3.0)
