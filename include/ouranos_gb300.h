@@ -147,7 +147,11 @@ int ouranos_rt_scattering_source(ouranos_rt* rt, const double* x);
  * scattering + boundary inflow when group_flux != NULL]).  group_flux is
  * [g][mom][dof] (the reference's group_flux vector of MPI vectors). */
 int ouranos_rt_sweep(ouranos_rt* rt, double* flux_moments, const double* group_flux);
-/* Epetra_Operator::Apply (src/RadiativeTransfer.cc:780-809): y = x - D L^-1 M2D S x. */
+/* Epetra_Operator::Apply (src/RadiativeTransfer.cc:780-809): y = x - D L^-1 M2D S x.
+ * x and y may be host or device pointers (y == x allowed).  With page-locked
+ * host vectors the copies travel in cell ranges on a second stream,
+ * overlapped with the kernels before and after the sweep; the result is
+ * bit-identical to the device-pointer call. */
 int ouranos_rt_apply(ouranos_rt* rt, const double* x, double* y);
 /* Right-hand side of the Krylov form (src/ouranos.cc:149-158): rhs += D L^-1 (q +
  * other-group scattering + boundary inflow), with the in-group scattering source

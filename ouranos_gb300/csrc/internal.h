@@ -127,21 +127,25 @@ template <typename real>
 cudaError_t launch_sweep_batch(int dim, int p1, int fused_moments, int lanes_per_cell,
                                const SweepArgs<real>* args, const int2* tmap, int n_total, int* ticket,
                                const int* status, const unsigned* epoch, int grid, int block, cudaStream_t s);
-// q[d][e] = sum_m M2D[d][m] T[m][e] (+ iso[e])  -- moment -> direction expansion
+// q[d][e] = sum_m M2D[d][m] T[m][e] (+ iso[e])  -- moment -> direction expansion.
+// Every contraction below strides its rows by n_dofs and covers the dofs
+// [0, len) of the pointers it gets (len < 0: all n_dofs), so a caller runs it
+// on the dof range [e0, e0 + len) by offsetting each pointer by e0.
 template <typename real>
 cudaError_t launch_expand_source(const real* T, const real* iso, const real* m2d, real* q,
-                                 int n_dir, int n_mom, long n_dofs, cudaStream_t s);
+                                 int n_dir, int n_mom, long n_dofs, cudaStream_t s, long len = -1);
 // the same two contractions for FP64 data in double-float arithmetic (df64.cuh)
 cudaError_t launch_expand_source_df64(const double* T, const double* iso, const double* m2d,
-                                      double* q, int n_dir, int n_mom, long n_dofs, cudaStream_t s);
+                                      double* q, int n_dir, int n_mom, long n_dofs, cudaStream_t s,
+                                      long len = -1);
 cudaError_t launch_reduce_moments_df64(const double* psi, const double* d2m_t, double* phi,
-                                       int n_dir, int n_mom, long n_dofs, cudaStream_t s);
+                                       int n_dir, int n_mom, long n_dofs, cudaStream_t s, long len = -1);
 // the same with T, iso, q (and psi) stored as double-float pairs (the
 // double-float sweep's storage)
 cudaError_t launch_expand_source_pairs(const df64* T, const df64* iso, const double* m2d, df64* q,
-                                       int n_dir, int n_mom, long n_dofs, cudaStream_t s);
+                                       int n_dir, int n_mom, long n_dofs, cudaStream_t s, long len = -1);
 cudaError_t launch_reduce_moments_pairs(const df64* psi, const double* d2m_t, double* phi, int n_dir,
-                                        int n_mom, long n_dofs, cudaStream_t s);
+                                        int n_mom, long n_dofs, cudaStream_t s, long len = -1);
 // Octant symmetry of a quadrature: the directions form classes of P = 2^dim
 // members with the same |Omega|, member f having Omega_a < 0 exactly for the
 // bits a of f; every moment m belongs to a parity group g whose M2D (and D2M)
@@ -159,13 +163,13 @@ struct SymTables {
 // its products once per parity group (expansion) or its signed sums of psi
 // once per group (reduction), about half the arithmetic of the direct form
 cudaError_t launch_expand_sym_pairs(const df64* T, const df64* iso, const SymTables& st, df64* q, int n_mom,
-                                    long n_dofs, cudaStream_t s);
+                                    long n_dofs, cudaStream_t s, long len = -1);
 cudaError_t launch_reduce_sym_pairs(const df64* psi, const SymTables& st, double* phi, int n_mom, long n_dofs,
-                                    cudaStream_t s);
+                                    cudaStream_t s, long len = -1);
 // phi[m][e] = sum_d D2M[m][d] psi[d][e]  -- direction -> moment reduction
 template <typename real>
 cudaError_t launch_reduce_moments(const real* psi, const real* d2m_t, real* phi, int n_dir,
-                                  int n_mom, long n_dofs, cudaStream_t s);
+                                  int n_mom, long n_dofs, cudaStream_t s, long len = -1);
 
 // ------------------------------------------------------------ vector kernels
 template <typename real>
@@ -180,6 +184,9 @@ cudaError_t launch_iso_source(real* iso, const double* qcell, const double* rows
 template <typename real>
 cudaError_t launch_combine(const double* x, const real* phi, double* y, long len, double sx,
                            double sp, cudaStream_t s);
+template <typename real>
+cudaError_t launch_combine_rows(const double* x, const real* phi, double* y, int rows, long len, long stride,
+                                double sx, double sp, cudaStream_t s);
 cudaError_t launch_permute(const double* in, double* out, const long* order, long n_cells,
                            int n, int n_vec, int to_internal, cudaStream_t s);
 cudaError_t launch_axpby(double a, const double* x, double b, double* y, long len, cudaStream_t s);
@@ -263,11 +270,17 @@ int rt_stage_in(ouranos_rt* rt, const double* v, DevBuf& buf, int n_vec, const d
 int rt_stage_out(ouranos_rt* rt, const double* dv, double* user);
 }  // namespace ouranos
 
+// cell ranges of the host-vector Apply's overlapped copies
+#define OURANOS_OVERLAP_CHUNKS 4
+
 struct ouranos_rt {
   int device = 0;
   cudaStream_t stream = nullptr;      // stream in use
   cudaStream_t own_stream = nullptr;  // the handle's own stream
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // host-vector Apply: the copy stream and its chunk events (created on first use)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_chunk[2 * OURANOS_OVERLAP_CHUNKS + 2] = {};
   std::string err;
   // problem
   int dim = 2, p = 1, p1 = 2, n = 4, fd = 2;

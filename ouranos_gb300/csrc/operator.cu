@@ -83,6 +83,17 @@ const real* table(const DevBuf& b64, const DevBuf& b32, const DevBuf& bdf) {
   return (const real*)b64.p;
 }
 
+// page-locked host memory (the copies of it are asynchronous)
+bool is_pinned_host_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
 bool is_device_ptr(const void* p) {
   if (!p) return false;
   cudaPointerAttributes at;
@@ -328,10 +339,35 @@ constexpr int kFusedMomentsMax = 2;
 // Sweep arguments for one problem (pointers into the handle's buffers) and,
 // when the source is expanded (fm = 0), the expansion launch.  Epoch, ticket
 // and status are left for the caller.
+// q = M2D src (+ iso) on the dofs [e0, e0 + len) into the expanded-source
+// buffer, in the contraction form of the sweep's precision
+template <typename real>
+int sweep_expand(ouranos_rt* rt, const real* src, const real* iso, long e0, long len) {
+  const long nd = rt->n_dofs;
+  src += e0;
+  if (iso) iso += e0;
+  if (std::is_same<real, df64>::value && rt->sym.n_class)  // pairs, through the octant symmetry
+    CU(launch_expand_sym_pairs((const df64*)src, (const df64*)iso, rt->sym, rt->d_q.as<df64>() + e0, rt->n_mom,
+                               nd, rt->stream, len),
+       "source expansion");
+  else if (std::is_same<real, df64>::value)  // pairs in, pairs out
+    CU(launch_expand_source_pairs((const df64*)src, (const df64*)iso, rt->d_m2d64.as<double>(),
+                                  rt->d_q.as<df64>() + e0, rt->n_dir, rt->n_mom, nd, rt->stream, len),
+       "source expansion");
+  else if (std::is_same<real, double>::value && rt->fp64_contract != OURANOS_FP64_NATIVE)
+    CU(launch_expand_source_df64((const double*)src, (const double*)iso, rt->d_m2d64.as<double>(),
+                                 rt->d_q.as<double>() + e0, rt->n_dir, rt->n_mom, nd, rt->stream, len),
+       "source expansion");
+  else
+    CU(launch_expand_source<real>(src, iso, table<real>(rt->d_m2d64, rt->d_m2d32, rt->d_m2ddf),
+                                  rt->d_q.as<real>() + e0, rt->n_dir, rt->n_mom, nd, rt->stream, len),
+       "source expansion");
+  return OURANOS_OK;
+}
+
 template <typename real>
 int sweep_prepare(ouranos_rt* rt, const real* src, const real* iso, const real* bnd, SweepArgs<real>& a,
-                  int& fm, int& kernels) {
-  const bool f64 = sizeof(real) == 8;
+                  int& fm, int& kernels, bool expand = true) {
   const long len_dir = (long)rt->n_dir * rt->n_dofs;
   a.nx = rt->nx[0];
   a.ny = rt->nx[1];
@@ -377,25 +413,11 @@ int sweep_prepare(ouranos_rt* rt, const real* src, const real* iso, const real* 
   if (angular) fm = 0;
   if (fm == 0) {
     CU(rt->d_q.alloc(sizeof(real) * len_dir), "expanded source");
-    if (std::is_same<real, df64>::value && rt->sym.n_class)  // pairs, through the octant symmetry
-      CU(launch_expand_sym_pairs((const df64*)src, (const df64*)iso, rt->sym, rt->d_q.as<df64>(), rt->n_mom,
-                                 rt->n_dofs, rt->stream),
-         "source expansion");
-    else if (std::is_same<real, df64>::value)  // pairs in, pairs out
-      CU(launch_expand_source_pairs((const df64*)src, (const df64*)iso, rt->d_m2d64.as<double>(),
-                                    rt->d_q.as<df64>(), rt->n_dir, rt->n_mom, rt->n_dofs, rt->stream),
-         "source expansion");
-    else if (std::is_same<real, double>::value && rt->fp64_contract != OURANOS_FP64_NATIVE)
-      CU(launch_expand_source_df64((const double*)src, (const double*)iso, rt->d_m2d64.as<double>(),
-                                   rt->d_q.as<double>(), rt->n_dir, rt->n_mom, rt->n_dofs,
-                                   rt->stream),
-         "source expansion");
-    else
-      CU(launch_expand_source<real>(src, iso, a.m2d, rt->d_q.as<real>(), rt->n_dir, rt->n_mom,
-                                    rt->n_dofs, rt->stream),
-         "source expansion");
-    kernels += (rt->n_mom + 15) / 16;
     a.q = rt->d_q.as<real>();
+    if (expand) {
+      OK_OR_RETURN(sweep_expand<real>(rt, src, iso, 0, rt->n_dofs));
+      kernels += (rt->n_mom + 15) / 16;
+    }
     if (angular) {
       CU(launch_angular_source<real>(rt->d_q.as<real>(), rt->d_psi_prev.as<float>(), rt->d_cell_mass.as<double>(),
                                      rt->inv_vdt, rt->n, rt->n_cells, rt->n_dir, rt->stream),
@@ -409,34 +431,38 @@ int sweep_prepare(ouranos_rt* rt, const real* src, const real* iso, const real* 
 // phi = D2M psi (the moment reduction after a sweep); phi is float for the
 // FP32 sweep, double for the FP64 and double-float sweeps
 template <typename real>
-int sweep_reduce(ouranos_rt* rt, const real* psi, void* phi) {
+int sweep_reduce(ouranos_rt* rt, const real* psi, void* phi, long e0 = 0, long len = -1) {
+  // dofs [e0, e0 + len): psi and phi move by e0, their row stride stays n_dofs
+  const long nd = rt->n_dofs;
+  if (len < 0) len = nd;
+  psi += e0;
+  double* phi64 = (double*)phi + e0;
   if (std::is_same<real, df64>::value && rt->sym.n_class)
-    CU(launch_reduce_sym_pairs((const df64*)psi, rt->sym, (double*)phi, rt->n_mom, rt->n_dofs, rt->stream),
+    CU(launch_reduce_sym_pairs((const df64*)psi, rt->sym, phi64, rt->n_mom, nd, rt->stream, len),
        "moment reduction");
   else if (std::is_same<real, df64>::value)
-    CU(launch_reduce_moments_pairs((const df64*)psi, rt->d_d2m64.as<double>(), (double*)phi, rt->n_dir,
-                                   rt->n_mom, rt->n_dofs, rt->stream),
+    CU(launch_reduce_moments_pairs((const df64*)psi, rt->d_d2m64.as<double>(), phi64, rt->n_dir, rt->n_mom, nd,
+                                   rt->stream, len),
        "moment reduction");
   else if (std::is_same<real, double>::value && rt->fp64_contract != OURANOS_FP64_NATIVE)
-    CU(launch_reduce_moments_df64((const double*)psi, rt->d_d2m64.as<double>(), (double*)phi,
-                                  rt->n_dir, rt->n_mom, rt->n_dofs, rt->stream),
+    CU(launch_reduce_moments_df64((const double*)psi, rt->d_d2m64.as<double>(), phi64, rt->n_dir, rt->n_mom,
+                                  nd, rt->stream, len),
        "moment reduction");
   else if (std::is_same<real, double>::value)
-    CU(launch_reduce_moments<double>((const double*)psi, rt->d_d2m64.as<double>(), (double*)phi, rt->n_dir,
-                                     rt->n_mom, rt->n_dofs, rt->stream),
+    CU(launch_reduce_moments<double>((const double*)psi, rt->d_d2m64.as<double>(), phi64, rt->n_dir,
+                                     rt->n_mom, nd, rt->stream, len),
        "moment reduction");
   else
-    CU(launch_reduce_moments<float>((const float*)psi, rt->d_d2m32.as<float>(), (float*)phi, rt->n_dir,
-                                    rt->n_mom, rt->n_dofs, rt->stream),
+    CU(launch_reduce_moments<float>((const float*)psi, rt->d_d2m32.as<float>(), (float*)phi + e0, rt->n_dir,
+                                    rt->n_mom, nd, rt->stream, len),
        "moment reduction");
   return OURANOS_OK;
 }
 
+// The sweep launch of prepared arguments: a fresh epoch, the ticket reset,
+// the kernel between the handle's timing events
 template <typename real>
-int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd, void* phi) {
-  SweepArgs<real> a;
-  int fm = 0, kernels = 0;
-  OK_OR_RETURN(sweep_prepare<real>(rt, src, iso, bnd, a, fm, kernels));
+int sweep_launch(ouranos_rt* rt, SweepArgs<real>& a, int fm) {
   // epochs cycle through [1, 0x7fff]; every sweep rewrites every edge word it
   // reads, so a stale word carries the previous epoch and never matches
   rt->epoch = rt->epoch % 0x7fffu + 1u;
@@ -458,6 +484,15 @@ int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd,
   CU(cudaEventRecord(rt->ev0, rt->stream), "event");
   CU(launch_sweep<real>(rt->dim, rt->p1, fm, a, grid, block, rt->stream), "sweep launch");
   CU(cudaEventRecord(rt->ev1, rt->stream), "event");
+  return OURANOS_OK;
+}
+
+template <typename real>
+int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd, void* phi) {
+  SweepArgs<real> a;
+  int fm = 0, kernels = 0;
+  OK_OR_RETURN(sweep_prepare<real>(rt, src, iso, bnd, a, fm, kernels));
+  OK_OR_RETURN(sweep_launch<real>(rt, a, fm));
   ++kernels;
   OK_OR_RETURN(sweep_reduce<real>(rt, a.psi, phi));
   kernels += (rt->n_mom + 15) / 16;
@@ -543,29 +578,33 @@ int stage_out(ouranos_rt* rt, const double* dv, double* user) {
 // Source moments T (precision of the sweep) from x (FP64, device) and the
 // other groups' fluxes gf (device or NULL).
 // (pairs: the double-float sweep's storage, in the same buffer as the FP64 source)
-int build_source(ouranos_rt* rt, const double* x, const double* gf, bool pairs) {
+int build_source(ouranos_rt* rt, const double* x, const double* gf, bool pairs, long c0 = 0, long nc = -1) {
   const long len = vec_len(rt);
   const double* M = rt->d_cell_mass.as<double>();
+  // cells [c0, c0 + nc): every per-cell pointer moves by c0 cells, the moment
+  // stride stays n_dofs
+  if (nc < 0) nc = rt->n_cells;
+  const long o = c0 * rt->n;
+  if (x) x += o;
+  if (gf) gf += o;
+  const int* mat = rt->d_material.as<int>() + c0;
   if (rt->precision == OURANOS_FP64 && pairs) {
     CU(rt->d_src64.alloc(sizeof(df64) * len), "source");
-    CU(launch_scatter_source<df64>(x, gf, rt->d_src64.as<df64>(), M, rt->d_sscale.as<double>(),
-                                   rt->d_oscale.as<double>(), rt->d_material.as<int>(), rt->n_mat,
-                                   rt->G, rt->group, rt->n_cells, rt->n, rt->n_mom, rt->n_dofs,
-                                   rt->stream),
+    CU(launch_scatter_source<df64>(x, gf, rt->d_src64.as<df64>() + o, M, rt->d_sscale.as<double>(),
+                                   rt->d_oscale.as<double>(), mat, rt->n_mat, rt->G, rt->group, nc, rt->n,
+                                   rt->n_mom, rt->n_dofs, rt->stream),
        "scattering source");
   } else if (rt->precision == OURANOS_FP64) {
     CU(rt->d_src64.alloc(sizeof(double) * len), "source");
-    CU(launch_scatter_source<double>(x, gf, rt->d_src64.as<double>(), M, rt->d_sscale.as<double>(),
-                                     rt->d_oscale.as<double>(), rt->d_material.as<int>(), rt->n_mat,
-                                     rt->G, rt->group, rt->n_cells, rt->n, rt->n_mom, rt->n_dofs,
-                                     rt->stream),
+    CU(launch_scatter_source<double>(x, gf, rt->d_src64.as<double>() + o, M, rt->d_sscale.as<double>(),
+                                     rt->d_oscale.as<double>(), mat, rt->n_mat, rt->G, rt->group, nc, rt->n,
+                                     rt->n_mom, rt->n_dofs, rt->stream),
        "scattering source");
   } else {
     CU(rt->d_src32.alloc(sizeof(float) * len), "source");
-    CU(launch_scatter_source<float>(x, gf, rt->d_src32.as<float>(), M, rt->d_sscale.as<double>(),
-                                    rt->d_oscale.as<double>(), rt->d_material.as<int>(), rt->n_mat,
-                                    rt->G, rt->group, rt->n_cells, rt->n, rt->n_mom, rt->n_dofs,
-                                    rt->stream),
+    CU(launch_scatter_source<float>(x, gf, rt->d_src32.as<float>() + o, M, rt->d_sscale.as<double>(),
+                                    rt->d_oscale.as<double>(), mat, rt->n_mat, rt->G, rt->group, nc, rt->n,
+                                    rt->n_mom, rt->n_dofs, rt->stream),
        "scattering source");
   }
   return OURANOS_OK;
@@ -623,6 +662,85 @@ int phi_combine(ouranos_rt* rt, const double* x, double* y, double sx, double sp
     CU(launch_combine<double>(x, rt->d_phi64.as<double>(), y, len, sx, sp, rt->stream), "combine");
   else
     CU(launch_combine<float>(x, rt->d_phi32.as<float>(), y, len, sx, sp, rt->stream), "combine");
+  return OURANOS_OK;
+}
+
+// Apply for page-locked host vectors with the copies overlapped.  The cells
+// are cut into OURANOS_OVERLAP_CHUNKS ranges.  Each range of x travels on the
+// copy stream (one 2-D copy: the range's dofs of every moment) while the
+// handle's stream builds the scattering source (and the expanded source) of
+// the ranges that have landed; after the sweep each range is reduced and
+// combined and travels back while the next one is reduced.  The kernels and
+// their arithmetic per dof are those of the device Apply, so y is identical.
+template <typename real>
+int apply_overlapped(ouranos_rt* rt, const double* hx, double* hy) {
+  constexpr int K = OURANOS_OVERLAP_CHUNKS;
+  const long n = rt->n, nd = rt->n_dofs, nc = rt->n_cells;
+  const int nm = rt->n_mom;
+  const long len = vec_len(rt);
+  const bool f64 = rt->precision == OURANOS_FP64;
+  const bool pairs = std::is_same<real, df64>::value;
+  CU(rt->d_x.alloc(sizeof(double) * len), "staging");
+  CU(rt->d_y.alloc(sizeof(double) * len), "apply");
+  DevBuf& sb = f64 ? rt->d_src64 : rt->d_src32;
+  CU(sb.alloc(sizeof(real) * len), "source");
+  DevBuf& pb = f64 ? rt->d_phi64 : rt->d_phi32;
+  CU(pb.alloc((f64 ? sizeof(double) : sizeof(float)) * len), "flux");
+  if (!rt->copy_stream) {
+    CU(cudaStreamCreateWithFlags(&rt->copy_stream, cudaStreamNonBlocking), "copy stream");
+    for (cudaEvent_t& e : rt->ev_chunk) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "copy events");
+  }
+  double* dx = rt->d_x.as<double>();
+  double* dy = rt->d_y.as<double>();
+  cudaEvent_t* ev = rt->ev_chunk;  // [0, K) in, [K, 2K) out, [2K] start, [2K + 1] done
+  // the copies wait for the work already queued on the handle's stream
+  CU(cudaEventRecord(ev[2 * K], rt->stream), "copy order");
+  CU(cudaStreamWaitEvent(rt->copy_stream, ev[2 * K], 0), "copy order");
+  SweepArgs<real> a;
+  int fm = 0, kernels = 0;
+  const real* src = sb.as<real>();
+  OK_OR_RETURN(sweep_prepare<real>(rt, src, nullptr, nullptr, a, fm, kernels, false));
+  const long cc = (nc + K - 1) / K;
+  const size_t pitch = sizeof(double) * nd;
+  for (int k = 0; k < K; ++k) {
+    const long c0 = std::min(nc, k * cc), cn = std::min(nc, c0 + cc) - c0;
+    if (cn > 0) {
+      CU(cudaMemcpy2DAsync(dx + c0 * n, pitch, hx + c0 * n, pitch, sizeof(double) * cn * n, nm,
+                           cudaMemcpyHostToDevice, rt->copy_stream),
+         "copy in");
+    }
+    CU(cudaEventRecord(ev[k], rt->copy_stream), "copy order");
+    CU(cudaStreamWaitEvent(rt->stream, ev[k], 0), "copy order");
+    if (cn == 0) continue;
+    OK_OR_RETURN(build_source(rt, dx, nullptr, pairs, c0, cn));
+    if (fm == 0) OK_OR_RETURN(sweep_expand<real>(rt, src, nullptr, c0 * n, cn * n));
+  }
+  OK_OR_RETURN(sweep_launch<real>(rt, a, fm));
+  for (int k = 0; k < K; ++k) {
+    const long c0 = std::min(nc, k * cc), cn = std::min(nc, c0 + cc) - c0;
+    if (cn > 0) {
+      const long e0 = c0 * n;
+      OK_OR_RETURN(sweep_reduce<real>(rt, a.psi, pb.p, e0, cn * n));
+      if (f64)
+        CU(launch_combine_rows<double>(dx + e0, pb.as<double>() + e0, dy + e0, nm, cn * n, nd, 1.0, -1.0,
+                                       rt->stream),
+           "combine");
+      else
+        CU(launch_combine_rows<float>(dx + e0, pb.as<float>() + e0, dy + e0, nm, cn * n, nd, 1.0, -1.0,
+                                      rt->stream),
+           "combine");
+    }
+    CU(cudaEventRecord(ev[K + k], rt->stream), "copy order");
+    CU(cudaStreamWaitEvent(rt->copy_stream, ev[K + k], 0), "copy order");
+    if (cn > 0)
+      CU(cudaMemcpy2DAsync(hy + c0 * n, pitch, dy + c0 * n, pitch, sizeof(double) * cn * n, nm,
+                           cudaMemcpyDeviceToHost, rt->copy_stream),
+         "copy out");
+  }
+  // later work on the handle's stream (and its synchronisation) follows the copies
+  CU(cudaEventRecord(ev[2 * K + 1], rt->copy_stream), "copy order");
+  CU(cudaStreamWaitEvent(rt->stream, ev[2 * K + 1], 0), "copy order");
+  rt->last_kernels = 2 * K + 1 + (fm == 0 ? K : 0);
   return OURANOS_OK;
 }
 
@@ -862,6 +980,12 @@ int ouranos_rt_destroy(ouranos_rt* rt) {
   }
   if (rt->ev0) cudaEventDestroy(rt->ev0);
   if (rt->ev1) cudaEventDestroy(rt->ev1);
+  for (cudaEvent_t e : rt->ev_chunk)
+    if (e) cudaEventDestroy(e);
+  if (rt->copy_stream) {
+    cudaStreamSynchronize(rt->copy_stream);
+    cudaStreamDestroy(rt->copy_stream);
+  }
   if (rt->own_stream) cudaStreamDestroy(rt->own_stream);
   delete rt;
   return OURANOS_OK;
@@ -940,6 +1064,13 @@ int ouranos_rt_apply(ouranos_rt* rt, const double* x, double* y) {
   if (!rt || !x || !y) return OURANOS_ERR_BAD_INPUT;
   cudaSetDevice(rt->device);
   OK_OR_RETURN(clear_status(rt));
+  if (rt->cell_order.empty() && is_pinned_host_ptr(x) && is_pinned_host_ptr(y) &&
+      rt->n_cells >= 64 * OURANOS_OVERLAP_CHUNKS) {
+    if (df64_sweep(rt)) OK_OR_RETURN(apply_overlapped<df64>(rt, x, y));
+    else if (rt->precision == OURANOS_FP64) OK_OR_RETURN(apply_overlapped<double>(rt, x, y));
+    else OK_OR_RETURN(apply_overlapped<float>(rt, x, y));
+    return finish(rt);
+  }
   const double* dx = nullptr;
   OK_OR_RETURN(stage_in(rt, x, rt->d_x, 1, &dx));
   CU(rt->d_y.alloc(sizeof(double) * vec_len(rt)), "apply");

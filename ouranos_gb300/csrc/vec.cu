@@ -117,6 +117,18 @@ __global__ void combine_kernel(const double* x, const real* phi, double* y, long
     y[e] = (x ? sx * x[e] : 0.0) + sp * (double)phi[e];
 }
 
+// y = sx x + sp phi on rows x len elements of row stride `stride` (one dof
+// range of every moment)
+template <typename real>
+__global__ void combine_rows_kernel(const double* x, const real* phi, double* y, int rows, long len,
+                                    long stride, double sx, double sp) {
+  const long total = (long)rows * len;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < total; k += (long)gridDim.x * blockDim.x) {
+    const long e = (k / len) * stride + k % len;
+    y[e] = (x ? sx * x[e] : 0.0) + sp * (double)phi[e];
+  }
+}
+
 // Gather between the caller's cell numbering and the lexicographic one.
 __global__ void permute_kernel(const double* in, double* out, const long* order, long n_cells,
                                int n, int n_vec, int to_internal) {
@@ -222,12 +234,12 @@ __global__ void __launch_bounds__(kBlock) dots_final_kernel(const double* partia
 template <typename real, int NM>
 __global__ void expand_kernel(const real* __restrict__ T, const real* __restrict__ iso,
                               const real* __restrict__ m2d, int ld, real* __restrict__ q,
-                              int n_dir, int nm, long n_dofs, int accumulate) {
+                              int n_dir, int nm, long n_dofs, long len, int accumulate) {
   extern __shared__ unsigned char smem_raw[];
   real* sm = reinterpret_cast<real*>(smem_raw);
   for (int k = threadIdx.x; k < n_dir * nm; k += blockDim.x) sm[k] = m2d[(k / nm) * ld + k % nm];
   __syncthreads();
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n_dofs;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len;
        e += (long)gridDim.x * blockDim.x) {
     real t[NM];
 #pragma unroll
@@ -245,12 +257,12 @@ __global__ void expand_kernel(const real* __restrict__ T, const real* __restrict
 
 template <typename real, int NM>
 __global__ void reduce_kernel(const real* __restrict__ psi, const real* __restrict__ d2m_t, int ld,
-                              real* __restrict__ phi, int n_dir, int nm, long n_dofs) {
+                              real* __restrict__ phi, int n_dir, int nm, long n_dofs, long len) {
   extern __shared__ unsigned char smem_raw[];
   real* sm = reinterpret_cast<real*>(smem_raw);
   for (int k = threadIdx.x; k < n_dir * nm; k += blockDim.x) sm[k] = d2m_t[(k / nm) * ld + k % nm];
   __syncthreads();
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n_dofs;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len;
        e += (long)gridDim.x * blockDim.x) {
     real acc[NM];
 #pragma unroll
@@ -281,12 +293,12 @@ __device__ __forceinline__ df64 store_df64<df64>(df64 v) { return v; }
 template <int NM, typename S>
 __global__ void expand_df64_kernel(const S* __restrict__ T, const S* __restrict__ iso,
                                    const double* __restrict__ m2d, int ld, S* __restrict__ q,
-                                   int n_dir, int nm, long n_dofs, int accumulate) {
+                                   int n_dir, int nm, long n_dofs, long len, int accumulate) {
   extern __shared__ unsigned char smem_raw[];
   df64* sm = reinterpret_cast<df64*>(smem_raw);
   for (int k = threadIdx.x; k < n_dir * nm; k += blockDim.x) sm[k] = df64_from(m2d[(k / nm) * ld + k % nm]);
   __syncthreads();
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n_dofs;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len;
        e += (long)gridDim.x * blockDim.x) {
     df64 t[NM];
 #pragma unroll
@@ -304,12 +316,12 @@ __global__ void expand_df64_kernel(const S* __restrict__ T, const S* __restrict_
 
 template <int NM, typename S>
 __global__ void reduce_df64_kernel(const S* __restrict__ psi, const double* __restrict__ d2m_t,
-                                   int ld, double* __restrict__ phi, int n_dir, int nm, long n_dofs) {
+                                   int ld, double* __restrict__ phi, int n_dir, int nm, long n_dofs, long len) {
   extern __shared__ unsigned char smem_raw[];
   df64* sm = reinterpret_cast<df64*>(smem_raw);
   for (int k = threadIdx.x; k < n_dir * nm; k += blockDim.x) sm[k] = df64_from(d2m_t[(k / nm) * ld + k % nm]);
   __syncthreads();
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n_dofs;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len;
        e += (long)gridDim.x * blockDim.x) {
     df64_acc acc[NM];
 #pragma unroll
@@ -331,7 +343,7 @@ __global__ void reduce_df64_kernel(const S* __restrict__ psi, const double* __re
 
 template <typename S>
 static cudaError_t expand_df64_any(const S* T, const S* iso, const double* m2d, S* q, int n_dir, int n_mom,
-                                   long n_dofs, cudaStream_t s) {
+                                   long n_dofs, cudaStream_t s, long len) {
   for (int m0 = 0; m0 < n_mom; m0 += 16) {
     const int nm = n_mom - m0 < 16 ? n_mom - m0 : 16;
     const size_t sh = sizeof(df64) * (size_t)n_dir * nm;
@@ -339,11 +351,11 @@ static cudaError_t expand_df64_any(const S* T, const S* iso, const double* m2d, 
     const int acc = m0 > 0;
     const S* is = m0 == 0 ? iso : nullptr;
     if (nm <= 4)
-      expand_df64_kernel<4, S><<<resident_grid(expand_df64_kernel<4, S>, n_dofs, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+      expand_df64_kernel<4, S><<<resident_grid(expand_df64_kernel<4, S>, len, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, len, acc);
     else if (nm <= 10)
-      expand_df64_kernel<10, S><<<resident_grid(expand_df64_kernel<10, S>, n_dofs, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+      expand_df64_kernel<10, S><<<resident_grid(expand_df64_kernel<10, S>, len, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, len, acc);
     else
-      expand_df64_kernel<16, S><<<resident_grid(expand_df64_kernel<16, S>, n_dofs, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+      expand_df64_kernel<16, S><<<resident_grid(expand_df64_kernel<16, S>, len, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, len, acc);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -352,19 +364,19 @@ static cudaError_t expand_df64_any(const S* T, const S* iso, const double* m2d, 
 
 template <typename S>
 static cudaError_t reduce_df64_any(const S* psi, const double* d2m_t, double* phi, int n_dir, int n_mom,
-                                   long n_dofs, cudaStream_t s) {
+                                   long n_dofs, cudaStream_t s, long len) {
   for (int m0 = 0; m0 < n_mom; m0 += 16) {
     const int nm = n_mom - m0 < 16 ? n_mom - m0 : 16;
     const size_t sh = sizeof(df64) * (size_t)n_dir * nm;
     double* ph = phi + (size_t)m0 * n_dofs;
     if (nm <= 1)
-      reduce_df64_kernel<1, S><<<resident_grid(reduce_df64_kernel<1, S>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_df64_kernel<1, S><<<resident_grid(reduce_df64_kernel<1, S>, len, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs, len);
     else if (nm <= 4)
-      reduce_df64_kernel<4, S><<<resident_grid(reduce_df64_kernel<4, S>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_df64_kernel<4, S><<<resident_grid(reduce_df64_kernel<4, S>, len, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs, len);
     else if (nm <= 10)
-      reduce_df64_kernel<10, S><<<resident_grid(reduce_df64_kernel<10, S>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_df64_kernel<10, S><<<resident_grid(reduce_df64_kernel<10, S>, len, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs, len);
     else
-      reduce_df64_kernel<16, S><<<resident_grid(reduce_df64_kernel<16, S>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_df64_kernel<16, S><<<resident_grid(reduce_df64_kernel<16, S>, len, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs, len);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -390,7 +402,7 @@ __device__ __forceinline__ df64 neg_if(df64 v, bool neg) { return neg ? df64(-v.
 // group sums with its signs (+ iso)
 template <int NM, int P>
 __global__ void __launch_bounds__(256) expand_sym_kernel(const df64* __restrict__ T, const df64* __restrict__ iso,
-                                                         SymTables st, df64* __restrict__ q, int nm, long n_dofs) {
+                                                         SymTables st, df64* __restrict__ q, int nm, long n_dofs, long len) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   df64* srep = reinterpret_cast<df64*>(smem_raw);
   int* sdir = reinterpret_cast<int*>(srep + st.n_class * nm);
@@ -398,7 +410,7 @@ __global__ void __launch_bounds__(256) expand_sym_kernel(const df64* __restrict_
   unsigned* ssign = reinterpret_cast<unsigned*>(sgrp + 16);
   load_sym<P>(st, st.m2d_rep, nm, srep, sdir, sgrp, ssign);
   const int G = st.G;
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n_dofs; e += (long)gridDim.x * blockDim.x) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len; e += (long)gridDim.x * blockDim.x) {
     df64 t[NM];
 #pragma unroll
     for (int m = 0; m < NM; ++m) t[m] = m < nm ? T[(size_t)m * n_dofs + e] : df64(0.f);
@@ -436,7 +448,7 @@ __global__ void __launch_bounds__(256) expand_sym_kernel(const df64* __restrict_
 // per parity group, then every moment takes D2M_rep[m] times its group's sum
 template <int NM, int P>
 __global__ void __launch_bounds__(256) reduce_sym_kernel(const df64* __restrict__ psi, SymTables st,
-                                                         double* __restrict__ phi, int nm, long n_dofs) {
+                                                         double* __restrict__ phi, int nm, long n_dofs, long len) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   df64* srep = reinterpret_cast<df64*>(smem_raw);
   int* sdir = reinterpret_cast<int*>(srep + st.n_class * nm);
@@ -444,7 +456,7 @@ __global__ void __launch_bounds__(256) reduce_sym_kernel(const df64* __restrict_
   unsigned* ssign = reinterpret_cast<unsigned*>(sgrp + 16);
   load_sym<P>(st, st.d2m_rep, nm, srep, sdir, sgrp, ssign);
   const int G = st.G;
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n_dofs; e += (long)gridDim.x * blockDim.x) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len; e += (long)gridDim.x * blockDim.x) {
     df64_acc acc[NM];
 #pragma unroll
     for (int m = 0; m < NM; ++m) acc[m] = acc_zero();
@@ -484,67 +496,71 @@ __global__ void __launch_bounds__(256) reduce_sym_kernel(const df64* __restrict_
 
 template <int P>
 cudaError_t expand_sym_any(const df64* T, const df64* iso, const SymTables& st, df64* q, int nm, long n_dofs,
-                           cudaStream_t s) {
+                           cudaStream_t s, long len) {
   const size_t sh = sizeof(df64) * st.n_class * nm + sizeof(int) * (st.n_class * P + 16) + sizeof(unsigned) * 8;
   if (nm <= 4)
-    expand_sym_kernel<4, P><<<resident_grid(expand_sym_kernel<4, P>, n_dofs, sh), kBlock, sh, s>>>(T, iso, st, q, nm, n_dofs);
+    expand_sym_kernel<4, P><<<resident_grid(expand_sym_kernel<4, P>, len, sh), kBlock, sh, s>>>(T, iso, st, q, nm, n_dofs, len);
   else if (nm <= 10)
-    expand_sym_kernel<10, P><<<resident_grid(expand_sym_kernel<10, P>, n_dofs, sh), kBlock, sh, s>>>(T, iso, st, q, nm, n_dofs);
+    expand_sym_kernel<10, P><<<resident_grid(expand_sym_kernel<10, P>, len, sh), kBlock, sh, s>>>(T, iso, st, q, nm, n_dofs, len);
   else
-    expand_sym_kernel<16, P><<<resident_grid(expand_sym_kernel<16, P>, n_dofs, sh), kBlock, sh, s>>>(T, iso, st, q, nm, n_dofs);
+    expand_sym_kernel<16, P><<<resident_grid(expand_sym_kernel<16, P>, len, sh), kBlock, sh, s>>>(T, iso, st, q, nm, n_dofs, len);
   return cudaGetLastError();
 }
 template <int P>
-cudaError_t reduce_sym_any(const df64* psi, const SymTables& st, double* phi, int nm, long n_dofs, cudaStream_t s) {
+cudaError_t reduce_sym_any(const df64* psi, const SymTables& st, double* phi, int nm, long n_dofs, cudaStream_t s,
+                           long len) {
   const size_t sh = sizeof(df64) * st.n_class * nm + sizeof(int) * (st.n_class * P + 16) + sizeof(unsigned) * 8;
   if (nm <= 1)
-    reduce_sym_kernel<1, P><<<resident_grid(reduce_sym_kernel<1, P>, n_dofs, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs);
+    reduce_sym_kernel<1, P><<<resident_grid(reduce_sym_kernel<1, P>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
   else if (nm <= 4)
-    reduce_sym_kernel<4, P><<<resident_grid(reduce_sym_kernel<4, P>, n_dofs, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs);
+    reduce_sym_kernel<4, P><<<resident_grid(reduce_sym_kernel<4, P>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
   else if (nm <= 10)
-    reduce_sym_kernel<10, P><<<resident_grid(reduce_sym_kernel<10, P>, n_dofs, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs);
+    reduce_sym_kernel<10, P><<<resident_grid(reduce_sym_kernel<10, P>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
   else
-    reduce_sym_kernel<16, P><<<resident_grid(reduce_sym_kernel<16, P>, n_dofs, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs);
+    reduce_sym_kernel<16, P><<<resident_grid(reduce_sym_kernel<16, P>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
   return cudaGetLastError();
 }
 }  // namespace
 
 cudaError_t launch_expand_sym_pairs(const df64* T, const df64* iso, const SymTables& st, df64* q, int n_mom,
-                                    long n_dofs, cudaStream_t s) {
+                                    long n_dofs, cudaStream_t s, long len) {
   if (n_mom > 16 || st.G > st.P) return cudaErrorInvalidValue;
-  if (st.P == 4) return expand_sym_any<4>(T, iso, st, q, n_mom, n_dofs, s);
-  if (st.P == 8) return expand_sym_any<8>(T, iso, st, q, n_mom, n_dofs, s);
+  if (len < 0) len = n_dofs;
+  if (st.P == 4) return expand_sym_any<4>(T, iso, st, q, n_mom, n_dofs, s, len);
+  if (st.P == 8) return expand_sym_any<8>(T, iso, st, q, n_mom, n_dofs, s, len);
   return cudaErrorInvalidValue;
 }
 cudaError_t launch_reduce_sym_pairs(const df64* psi, const SymTables& st, double* phi, int n_mom, long n_dofs,
-                                    cudaStream_t s) {
+                                    cudaStream_t s, long len) {
   if (n_mom > 16 || st.G > st.P) return cudaErrorInvalidValue;
-  if (st.P == 4) return reduce_sym_any<4>(psi, st, phi, n_mom, n_dofs, s);
-  if (st.P == 8) return reduce_sym_any<8>(psi, st, phi, n_mom, n_dofs, s);
+  if (len < 0) len = n_dofs;
+  if (st.P == 4) return reduce_sym_any<4>(psi, st, phi, n_mom, n_dofs, s, len);
+  if (st.P == 8) return reduce_sym_any<8>(psi, st, phi, n_mom, n_dofs, s, len);
   return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_expand_source_df64(const double* T, const double* iso, const double* m2d,
                                       double* q, int n_dir, int n_mom, long n_dofs,
-                                      cudaStream_t s) {
-  return expand_df64_any<double>(T, iso, m2d, q, n_dir, n_mom, n_dofs, s);
+                                      cudaStream_t s, long len) {
+  return expand_df64_any<double>(T, iso, m2d, q, n_dir, n_mom, n_dofs, s, len < 0 ? n_dofs : len);
 }
 cudaError_t launch_reduce_moments_df64(const double* psi, const double* d2m_t, double* phi,
-                                       int n_dir, int n_mom, long n_dofs, cudaStream_t s) {
-  return reduce_df64_any<double>(psi, d2m_t, phi, n_dir, n_mom, n_dofs, s);
+                                       int n_dir, int n_mom, long n_dofs, cudaStream_t s, long len) {
+  return reduce_df64_any<double>(psi, d2m_t, phi, n_dir, n_mom, n_dofs, s, len < 0 ? n_dofs : len);
 }
 cudaError_t launch_expand_source_pairs(const df64* T, const df64* iso, const double* m2d, df64* q,
-                                       int n_dir, int n_mom, long n_dofs, cudaStream_t s) {
-  return expand_df64_any<df64>(T, iso, m2d, q, n_dir, n_mom, n_dofs, s);
+                                       int n_dir, int n_mom, long n_dofs, cudaStream_t s, long len) {
+  return expand_df64_any<df64>(T, iso, m2d, q, n_dir, n_mom, n_dofs, s, len < 0 ? n_dofs : len);
 }
 cudaError_t launch_reduce_moments_pairs(const df64* psi, const double* d2m_t, double* phi, int n_dir,
-                                        int n_mom, long n_dofs, cudaStream_t s) {
-  return reduce_df64_any<df64>(psi, d2m_t, phi, n_dir, n_mom, n_dofs, s);
+                                        int n_mom, long n_dofs, cudaStream_t s, long len) {
+  return reduce_df64_any<df64>(psi, d2m_t, phi, n_dir, n_mom, n_dofs, s, len < 0 ? n_dofs : len);
 }
 
 template <typename real>
 cudaError_t launch_expand_source(const real* T, const real* iso, const real* m2d, real* q,
-                                 int n_dir, int n_mom, long n_dofs, cudaStream_t s) {
+                                 int n_dir, int n_mom, long n_dofs, cudaStream_t s, long len) {
+  if (len < 0) len = n_dofs;
   // moments in chunks of at most 16 (Galerkin sets have n_mom = n_dir)
   for (int m0 = 0; m0 < n_mom; m0 += 16) {
     const int nm = n_mom - m0 < 16 ? n_mom - m0 : 16;
@@ -553,45 +569,46 @@ cudaError_t launch_expand_source(const real* T, const real* iso, const real* m2d
     const int acc = m0 > 0;
     const real* is = m0 == 0 ? iso : nullptr;
     if (nm <= 4)
-      expand_kernel<real, 4><<<resident_grid(expand_kernel<real, 4>, n_dofs, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+      expand_kernel<real, 4><<<resident_grid(expand_kernel<real, 4>, len, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, len, acc);
     else if (nm <= 10)
-      expand_kernel<real, 10><<<resident_grid(expand_kernel<real, 10>, n_dofs, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+      expand_kernel<real, 10><<<resident_grid(expand_kernel<real, 10>, len, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, len, acc);
     else
-      expand_kernel<real, 16><<<resident_grid(expand_kernel<real, 16>, n_dofs, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, acc);
+      expand_kernel<real, 16><<<resident_grid(expand_kernel<real, 16>, len, sh), kBlock, sh, s>>>(Tm, is, m2d + m0, n_mom, q, n_dir, nm, n_dofs, len, acc);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 template cudaError_t launch_expand_source<double>(const double*, const double*, const double*,
-                                                  double*, int, int, long, cudaStream_t);
+                                                  double*, int, int, long, cudaStream_t, long);
 template cudaError_t launch_expand_source<float>(const float*, const float*, const float*, float*,
-                                                 int, int, long, cudaStream_t);
+                                                 int, int, long, cudaStream_t, long);
 
 template <typename real>
 cudaError_t launch_reduce_moments(const real* psi, const real* d2m_t, real* phi, int n_dir,
-                                  int n_mom, long n_dofs, cudaStream_t s) {
+                                  int n_mom, long n_dofs, cudaStream_t s, long len) {
+  if (len < 0) len = n_dofs;
   for (int m0 = 0; m0 < n_mom; m0 += 16) {
     const int nm = n_mom - m0 < 16 ? n_mom - m0 : 16;
     const size_t sh = sizeof(real) * (size_t)n_dir * nm;
     real* ph = phi + (size_t)m0 * n_dofs;
     if (nm <= 1)
-      reduce_kernel<real, 1><<<resident_grid(reduce_kernel<real, 1>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_kernel<real, 1><<<resident_grid(reduce_kernel<real, 1>, len, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs, len);
     else if (nm <= 4)
-      reduce_kernel<real, 4><<<resident_grid(reduce_kernel<real, 4>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_kernel<real, 4><<<resident_grid(reduce_kernel<real, 4>, len, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs, len);
     else if (nm <= 10)
-      reduce_kernel<real, 10><<<resident_grid(reduce_kernel<real, 10>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_kernel<real, 10><<<resident_grid(reduce_kernel<real, 10>, len, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs, len);
     else
-      reduce_kernel<real, 16><<<resident_grid(reduce_kernel<real, 16>, n_dofs, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs);
+      reduce_kernel<real, 16><<<resident_grid(reduce_kernel<real, 16>, len, sh), kBlock, sh, s>>>(psi, d2m_t + m0, n_mom, ph, n_dir, nm, n_dofs, len);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 template cudaError_t launch_reduce_moments<double>(const double*, const double*, double*, int, int,
-                                                   long, cudaStream_t);
+                                                   long, cudaStream_t, long);
 template cudaError_t launch_reduce_moments<float>(const float*, const float*, float*, int, int,
-                                                  long, cudaStream_t);
+                                                  long, cudaStream_t, long);
 
 template <typename real>
 cudaError_t launch_scatter_source(const double* x, const double* gf, real* src,
@@ -635,6 +652,16 @@ cudaError_t launch_combine(const double* x, const real* phi, double* y, long len
   combine_kernel<real><<<grid_for(len), kBlock, 0, s>>>(x, phi, y, len, sx, sp);
   return cudaGetLastError();
 }
+template <typename real>
+cudaError_t launch_combine_rows(const double* x, const real* phi, double* y, int rows, long len, long stride,
+                                double sx, double sp, cudaStream_t s) {
+  combine_rows_kernel<real><<<grid_for((long)rows * len), kBlock, 0, s>>>(x, phi, y, rows, len, stride, sx, sp);
+  return cudaGetLastError();
+}
+template cudaError_t launch_combine_rows<double>(const double*, const double*, double*, int, long, long, double,
+                                                 double, cudaStream_t);
+template cudaError_t launch_combine_rows<float>(const double*, const float*, double*, int, long, long, double,
+                                                double, cudaStream_t);
 template cudaError_t launch_combine<double>(const double*, const double*, double*, long, double,
                                             double, cudaStream_t);
 template cudaError_t launch_combine<float>(const double*, const float*, double*, long, double,
