@@ -313,6 +313,10 @@ int ouranos_batch_set_graphs(ouranos_batch* b, int enable);
  * ouranos_batch_solve uses it when OURANOS_SOLVER_DSA is OR'ed into `inner`
  * (FGMRES with each problem's diffusion correction as right preconditioner) */
 int ouranos_batch_set_dsa(ouranos_batch* b, int cg_iterations);
+/* z = P x for every member (concatenated layout, host or device pointers):
+ * each member's diffusion correction, all members' CG solves in one
+ * cooperative launch (the form OURANOS_SOLVER_DSA batch solves use). */
+int ouranos_batch_dsa_apply(ouranos_batch* b, const double* x, double* z);
 /* device time of the last batched sweep launches, graph launches so far */
 int ouranos_batch_stats(const ouranos_batch* b, double* last_sweep_ms, int* graph_launches);
 int ouranos_batch_last_error(const ouranos_batch* b, char* buf, size_t len);

@@ -47,6 +47,7 @@ EXPORTS = [
     "ouranos_rt_set_time_step", "ouranos_rt_set_source", "ouranos_rt_time_advance",
     "ouranos_rt_get_angular_flux", "ouranos_rt_set_angular_flux",
     "ouranos_rt_set_dsa", "ouranos_rt_dsa_apply", "ouranos_solve_multigroup", "ouranos_batch_set_dsa",
+    "ouranos_batch_dsa_apply",
 ]
 
 
@@ -138,6 +139,7 @@ def lib():
         "ouranos_rt_dsa_apply": [vp, vp, vp],
         "ouranos_solve_multigroup": [vp, i, i, i, d, i, d, vp, C.POINTER(MultigroupInfo)],
         "ouranos_batch_set_dsa": [vp, i],
+        "ouranos_batch_dsa_apply": [vp, vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

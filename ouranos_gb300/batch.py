@@ -93,6 +93,13 @@ class Batch:
         """Diffusion synthetic acceleration on every problem (0 switches it off)."""
         self._check(_capi.lib().ouranos_batch_set_dsa(self._h, int(cg_iterations)))
 
+    def dsa_apply(self, x, out=None):
+        """z = P x for every problem (its diffusion correction), all problems'
+        CG solves in one launch."""
+        z = self._out(x) if out is None else out
+        self._check(_capi.lib().ouranos_batch_dsa_apply(self._h, _ptr(x), _ptr(z)))
+        return z
+
     def solve(self, inner="fp32", tol=1e-8, max_it=2000, restart=30, out=None, dsa=False):
         """Restarted GMRES on all problems at once; dsa=True: FGMRES with each
         problem's diffusion correction (set_dsa) as right preconditioner."""

@@ -77,6 +77,7 @@ struct ouranos_batch {
   bool use_graphs = true;
   int graph_launches = 0;
   double last_ms = 0.0;
+  DsaBatchScratch dsa;  // the members' diffusion solves in one launch
 };
 
 namespace {
@@ -271,7 +272,7 @@ int check_status(ouranos_batch* b) {
   if (cudaEventElapsedTime(&ms, b->ev0, b->ev1) == cudaSuccess) b->last_ms = ms;
   else cudaGetLastError();  // not recorded yet: leave no error for the next launch check
   if (st) {
-    b->err = "sweep dependency wait timed out";
+    b->err = (st & 2) ? "diffusion acceleration: grid barrier wait timed out" : "sweep dependency wait timed out";
     return OURANOS_ERR_TIMEOUT;
   }
   return OURANOS_OK;
@@ -637,13 +638,23 @@ int batch_solve(ouranos_batch* b, int inner, bool dsa, int m, int max_it, double
     }
     if (!any_i && !any_r) break;
     if (any_i) {  // one Arnoldi step: w = A v_k (or A P v_k) in the inner precision, orthogonalised
+      if (dsa) {  // z_k = P v_k: every iterating member's diffusion correction, one launch
+        std::vector<ouranos_rt*> rts;
+        std::vector<const double*> vin;
+        std::vector<double*> zout;
+        for (int p = 0; p < P; ++p)
+          if (mi[p]) {
+            rts.push_back(b->rt[p]);
+            vin.push_back(S[p].V[S[p].k]);
+            zout.push_back(S[p].Z[S[p].k]);
+          }
+        const int rc = rt_dsa_apply_batch(rts.data(), vin.data(), zout.data(), (int)rts.size(), b->stream,
+                                          b->d_ctrl.as<int>() + kStatus, b->dsa, b->err);
+        if (rc) return rc;
+      }
       for (int p = 0; p < P; ++p)
         if (mi[p]) {
-          const double* in = S[p].V[S[p].k];
-          if (dsa) {  // z_k = P v_k: the member's diffusion correction (on the batch stream)
-            BR(member(b, p, rt_dsa_apply(b->rt[p], in, S[p].Z[S[p].k])));
-            in = S[p].Z[S[p].k];
-          }
+          const double* in = dsa ? S[p].Z[S[p].k] : S[p].V[S[p].k];
           BC(cudaMemcpyAsync(X + b->off[p], in, sizeof(double) * S[p].len, cudaMemcpyDeviceToDevice, b->stream),
              "arnoldi");
         }
@@ -727,6 +738,29 @@ int ouranos_batch_set_dsa(ouranos_batch* b, int cg_iterations) {
   cudaSetDevice(b->device);
   for (size_t p = 0; p < b->rt.size(); ++p) BR(member(b, (int)p, ouranos_rt_set_dsa(b->rt[p], cg_iterations)));
   return OURANOS_OK;
+}
+
+// z = P x for every member (concatenated layout, host or device): each
+// member's diffusion correction, all in one cooperative launch
+int ouranos_batch_dsa_apply(ouranos_batch* b, const double* x, double* z) {
+  if (!b || !x || !z) return OURANOS_ERR_BAD_INPUT;
+  for (ouranos_rt* r : b->rt)
+    if (r->dsa_iters < 1) return bbad(b, "diffusion acceleration is off (ouranos_batch_set_dsa)");
+  cudaSetDevice(b->device);
+  BR(order_after_caller(b));
+  BR(copy_in(b, x));
+  const int P = (int)b->rt.size();
+  std::vector<const double*> vin(P);
+  std::vector<double*> zout(P);
+  for (int p = 0; p < P; ++p) {
+    vin[p] = b->d_X.as<double>() + b->off[p];
+    zout[p] = b->d_Y.as<double>() + b->off[p];
+  }
+  const int rc = rt_dsa_apply_batch(b->rt.data(), vin.data(), zout.data(), P, b->stream,
+                                    b->d_ctrl.as<int>() + kStatus, b->dsa, b->err);
+  if (rc) return rc;
+  BR(copy_out(b, z));
+  return check_status(b);
 }
 
 // Restarted GMRES on every problem of the batch at once (right-hand side from

@@ -193,12 +193,12 @@ __device__ __forceinline__ double block_sum(double t) {
   return t;
 }
 
-// Sum of the per-block partials of a phase, in block order (every block gets
-// the same value).
-__device__ __forceinline__ double all_sum(const double* part) {
+// Sum of the nb per-block partials of a phase, in block order (every block
+// of the problem gets the same value).
+__device__ __forceinline__ double all_sum(const double* part, int nb) {
   __shared__ double total;
   double u = 0.0;
-  for (unsigned i = threadIdx.x; i < gridDim.x; i += kCgThreads) u += part[i];
+  for (int i = threadIdx.x; i < nb; i += kCgThreads) u += part[i];
   u = block_sum(u);
   if (threadIdx.x == 0) total = u;
   __syncthreads();
@@ -312,22 +312,23 @@ __device__ __forceinline__ float assemble_rhs(const DsaGeom& g, const float4* __
   return acc;
 }
 
-// The whole preconditioner in one cooperative launch: assemble the right-hand
-// side, `iters` Jacobi-CG steps, and out = v + f on the scalar moment's nodes.
-// Each thread owns the same vertices (grid stride) in every phase, so its own
-// x, r, p, q need no synchronisation; z of the neighbours and the partials
-// cross blocks, and the barrier's release/acquire fences order them (plain
-// loads after it see every write made before it).  Dot products: FP32 per
-// thread, FP64 from the block sums on.
+// The whole preconditioner of one problem: assemble the right-hand side,
+// `iters` Jacobi-CG steps, and out = v + f on the scalar moment's nodes, run
+// by the nb blocks lb = 0..nb-1 of a cooperative launch (the whole grid for
+// one problem, a slice of it in a batch).  Each thread owns the same vertices
+// (stride over the problem's blocks) in every phase, so its own x, r, p, q
+// need no synchronisation; z of the neighbours and the partials cross
+// blocks, and the barrier's release/acquire fences order them (plain loads
+// after it see every write made before it).  Every block of the grid passes
+// the same 2 iters grid barriers.  Dot products: FP32 per thread, FP64 from
+// the block sums on; part_a/part_b hold the problem's nb partials.
 template <int DIM>
-__global__ void __launch_bounds__(kCgThreads, 1) dsa_cg_kernel(DsaGeom g, const float4* __restrict__ cell,
-                                                          const float* __restrict__ coef, const double* v,
-                                                          double* out, long len, long n0,
-                                                          const float* __restrict__ dinv, float* x, float* r,
-                                                          float* z, float* p, float* q, double* part_a,
-                                                          double* part_b, DsaSync* sync, int* status,
-                                                          long long limit_ns, int iters,
-                                                          const float* __restrict__ fe, int n) {
+__device__ __forceinline__ void cg_body(const DsaGeom& g, const float4* __restrict__ cell,
+                                        const float* __restrict__ coef, const double* v, double* out, long len,
+                                        long n0, const float* __restrict__ dinv, float* x, float* r, float* z,
+                                        float* p, float* q, double* part_a, double* part_b, int lb, int nb,
+                                        DsaSync* sync, int* status, long long limit_ns, int iters,
+                                        const float* __restrict__ fe, int n) {
   constexpr int NCORNER = DIM == 3 ? 8 : 4;
   // the cell tables: mixed mass [corner][n] (measure folded in), then the
   // interpolation of the vertex values at the nodes [n][corner]
@@ -337,8 +338,8 @@ __global__ void __launch_bounds__(kCgThreads, 1) dsa_cg_kernel(DsaGeom g, const 
     sipl[k] = fe[NCORNER * n + k];
   }
   __syncthreads();
-  const int stride = gridDim.x * kCgThreads;
-  const int first = blockIdx.x * kCgThreads + threadIdx.x;
+  const int stride = nb * kCgThreads;
+  const int first = lb * kCgThreads + threadIdx.x;
   // r = rhs, z = r / diag, x = 0
   float t = 0.f;
   for (int vid = first; vid < g.nv; vid += stride) {
@@ -352,9 +353,9 @@ __global__ void __launch_bounds__(kCgThreads, 1) dsa_cg_kernel(DsaGeom g, const 
     t += rr * zz;
   }
   double bt = block_sum(t);
-  if (threadIdx.x == 0) part_b[blockIdx.x] = bt;
+  if (threadIdx.x == 0) part_b[lb] = bt;
   if (!grid_barrier(sync, status, limit_ns)) return;
-  double rz = all_sum(part_b), beta = 0.0, alpha = 0.0;
+  double rz = all_sum(part_b, nb), beta = 0.0, alpha = 0.0;
   for (int it = 0; it < iters; ++it) {
     // w = C z; p = z + beta p; q = w + beta q
     const float fb = (float)beta;
@@ -373,9 +374,9 @@ __global__ void __launch_bounds__(kCgThreads, 1) dsa_cg_kernel(DsaGeom g, const 
       t += pn * qn;
     }
     bt = block_sum(t);
-    if (threadIdx.x == 0) part_a[blockIdx.x] = bt;
+    if (threadIdx.x == 0) part_a[lb] = bt;
     if (!grid_barrier(sync, status, limit_ns)) return;
-    const double pq = all_sum(part_a);
+    const double pq = all_sum(part_a, nb);
     alpha = pq > 0.0 ? rz / pq : 0.0;
     if (it == iters - 1) break;  // the last update folds into the output
     // x += alpha p; r -= alpha q; z = r / diag
@@ -390,9 +391,9 @@ __global__ void __launch_bounds__(kCgThreads, 1) dsa_cg_kernel(DsaGeom g, const 
       t += rn * zn;
     }
     bt = block_sum(t);
-    if (threadIdx.x == 0) part_b[blockIdx.x] = bt;
+    if (threadIdx.x == 0) part_b[lb] = bt;
     if (!grid_barrier(sync, status, limit_ns)) return;
-    const double rzn = all_sum(part_b);
+    const double rzn = all_sum(part_b, nb);
     beta = rz > 0.0 ? rzn / rz : 0.0;
     rz = rzn;
   }
@@ -424,6 +425,51 @@ __global__ void __launch_bounds__(kCgThreads, 1) dsa_cg_kernel(DsaGeom g, const 
     }
     out[e] = val;
   }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kCgThreads, 1) dsa_cg_kernel(DsaGeom g, const float4* __restrict__ cell,
+                                                          const float* __restrict__ coef, const double* v,
+                                                          double* out, long len, long n0,
+                                                          const float* __restrict__ dinv, float* x, float* r,
+                                                          float* z, float* p, float* q, double* part_a,
+                                                          double* part_b, DsaSync* sync, int* status,
+                                                          long long limit_ns, int iters,
+                                                          const float* __restrict__ fe, int n) {
+  cg_body<DIM>(g, cell, coef, v, out, len, n0, dinv, x, r, z, p, q, part_a, part_b, (int)blockIdx.x,
+               (int)gridDim.x, sync, status, limit_ns, iters, fe, n);
+}
+
+// One problem of a batched diffusion solve: its tables, vectors and the
+// blocks [block0, block0 + nblk) of the batched grid
+struct DsaProb {
+  DsaGeom g;
+  const float4* cell;
+  const float* coef;
+  const float* dinv;
+  float *x, *r, *z, *p, *q;
+  const float* fe;
+  const double* v;
+  double* out;
+  long len, n0;
+  int n, block0, nblk;
+};
+
+// Every problem of a batch in one cooperative launch: block b works on
+// problem block_prob[b]; all problems run the same number of CG steps, so
+// all blocks meet at the same grid barriers.  part_a/part_b: one partial per
+// block of the grid, each problem using its slice.
+template <int DIM>
+__global__ void __launch_bounds__(kCgThreads, 1) dsa_cg_batch_kernel(const DsaProb* __restrict__ probs,
+                                                                const int* __restrict__ block_prob,
+                                                                double* part_a, double* part_b, DsaSync* sync,
+                                                                int* status, long long limit_ns, int iters) {
+  __shared__ DsaProb P;
+  if (threadIdx.x == 0) P = probs[block_prob[blockIdx.x]];
+  __syncthreads();
+  const int lb = (int)blockIdx.x - P.block0;
+  cg_body<DIM>(P.g, P.cell, P.coef, P.v, P.out, P.len, P.n0, P.dinv, P.x, P.r, P.z, P.p, P.q,
+               part_a + P.block0, part_b + P.block0, lb, P.nblk, sync, status, limit_ns, iters, P.fe, P.n);
 }
 
 int dfail(ouranos_rt* rt, cudaError_t e, const char* what) {
@@ -633,9 +679,151 @@ int dsa_run(ouranos_rt* rt, const double* v, double* out, int iters) {
   return OURANOS_OK;
 }
 
+// One batched launch of the problems idx[0..count) (same mesh dimension DIM,
+// count <= the cooperative grid's capacity).  Blocks go to the problems by
+// their vertex counts: every problem gets one, then each further block goes to
+// the problem with the most vertices per block, up to one vertex per thread.
+template <int DIM>
+int dsa_batch_launch(ouranos_rt* const* rts, const double* const* v, double* const* out, const int* idx, int count,
+                     cudaStream_t stream, int* status, DsaBatchScratch& sc, int grid_cap, std::string& err) {
+  std::vector<int> nblk(count, 1);
+  std::vector<long> nv(count);
+  for (int i = 0; i < count; ++i) nv[i] = geom(rts[idx[i]]).nv;
+  int total = count;
+  while (total < grid_cap) {
+    int best = -1;
+    double work = 0.0;
+    for (int i = 0; i < count; ++i) {
+      const double w = (double)nv[i] / nblk[i];
+      if (nblk[i] * (long)kCgThreads < nv[i] && w > work) {
+        work = w;
+        best = i;
+      }
+    }
+    if (best < 0) break;
+    ++nblk[best];
+    ++total;
+  }
+  const size_t probs_bytes = (sizeof(DsaProb) * count + 15) / 16 * 16;
+  const size_t map_bytes = (sizeof(int) * total + 15) / 16 * 16;
+  const size_t host_bytes = probs_bytes + map_bytes;
+  const size_t dev_bytes = host_bytes + sizeof(double) * 2 * total + sizeof(DsaSync);
+  if (sc.dev.alloc(dev_bytes) != cudaSuccess) {
+    err = "diffusion acceleration: batch scratch allocation failed";
+    return OURANOS_ERR_CUDA;
+  }
+  if (sc.host_bytes < host_bytes) {
+    if (sc.host) cudaFreeHost(sc.host);
+    sc.host = nullptr;
+    sc.host_bytes = 0;
+    if (cudaMallocHost(&sc.host, host_bytes) != cudaSuccess) {
+      err = "diffusion acceleration: batch staging allocation failed";
+      return OURANOS_ERR_CUDA;
+    }
+    sc.host_bytes = host_bytes;
+  }
+  DsaProb* hp = reinterpret_cast<DsaProb*>(sc.host);
+  int* hmap = reinterpret_cast<int*>(static_cast<char*>(sc.host) + probs_bytes);
+  int b0 = 0;
+  for (int i = 0; i < count; ++i) {
+    ouranos_rt* rt = rts[idx[i]];
+    DsaProb& P = hp[i];
+    P.g = geom(rt);
+    const long n = P.g.nv;
+    float* base = rt->d_dsa_vec.as<float>();
+    P.x = base;
+    P.r = base + n;
+    P.p = base + 2 * n;
+    P.q = base + 3 * n;
+    P.dinv = base + 4 * n;
+    P.z = base + 5 * n + halo(P.g);
+    P.cell = rt->d_dsa_cell.as<float4>();
+    P.coef = rt->d_dsa_coef.as<float>();
+    P.fe = rt->d_dsa_fe.as<float>();
+    P.v = v[idx[i]];
+    P.out = out[idx[i]];
+    P.len = (long)rt->n_mom * rt->n_dofs;
+    P.n0 = rt->n_cells * (long)rt->n;
+    P.n = rt->n;
+    P.block0 = b0;
+    P.nblk = nblk[i];
+    for (int k = 0; k < nblk[i]; ++k) hmap[b0 + k] = i;
+    b0 += nblk[i];
+  }
+  char* dbase = sc.dev.as<char>();
+  const DsaProb* dprobs = reinterpret_cast<const DsaProb*>(dbase);
+  const int* dmap = reinterpret_cast<const int*>(dbase + probs_bytes);
+  double* part_a = reinterpret_cast<double*>(dbase + host_bytes);
+  double* part_b = part_a + total;
+  DsaSync* sync = reinterpret_cast<DsaSync*>(part_b + total);
+  // the staging block is rewritten by the next call only after the caller has
+  // synchronised the stream (one batched application per solver step)
+  cudaError_t e = cudaMemcpyAsync(dbase, sc.host, host_bytes, cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(sync, 0, sizeof(DsaSync), stream);
+  long long limit = rts[idx[0]]->wait_limit_ns;
+  int iters = rts[idx[0]]->dsa_iters;
+  void* args[] = {&dprobs, &dmap, &part_a, &part_b, &sync, &status, &limit, &iters};
+  if (e == cudaSuccess)
+    e = cudaLaunchCooperativeKernel((const void*)dsa_cg_batch_kernel<DIM>, dim3(total), dim3(kCgThreads), args, 0,
+                                    stream);
+  if (e != cudaSuccess) {
+    err = std::string("diffusion acceleration, batched solve: ") + cudaGetErrorString(e);
+    return OURANOS_ERR_CUDA;
+  }
+  return OURANOS_OK;
+}
+
 }  // namespace
 
 namespace ouranos {
+DsaBatchScratch::~DsaBatchScratch() {
+  if (host) cudaFreeHost(host);
+}
+
+int rt_dsa_apply_batch(ouranos_rt* const* rts, const double* const* v, double* const* out, int count,
+                       cudaStream_t stream, int* status, DsaBatchScratch& sc, std::string& err) {
+  if (count <= 0) return OURANOS_OK;
+  const int iters = rts[0]->dsa_iters;
+  for (int i = 0; i < count; ++i) {
+    if (rts[i]->dsa_iters < 1 || rts[i]->dsa_iters != iters) {
+      err = "diffusion acceleration: every problem of a batch needs the same CG step count (>= 1)";
+      return OURANOS_ERR_BAD_INPUT;
+    }
+    const int rc = ensure_tables(rts[i]);
+    if (rc) {
+      err = rts[i]->err;
+      return rc;
+    }
+  }
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, rts[0]->device) != cudaSuccess) {
+    err = "diffusion acceleration: device query failed";
+    return OURANOS_ERR_CUDA;
+  }
+  for (int dim = 2; dim <= 3; ++dim) {
+    int per_sm = 0;
+    const cudaError_t e =
+        dim == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dsa_cg_batch_kernel<3>, kCgThreads, 0)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dsa_cg_batch_kernel<2>, kCgThreads, 0);
+    if (e != cudaSuccess || per_sm < 1) {
+      err = "diffusion acceleration: the batched CG kernel does not fit on a multiprocessor";
+      return OURANOS_ERR_CUDA;
+    }
+    // one block per multiprocessor keeps the grid barrier to a few participants
+    const int cap = sms;
+    std::vector<int> idx;
+    for (int i = 0; i < count; ++i)
+      if (rts[i]->dim == dim) idx.push_back(i);
+    for (size_t s0 = 0; s0 < idx.size(); s0 += cap) {  // at most one block per problem and SM per launch
+      const int cnt = (int)std::min<size_t>(cap, idx.size() - s0);
+      const int rc = dim == 3 ? dsa_batch_launch<3>(rts, v, out, idx.data() + s0, cnt, stream, status, sc, cap, err)
+                              : dsa_batch_launch<2>(rts, v, out, idx.data() + s0, cnt, stream, status, sc, cap, err);
+      if (rc) return rc;
+    }
+  }
+  return OURANOS_OK;
+}
+
 // out = P v on the handle's stream (device vectors, internal cell order);
 // out may equal v
 int rt_dsa_apply(ouranos_rt* rt, const double* v, double* out) {

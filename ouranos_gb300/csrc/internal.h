@@ -266,6 +266,21 @@ int rt_batch_prepare(ouranos_rt* rt, const double* x, SweepArgs<double>* a, int*
 int rt_batch_prepare(ouranos_rt* rt, const double* x, SweepArgs<float>* a, int* fm, bool sources);
 int rt_batch_finish(ouranos_rt* rt, const double* x, double* y, bool sources);
 int rt_clear_status(ouranos_rt* rt);
+// Scratch of the batched diffusion solve: the device problem table, block
+// map, partials and barrier, and the page-locked staging of the table.
+struct DsaBatchScratch {
+  DevBuf dev;
+  void* host = nullptr;
+  size_t host_bytes = 0;
+  ~DsaBatchScratch();
+};
+// out[i] = P_i v[i] for the problems rts[0..count) (device vectors, internal
+// cell order) in one cooperative launch per mesh dimension on `stream`; a
+// barrier wait that runs out sets bit 2 of *status.  Every problem must have
+// the same CG step count.  One call per stream synchronisation (the staging
+// block is reused).
+int rt_dsa_apply_batch(ouranos_rt* const* rts, const double* const* v, double* const* out, int count,
+                       cudaStream_t stream, int* status, DsaBatchScratch& sc, std::string& err);
 int rt_stage_in(ouranos_rt* rt, const double* v, DevBuf& buf, int n_vec, const double** out);
 int rt_stage_out(ouranos_rt* rt, const double* dv, double* user);
 }  // namespace ouranos

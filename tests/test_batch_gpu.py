@@ -112,6 +112,28 @@ def test_batched_solve_with_dsa():
         assert sum(i["iterations"] for i in infos) < sum(i["iterations"] for i in i0)
 
 
+@pytest.mark.parametrize("steps", [1, 15])
+def test_batched_dsa_matches_each_problems_own(steps):
+    """All members' diffusion corrections in one cooperative launch (blocks
+    split over the problems by vertex count) against each problem's own
+    single-problem launch: the same CG in FP32 with FP64 scalars, only the
+    order of the partial sums differs."""
+    import ouranos_gb300 as og
+    probs = _problems(count=5, seed=47)
+    with og.Batch(probs) as b:
+        b.set_dsa(steps)
+        x = np.random.default_rng(6).standard_normal(b.length)
+        z = b.dsa_apply(x)
+        for p, xs, zs in zip(probs, b.slices(x), b.slices(z)):
+            with og.RadiativeTransfer(p) as rt:
+                rt.set_dsa(steps)
+                zr = rt.dsa_apply(np.ascontiguousarray(xs))
+            # the correction itself (z - x), relative to its own size
+            assert rel_err(zs - xs, zr - xs) < 1e-4
+            n0 = p.total_cells * p.dofs_per_cell
+            assert np.array_equal(zs[n0:], xs[n0:])  # higher moments pass unchanged
+
+
 def test_autotune_keeps_results_and_reports_tilings():
     import ouranos_gb300 as og
     probs = _problems(count=4, seed=41)
