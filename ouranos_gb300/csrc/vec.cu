@@ -146,9 +146,23 @@ __global__ void permute_kernel(const double* in, double* out, const long* order,
   }
 }
 
-// w += scale * sum_j coef[j] V_j  (coef on the device)
 // w += scale * sum_j coef[j] V[j]; pointers and coefficients staged in shared
-// memory, the sum split over four accumulators so the k loads overlap
+// memory.  GB300's FP64 pipe runs at 1/64 of the FP32 rate and binds these
+// FP64 vector kernels, so they issue exactly k multiply-adds per element: the
+// k vectors go in chunks of 8, 4, 2 and 1 (a predicated-off multiply-add of a
+// wider unrolled loop still takes its FP64 issue slot).  Fixed order, so the
+// result is deterministic.
+template <int W>
+__device__ __forceinline__ double axpy_chunk(const double* const* sv, const double* sc, int j0, long e) {
+  double a0 = 0.0, a1 = 0.0;
+#pragma unroll
+  for (int jj = 0; jj < W; ++jj) {
+    const double t = sc[j0 + jj] * __ldg(sv[j0 + jj] + e);
+    if (jj & 1) a1 += t;
+    else a0 += t;
+  }
+  return a0 + a1;
+}
 template <int KMAX>
 __global__ void multi_axpy_kernel(const double* const* V, int k, const double* coef, double scale,
                                   double* w, long len) {
@@ -161,11 +175,19 @@ __global__ void multi_axpy_kernel(const double* const* V, int k, const double* c
   __syncthreads();
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len;
        e += (long)gridDim.x * blockDim.x) {
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll
-    for (int j = 0; j < KMAX; ++j)
-      if (j < k) acc[j & 3] += sc[j] * __ldg(sv[j] + e);
-    w[e] += (acc[0] + acc[1]) + (acc[2] + acc[3]);
+    double acc = 0.0;
+    int j0 = 0;
+    for (; j0 + 8 <= k; j0 += 8) acc += axpy_chunk<8>(sv, sc, j0, e);
+    if (j0 + 4 <= k) {
+      acc += axpy_chunk<4>(sv, sc, j0, e);
+      j0 += 4;
+    }
+    if (j0 + 2 <= k) {
+      acc += axpy_chunk<2>(sv, sc, j0, e);
+      j0 += 2;
+    }
+    if (j0 < k) acc += axpy_chunk<1>(sv, sc, j0, e);
+    w[e] += acc;
   }
 }
 
@@ -177,42 +199,54 @@ __global__ void axpby_kernel(double a, const double* x, double b, double* y, lon
 
 // out[j] = sum_i xs[j][i] * y[i], j < k, in two launches.  Block b reduces its
 // grid-stride slice into partial[j * gridDim.x + b], taking the vectors in
-// chunks of 8 (8 accumulators and 8 loads in flight per element; y is re-read
-// once per chunk); then one warp per output sums the partials in a fixed order
-// (deterministic, no atomics).
+// chunks of 8, 4, 2 and 1 (W accumulators and W + 1 loads in flight per
+// element, y re-read once per chunk; exactly k FP64 multiply-adds per element,
+// see multi_axpy_kernel); then one warp per output sums the partials in a
+// fixed order (deterministic, no atomics).
 constexpr int kDotChunk = 8;
+template <int W>
+__device__ __forceinline__ void dots_chunk(const double* const* sx, const double* y, int j0, long len,
+                                           double* partial, double (*red)[kBlock / 32]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double acc[W];
+#pragma unroll
+  for (int jj = 0; jj < W; ++jj) acc[jj] = 0.0;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len; e += (long)gridDim.x * blockDim.x) {
+    const double yv = __ldg(y + e);
+#pragma unroll
+    for (int jj = 0; jj < W; ++jj) acc[jj] += __ldg(sx[j0 + jj] + e) * yv;
+  }
+#pragma unroll
+  for (int jj = 0; jj < W; ++jj) {
+    double v = acc[jj];
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[jj][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < W) {
+    double v = 0.0;
+    for (int w = 0; w < kBlock / 32; ++w) v += red[threadIdx.x][w];
+    partial[(size_t)(j0 + threadIdx.x) * gridDim.x + blockIdx.x] = v;
+  }
+  __syncthreads();
+}
 __global__ void __launch_bounds__(kBlock) dots_partial_kernel(const double* const* xs, const double* y, int k,
                                                               long len, double* partial) {
   __shared__ const double* sx[32];
   __shared__ double red[kDotChunk][kBlock / 32];
   for (int j = threadIdx.x; j < 32; j += blockDim.x) sx[j] = j < k ? xs[j] : nullptr;
   __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int j0 = 0; j0 < k; j0 += kDotChunk) {
-    double acc[kDotChunk];
-#pragma unroll
-    for (int jj = 0; jj < kDotChunk; ++jj) acc[jj] = 0.0;
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < len;
-         e += (long)gridDim.x * blockDim.x) {
-      const double yv = __ldg(y + e);
-#pragma unroll
-      for (int jj = 0; jj < kDotChunk; ++jj)
-        if (j0 + jj < k) acc[jj] += __ldg(sx[j0 + jj] + e) * yv;
-    }
-#pragma unroll
-    for (int jj = 0; jj < kDotChunk; ++jj) {
-      double v = acc[jj];
-      for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) red[jj][warp] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < kDotChunk && j0 + (int)threadIdx.x < k) {
-      double v = 0.0;
-      for (int w = 0; w < kBlock / 32; ++w) v += red[threadIdx.x][w];
-      partial[(size_t)(j0 + threadIdx.x) * gridDim.x + blockIdx.x] = v;
-    }
-    __syncthreads();
+  int j0 = 0;
+  for (; j0 + 8 <= k; j0 += 8) dots_chunk<8>(sx, y, j0, len, partial, red);
+  if (j0 + 4 <= k) {
+    dots_chunk<4>(sx, y, j0, len, partial, red);
+    j0 += 4;
   }
+  if (j0 + 2 <= k) {
+    dots_chunk<2>(sx, y, j0, len, partial, red);
+    j0 += 2;
+  }
+  if (j0 < k) dots_chunk<1>(sx, y, j0, len, partial, red);
 }
 __global__ void __launch_bounds__(kBlock) dots_final_kernel(const double* partial, int k, int nblocks,
                                                             double* out) {
