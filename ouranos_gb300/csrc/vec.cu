@@ -3,6 +3,7 @@
 // the Krylov drivers.  All are HBM-streaming, one grid-stride loop each.
 #include <algorithm>
 #include <mutex>
+#include <type_traits>
 #include <unordered_map>
 
 #include "df64.cuh"
@@ -644,12 +645,107 @@ template cudaError_t launch_reduce_moments<double>(const double*, const double*,
 template cudaError_t launch_reduce_moments<float>(const float*, const float*, float*, int, int,
                                                   long, cudaStream_t, long);
 
+// Arithmetic of the per-cell scattering source: FP32 for the FP32 sweep,
+// double-float for the FP64 sweep's pair storage
+template <typename real>
+struct SrcArith;
+template <>
+struct SrcArith<float> {
+  using T = float;
+  using Acc = float;
+  __device__ static T from(double v) { return (float)v; }
+  __device__ static Acc zero() { return 0.f; }
+  __device__ static void fma(Acc& a, T u, T v) { a = __fmaf_rn(u, v, a); }
+  __device__ static float out(Acc a, T sc) { return a * sc; }
+};
+template <>
+struct SrcArith<df64> {
+  using T = df64;
+  using Acc = df64_acc;
+  __device__ static T from(double v) { return df64_from(v); }
+  __device__ static Acc zero() { return acc_zero(); }
+  __device__ static void fma(Acc& a, T u, T v) { acc_fma(a, u, v); }
+  __device__ static df64 out(Acc a, T sc) {
+    df64_acc r = acc_zero();
+    acc_fma(r, acc_result(a), sc);
+    return acc_result(r);
+  }
+};
+
+// The scattering source of one (moment, cell) per thread, without
+// other-group terms: the cell's N values of x are converted once and the
+// N x N mass-matrix products run on the FP32 pipes.  (One thread per output
+// in FP64 spent N FP64 multiply-adds per value on GB300's 1/64-rate FP64
+// pipe.)  Cells are the fastest index, so a warp reads and writes 32 * N
+// consecutive values.
+template <typename real, int N>
+__global__ void __launch_bounds__(kBlock) scatter_cell_kernel(const double* __restrict__ x, real* __restrict__ src,
+                                                              const double* __restrict__ M,
+                                                              const double* __restrict__ sscale,
+                                                              const int* __restrict__ material, long n_cells,
+                                                              int n_mom, long n_dofs) {
+  using A = SrcArith<real>;
+  __shared__ typename A::T sM[N * N];
+  for (int k = threadIdx.x; k < N * N; k += blockDim.x) sM[k] = A::from(M[k]);
+  __syncthreads();
+  const long total = (long)n_mom * n_cells;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    const long c = t % n_cells;
+    const int m = (int)(t / n_cells);
+    const double* xc = x + (size_t)m * n_dofs + c * N;
+    typename A::T xv[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) xv[j] = A::from(__ldg(xc + j));
+    const typename A::T sc = A::from(__ldg(sscale + (size_t)material[c] * n_mom + m));
+    real* out = src + (size_t)m * n_dofs + c * N;
+#pragma unroll 1
+    for (int i = 0; i < N; ++i) {
+      typename A::Acc acc = A::zero();
+#pragma unroll
+      for (int j = 0; j < N; ++j) A::fma(acc, sM[i * N + j], xv[j]);
+      out[i] = A::out(acc, sc);
+    }
+  }
+}
+
+template <typename real, int N>
+static cudaError_t scatter_cell(const double* x, real* src, const double* M, const double* sscale,
+                                const int* material, long n_cells, int n_mom, long n_dofs, cudaStream_t s) {
+  long g = ((long)n_mom * n_cells + kBlock - 1) / kBlock;
+  if (g > 152L * 8) g = 152L * 8;  // each block converts the mass matrix once
+  scatter_cell_kernel<real, N><<<(int)(g < 1 ? 1 : g), kBlock, 0, s>>>(x, src, M, sscale, material, n_cells, n_mom,
+                                                                       n_dofs);
+  return cudaGetLastError();
+}
+template <typename real>
+static cudaError_t scatter_cell_any(const double* x, real* src, const double* M, const double* sscale,
+                                    const int* material, long n_cells, int n, int n_mom, long n_dofs,
+                                    cudaStream_t s, bool* done) {
+  *done = true;
+  switch (n) {
+    case 4: return scatter_cell<real, 4>(x, src, M, sscale, material, n_cells, n_mom, n_dofs, s);
+    case 8: return scatter_cell<real, 8>(x, src, M, sscale, material, n_cells, n_mom, n_dofs, s);
+    case 9: return scatter_cell<real, 9>(x, src, M, sscale, material, n_cells, n_mom, n_dofs, s);
+    case 16: return scatter_cell<real, 16>(x, src, M, sscale, material, n_cells, n_mom, n_dofs, s);
+    case 25: return scatter_cell<real, 25>(x, src, M, sscale, material, n_cells, n_mom, n_dofs, s);
+    case 27: return scatter_cell<real, 27>(x, src, M, sscale, material, n_cells, n_mom, n_dofs, s);
+    default: *done = false; return cudaSuccess;
+  }
+}
+
 template <typename real>
 cudaError_t launch_scatter_source(const double* x, const double* gf, real* src,
                                   const double* M, const double* sscale, const double* oscale,
                                   const int* material, int n_mat, int n_groups, int group,
                                   long n_cells, int n, int n_mom, long n_dofs, cudaStream_t s) {
   (void)n_mat;
+  if constexpr (!std::is_same<real, double>::value) {
+    if (x && !gf) {  // the Apply's form: per-cell kernel on the FP32 pipes
+      bool done = false;
+      const cudaError_t e = scatter_cell_any<real>(x, src, M, sscale, material, n_cells, n, n_mom, n_dofs, s, &done);
+      if (done) return e;
+    }
+  }
   scatter_source_kernel<real><<<grid_for((long)n_mom * n_cells * n), kBlock, 0, s>>>(
       x, gf, src, M, sscale, oscale, material, n_groups, group, n_cells, n, n_mom, n_dofs);
   return cudaGetLastError();
