@@ -153,6 +153,7 @@ cudaError_t launch_reduce_moments_pairs(const df64* psi, const double* d2m_t, do
 // is set.  Built on the host (operator.cu) when the quadrature has it.
 struct SymTables {
   int n_class = 0, P = 0, G = 0;
+  int pattern = 0;                    // 2 / 3: the canonical 2-D / 3-D groups (compile-time kernels), 0: other
   const int* cls_dir = nullptr;       // [n_class][P] direction of member f
   const int* mom_group = nullptr;     // [n_mom] parity group
   const unsigned* sign = nullptr;     // [G] bit f set: negative on member f
@@ -162,6 +163,9 @@ struct SymTables {
 // the double-float pair contractions through the symmetry: each class forms
 // its products once per parity group (expansion) or its signed sums of psi
 // once per group (reduction), about half the arithmetic of the direct form
+// 2 or 3 when the groups and signs are the canonical ones of the harmonic
+// moments of a 2-D (P = 4) or 3-D (P = 8) set, else 0
+int sym_canonical_pattern(int P, int nm, int G, const int* mom_group, const unsigned* sign);
 cudaError_t launch_expand_sym_pairs(const df64* T, const df64* iso, const SymTables& st, df64* q, int n_mom,
                                     long n_dofs, cudaStream_t s, long len = -1);
 cudaError_t launch_reduce_sym_pairs(const df64* psi, const SymTables& st, double* phi, int n_mom, long n_dofs,

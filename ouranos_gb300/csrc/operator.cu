@@ -180,6 +180,7 @@ int build_symmetry(ouranos_rt* rt) {
   rt->sym.n_class = nc;
   rt->sym.P = P;
   rt->sym.G = (int)group_sign.size();
+  rt->sym.pattern = sym_canonical_pattern(P, nm, rt->sym.G, mom_group.data(), group_sign.data());
   rt->sym.cls_dir = rt->d_sym_dir.as<int>();
   rt->sym.mom_group = rt->d_sym_group.as<int>();
   rt->sym.sign = rt->d_sym_sign.as<unsigned>();

@@ -432,10 +432,37 @@ __device__ __forceinline__ void load_sym(const SymTables& st, const double* rep,
 }
 __device__ __forceinline__ df64 neg_if(df64 v, bool neg) { return neg ? df64(-v.hi, -v.lo) : v; }
 
+// The parity groups of the real spherical-harmonic moments under the octant
+// reflections, in the moment order of the quadrature tables (for l, then
+// m = l..0 cosine parts, then m = 1..l sine parts), numbered by first
+// appearance; a lower scattering order uses a prefix.  PAT 2: 2-D (P = 4,
+// moments up to P3), PAT 3: 3-D (P = 8, up to P3); sign of group g on member
+// f: bit f of the group's sign word.  PAT 0: the tables' own, read at run time.
+// With PAT set, each moment's product goes to its group's accumulator and each
+// member's signs are constants once the loops are unrolled (a run-time group
+// index made the compiler predicate one multiply-add per possible group).
+__host__ __device__ constexpr int sym_group(int pat, int m) {
+  return pat == 2 ? (int)((0x12258088ull >> (3 * m)) & 7u)
+                  : (int)((0x7da28ea20688ull >> (3 * m)) & 7u);
+}
+constexpr bool sym_pattern_is(int pat, const int* g, int n) {
+  for (int m = 0; m < n; ++m)
+    if (sym_group(pat, m) != g[m]) return false;
+  return true;
+}
+constexpr int kSymGroups2[10] = {0, 1, 2, 0, 0, 3, 1, 1, 2, 2};
+constexpr int kSymGroups3[16] = {0, 1, 2, 3, 0, 4, 0, 5, 6, 1, 2, 1, 2, 3, 7, 3};
+static_assert(sym_pattern_is(2, kSymGroups2, 10) && sym_pattern_is(3, kSymGroups3, 16), "packed group tables");
+__host__ __device__ constexpr unsigned sym_sign(int pat, int g) {
+  return pat == 2 ? (g == 0 ? 0u : g == 1 ? 10u : g == 2 ? 12u : 6u)
+                  : (g == 0 ? 0u : g == 1 ? 170u : g == 2 ? 240u : g == 3 ? 204u
+                     : g == 4 ? 90u : g == 5 ? 60u : g == 6 ? 102u : 150u);
+}
+
 // q[d][e] for the P members d of each class: the class's products
 // M2D_rep[m] T_m are summed per parity group once, then each member adds the
 // group sums with its signs (+ iso)
-template <int NM, int P>
+template <int NM, int P, int PAT>
 __global__ void __launch_bounds__(256) expand_sym_kernel(const df64* __restrict__ T, const df64* __restrict__ iso,
                                                          SymTables st, df64* __restrict__ q, int nm, long n_dofs, long len) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -459,10 +486,14 @@ __global__ void __launch_bounds__(256) expand_sym_kernel(const df64* __restrict_
       for (int m = 0; m < NM; ++m) {
         if (m >= nm) break;
         const df64 r = rep[m];
-        const int grp = sgrp[m];  // the same for every thread: uniform branches
+        if (PAT) {
+          acc_fma(S[sym_group(PAT, m)], r, t[m]);
+        } else {
+          const int grp = sgrp[m];  // the same for every thread: uniform branches
 #pragma unroll
-        for (int g = 0; g < P; ++g)
-          if (grp == g) acc_fma(S[g], r, t[m]);
+          for (int g = 0; g < P; ++g)
+            if (grp == g) acc_fma(S[g], r, t[m]);
+        }
       }
       df64 sg[P];
 #pragma unroll
@@ -472,7 +503,7 @@ __global__ void __launch_bounds__(256) expand_sym_kernel(const df64* __restrict_
         df64_acc o = acc_from(is);
 #pragma unroll
         for (int g = 0; g < P; ++g)
-          if (g < G) acc_add(o, neg_if(sg[g], (ssign[g] >> f) & 1u));
+          if (g < G) acc_add(o, neg_if(sg[g], ((PAT ? sym_sign(PAT, g) : ssign[g]) >> f) & 1u));
         q[(size_t)sdir[c * P + f] * n_dofs + e] = acc_result(o);
       }
     }
@@ -481,7 +512,7 @@ __global__ void __launch_bounds__(256) expand_sym_kernel(const df64* __restrict_
 
 // phi[m][e]: each class's P values of psi are combined into one signed sum
 // per parity group, then every moment takes D2M_rep[m] times its group's sum
-template <int NM, int P>
+template <int NM, int P, int PAT>
 __global__ void __launch_bounds__(256) reduce_sym_kernel(const df64* __restrict__ psi, SymTables st,
                                                          double* __restrict__ phi, int nm, long n_dofs, long len) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -504,7 +535,7 @@ __global__ void __launch_bounds__(256) reduce_sym_kernel(const df64* __restrict_
       for (int g = 0; g < P; ++g) {
         C[g] = df64(0.f);
         if (g < G) {
-          const unsigned sg = ssign[g];
+          const unsigned sg = PAT ? sym_sign(PAT, g) : ssign[g];
           df64_acc o = acc_from(neg_if(ps[0], sg & 1u));
 #pragma unroll
           for (int f = 1; f < P; ++f) acc_add(o, neg_if(ps[f], (sg >> f) & 1u));
@@ -515,11 +546,15 @@ __global__ void __launch_bounds__(256) reduce_sym_kernel(const df64* __restrict_
 #pragma unroll
       for (int m = 0; m < NM; ++m) {
         if (m >= nm) break;
-        const int grp = sgrp[m];
         df64 cg = C[0];
+        if (PAT) {
+          cg = C[sym_group(PAT, m)];
+        } else {
+          const int grp = sgrp[m];
 #pragma unroll
-        for (int g = 1; g < P; ++g)
-          if (grp == g) cg = C[g];
+          for (int g = 1; g < P; ++g)
+            if (grp == g) cg = C[g];
+        }
         acc_fma(acc[m], rep[m], cg);
       }
     }
@@ -529,48 +564,63 @@ __global__ void __launch_bounds__(256) reduce_sym_kernel(const df64* __restrict_
   }
 }
 
-template <int P>
+template <int P, int PAT>
 cudaError_t expand_sym_any(const df64* T, const df64* iso, const SymTables& st, df64* q, int nm, long n_dofs,
                            cudaStream_t s, long len) {
   const size_t sh = sizeof(df64) * st.n_class * nm + sizeof(int) * (st.n_class * P + 16) + sizeof(unsigned) * 8;
   if (nm <= 4)
-    expand_sym_kernel<4, P><<<resident_grid(expand_sym_kernel<4, P>, len, sh), kBlock, sh, s>>>(T, iso, st, q, nm, n_dofs, len);
+    expand_sym_kernel<4, P, PAT><<<resident_grid(expand_sym_kernel<4, P, PAT>, len, sh), kBlock, sh, s>>>(T, iso, st, q, nm, n_dofs, len);
   else if (nm <= 10)
-    expand_sym_kernel<10, P><<<resident_grid(expand_sym_kernel<10, P>, len, sh), kBlock, sh, s>>>(T, iso, st, q, nm, n_dofs, len);
+    expand_sym_kernel<10, P, PAT><<<resident_grid(expand_sym_kernel<10, P, PAT>, len, sh), kBlock, sh, s>>>(T, iso, st, q, nm, n_dofs, len);
   else
-    expand_sym_kernel<16, P><<<resident_grid(expand_sym_kernel<16, P>, len, sh), kBlock, sh, s>>>(T, iso, st, q, nm, n_dofs, len);
+    expand_sym_kernel<16, P, PAT><<<resident_grid(expand_sym_kernel<16, P, PAT>, len, sh), kBlock, sh, s>>>(T, iso, st, q, nm, n_dofs, len);
   return cudaGetLastError();
 }
-template <int P>
+template <int P, int PAT>
 cudaError_t reduce_sym_any(const df64* psi, const SymTables& st, double* phi, int nm, long n_dofs, cudaStream_t s,
                            long len) {
   const size_t sh = sizeof(df64) * st.n_class * nm + sizeof(int) * (st.n_class * P + 16) + sizeof(unsigned) * 8;
   if (nm <= 1)
-    reduce_sym_kernel<1, P><<<resident_grid(reduce_sym_kernel<1, P>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
+    reduce_sym_kernel<1, P, PAT><<<resident_grid(reduce_sym_kernel<1, P, PAT>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
   else if (nm <= 4)
-    reduce_sym_kernel<4, P><<<resident_grid(reduce_sym_kernel<4, P>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
+    reduce_sym_kernel<4, P, PAT><<<resident_grid(reduce_sym_kernel<4, P, PAT>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
   else if (nm <= 10)
-    reduce_sym_kernel<10, P><<<resident_grid(reduce_sym_kernel<10, P>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
+    reduce_sym_kernel<10, P, PAT><<<resident_grid(reduce_sym_kernel<10, P, PAT>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
   else
-    reduce_sym_kernel<16, P><<<resident_grid(reduce_sym_kernel<16, P>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
+    reduce_sym_kernel<16, P, PAT><<<resident_grid(reduce_sym_kernel<16, P, PAT>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
   return cudaGetLastError();
 }
 }  // namespace
+
+// the canonical pattern (2 or 3) the tables follow for their moments, else 0
+int sym_canonical_pattern(int P, int nm, int G, const int* mom_group, const unsigned* sign) {
+  const int pat = P == 4 ? 2 : P == 8 ? 3 : 0;
+  if (!pat || nm > (pat == 2 ? 10 : 16)) return 0;
+  for (int m = 0; m < nm; ++m)
+    if (mom_group[m] != sym_group(pat, m)) return 0;
+  for (int g = 0; g < G; ++g)
+    if (sign[g] != sym_sign(pat, g)) return 0;
+  return pat;
+}
 
 cudaError_t launch_expand_sym_pairs(const df64* T, const df64* iso, const SymTables& st, df64* q, int n_mom,
                                     long n_dofs, cudaStream_t s, long len) {
   if (n_mom > 16 || st.G > st.P) return cudaErrorInvalidValue;
   if (len < 0) len = n_dofs;
-  if (st.P == 4) return expand_sym_any<4>(T, iso, st, q, n_mom, n_dofs, s, len);
-  if (st.P == 8) return expand_sym_any<8>(T, iso, st, q, n_mom, n_dofs, s, len);
+  if (st.P == 4) return st.pattern == 2 ? expand_sym_any<4, 2>(T, iso, st, q, n_mom, n_dofs, s, len)
+                                        : expand_sym_any<4, 0>(T, iso, st, q, n_mom, n_dofs, s, len);
+  if (st.P == 8) return st.pattern == 3 ? expand_sym_any<8, 3>(T, iso, st, q, n_mom, n_dofs, s, len)
+                                        : expand_sym_any<8, 0>(T, iso, st, q, n_mom, n_dofs, s, len);
   return cudaErrorInvalidValue;
 }
 cudaError_t launch_reduce_sym_pairs(const df64* psi, const SymTables& st, double* phi, int n_mom, long n_dofs,
                                     cudaStream_t s, long len) {
   if (n_mom > 16 || st.G > st.P) return cudaErrorInvalidValue;
   if (len < 0) len = n_dofs;
-  if (st.P == 4) return reduce_sym_any<4>(psi, st, phi, n_mom, n_dofs, s, len);
-  if (st.P == 8) return reduce_sym_any<8>(psi, st, phi, n_mom, n_dofs, s, len);
+  if (st.P == 4) return st.pattern == 2 ? reduce_sym_any<4, 2>(psi, st, phi, n_mom, n_dofs, s, len)
+                                        : reduce_sym_any<4, 0>(psi, st, phi, n_mom, n_dofs, s, len);
+  if (st.P == 8) return st.pattern == 3 ? reduce_sym_any<8, 3>(psi, st, phi, n_mom, n_dofs, s, len)
+                                        : reduce_sym_any<8, 0>(psi, st, phi, n_mom, n_dofs, s, len);
   return cudaErrorInvalidValue;
 }
 

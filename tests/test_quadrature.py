@@ -143,3 +143,49 @@ def test_unsupported_orders():
         og.build_quadrature("LS", 8, 0, True, 4 * np.pi, 3)  # Galerkin 3-D
     with pytest.raises(_capi.OuranosError):
         og.build_quadrature("LS", 5, 0)
+
+
+def _parity_groups(q):
+    """Moment -> parity-group map and group sign words of a quadrature under
+    the octant reflections, numbered by first appearance (the host's
+    symmetry detection restated)."""
+    dim, nd, nm = q.dim, q.n_dir, q.n_mom
+    P = 1 << dim
+    om = np.asarray(q.omega).reshape(nd, -1)
+    m2d = np.asarray(q.m2d).reshape(nd, nm)
+    key = [tuple(np.round(np.abs(om[d, :dim]), 13)) for d in range(nd)]
+    cls = {k: i for i, k in enumerate(sorted(set(key)))}
+    slot = -np.ones((len(cls), P), dtype=int)
+    for d in range(nd):
+        slot[cls[key[d]], sum(1 << a for a in range(dim) if om[d, a] < 0)] = d
+    assert (slot >= 0).all()
+    signs, groups = [], []
+    for m in range(nm):
+        tol = 32 * np.finfo(float).eps * np.abs(m2d[:, m]).max()
+        value = 0
+        for c in range(len(cls)):
+            a = m2d[slot[c, 0], m]
+            for f in range(P):
+                b = m2d[slot[c, f], m]
+                assert abs(b - a) <= tol or abs(b + a) <= tol
+                if abs(b + a) <= tol < abs(b - a):
+                    value |= 1 << f
+        if value not in signs:
+            signs.append(value)
+        groups.append(signs.index(value))
+    return groups, signs
+
+
+@pytest.mark.parametrize("kind,dim,sn", [("LS", 2, 8), ("LS", 2, 16), ("GLC", 2, 4), ("LS", 3, 8), ("GLC", 3, 12)])
+def test_octant_parity_groups_are_canonical(kind, dim, sn):
+    """The symmetric contraction kernels are specialised on the parity groups
+    of the harmonic moments (csrc/vec.cu sym_group / sym_sign): one pattern per
+    dimension, every lower scattering order a prefix of P3."""
+    import ouranos_gb300 as og
+    canon = {2: ([0, 1, 2, 0, 0, 3, 1, 1, 2, 2], [0, 10, 12, 6]),
+             3: ([0, 1, 2, 3, 0, 4, 0, 5, 6, 1, 2, 1, 2, 3, 7, 3], [0, 170, 240, 204, 90, 60, 102, 150])}
+    for L in range(4):
+        q = og.build_quadrature(kind, sn, L, dim=dim)
+        groups, signs = _parity_groups(q)
+        assert groups == canon[dim][0][:q.n_mom]
+        assert signs == canon[dim][1][:len(signs)]
