@@ -800,6 +800,7 @@ int rt_dsa_apply_batch(ouranos_rt* const* rts, const double* const* v, double* c
     err = "diffusion acceleration: device query failed";
     return OURANOS_ERR_CUDA;
   }
+  int launches = 0;
   for (int dim = 2; dim <= 3; ++dim) {
     int per_sm = 0;
     const cudaError_t e =
@@ -816,6 +817,12 @@ int rt_dsa_apply_batch(ouranos_rt* const* rts, const double* const* v, double* c
       if (rts[i]->dim == dim) idx.push_back(i);
     for (size_t s0 = 0; s0 < idx.size(); s0 += cap) {  // at most one block per problem and SM per launch
       const int cnt = (int)std::min<size_t>(cap, idx.size() - s0);
+      // a further launch rewrites the page-locked staging block: the copy
+      // queued by the previous one must have run
+      if (launches++ > 0 && cudaStreamSynchronize(stream) != cudaSuccess) {
+        err = "diffusion acceleration: batch synchronisation failed";
+        return OURANOS_ERR_CUDA;
+      }
       const int rc = dim == 3 ? dsa_batch_launch<3>(rts, v, out, idx.data() + s0, cnt, stream, status, sc, cap, err)
                               : dsa_batch_launch<2>(rts, v, out, idx.data() + s0, cnt, stream, status, sc, cap, err);
       if (rc) return rc;
