@@ -1,10 +1,13 @@
 """Train the learned preconditioner on the GPU and write its weights.
 
     python -m ouranos_gb300.train_preconditioner [--n 64] [--maps 128] [--fields 4]
-        [--epochs 8] [--out ouranos_gb300/weights/precond_thick3d.npz]
+        [--epochs 8] [--pairs synthetic|solver] [--out ouranos_gb300/weights/precond_thick3d.npz]
 
 Training maps are the seeded 3-D thick diffusive material maps (seeds
-2000, 2001, ...; GLC S12); evaluation maps use other seeds.
+2000, 2001, ...; GLC S12); evaluation maps use other seeds.  --pairs synthetic
+trains on (A e, e) for seeded error fields e; --pairs solver on the Krylov
+vectors FGMRES meets, each with its converged diffusion correction as the
+target (--fields is then the number of Arnoldi steps per map and round).
 """
 import argparse
 import json
@@ -24,18 +27,26 @@ def main():
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--lr", type=float, default=3e-4)
     ap.add_argument("--sn", type=int, default=12)
+    ap.add_argument("--pairs", choices=("synthetic", "solver"), default="synthetic")
+    ap.add_argument("--rounds", type=int, default=2, help="solver pairs: collection rounds")
     ap.add_argument("--out", default=os.path.join(HERE, "weights", "precond_thick3d.npz"))
     args = ap.parse_args()
     import ouranos_gb300
     ouranos_gb300.build()
-    from ouranos_gb300.learned import train
+    from ouranos_gb300.learned import train, train_on_solver_pairs
     t0 = time.time()
-    net, hist = train(n=args.n, maps=args.maps, fields_per_map=args.fields, epochs=args.epochs,
-                      lr=args.lr, sn=args.sn, log=lambda s: print(s, flush=True))
+    log = lambda s: print(s, flush=True)  # noqa: E731
+    if args.pairs == "solver":
+        net, hist = train_on_solver_pairs(n=args.n, maps=args.maps, steps_per_map=args.fields,
+                                          rounds=args.rounds, epochs=args.epochs, lr=args.lr, sn=args.sn,
+                                          log=log)
+    else:
+        net, hist = train(n=args.n, maps=args.maps, fields_per_map=args.fields, epochs=args.epochs,
+                          lr=args.lr, sn=args.sn, log=log)
     dt = time.time() - t0
     os.makedirs(os.path.dirname(args.out), exist_ok=True)
     net.save(args.out, meta={"loss_history": hist, "maps": args.maps, "fields": args.fields,
-                             "epochs": args.epochs, "train_seconds": dt, "n": args.n})
+                             "epochs": args.epochs, "train_seconds": dt, "n": args.n, "pairs": args.pairs})
     print(json.dumps({"trained": args.out, "seconds": dt, "final_loss": hist[-1]}))
 
 
