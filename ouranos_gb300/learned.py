@@ -302,7 +302,7 @@ def learned_precondition(rt, dsa=False):
     return pc
 
 
-def train_on_solver_pairs(n=32, maps=32, steps_per_map=60, rounds=2, epochs=6, lr=3e-4, seed=7,
+def train_on_solver_pairs(n=32, maps=32, steps_per_map=60, passes=2, epochs=6, lr=3e-4, seed=7,
                           map_seed0=2000, sn=12, dsa=100, log=print):
     """Train the network to predict the diffusion correction of the residuals
     FGMRES meets on seeded thick maps.
@@ -312,17 +312,17 @@ def train_on_solver_pairs(n=32, maps=32, steps_per_map=60, rounds=2, epochs=6, l
     solved to convergence (`dsa` CG steps): the correction is a linear,
     material-dependent, local-scale map of the scalar flux (its range is the
     diffusion length: ~12 cells in the scattering cells, ~1 in the thick
-    ones), which the gated-linear network can represent.  Round 0 collects
-    the vectors of FGMRES(30) preconditioned by that correction; every later
-    round installs the network trained so far and collects the vectors of the
-    learned-preconditioned FGMRES, which are the ones the network meets in
-    use, and trains on all pairs so far.  Returns (net, loss history per
+    ones), which the gated-linear network can represent.  The first
+    collection pass takes the vectors of FGMRES(30) preconditioned by that
+    correction; every later pass installs the network trained so far and takes
+    the vectors of the learned-preconditioned FGMRES, which are the ones the
+    network meets in use, and trains on all pairs so far.  Returns (net, loss history per
     epoch)."""
     import torch
     from .transport import RadiativeTransfer
     rng = np.random.default_rng(seed)
     L = _lib()
-    cap = maps * steps_per_map * rounds
+    cap = maps * steps_per_map * passes
     cells = n ** 3
     feats = torch.empty((cap, cells * FEATURES), dtype=torch.float32, device="cuda")
     targets = torch.empty((cap, cells * OUTPUTS), dtype=torch.float32, device="cuda")
@@ -334,7 +334,7 @@ def train_on_solver_pairs(n=32, maps=32, steps_per_map=60, rounds=2, epochs=6, l
     try:
         for rt in rts:
             rt.set_dsa(dsa)
-        for rnd in range(rounds):
+        for rnd in range(passes):
             for rt in rts:
                 if rnd:
                     install(rt, net)
@@ -365,7 +365,7 @@ def train_on_solver_pairs(n=32, maps=32, steps_per_map=60, rounds=2, epochs=6, l
                 for i in order:
                     tot += net.train_step(feats[i], targets[i], rate)
                 hist.append(tot / filled)
-                log("round %d epoch %d pairs %d loss %.4e" % (rnd, ep, filled, hist[-1]))
+                log("pass %d epoch %d pairs %d loss %.4e" % (rnd, ep, filled, hist[-1]))
     finally:
         for rt in rts:
             rt.close()

@@ -7,7 +7,7 @@ Training maps are the seeded 3-D thick diffusive material maps (seeds
 2000, 2001, ...; GLC S12); evaluation maps use other seeds.  --pairs synthetic
 trains on (A e, e) for seeded error fields e; --pairs solver on the Krylov
 vectors FGMRES meets, each with its converged diffusion correction as the
-target (--fields is then the number of Arnoldi steps per map and round).
+target (--fields is then the number of Arnoldi steps per map and pass).
 """
 import argparse
 import json
@@ -28,7 +28,7 @@ def main():
     ap.add_argument("--lr", type=float, default=3e-4)
     ap.add_argument("--sn", type=int, default=12)
     ap.add_argument("--pairs", choices=("synthetic", "solver"), default="synthetic")
-    ap.add_argument("--rounds", type=int, default=2, help="solver pairs: collection rounds")
+    ap.add_argument("--passes", type=int, default=2, help="solver pairs: collection passes")
     ap.add_argument("--out", default=os.path.join(HERE, "weights", "precond_thick3d.npz"))
     args = ap.parse_args()
     import ouranos_gb300
@@ -38,7 +38,7 @@ def main():
     log = lambda s: print(s, flush=True)  # noqa: E731
     if args.pairs == "solver":
         net, hist = train_on_solver_pairs(n=args.n, maps=args.maps, steps_per_map=args.fields,
-                                          rounds=args.rounds, epochs=args.epochs, lr=args.lr, sn=args.sn,
+                                          passes=args.passes, epochs=args.epochs, lr=args.lr, sn=args.sn,
                                           log=log)
     else:
         net, hist = train(n=args.n, maps=args.maps, fields_per_map=args.fields, epochs=args.epochs,

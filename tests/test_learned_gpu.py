@@ -162,7 +162,7 @@ def test_solver_pairs_are_exact_and_the_trainer_runs():
     """The Arnoldi pairs of fgmres_pairs satisfy w = A z to the operator's
     accuracy (z is the exact error of the residual w), its FGMRES converges
     like the device solver's, and the trainer on solver-generated pairs runs
-    end to end (both rounds) on a small grid with a finite loss."""
+    end to end (both collection passes) on a small grid with a finite loss."""
     torch = pytest.importorskip("torch")
     import ouranos_gb300 as og
     from ouranos_gb300 import learned
@@ -179,6 +179,6 @@ def test_solver_pairs_are_exact_and_the_trainer_runs():
         xg, info, _ = rt.solve("gmres", tol=1e-8, max_it=800)
         assert float((b - rt.apply(x)).norm() / b.norm()) < 1e-7
         assert _rel(x.cpu().numpy(), xg) < 1e-6
-    net, hist = learned.train_on_solver_pairs(n=8, maps=2, steps_per_map=6, rounds=2, epochs=3, lr=1e-3,
+    net, hist = learned.train_on_solver_pairs(n=8, maps=2, steps_per_map=6, passes=2, epochs=3, lr=1e-3,
                                               sn=4, dsa=40, log=lambda s: None)
     assert len(hist) == 6 and all(np.isfinite(hist))
