@@ -227,6 +227,22 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def replica_max(values, dist, device):
+    """Each figure's maximum over the ranks (the slowest replica bounds the
+    whole job); every rank gets the same numbers.  dist None: one process."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def whole_job_rate(world, units_per_rank, seconds):
+    """Units all ranks processed (each the same work) over the job's time."""
+    return world * units_per_rank / seconds
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -279,13 +295,10 @@ def run_ours(args):
         launches += k + 2  # sweep-side kernels + scattering source + combine
     torch.cuda.synchronize(dev)
     clocks = sampler.stop()
-    total_ms = sum(step_ms)
+    total_ms = replica_max([sum(step_ms)], dist, dev)[0]
     if dist:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = t.item()
         dist.barrier()
-    value = world * solves * args.steps / (total_ms / 1e3)
+    value = whole_job_rate(world, solves * args.steps, total_ms / 1e3)
 
     # end-to-end through the C-ABI with pinned host buffers
     xh = x.cpu().pin_memory()
@@ -297,12 +310,8 @@ def run_ours(args):
         t0 = time.perf_counter()
         rt.Apply(xh, yh)
         e2e_times.append(time.perf_counter() - t0)
-    e2e_total = sum(e2e_times)
-    if dist:
-        t = torch.tensor([e2e_total], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = t.item()
-    e2e_value = world * solves * args.steps / e2e_total
+    e2e_total = replica_max([sum(e2e_times)], dist, dev)[0]
+    e2e_value = whole_job_rate(world, solves * args.steps, e2e_total)
     if not np.isfinite(yh.numpy()).all():
         raise RuntimeError("non-finite operator output")
 
