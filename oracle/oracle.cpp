@@ -140,6 +140,8 @@ struct orc_problem {
   std::vector<std::vector<long>> required;     // task -> upwind tasks (sorted)
   std::vector<std::vector<long>> waiting;      // task -> downwind tasks (sorted)
   std::vector<long> last_order;
+  bool tasks_built = false;  /* the graph is built on first use (build_tasks) */
+  int scheduler = 0;         /* the order orc_apply / orc_solve sweep in */
   /* state */
   std::vector<double> scat;                    // [mom][dof]
   /* implicit Euler (an extension, see orc_set_time_step): sigma_t shift and psi^n */
@@ -252,6 +254,8 @@ void build_fe(orc_problem* P) {
  * waiting/required maps (:234-584) reduce, on one domain, to the upwind and
  * downwind neighbour tasks of the same direction. */
 void build_tasks(orc_problem* P) {
+  if (P->tasks_built) return;
+  P->tasks_built = true;
   const int dim = P->dim;
   const long nc = P->n_cells;
   std::vector<std::set<long>> boundary(2 * dim);
@@ -325,11 +329,10 @@ struct SweepCtx {
   std::vector<int> piv;
 };
 
-/* RadiativeTransfer::sweep, src/RadiativeTransfer.cc:878-1012, one task. */
-void sweep_task(orc_problem* P, long t, SweepCtx& ctx, double* phi, int dir_base) {
+/* RadiativeTransfer::sweep, src/RadiativeTransfer.cc:878-1012, one task: the
+ * cell c in direction d. */
+void sweep_task(orc_problem* P, int d, long c, SweepCtx& ctx, double* phi, int dir_base) {
   const int n = P->n, dim = P->dim;
-  const int d = P->task_dir[t];
-  const long c = P->task_cell[t];
   const double* om = &P->omega[d * 3];
   const int mat = P->material_id[c];
   std::vector<double>& A = ctx.A;
@@ -444,7 +447,7 @@ void run_sweep(orc_problem* P, double* phi, const double* group_flux, int schedu
     long t = ready.front();
     ready.pop_front();
     --left;
-    sweep_task(P, t, ctx, phi, d0);
+    sweep_task(P, P->task_dir[t], P->task_cell[t], ctx, phi, d0);
     if (order) order->push_back((long)P->task_dir[t] * nc + P->task_cell[t]);
     if (scheduler == 1) {
       // the reference's scan of every task after each completion (:673-689)
@@ -465,6 +468,42 @@ void run_sweep(orc_problem* P, double* phi, const double* group_flux, int schedu
   // the angular flux of directions [d0, d1) for orc_advance_angular
   if (P->psi_capture)
     std::copy(ctx.psi.begin(), ctx.psi.end(), P->psi_capture->begin() + (long)d0 * P->n_dofs);
+}
+
+/* The same tasks in another topological order of the same graph, without
+ * the graph: each direction of [d0, d1) in turn, its cells in lexicographic
+ * order along the sweep (ascending along axis a when Omega_a > 0, descending
+ * otherwise), so every upwind neighbour of a cell (src/RadiativeTransfer.cc:
+ * 113-125) is solved before it.  Each task then sees the same inputs as under
+ * the ready-list scheduler and computes the same values; only the order of
+ * the additions into the flux moments differs.  The graph of a large mesh
+ * costs O(tasks) memory (tens of GB at 10^8 tasks); this order needs one
+ * direction's angular flux per worker. */
+void run_sweep_cartesian(orc_problem* P, double* phi, const double* group_flux, int d0, int d1) {
+  const long nc = P->n_cells;
+  SweepCtx ctx;
+  ctx.group_flux = group_flux;
+  ctx.psi.assign(nc * P->n, 0.0);
+  ctx.A.assign(P->n * P->n, 0.0);
+  ctx.b.assign(P->n, 0.0);
+  ctx.x.assign(P->n, 0.0);
+  ctx.piv.assign(P->n, 0);
+  for (int d = d0; d < d1; ++d) {
+    int lo[3], step[3];
+    for (int a = 0; a < 3; ++a) {
+      const bool up = a < P->dim && P->omega[d * 3 + a] > 0.;
+      lo[a] = up ? 0 : P->nx[a] - 1;
+      step[a] = up ? 1 : -1;
+    }
+    for (int kk = 0; kk < P->nx[2]; ++kk)
+      for (int jj = 0; jj < P->nx[1]; ++jj)
+        for (int ii = 0; ii < P->nx[0]; ++ii) {
+          const long c = P->cell_index(lo[0] + step[0] * ii, lo[1] + step[1] * jj, lo[2] + step[2] * kk);
+          sweep_task(P, d, c, ctx, phi, d);
+        }
+    if (P->psi_capture)
+      std::copy(ctx.psi.begin(), ctx.psi.end(), P->psi_capture->begin() + (long)d * P->n_dofs);
+  }
 }
 
 double dot(const std::vector<double>& a, const std::vector<double>& b) {
@@ -513,7 +552,6 @@ orc_problem* orc_create(const orc_desc* D) {
   for (int f = 0; f < 6; ++f) P->bc[f] = D->bc_type[f];
   if (D->inc_flux) P->inc_flux.assign(D->inc_flux, D->inc_flux + 2 * P->dim * P->G);
   build_fe(P);
-  build_tasks(P);
   P->scat.assign((long)P->n_mom * P->n_dofs, 0.0);
   return P;
 }
@@ -538,7 +576,7 @@ void orc_advance_angular(orc_problem* p, const double* phi, int n_threads) {
   std::vector<double> gf((long)p->G * p->n_mom * p->n_dofs, 0.0), out((long)p->n_mom * p->n_dofs, 0.0);
   orc_scattering_source(p, phi);
   p->psi_capture = &psi;
-  orc_sweep(p, out.data(), gf.data(), 0, n_threads);
+  orc_sweep(p, out.data(), gf.data(), p->scheduler, n_threads);
   p->psi_capture = nullptr;
   p->psi_prev.swap(psi);
 }
@@ -549,6 +587,7 @@ void orc_set_angular(orc_problem* p, const double* psi) {
   std::copy(psi, psi + (long)p->n_dir * p->n_dofs, p->psi_prev.begin());
 }
 void orc_set_group(orc_problem* p, int g) { p->group = g; }
+void orc_set_scheduler(orc_problem* p, int scheduler) { p->scheduler = scheduler; }
 long orc_n_dofs(const orc_problem* p) { return p->n_dofs; }
 long orc_n_tasks(const orc_problem* p) { return p->n_cells * p->n_dir; }
 
@@ -573,9 +612,13 @@ void orc_scattering_source(orc_problem* P, const double* x) {
 
 void orc_sweep(orc_problem* P, double* phi, const double* group_flux, int scheduler,
                int n_threads) {
+  if (scheduler != 2) build_tasks(P);
   if (n_threads <= 1) {
     P->last_order.clear();
-    run_sweep(P, phi, group_flux, scheduler, 0, P->n_dir, &P->last_order);
+    if (scheduler == 2)
+      run_sweep_cartesian(P, phi, group_flux, 0, P->n_dir);
+    else
+      run_sweep(P, phi, group_flux, scheduler, 0, P->n_dir, &P->last_order);
     return;
   }
   const long len = (long)P->n_mom * P->n_dofs;
@@ -583,7 +626,12 @@ void orc_sweep(orc_problem* P, double* phi, const double* group_flux, int schedu
   std::vector<std::thread> th;
   for (int w = 0; w < n_threads; ++w) {
     int d0 = (int)((long)P->n_dir * w / n_threads), d1 = (int)((long)P->n_dir * (w + 1) / n_threads);
-    th.emplace_back([=, &part]() { run_sweep(P, part[w].data(), group_flux, scheduler, d0, d1, nullptr); });
+    th.emplace_back([=, &part]() {
+      if (scheduler == 2)
+        run_sweep_cartesian(P, part[w].data(), group_flux, d0, d1);
+      else
+        run_sweep(P, part[w].data(), group_flux, scheduler, d0, d1, nullptr);
+    });
   }
   for (auto& t : th) t.join();
   for (int w = 0; w < n_threads; ++w)
@@ -594,7 +642,7 @@ void orc_apply(orc_problem* P, const double* x, double* y, int n_threads) {
   const long len = (long)P->n_mom * P->n_dofs;
   orc_scattering_source(P, x);
   std::vector<double> phi(len, 0.0);
-  orc_sweep(P, phi.data(), nullptr, 0, n_threads);
+  orc_sweep(P, phi.data(), nullptr, P->scheduler, n_threads);
   for (long i = 0; i < len; ++i) y[i] = x[i] - phi[i];
 }
 
@@ -602,7 +650,8 @@ void orc_last_order(const orc_problem* P, long* order) {
   std::copy(P->last_order.begin(), P->last_order.end(), order);
 }
 
-void orc_task_levels(const orc_problem* P, int* levels) {
+void orc_task_levels(orc_problem* P, int* levels) {
+  build_tasks(P);
   const long nt = (long)P->n_cells * P->n_dir;
   std::vector<long> indeg(nt);
   std::vector<int> lev(nt, 0);
@@ -622,7 +671,8 @@ void orc_task_levels(const orc_problem* P, int* levels) {
   for (long t = 0; t < nt; ++t) levels[(long)P->task_dir[t] * P->n_cells + P->task_cell[t]] = lev[t];
 }
 
-void orc_task_ids(const orc_problem* P, long* ids) {
+void orc_task_ids(orc_problem* P, long* ids) {
+  build_tasks(P);
   std::copy(P->task_id_of.begin(), P->task_id_of.end(), ids);
 }
 
@@ -653,7 +703,7 @@ int orc_solve(orc_problem* P, int kind, int restart, int max_it, double tol,
   // right-hand side: one sweep of the fixed sources with no in-group scattering
   std::vector<double> rhs(len, 0.0);
   orc_clear_scattering_source(P);
-  orc_sweep(P, rhs.data(), group_flux, 0, n_threads);
+  orc_sweep(P, rhs.data(), group_flux, P->scheduler, n_threads);
   std::vector<double> x(len, 0.0);
   int it = 0;
   const double bnorm = std::sqrt(dot(rhs, rhs));
@@ -663,7 +713,7 @@ int orc_solve(orc_problem* P, int kind, int restart, int max_it, double tol,
     for (it = 0; it < max_it; ++it) {
       orc_scattering_source(P, x.data());
       std::fill(nx.begin(), nx.end(), 0.0);
-      orc_sweep(P, nx.data(), group_flux, 0, n_threads);
+      orc_sweep(P, nx.data(), group_flux, P->scheduler, n_threads);
       double num = 0.0, den = 0.0;
       for (long i = 0; i < len; ++i) {
         num += (nx[i] - x[i]) * (nx[i] - x[i]);

@@ -74,11 +74,14 @@ typedef struct {
 
 typedef struct orc_problem orc_problem;
 
-/* Build the FE tables and the task graph (RadiativeTransfer::setup,
- * src/RadiativeTransfer.cc:50-78). Returns NULL on bad input. */
+/* Build the FE tables (RadiativeTransfer::setup, src/RadiativeTransfer.cc:50-78);
+ * the task graph is built on its first use. Returns NULL on bad input. */
 orc_problem* orc_create(const orc_desc* desc);
 void orc_destroy(orc_problem* p);
 void orc_set_group(orc_problem* p, int g);
+/* The scheduler orc_apply, orc_solve and orc_advance_angular sweep with
+ * (orc_sweep's argument; 0 by default). */
+void orc_set_scheduler(orc_problem* p, int scheduler);
 /* implicit Euler in time (an extension, not in the reference operator) */
 void orc_set_time_step(orc_problem* p, double inv_vdt);
 void orc_set_source(orc_problem* p, const double* source);   /* [n_sources][n_groups] */
@@ -98,7 +101,10 @@ void orc_clear_scattering_source(orc_problem* p);
 /* One full sweep: flux_moments += D L^-1 (M2D S [+ q + outer + inflow]).
  * group_flux != NULL selects the right-hand-side form (src/RadiativeTransfer.cc:914-925,
  * 958-975): [g][mom][dof].  scheduler: 0 = linear ready counters,
- * 1 = the reference's all-task scan (O(T^2)).  n_threads > 1 splits the
+ * 1 = the reference's all-task scan (O(T^2)), 2 = no task graph: each
+ * direction's cells in lexicographic upwind-first order (the same task
+ * values, another order of the additions into the moments; for meshes whose
+ * graph would not fit in memory).  n_threads > 1 splits the
  * directions over std::threads (each thread owns its directions' tasks). */
 void orc_sweep(orc_problem* p, double* flux_moments, const double* group_flux,
                int scheduler, int n_threads);
@@ -111,10 +117,10 @@ void orc_apply(orc_problem* p, const double* x, double* y, int n_threads);
 void orc_last_order(const orc_problem* p, long* order);
 /* Longest-path depth of every task in the reference task DAG
  * (compute_sweep_ordering + build_*_tasks_maps): [dir][cell]. */
-void orc_task_levels(const orc_problem* p, int* levels);
+void orc_task_levels(orc_problem* p, int* levels);
 /* Task ids as the reference assigns them (direction-major, breadth-first
  * from the upwind boundary): [dir][cell] -> id. */
-void orc_task_ids(const orc_problem* p, long* ids);
+void orc_task_ids(orc_problem* p, long* ids);
 
 /* FE matrices of one cell (FECell, src/FECell.cc:10-78): mass [n][n],
  * grad [dim][n][n], downwind [2dim][n][n], upwind [2dim][n][n], normals [2dim][3]. */

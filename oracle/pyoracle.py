@@ -56,6 +56,7 @@ def lib():
         L.orc_create.argtypes = [C.POINTER(OrcDesc)]
         L.orc_destroy.argtypes = [vp]
         L.orc_set_group.argtypes = [vp, i]
+        L.orc_set_scheduler.argtypes = [vp, i]
         L.orc_set_time_step.argtypes = [vp, C.c_double]
         L.orc_set_source.argtypes = [vp, vp]
         L.orc_advance_angular.argtypes = [vp, vp, i]
@@ -128,9 +129,17 @@ class OracleProblem:
     (dim, fe_order, n_cells, lower, upper, n_groups, omega, m2d, d2m, moment_l,
     most_normal, weight_sum, sigma_t, sigma_s, l_max, material_id, source_id,
     source, bc_type, inc_flux).
+
+    ``order`` picks the task order of apply/solve: "fifo" is the reference's
+    ready list with linear dependency counters (src/RadiativeTransfer.cc:
+    605-692); "cartesian" runs each direction's cells in upwind-first
+    lexicographic order without building the task graph (identical task
+    values, for meshes whose graph would not fit in memory).
     """
 
-    def __init__(self, spec):
+    ORDERS = {"fifo": 0, "cartesian": 2}
+
+    def __init__(self, spec, order="fifo"):
         L = lib()
         self._keep = {}
 
@@ -179,6 +188,7 @@ class OracleProblem:
         self.h = L.orc_create(C.byref(d))
         if not self.h:
             raise ValueError("oracle rejected the problem")
+        L.orc_set_scheduler(self.h, self.ORDERS[order])
         self.n_dofs = L.orc_n_dofs(self.h)
         self.n_mom = d.n_mom
         self.n_dir = d.n_dir
@@ -224,6 +234,7 @@ class OracleProblem:
         lib().orc_clear_scattering_source(self.h)
 
     def sweep(self, flux=None, group_flux=None, scheduler=0, threads=1):
+        """scheduler: 0 ready list, 1 the reference's all-task scan, 2 cartesian."""
         flux = np.zeros(self.length) if flux is None else np.ascontiguousarray(flux, dtype=np.float64)
         gf = None if group_flux is None else np.ascontiguousarray(group_flux, dtype=np.float64)
         lib().orc_sweep(self.h, _ptr(flux), _ptr(gf), scheduler, threads)
