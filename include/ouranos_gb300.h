@@ -199,10 +199,13 @@ int ouranos_rt_debug_wait_bias(ouranos_rt* rt, int extra);
  * scratch buffer of the Apply lives in one file-scope device array of
  * OURANOS_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
  * the process exits; problems needing more scratch are rejected with
- * OURANOS_ERR_BAD_INPUT.  x and y must be device pointers.  The first call on a
- * device looks up the array's address (cudaGetSymbolAddress): make it before
- * any stream capture.  All calls share the array, so calls whose GPU work
- * overlaps (two streams, threads or handles) race. */
+ * OURANOS_ERR_BAD_INPUT.  x and y must be device pointers.  ouranos_rt_create
+ * looks the array's address up on the handle's device (cudaGetSymbolAddress,
+ * which under CUDA's lazy module loading is also what places the array
+ * there), so the call itself only reads that address.  It runs the kernels
+ * ouranos_rt_apply runs for the handle's precision and FP64 arithmetic, and
+ * returns once its GPU work has finished.  All calls share the array, so
+ * calls whose GPU work overlaps (two streams, threads or handles) race. */
 #define OURANOS_NOALLOC_SCRATCH_BYTES (32u << 20)
 int ouranos_rt_apply_noalloc(ouranos_rt* rt, const double* x, double* y);
 

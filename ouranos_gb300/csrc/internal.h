@@ -263,6 +263,9 @@ int rt_dsa_apply(ouranos_rt* rt, const double* v, double* out);
 void cnn_grid(const ouranos_cnn* net, int* nx, int* ny, int* nz);
 // Device-side pieces the solvers use (operator.cu).
 int rt_apply_device(ouranos_rt* rt, const double* x, double* y);
+// allocation-free Apply (noalloc.cu): resolve its scratch array on `device`,
+// which must be current; once per device, called by ouranos_rt_create
+int noalloc_setup(int device);
 int rt_rhs_device(ouranos_rt* rt, const double* gf, double* rhs);
 int rt_check_status(ouranos_rt* rt);
 // batched Apply pieces (see operator.cu)

@@ -11,17 +11,21 @@
 // kNoAllocScratchBytes.  Every GPU that loads the library holds that array
 // until the process exits.
 //
-// Host code may not use the array's name as a device address: the first call
-// on each device looks the address up with cudaGetSymbolAddress, with that
-// device current, and caches it.  That first call must therefore come before
-// any stream capture.  All calls share the array and it keeps the previous
-// call's contents: the ticket/status words and the edge buffers are cleared
-// at the start of every call, everything else is fully overwritten before it
-// is read.  Calls whose GPU work overlaps (two streams, two threads, two
-// handles) race on the array.
+// Host code may not use the array's name as a device address: set-up looks
+// the address up with cudaGetSymbolAddress, once per device, with that device
+// current, and caches it.  Set-up runs inside ouranos_rt_create (under CUDA's
+// lazy module loading that lookup is also what places the array on the
+// device), so the entry point itself only reads the cached address.  It runs
+// the kernels of ouranos_rt_apply for the handle's arithmetic, with the same
+// launch shapes, so its result is the same bit for bit.  All calls share the
+// array and it keeps the previous call's contents: the ticket/status words
+// and the edge buffers are cleared at the start of every call, everything
+// else is fully overwritten before it is read.  Calls whose GPU work overlaps
+// (two streams, two threads, two handles) race on the array.
 #include <algorithm>
 #include <cstdio>
 #include <mutex>
+#include <type_traits>
 
 #include "internal.h"
 
@@ -97,17 +101,60 @@ Layout layout_for(const ouranos_rt* rt, size_t real_bytes, bool expand) {
   return L;
 }
 
+// the table of the sweep's arithmetic type (as the regular Apply reads them)
 template <typename real>
-int apply_noalloc(ouranos_rt* rt, unsigned char* base, const Layout& L, bool expand,
+const real* tbl(const DevBuf& b64, const DevBuf& b32, const DevBuf& bdf) {
+  if constexpr (std::is_same<real, float>::value) return (const real*)b32.p;
+  else if constexpr (std::is_same<real, df64>::value) return (const real*)bdf.p;
+  else return (const real*)b64.p;
+}
+
+// q = M2D T in the contraction form of the regular Apply for this arithmetic
+template <typename real>
+cudaError_t expand(const ouranos_rt* rt, const real* T, real* q, cudaStream_t st) {
+  const long nd = rt->n_dofs;
+  if constexpr (std::is_same<real, df64>::value) {
+    if (rt->sym.n_class) return launch_expand_sym_pairs(T, nullptr, rt->sym, q, rt->n_mom, nd, st);
+    return launch_expand_source_pairs(T, nullptr, rt->d_m2d64.as<double>(), q, rt->n_dir, rt->n_mom, nd, st);
+  } else if constexpr (std::is_same<real, double>::value) {
+    if (rt->fp64_contract != OURANOS_FP64_NATIVE)
+      return launch_expand_source_df64(T, nullptr, rt->d_m2d64.as<double>(), q, rt->n_dir, rt->n_mom, nd, st);
+    return launch_expand_source<double>(T, nullptr, rt->d_m2d64.as<double>(), q, rt->n_dir, rt->n_mom, nd, st);
+  } else {
+    return launch_expand_source<float>(T, nullptr, rt->d_m2d32.as<float>(), q, rt->n_dir, rt->n_mom, nd, st);
+  }
+}
+
+// phi = D2M psi, likewise; phi is float for the FP32 sweep, double otherwise
+template <typename real>
+cudaError_t reduce(const ouranos_rt* rt, const real* psi, void* phi, cudaStream_t st) {
+  const long nd = rt->n_dofs;
+  if constexpr (std::is_same<real, df64>::value) {
+    if (rt->sym.n_class) return launch_reduce_sym_pairs(psi, rt->sym, (double*)phi, rt->n_mom, nd, st);
+    return launch_reduce_moments_pairs(psi, rt->d_d2m64.as<double>(), (double*)phi, rt->n_dir, rt->n_mom, nd, st);
+  } else if constexpr (std::is_same<real, double>::value) {
+    if (rt->fp64_contract != OURANOS_FP64_NATIVE)
+      return launch_reduce_moments_df64(psi, rt->d_d2m64.as<double>(), (double*)phi, rt->n_dir, rt->n_mom, nd,
+                                        st);
+    return launch_reduce_moments<double>(psi, rt->d_d2m64.as<double>(), (double*)phi, rt->n_dir, rt->n_mom, nd,
+                                         st);
+  } else {
+    return launch_reduce_moments<float>(psi, rt->d_d2m32.as<float>(), (float*)phi, rt->n_dir, rt->n_mom, nd, st);
+  }
+}
+
+// real: float (FP32 sweep), double (FP64 sweep) or df64 (double-float sweep,
+// sources and angular fluxes stored as pairs)
+template <typename real>
+int apply_noalloc(ouranos_rt* rt, unsigned char* base, const Layout& L, bool expand_source,
                   const double* x, double* y) {
-  const bool f64 = sizeof(real) == 8;
   const long len = (long)rt->n_mom * rt->n_dofs;
   cudaStream_t st = rt->stream;
   int* ctrl = reinterpret_cast<int*>(base + L.ctrl);
   real* T = reinterpret_cast<real*>(base + L.T);
-  real* q = expand ? reinterpret_cast<real*>(base + L.q) : nullptr;
+  real* q = expand_source ? reinterpret_cast<real*>(base + L.q) : nullptr;
   real* psi = reinterpret_cast<real*>(base + L.psi);
-  real* phi = reinterpret_cast<real*>(base + L.phi);
+  void* phi = base + L.phi;
   // the array keeps the last call's contents: clear what must start at zero
   NA_CU(cudaMemsetAsync(ctrl, 0, 256, st), "clear control words");
   NA_CU(cudaMemsetAsync(base + L.edge_x, 0, L.edge_x_bytes, st), "clear edge buffer");
@@ -126,10 +173,7 @@ int apply_noalloc(ouranos_rt* rt, unsigned char* base, const Layout& L, bool exp
                                     rt->d_material.as<int>(), rt->n_mat, rt->G, rt->group,
                                     rt->n_cells, rt->n, rt->n_mom, rt->n_dofs, st),
         "scattering source");
-  const real* m2d = (const real*)(f64 ? rt->d_m2d64.p : rt->d_m2d32.p);
-  if (expand)
-    NA_CU(launch_expand_source<real>(T, nullptr, m2d, q, rt->n_dir, rt->n_mom, rt->n_dofs, st),
-          "source expansion");
+  if (expand_source) NA_CU(expand<real>(rt, T, q, st), "source expansion");
   SweepArgs<real> a;
   a.nx = rt->nx[0];
   a.ny = rt->nx[1];
@@ -149,11 +193,11 @@ int apply_noalloc(ouranos_rt* rt, unsigned char* base, const Layout& L, bool exp
   a.group_flip = rt->d_group_flip.as<int>();
   a.dir_class = rt->d_dir_class.as<int>();
   a.n_dir_class = rt->n_dir_class;
-  a.abs_omega = (const real*)(f64 ? rt->d_abs64.p : rt->d_abs32.p);
-  a.m2d = m2d;
-  a.ainv = (const real*)(f64 ? rt->d_ainv64.p : rt->d_ainv32.p);
+  a.abs_omega = tbl<real>(rt->d_abs64, rt->d_abs32, rt->d_absdf);
+  a.m2d = tbl<real>(rt->d_m2d64, rt->d_m2d32, rt->d_m2ddf);
+  a.ainv = tbl<real>(rt->d_ainv64, rt->d_ainv32, rt->d_ainvdf);
   a.cell_class = rt->d_cell_class.as<int>();
-  a.face_mass = (const real*)(f64 ? rt->d_face64.p : rt->d_face32.p);
+  a.face_mass = tbl<real>(rt->d_face64, rt->d_face32, rt->d_facedf);
   a.src = T;
   a.iso = nullptr;
   a.q = q;
@@ -165,15 +209,16 @@ int apply_noalloc(ouranos_rt* rt, unsigned char* base, const Layout& L, bool exp
   a.ticket = ctrl;
   a.status = ctrl + 1;
   a.wait_limit_ns = rt->wait_limit_ns;
-  a.wait_bias = 0;
+  a.wait_bias = rt->wait_bias;
   int sms = 0;
   NA_CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, rt->device), "device query");
   const int grid = std::min((rt->n_tasks + 3) / 4, std::max(1, sms * 8));
-  NA_CU(launch_sweep<real>(rt->dim, rt->p1, expand ? 0 : rt->n_mom, a, grid, 128, st), "sweep");
-  NA_CU(launch_reduce_moments<real>(psi, (const real*)(f64 ? rt->d_d2m64.p : rt->d_d2m32.p), phi,
-                                    rt->n_dir, rt->n_mom, rt->n_dofs, st),
-        "moment reduction");
-  NA_CU(launch_combine<real>(xd, phi, yd, len, 1.0, -1.0, st), "combine");
+  NA_CU(launch_sweep<real>(rt->dim, rt->p1, expand_source ? 0 : rt->n_mom, a, grid, 128, st), "sweep");
+  NA_CU(reduce<real>(rt, psi, phi, st), "moment reduction");
+  if constexpr (std::is_same<real, float>::value)
+    NA_CU(launch_combine<float>(xd, (const float*)phi, yd, len, 1.0, -1.0, st), "combine");
+  else
+    NA_CU(launch_combine<double>(xd, (const double*)phi, yd, len, 1.0, -1.0, st), "combine");
   if (!rt->cell_order.empty())
     NA_CU(launch_permute(yd, y, rt->d_cell_order.as<long>(), rt->n_cells, rt->n, rt->n_mom, 0, st),
           "permute out");
@@ -186,6 +231,22 @@ int apply_noalloc(ouranos_rt* rt, unsigned char* base, const Layout& L, bool exp
 
 }  // namespace
 
+namespace ouranos {
+// Set-up of the allocation-free Apply on the current device (ouranos_rt_create
+// calls it once the handle's device is current): look the scratch array's
+// device address up once per device and keep it.
+int noalloc_setup(int device) {
+  if (device < 0 || device >= kMaxDevices) return OURANOS_ERR_BAD_INPUT;
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  if (g_scratch_ptr[device]) return OURANOS_OK;
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return OURANOS_ERR_CUDA;
+  g_scratch_ptr[device] = p;
+  return OURANOS_OK;
+}
+}  // namespace ouranos
+
 extern "C" int ouranos_rt_apply_noalloc(ouranos_rt* rt, const double* x, double* y) {
   if (!rt || !x || !y) return OURANOS_ERR_BAD_INPUT;
   if (cudaSetDevice(rt->device) != cudaSuccess) return cfail(rt, cudaGetLastError(), "set device");
@@ -194,9 +255,10 @@ extern "C" int ouranos_rt_apply_noalloc(ouranos_rt* rt, const double* x, double*
                 "ouranos_rt_apply_noalloc takes device pointers only (no staging buffers)");
   // same form choice as the regular Apply: expand the source when it has more
   // moments than the sweep applies in place
-  const bool expand = !(rt->n_mom <= 2 && rt->n * (rt->n_mom + 1) <= 32);
+  const bool expand_source = !(rt->n_mom <= 2 && rt->n * (rt->n_mom + 1) <= 32);
+  // double, and the double-float pairs, take 8 bytes a value
   const size_t rb = rt->precision == OURANOS_FP64 ? 8 : 4;
-  const Layout L = layout_for(rt, rb, expand);
+  const Layout L = layout_for(rt, rb, expand_source);
   if (L.total > kNoAllocScratchBytes) {
     char buf[256];
     std::snprintf(buf, sizeof buf,
@@ -209,17 +271,13 @@ extern "C" int ouranos_rt_apply_noalloc(ouranos_rt* rt, const double* x, double*
     return fail(rt, OURANOS_ERR_BAD_INPUT, "device ordinal out of range");
   void* base = nullptr;
   {
-    // set-up, once per device, with that device current
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[rt->device]) {
-      void* p = nullptr;
-      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (e != cudaSuccess) return cfail(rt, e, "scratch symbol address");
-      g_scratch_ptr[rt->device] = p;
-    }
     base = g_scratch_ptr[rt->device];
   }
-  if (rt->precision == OURANOS_FP64)
-    return apply_noalloc<double>(rt, (unsigned char*)base, L, expand, x, y);
-  return apply_noalloc<float>(rt, (unsigned char*)base, L, expand, x, y);
+  if (!base)
+    return fail(rt, OURANOS_ERR_CUDA, "the scratch array was not set up on this device at handle creation");
+  unsigned char* b = (unsigned char*)base;
+  if (rt->precision == OURANOS_FP32) return apply_noalloc<float>(rt, b, L, expand_source, x, y);
+  if (rt->fp64_contract == OURANOS_FP64_DF64_SWEEP) return apply_noalloc<df64>(rt, b, L, expand_source, x, y);
+  return apply_noalloc<double>(rt, b, L, expand_source, x, y);
 }

@@ -915,6 +915,10 @@ int ouranos_rt_create(const ouranos_problem_desc* D, int device, ouranos_rt** ou
       cudaEventCreate(&rt->ev0) != cudaSuccess || cudaEventCreate(&rt->ev1) != cudaSuccess)
     return fail(cuda_fail(rt, cudaGetLastError(), "stream"));
   rt->stream = rt->own_stream;
+  // the allocation-free Apply's scratch array is placed on the device here,
+  // at set-up, so that no call of ouranos_rt_apply_noalloc allocates
+  if (noalloc_setup(device) != OURANOS_OK)
+    return fail(cuda_fail(rt, cudaGetLastError(), "allocation-free Apply set-up"));
 
   // |Omega| classes (the canonical cell matrix depends on |Omega_a| only)
   std::vector<int> dcls(rt->n_dir);
