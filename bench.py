@@ -10,15 +10,26 @@ per step.  Prints one JSON line.
   value    = cell-direction solves/s over the timed steps, inputs resident in
              HBM, device time from CUDA events on the operator's stream, L2
              flushed (256 MiB write) before every step outside the timed span.
+             FP64 arithmetic is the default double-float form ("arithmetic");
+             fp64_native_apply times the same Apply in native FP64.
   e2e      = the same call with pinned host buffers (host->device copy of x and
              device->host copy of y inside the timed span), wall clock.
   roofline = the sweep kernel against measured HBM bandwidth, with the
-             algorithmic bytes per solve of the sweep's face hand-off model.
+             algorithmic bytes per solve of the sweep's face hand-off model;
+             traffic from the ncu capture of the current sweep source, else null.
   cpu_baseline = the CPU restatement of the reference sweep (oracle/), all
-             host threads, on the same workload (rank 0 at N = 1 only).
+             host threads, on the same workload and the same x (rank 0 at
+             N = 1 only); the same leg checks the timed Apply's output against
+             the oracle's (parity_rel_err) and solves the reduced thick map in
+             FP64 for the time-to-solution error check.
+  time_to_solution = time to a 1e-8 residual on the 64^3 thick map: plain FP64
+             GMRES(30) against FGMRES(30) with FP32 sweeps and the diffusion
+             synthetic acceleration, scalar-flux errors against the FP64 solve
+             and (on the reduced map) against the FP64 oracle.
 --impl reference: the CPU restatement of the reference's sweep (the reference
   itself needs deal.II/Trilinos/p4est/MPI, absent here), all host threads,
-  timed per step.  Under torchrun only rank 0 runs it.
+  timed per step, on inputs from the oracle's own generator (nothing of the
+  product is loaded).  Under torchrun only rank 0 runs it.
 
 Multi-GPU: replicas only (each rank sweeps its own seeded problem, no
 collective on the data path); value is the sum over ranks of solves divided by
@@ -42,17 +53,39 @@ UNIT = "cell-dir solves/s"
 WORKLOAD = "2d-hetero-256x256-dgq2-ls16-p3"
 
 
+WORKLOAD_ARGS = dict(seed=1001, n=256, fe_order=2, sn=16, l_max=3, blocks=8)
+
+
 def workload_problem(seed=1001):
     import ouranos_gb300 as og
-    return og.heterogeneous_2d(seed=seed, n=256, fe_order=2, sn=16, l_max=3, blocks=8)
+    return og.heterogeneous_2d(**dict(WORKLOAD_ARGS, seed=seed))
 
 
-# DRAM traffic of one sweep launch on the default workload, from the ncu
-# capture summarised in profiles/sweep_kernel_2d-hetero-256x256-dgq2-ls16-p3.md
-# (dram__bytes_read.sum + dram__bytes_write.sum), per precision, default tiling
-# and FP64 arithmetic
-PROFILED_TILING = (16, 1, 1)  # the default for Q2 cells: two lanes per cell
-SWEEP_TRAFFIC_BYTES = {"fp64": 702.409472e6 + 663.693312e6, "fp32": 361.657088e6 + 316.145664e6}
+def workload_config(cells, directions, moments, dofs_per_cell, world):
+    """The `config` object of both arms' lines (the same keys and values)."""
+    return {"workload": WORKLOAD, "cells": cells, "directions": directions, "moments": moments,
+            "dofs_per_cell": dofs_per_cell, "solves_per_step": cells * directions,
+            "parallelism": "replicas" if world > 1 else "none"}
+
+
+# DRAM traffic of one sweep launch on the default workload
+# (dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of the
+# default tiling, 16 x 1 cells with two lanes per cell, in the default FP64
+# arithmetic and in FP32), keyed by a digest of the sweep kernel's sources at
+# the time of the capture: after any change to those sources the figure no
+# longer describes the kernel and the line reports traffic as null.
+PROFILED_TILING = (16, 1, 1)
+SWEEP_SOURCES = ("sweep.cuh", "sweep_df64.cu", "sweep_f32.cu", "df64.cuh")
+SWEEP_TRAFFIC = {"digest": "a6da536b0a95d196", "bytes": {"fp64": 701757696 + 663408384}}
+
+
+def sweep_source_digest():
+    import hashlib
+    h = hashlib.sha256()
+    for name in SWEEP_SOURCES:
+        with open(os.path.join(ROOT, "ouranos_gb300", "csrc", name), "rb") as f:
+            h.update(name.encode() + f.read())
+    return h.hexdigest()[:16]
 
 
 def bytes_per_solve(prob, real_bytes=8):
@@ -95,7 +128,10 @@ class ClockSampler:
         self.proc = None
         self.lines = []
 
-    def start(self):
+    def start(self, settle_s=3.0):
+        """Start sampling and return once the first sample is in (or after
+        settle_s): nvidia-smi's start-up, which can stall the GPU briefly,
+        then happens before the timed region rather than inside it."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu_id), "--query-gpu=" + self.FIELDS,
@@ -105,6 +141,10 @@ class ClockSampler:
             self.thread.start()
         except Exception:
             self.proc = None
+            return
+        t0 = time.time()
+        while not self.lines and time.time() - t0 < settle_s:
+            time.sleep(0.02)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -192,31 +232,38 @@ def cpu_reference_rate(prob, threads, reps=1):
 
 
 def run_reference(args):
+    """The reference's sweep restated on the CPU (the oracle, all host
+    threads), one full sweep of the workload per step.  Its inputs come from
+    the oracle's own generator (oracle/workloads.py), so this arm loads
+    nothing of the product."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    prob = workload_problem()
-    threads = os.cpu_count() or 1
-    # warm-up steps, then K timed steps; each step is one full sweep
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     import numpy as np
-    from oracle import pyoracle
-    O = pyoracle.OracleProblem(prob.arrays())
-    x = np.random.default_rng(0).standard_normal(prob.vector_length)
+    from oracle import pyoracle, workloads
+    spec = workloads.heterogeneous_2d(**WORKLOAD_ARGS)
+    threads = os.cpu_count() or 1
+    O = pyoracle.OracleProblem(spec)
+    x = np.random.default_rng(0).standard_normal(workloads.vector_length(spec))
     for _ in range(args.warmup):
         O.apply(x, threads=threads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         O.apply(x, threads=threads)
     dt = time.perf_counter() - t0
-    solves = prob.total_cells * prob.quad.n_dir
+    cells = int(np.prod(spec["n_cells"]))
+    nd, nm = spec["m2d"].shape
+    n = (spec["fe_order"] + 1) ** spec["dim"]
+    solves = cells * nd
     value = solves * args.steps / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64 material map)",
-        "config": {"workload": WORKLOAD, "cells": prob.total_cells, "directions": prob.quad.n_dir,
-                   "moments": prob.quad.n_mom, "solves_per_step": solves},
+        "vs_baseline": None, "dtype": "f64", "arithmetic": "FP64",
+        "data": "synthetic (seeded SplitMix64 material map, random flux moments)",
+        "config": workload_config(cells, nd, nm, n, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": "full sweep of the workload per step (oracle/ C++ restatement "
                                    "of src/RadiativeTransfer.cc sweep + Crout LU, linear "
@@ -225,6 +272,57 @@ def run_reference(args):
         "gpu_launches": 0,
     }
     print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_leg(prob, x, y_device, y_host, threads, reps, solve_check):
+    """The CPU baseline, and the oracle as the checker of what the GPU arm
+    computed (outside every timed region):
+      - the oracle's sweep timed on all host cores over `reps` full sweeps of
+        the workload, its result compared with the GPU Apply of the same x
+        (the device-vector and the host-vector call);
+      - the reference scheduler's O(T^2) fit and the single-core rate;
+      - with solve_check, the FP64 oracle solve of a reduced thick map that
+        the time-to-solution figures are checked against."""
+    import numpy as np
+    from oracle import pyoracle
+    O = pyoracle.OracleProblem(prob.arrays())
+    times, y_ref = [], None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        y_ref = O.apply(x, threads=threads)
+        times.append(time.perf_counter() - t0)
+    solves = prob.total_cells * prob.quad.n_dir
+    rate = solves / (sum(times) / len(times))
+    out = {"cpu": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": "%d full sweep(s) of the workload (%.1f s of CPU work) with the oracle/ C++ "
+                             "restatement of the reference sweep, directions split over threads"
+                             % (len(times), sum(times)),
+                   "faithful_scheduler": faithful_scheduler_fit(solves),
+                   "single_core": single_core_rate()},
+           "parity": {"rel_err": rel_l2(y_device, y_ref), "rel_err_e2e": rel_l2(y_host, y_ref),
+                      "bound": 1e-12, "against": "oracle FP64 Apply of the same x"}}
+    if solve_check:
+        out["oracle_solve"] = oracle_reduced_solve(solve_check, threads)
+    return out
+
+
+def rel_l2(a, b):
+    import numpy as np
+    return float(np.linalg.norm(np.asarray(a) - b) / np.linalg.norm(b))
+
+
+def oracle_reduced_solve(args, threads):
+    """FP64 GMRES(30) of the oracle to a 1e-10 residual on the reduced thick
+    map (the same seed, material distribution and quadrature as the
+    time-to-solution workload, n^3 cells)."""
+    import ouranos_gb300 as og
+    from oracle import pyoracle
+    prob = og.thick_3d(seed=args["seed"], n=args["n"], sn=12)
+    O = pyoracle.OracleProblem(prob.arrays(), order="cartesian")
+    t0 = time.perf_counter()
+    x, it, _ = O.solve("gmres", tol=1e-10, max_it=5000, restart=30, threads=threads)
+    return {"n": args["n"], "seed": args["seed"], "iterations": int(it), "seconds": time.perf_counter() - t0,
+            "tol": 1e-10, "solution": x}
 
 
 def replica_max(values, dist, device):
@@ -315,10 +413,35 @@ def run_ours(args):
     if not np.isfinite(yh.numpy()).all():
         raise RuntimeError("non-finite operator output")
 
+    # the same Apply with native FP64 arithmetic (the double-float default is
+    # the line's value), a few steps timed the same way
+    native = None
+    if args.precision == "fp64":
+        rt.set_stream(stream.cuda_stream)
+        rt.set_fp64_contractions("native")
+        for _ in range(3):
+            rt.Apply(x, y)
+        nms = []
+        for _ in range(max(3, min(args.steps, 10))):
+            flush.zero_()
+            ev0.record(stream)
+            rt.Apply(x, y)
+            ev1.record(stream)
+            ev1.synchronize()
+            nms.append(ev0.elapsed_time(ev1))
+        rt.set_fp64_contractions("df64_sweep")
+        rt.Apply(x, y)
+        torch.cuda.synchronize(dev)
+        native = {"ms_per_step": sum(nms) / len(nms), "value": solves / (sum(nms) / len(nms) / 1e3),
+                  "unit": UNIT, "steps": len(nms)}
+
     peak, peak_kind = measured_peaks()
-    # the captured configuration only: default seed, tiling and FP64 arithmetic
+    # the captured configuration only: default seed, tiling and FP64 arithmetic,
+    # and the sweep sources unchanged since the capture
+    digest = sweep_source_digest()
     profiled = (rank == 0 and rt.tiling() == PROFILED_TILING and world == 1)
-    traffic = SWEEP_TRAFFIC_BYTES.get(args.precision) if profiled else None
+    fresh = digest == SWEEP_TRAFFIC["digest"]
+    traffic = SWEEP_TRAFFIC["bytes"].get(args.precision) if (profiled and fresh) else None
     rb = 8 if args.precision == "fp64" else 4
     bps = bytes_per_solve(prob, rb)
     avg_sweep_s = sum(sweep_ms) / len(sweep_ms) / 1e3
@@ -326,36 +449,40 @@ def run_ours(args):
     fps = flops_per_solve(prob)
 
     cpu = None
+    parity = None
+    oracle_solve = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        rate, times = cpu_reference_rate(prob, threads, reps=max(1, args.cpu_reps))
-        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "%d full sweep(s) of the workload (%.1f s of CPU work) with the oracle/ C++ "
-                         "restatement of the reference sweep, directions split over threads"
-                         % (len(times), sum(times)),
-               "faithful_scheduler": faithful_scheduler_fit(solves),
-               "single_core": single_core_rate()}
+        leg = cpu_baseline_leg(prob, x.cpu().numpy(), y.cpu().numpy(), yh.numpy(), threads,
+                               max(1, args.cpu_reps),
+                               None if args.no_solve else {"seed": args.solve_seed, "n": args.oracle_n})
+        cpu, parity, oracle_solve = leg["cpu"], leg["parity"], leg.get("oracle_solve")
     tts = None
     if rank == 0 and world == 1 and not args.no_solve:
-        tts = time_to_solution(args.solve_seed, args.solve_n, args.tol, args.dsa_cg, args.max_it)
+        tts = time_to_solution(args.solve_seed, args.solve_n, args.tol, args.dsa_cg, args.max_it, oracle_solve)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "f32",
+            "arithmetic": ("double-float (FP32 pairs, ~48-bit significand) sweep and contractions, "
+                           "FP64 vectors" if args.precision == "fp64" else "FP32 sweep, FP64 vectors"),
             "data": "synthetic (seeded SplitMix64 material map, random flux moments)",
-            "config": {"workload": WORKLOAD, "cells": prob.total_cells,
-                       "directions": prob.quad.n_dir, "moments": prob.quad.n_mom,
-                       "dofs_per_cell": prob.dofs_per_cell, "solves_per_step": solves,
-                       "parallelism": "replicas" if world > 1 else "single-gpu",
-                       "l2": "flushed (256 MiB write) before every timed step",
-                       "tiling": list(rt.tiling())},
+            "config": workload_config(prob.total_cells, prob.quad.n_dir, prob.quad.n_mom,
+                                      prob.dofs_per_cell, world),
+            "timing": {"l2": "flushed (256 MiB write) before every timed step",
+                       "tiling": list(rt.tiling()), "events": "CUDA events on the operator's stream"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * L,
                     "d2h_bytes_per_step": 8 * L},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
                          "traffic": traffic,
+                         "traffic_source": ("ncu capture of this kernel source (digest %s)" % digest
+                                            if traffic is not None else
+                                            "none: sweep sources (digest %s) differ from the last capture "
+                                            "(%s) or the run is not the captured configuration"
+                                            % (digest, SWEEP_TRAFFIC["digest"])),
                          "peak_kind": peak_kind, "bytes_per_solve": bps,
                          "sweep_ms": avg_sweep_s * 1e3,
                          "fp_flops_per_solve": fps,
@@ -363,6 +490,11 @@ def run_ours(args):
             "gpu_launches": launches,
             "clocks": clocks,
         }
+        if native:
+            line["fp64_native_apply"] = native
+        if parity:
+            line["parity_rel_err"] = parity["rel_err"]
+            line["parity"] = parity
         if cpu:
             line["cpu_baseline"] = cpu
         if tts:
@@ -373,14 +505,23 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def time_to_solution(seed, n, tol, dsa_cg, max_it):
+def flux_errors(x, ref, n0):
+    """Scalar-flux (moment 0) relative L2 and relative max error of x against ref."""
+    import numpy as np
+    a, b = np.asarray(x)[:n0], np.asarray(ref)[:n0]
+    return {"rel_l2": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+            "rel_max": float(np.abs(a - b).max() / np.abs(b).max())}
+
+
+def time_to_solution(seed, n, tol, dsa_cg, max_it, oracle_solve=None):
     """Time to a `tol` relative residual on the 3-D thick diffusive map (n^3
     hexes, DG Q1, GLC S12): plain FP64 GMRES(30) against FGMRES(30) with FP32
     sweeps, FP64 restarts and the diffusion synthetic acceleration (dsa_cg CG
     steps).  Wall time of each ouranos_solve call (right-hand side, solve and
-    final FP64 residual on the device), iterations, the final FP64 residual
-    and the scalar-flux difference between the two solutions."""
-    import numpy as np
+    final FP64 residual on the device), iterations, the final FP64 residual.
+    Scalar-flux errors: at n^3 against the GPU's FP64 GMRES solve; and, when
+    the CPU leg has solved the reduced map of the same seed with the FP64
+    oracle, both methods on that map against the oracle."""
     import ouranos_gb300 as og
     prob = og.thick_3d(seed=seed, n=n, sn=12)
     out = {"workload": "3d-thick-%d^3-dgq1-glc12-seed%d" % (n, seed), "tol": tol, "dsa_cg_steps": dsa_cg,
@@ -393,8 +534,22 @@ def time_to_solution(seed, n, tol, dsa_cg, max_it):
     for name, info in (("fp64_gmres", i64), ("fp32_fgmres_dsa", idsa)):
         out[name] = {k: info[k] for k in ("seconds", "iterations", "restarts", "residual", "converged")}
     out["speedup"] = i64["seconds"] / idsa["seconds"]
-    out["flux_rel_l2_vs_fp64"] = float(np.linalg.norm(xd[:n0] - x64[:n0]) / np.linalg.norm(x64[:n0]))
-    out["flux_max_abs_vs_fp64"] = float(np.abs(xd[:n0] - x64[:n0]).max())
+    e = flux_errors(xd, x64, n0)
+    out["fp32_fgmres_dsa"]["flux_vs_gpu_fp64"] = e
+    out["flux_rel_l2_vs_fp64"] = e["rel_l2"]
+    if oracle_solve is not None:
+        small = og.thick_3d(seed=oracle_solve["seed"], n=oracle_solve["n"], sn=12)
+        ref = oracle_solve["solution"]
+        m0 = small.total_cells * small.dofs_per_cell
+        check = {"workload": "3d-thick-%d^3-dgq1-glc12-seed%d" % (oracle_solve["n"], oracle_solve["seed"]),
+                 "oracle": {k: oracle_solve[k] for k in ("iterations", "seconds", "tol")}}
+        with og.RadiativeTransfer(small) as rt:
+            rt.set_dsa(dsa_cg)
+            for name, method, dsa in (("fp64_gmres", "gmres", False), ("fp32_fgmres_dsa", "fgmres_mixed", True)):
+                xs, info, _ = rt.solve(method, tol=tol, max_it=max_it, restart=30, dsa=dsa)
+                check[name] = dict(flux_errors(xs, ref, m0), iterations=info["iterations"],
+                                   residual=info["residual"])
+        out["vs_fp64_oracle"] = check
     return out
 
 
@@ -434,10 +589,10 @@ def run_solve(args):
                                                 "converged")}
         if "gmres" in res:
             ref = res["gmres"][0]
+            n0 = prob.total_cells * prob.dofs_per_cell
             for m, (x, info) in res.items():
                 if m != "gmres":
-                    out[m]["flux_rel_l2_vs_fp64"] = float(np.linalg.norm(x - ref) / np.linalg.norm(ref))
-                    out[m]["flux_max_abs_vs_fp64"] = float(np.abs(x - ref).max())
+                    out[m]["flux_vs_gpu_fp64"] = flux_errors(x, ref, n0)
                     out[m]["speedup_vs_fp64_gmres"] = res["gmres"][1]["seconds"] / info["seconds"]
     print(json.dumps({"solve": out}), flush=True)
 
@@ -586,6 +741,8 @@ def main():
     ap.add_argument("--solve", action="store_true", help="time-to-solution mode")
     ap.add_argument("--solve-n", type=int, default=64)
     ap.add_argument("--solve-seed", type=int, default=7000, help="evaluation map (training uses 2000+)")
+    ap.add_argument("--oracle-n", type=int, default=16,
+                    help="side of the reduced thick map solved by the FP64 oracle for the error check")
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--max-it", type=int, default=3000)
     ap.add_argument("--methods", default="gmres,fgmres_mixed,gmres+dsa,fgmres_mixed+dsa,fgmres_learned")

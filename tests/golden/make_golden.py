@@ -19,9 +19,10 @@ boost and MPI are absent), so its numbers reach the test-suite this way:
                              values its Geometry/material tests expect
                              (``tests/Geometry_test.cc``, ``tests/RTMaterialProperties_test.cc``).
 
-Run:  python tests/golden/make_golden.py [reference_root]
-(default reference root: /root/reference).  The output is committed; the
-test-suite never reads the reference tree at run time.
+Run:  python tests/golden/make_golden.py <reference_root>
+(or with the root in the environment variable OURANOS_REFERENCE_ROOT).  The
+output is committed; the test-suite never reads the reference tree at run
+time.
 """
 import json
 import os
@@ -356,7 +357,9 @@ def inputs(root):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("OURANOS_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_golden.py <reference_root> (or set OURANOS_REFERENCE_ROOT)")
     outputs = {
         "ls_tables.json": ls_tables(root),
         "glc_gauss.json": glc_gauss(root),

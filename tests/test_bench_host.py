@@ -47,3 +47,33 @@ def test_one_process_keeps_its_own_figures():
     import bench
     assert bench.replica_max([2.5, 7], None, None) == [2.5, 7.0]
     assert bench.whole_job_rate(1, 500, 0.25) == 2000.0
+
+
+_REFERENCE_ARM = r"""
+import json, sys, types
+sys.path.insert(0, %r)
+import bench
+bench.WORKLOAD_ARGS = dict(bench.WORKLOAD_ARGS, n=16)
+bench.run_reference(types.SimpleNamespace(gpus=1, steps=1, warmup=0))
+maps = open("/proc/self/maps").read()
+print(json.dumps({"product_imported": "ouranos_gb300" in sys.modules,
+                  "product_mapped": "libouranos_gb300" in maps,
+                  "oracle_mapped": "liboracle" in maps}))
+"""
+
+
+def test_reference_arm_loads_nothing_of_the_product():
+    """The CPU reference arm builds its inputs with the oracle's own generator:
+    the product package is never imported and its library never mapped; its
+    config object carries the same keys as the GPU arm's."""
+    import subprocess
+    r = subprocess.run([sys.executable, "-c", _REFERENCE_ARM % ROOT], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
+    line, probe = lines[0], lines[-1]
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert not probe["product_imported"] and not probe["product_mapped"] and probe["oracle_mapped"]
+    sys.path.insert(0, ROOT)
+    import bench
+    assert line["config"] == bench.workload_config(16 * 16, 144, 10, 9, 1)
