@@ -357,6 +357,8 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     prob = workload_problem(seed=1001 + rank)
     rt = og.RadiativeTransfer(prob, device=local, precision=args.precision)
+    if args.precision == "fp32":
+        rt.set_fp32_contractions(args.fp32_contractions)
     stream = torch.cuda.current_stream(dev)
     rt.set_stream(stream.cuda_stream)
     L = prob.vector_length
@@ -434,6 +436,29 @@ def run_ours(args):
         torch.cuda.synchronize(dev)
         native = {"ms_per_step": sum(nms) / len(nms), "value": solves / (sum(nms) / len(nms) / 1e3),
                   "unit": UNIT, "steps": len(nms)}
+        # the FP32 Apply (the Arnoldi operator of the mixed-precision solves)
+        # with its contractions on the CUDA cores and on the tensor cores
+        fp32 = {}
+        rt.set_precision("fp32")
+        for mode in ("cuda_cores", "tensor"):
+            rt.set_fp32_contractions(mode)
+            for _ in range(3):
+                rt.Apply(x, y)
+            fms, fsw = [], []
+            for _ in range(max(3, min(args.steps, 10))):
+                flush.zero_()
+                ev0.record(stream)
+                rt.Apply(x, y)
+                ev1.record(stream)
+                ev1.synchronize()
+                fms.append(ev0.elapsed_time(ev1))
+                fsw.append(rt.last_sweep_ms()[0])
+            fp32[mode] = {"ms_per_step": sum(fms) / len(fms), "value": solves / (sum(fms) / len(fms) / 1e3),
+                          "sweep_ms": sum(fsw) / len(fsw), "unit": UNIT, "steps": len(fms)}
+        rt.set_precision("fp64")
+        rt.Apply(x, y)
+        torch.cuda.synchronize(dev)
+        native["fp32_apply"] = fp32
 
     peak, peak_kind = measured_peaks()
     # the captured configuration only: default seed, tiling and FP64 arithmetic,
@@ -491,6 +516,7 @@ def run_ours(args):
             "clocks": clocks,
         }
         if native:
+            line["fp32_apply"] = native.pop("fp32_apply")
             line["fp64_native_apply"] = native
         if parity:
             line["parity_rel_err"] = parity["rel_err"]
@@ -734,6 +760,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--fp32-contractions", default="tensor", choices=["cuda_cores", "tensor"],
+                    help="where an FP32 run's moment/direction contractions run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-reps", type=int, default=14, help="full CPU sweeps timed (~10 s on 16 cores)")
     ap.add_argument("--no-solve", action="store_true",

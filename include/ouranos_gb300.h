@@ -70,6 +70,13 @@ extern "C" {
 #define OURANOS_FP64_NATIVE 0
 #define OURANOS_FP64_DF64 1
 #define OURANOS_FP64_DF64_SWEEP 2
+/* Where the FP32 path's moment <-> direction contractions run:
+ *   CUDA_CORES FP32 multiply-adds on the CUDA cores;
+ *   TENSOR     tcgen05 MMAs on the tensor cores, every FP32 operand split
+ *              into three BF16 parts (products of part order <= 2 summed in
+ *              FP32: FP32 accuracy); up to 256 directions and 16 moments. */
+#define OURANOS_FP32_CONTRACT_CUDA_CORES 0
+#define OURANOS_FP32_CONTRACT_TENSOR 1
 
 /* Problem description: the data the reference spreads over Parameters,
  * Geometry, RTQuadrature and RTMaterialProperties (src/*.hh), restricted to a
@@ -133,6 +140,10 @@ int ouranos_rt_set_precision(ouranos_rt* rt, int precision);
 /* Select OURANOS_FP64_NATIVE, OURANOS_FP64_DF64 or OURANOS_FP64_DF64_SWEEP for
  * the FP64 path.  No reference counterpart. */
 int ouranos_rt_set_fp64_contractions(ouranos_rt* rt, int mode);
+/* Select OURANOS_FP32_CONTRACT_CUDA_CORES or OURANOS_FP32_CONTRACT_TENSOR for
+ * the FP32 path (UNSUPPORTED beyond 256 directions or 16 moments).  No
+ * reference counterpart. */
+int ouranos_rt_set_fp32_contractions(ouranos_rt* rt, int mode);
 /* Length of a flux-moment vector, n_mom * n_dofs: the size of the Epetra_Map
  * returned by OperatorDomainMap/OperatorRangeMap (src/RadiativeTransfer.hh:240-249). */
 int ouranos_rt_vector_length(const ouranos_rt* rt, long* length);

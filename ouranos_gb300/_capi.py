@@ -22,6 +22,7 @@ QUAD_LS, QUAD_GLC = 0, 1
 HARM_ORTHONORMAL, HARM_REFERENCE = 0, 1
 FP64, FP32 = 0, 1
 FP64_NATIVE, FP64_DF64, FP64_DF64_SWEEP = 0, 1, 2
+FP32_CONTRACT_CUDA_CORES, FP32_CONTRACT_TENSOR = 0, 1
 SOLVER_SI, SOLVER_GMRES, SOLVER_BICGSTAB, SOLVER_FGMRES_MIXED, SOLVER_FGMRES_LEARNED = 0, 1, 2, 3, 4
 SOLVER_WARM_START = 0x100
 SOLVER_DSA = 0x200
@@ -30,7 +31,7 @@ SOLVER_DSA = 0x200
 EXPORTS = [
     "ouranos_quadrature_sizes", "ouranos_quadrature_build",
     "ouranos_rt_create", "ouranos_rt_destroy", "ouranos_rt_set_group",
-    "ouranos_rt_set_precision", "ouranos_rt_set_fp64_contractions", "ouranos_rt_vector_length", "ouranos_rt_n_tasks",
+    "ouranos_rt_set_precision", "ouranos_rt_set_fp64_contractions", "ouranos_rt_set_fp32_contractions", "ouranos_rt_vector_length", "ouranos_rt_n_tasks",
     "ouranos_rt_scattering_source", "ouranos_rt_sweep", "ouranos_rt_apply",
     "ouranos_rt_sweep_rhs", "ouranos_rt_task_levels", "ouranos_wavefront_levels",
     "ouranos_rt_set_stream", "ouranos_rt_last_error",
@@ -103,6 +104,7 @@ def lib():
         "ouranos_rt_set_group": [vp, i],
         "ouranos_rt_set_precision": [vp, i],
         "ouranos_rt_set_fp64_contractions": [vp, i],
+        "ouranos_rt_set_fp32_contractions": [vp, i],
         "ouranos_rt_vector_length": [vp, C.POINTER(l)],
         "ouranos_rt_n_tasks": [vp, C.POINTER(l)],
         "ouranos_rt_scattering_source": [vp, vp],

@@ -170,6 +170,24 @@ cudaError_t launch_expand_sym_pairs(const df64* T, const df64* iso, const SymTab
                                     long n_dofs, cudaStream_t s, long len = -1);
 cudaError_t launch_reduce_sym_pairs(const df64* psi, const SymTables& st, double* phi, int n_mom, long n_dofs,
                                     cudaStream_t s, long len = -1);
+// The FP32 contractions on the tensor cores (contract_tc.cu): B operand
+// images of M2D and D2M (three BF16 parts each, K-major core-matrix layout),
+// built once per handle on the host.
+struct TcTables {
+  const uint8_t* m2d_img = nullptr;  // [3][npad directions][16 moments]
+  const uint8_t* d2m_img = nullptr;  // [3][16 moment slots][kpad directions]
+  int n_dir = 0, n_mom = 0, npad = 0, kpad = 0;
+};
+bool tc_contractions_fit(int n_dir, int n_mom);
+void tc_build_images(const std::vector<double>& m2d, const std::vector<double>& d2m, int n_dir, int n_mom,
+                     std::vector<uint8_t>& m2d_img, std::vector<uint8_t>& d2m_img, int& npad, int& kpad);
+// q[d][e] = sum_m M2D[d][m] T[m][e] (+ iso[e]) and phi[m][e] = sum_d D2M[m][d]
+// psi[d][e] for the dofs [0, len) of the pointers (rows n_dofs apart); a wait
+// for the tensor cores that runs past limit_ns sets bit 4 of *status
+cudaError_t launch_expand_tc(const float* T, const float* iso, const TcTables& t, float* q, long n_dofs, int* status,
+                             long long limit_ns, cudaStream_t s, long len = -1);
+cudaError_t launch_reduce_tc(const float* psi, const TcTables& t, float* phi, long n_dofs, int* status,
+                             long long limit_ns, cudaStream_t s, long len = -1);
 // phi[m][e] = sum_d D2M[m][d] psi[d][e]  -- direction -> moment reduction
 template <typename real>
 cudaError_t launch_reduce_moments(const real* psi, const real* d2m_t, real* phi, int n_dir,
@@ -318,6 +336,9 @@ struct ouranos_rt {
   ouranos::FETables fe;
   int precision = OURANOS_FP64;
   int fp64_contract = OURANOS_FP64_DF64_SWEEP;  // arithmetic of the FP64 path
+  int fp32_contract = OURANOS_FP32_CONTRACT_CUDA_CORES;  // where the FP32 path's contractions run
+  ouranos::TcTables tc;                                  // their tensor-core tables (tc.npad 0: none)
+  ouranos::DevBuf d_tc_m2d, d_tc_d2m;
   // schedule
   int wx = 0, wy = 1, kd = 0;          // 0 = not chosen yet
   int lpc = 1;                         // lanes per cell (2 only for cells of >= 9 dofs)

@@ -111,7 +111,7 @@ const real* tbl(const DevBuf& b64, const DevBuf& b32, const DevBuf& bdf) {
 
 // q = M2D T in the contraction form of the regular Apply for this arithmetic
 template <typename real>
-cudaError_t expand(const ouranos_rt* rt, const real* T, real* q, cudaStream_t st) {
+cudaError_t expand(const ouranos_rt* rt, const real* T, real* q, int* status, cudaStream_t st) {
   const long nd = rt->n_dofs;
   if constexpr (std::is_same<real, df64>::value) {
     if (rt->sym.n_class) return launch_expand_sym_pairs(T, nullptr, rt->sym, q, rt->n_mom, nd, st);
@@ -121,13 +121,15 @@ cudaError_t expand(const ouranos_rt* rt, const real* T, real* q, cudaStream_t st
       return launch_expand_source_df64(T, nullptr, rt->d_m2d64.as<double>(), q, rt->n_dir, rt->n_mom, nd, st);
     return launch_expand_source<double>(T, nullptr, rt->d_m2d64.as<double>(), q, rt->n_dir, rt->n_mom, nd, st);
   } else {
+    if (rt->fp32_contract == OURANOS_FP32_CONTRACT_TENSOR)
+      return launch_expand_tc(T, nullptr, rt->tc, q, nd, status, rt->wait_limit_ns, st);
     return launch_expand_source<float>(T, nullptr, rt->d_m2d32.as<float>(), q, rt->n_dir, rt->n_mom, nd, st);
   }
 }
 
 // phi = D2M psi, likewise; phi is float for the FP32 sweep, double otherwise
 template <typename real>
-cudaError_t reduce(const ouranos_rt* rt, const real* psi, void* phi, cudaStream_t st) {
+cudaError_t reduce(const ouranos_rt* rt, const real* psi, void* phi, int* status, cudaStream_t st) {
   const long nd = rt->n_dofs;
   if constexpr (std::is_same<real, df64>::value) {
     if (rt->sym.n_class) return launch_reduce_sym_pairs(psi, rt->sym, (double*)phi, rt->n_mom, nd, st);
@@ -139,6 +141,8 @@ cudaError_t reduce(const ouranos_rt* rt, const real* psi, void* phi, cudaStream_
     return launch_reduce_moments<double>(psi, rt->d_d2m64.as<double>(), (double*)phi, rt->n_dir, rt->n_mom, nd,
                                          st);
   } else {
+    if (rt->fp32_contract == OURANOS_FP32_CONTRACT_TENSOR)
+      return launch_reduce_tc(psi, rt->tc, (float*)phi, nd, status, rt->wait_limit_ns, st);
     return launch_reduce_moments<float>(psi, rt->d_d2m32.as<float>(), (float*)phi, rt->n_dir, rt->n_mom, nd, st);
   }
 }
@@ -173,7 +177,7 @@ int apply_noalloc(ouranos_rt* rt, unsigned char* base, const Layout& L, bool exp
                                     rt->d_material.as<int>(), rt->n_mat, rt->G, rt->group,
                                     rt->n_cells, rt->n, rt->n_mom, rt->n_dofs, st),
         "scattering source");
-  if (expand_source) NA_CU(expand<real>(rt, T, q, st), "source expansion");
+  if (expand_source) NA_CU(expand<real>(rt, T, q, ctrl + 1, st), "source expansion");
   SweepArgs<real> a;
   a.nx = rt->nx[0];
   a.ny = rt->nx[1];
@@ -214,7 +218,7 @@ int apply_noalloc(ouranos_rt* rt, unsigned char* base, const Layout& L, bool exp
   NA_CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, rt->device), "device query");
   const int grid = std::min((rt->n_tasks + 3) / 4, std::max(1, sms * 8));
   NA_CU(launch_sweep<real>(rt->dim, rt->p1, expand_source ? 0 : rt->n_mom, a, grid, 128, st), "sweep");
-  NA_CU(reduce<real>(rt, psi, phi, st), "moment reduction");
+  NA_CU(reduce<real>(rt, psi, phi, ctrl + 1, st), "moment reduction");
   if constexpr (std::is_same<real, float>::value)
     NA_CU(launch_combine<float>(xd, (const float*)phi, yd, len, 1.0, -1.0, st), "combine");
   else
@@ -225,7 +229,9 @@ int apply_noalloc(ouranos_rt* rt, unsigned char* base, const Layout& L, bool exp
   NA_CU(cudaStreamSynchronize(st), "apply");
   int status = 0;
   NA_CU(cudaMemcpy(&status, ctrl + 1, sizeof(int), cudaMemcpyDeviceToHost), "status");
-  if (status) return fail(rt, OURANOS_ERR_TIMEOUT, "sweep dependency wait timed out");
+  if (status)
+    return fail(rt, OURANOS_ERR_TIMEOUT,
+                (status & 4) ? "tensor-core contraction: MMA completion wait timed out" : "sweep dependency wait timed out");
   return OURANOS_OK;
 }
 

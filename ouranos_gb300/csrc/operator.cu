@@ -359,6 +359,10 @@ int sweep_expand(ouranos_rt* rt, const real* src, const real* iso, long e0, long
     CU(launch_expand_source_df64((const double*)src, (const double*)iso, rt->d_m2d64.as<double>(),
                                  rt->d_q.as<double>() + e0, rt->n_dir, rt->n_mom, nd, rt->stream, len),
        "source expansion");
+  else if (std::is_same<real, float>::value && rt->fp32_contract == OURANOS_FP32_CONTRACT_TENSOR)
+    CU(launch_expand_tc((const float*)src, (const float*)iso, rt->tc, rt->d_q.as<float>() + e0, nd,
+                        rt->d_ctrl.as<int>() + 1, rt->wait_limit_ns, rt->stream, len),
+       "source expansion");
   else
     CU(launch_expand_source<real>(src, iso, table<real>(rt->d_m2d64, rt->d_m2d32, rt->d_m2ddf),
                                   rt->d_q.as<real>() + e0, rt->n_dir, rt->n_mom, nd, rt->stream, len),
@@ -453,6 +457,10 @@ int sweep_reduce(ouranos_rt* rt, const real* psi, void* phi, long e0 = 0, long l
     CU(launch_reduce_moments<double>((const double*)psi, rt->d_d2m64.as<double>(), phi64, rt->n_dir,
                                      rt->n_mom, nd, rt->stream, len),
        "moment reduction");
+  else if (rt->fp32_contract == OURANOS_FP32_CONTRACT_TENSOR)
+    CU(launch_reduce_tc((const float*)psi, rt->tc, (float*)phi + e0, nd, rt->d_ctrl.as<int>() + 1,
+                        rt->wait_limit_ns, rt->stream, len),
+       "moment reduction");
   else
     CU(launch_reduce_moments<float>((const float*)psi, rt->d_d2m32.as<float>(), (float*)phi + e0, rt->n_dir,
                                     rt->n_mom, nd, rt->stream, len),
@@ -516,7 +524,9 @@ int finish(ouranos_rt* rt) {
   else
     (void)cudaGetLastError();  // no sweep recorded the events: not an error of this call
   if (st) {
-    rt->err = (st & 2) ? "diffusion acceleration: grid barrier wait timed out" : "sweep dependency wait timed out";
+    rt->err = (st & 2)   ? "diffusion acceleration: grid barrier wait timed out"
+              : (st & 4) ? "tensor-core contraction: MMA completion wait timed out"
+                         : "sweep dependency wait timed out";
     return OURANOS_ERR_TIMEOUT;
   }
   return OURANOS_OK;
@@ -969,6 +979,17 @@ int ouranos_rt_create(const ouranos_problem_desc* D, int device, ouranos_rt** ou
   if (!rt->cell_order.empty() && (rc = upload(rt, rt->d_cell_order, rt->cell_order, "cell order")))
     return fail(rc);
   if ((rc = build_symmetry(rt))) return fail(rc);
+  if (tc_contractions_fit(rt->n_dir, rt->n_mom)) {
+    std::vector<uint8_t> mi, di;
+    tc_build_images(rt->m2d, rt->d2m, rt->n_dir, rt->n_mom, mi, di, rt->tc.npad, rt->tc.kpad);
+    if ((rc = upload(rt, rt->d_tc_m2d, mi, "tensor-core tables")) ||
+        (rc = upload(rt, rt->d_tc_d2m, di, "tensor-core tables")))
+      return fail(rc);
+    rt->tc.m2d_img = rt->d_tc_m2d.as<uint8_t>();
+    rt->tc.d2m_img = rt->d_tc_d2m.as<uint8_t>();
+    rt->tc.n_dir = rt->n_dir;
+    rt->tc.n_mom = rt->n_mom;
+  }
   if ((rc = default_tiling(rt)) || (rc = build_schedule(rt)) || (rc = setup_group(rt)))
     return fail(rc);
   if (cudaStreamSynchronize(rt->stream) != cudaSuccess)
@@ -1018,6 +1039,18 @@ int ouranos_rt_set_fp64_contractions(ouranos_rt* rt, int mode) {
   if (mode != OURANOS_FP64_NATIVE && mode != OURANOS_FP64_DF64 && mode != OURANOS_FP64_DF64_SWEEP)
     return bad(rt, "unknown FP64 mode");
   rt->fp64_contract = mode;
+  return OURANOS_OK;
+}
+
+int ouranos_rt_set_fp32_contractions(ouranos_rt* rt, int mode) {
+  if (!rt) return OURANOS_ERR_BAD_INPUT;
+  if (mode != OURANOS_FP32_CONTRACT_CUDA_CORES && mode != OURANOS_FP32_CONTRACT_TENSOR)
+    return bad(rt, "unknown FP32 contraction mode");
+  if (mode == OURANOS_FP32_CONTRACT_TENSOR && !rt->tc.npad) {
+    rt->err = "tensor-core contractions take at most 256 directions and 16 moments";
+    return OURANOS_ERR_UNSUPPORTED;
+  }
+  rt->fp32_contract = mode;
   return OURANOS_OK;
 }
 

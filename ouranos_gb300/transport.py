@@ -95,6 +95,12 @@ class RadiativeTransfer:
              "df64_sweep": _capi.FP64_DF64_SWEEP}[mode]
         self._check(_capi.lib().ouranos_rt_set_fp64_contractions(self._h, m))
 
+    def set_fp32_contractions(self, mode):
+        """FP32 path contractions: 'cuda_cores' (FP32 multiply-adds) or
+        'tensor' (tcgen05 MMAs on three-part BF16 splits)."""
+        m = {"cuda_cores": _capi.FP32_CONTRACT_CUDA_CORES, "tensor": _capi.FP32_CONTRACT_TENSOR}[mode]
+        self._check(_capi.lib().ouranos_rt_set_fp32_contractions(self._h, m))
+
     def get_n_tasks_to_execute(self):
         return self.n_tasks
 
