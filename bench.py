@@ -24,8 +24,10 @@ per step.  Prints one JSON line.
              FP64 for the time-to-solution error check.
   time_to_solution = time to a 1e-8 residual on the 64^3 thick map: plain FP64
              GMRES(30) against FGMRES(30) with FP32 sweeps and the diffusion
-             synthetic acceleration, scalar-flux errors against the FP64 solve
-             and (on the reduced map) against the FP64 oracle.
+             synthetic acceleration, with its CG started from the trained
+             network's prediction (the metric's learned leg) and from zero;
+             scalar-flux errors against the FP64 solve and (on the reduced
+             map) against the FP64 oracle.
 --impl reference: the CPU restatement of the reference's sweep (the reference
   itself needs deal.II/Trilinos/p4est/MPI, absent here), all host threads,
   timed per step, on inputs from the oracle's own generator (nothing of the
@@ -539,42 +541,77 @@ def flux_errors(x, ref, n0):
             "rel_max": float(np.abs(a - b).max() / np.abs(b).max())}
 
 
-def time_to_solution(seed, n, tol, dsa_cg, max_it, oracle_solve=None):
+LEARNED_WEIGHTS = os.path.join(ROOT, "ouranos_gb300", "weights", "dsa_guess_thick3d.npz")
+LEARNED_CG = 3  # CG steps of the diffusion correction in the learned leg (and its comparison)
+
+
+def time_to_solution(seed, n, tol, dsa_cg, max_it, oracle_solve=None, learned_cg=LEARNED_CG):
     """Time to a `tol` relative residual on the 3-D thick diffusive map (n^3
-    hexes, DG Q1, GLC S12): plain FP64 GMRES(30) against FGMRES(30) with FP32
-    sweeps, FP64 restarts and the diffusion synthetic acceleration (dsa_cg CG
-    steps).  Wall time of each ouranos_solve call (right-hand side, solve and
-    final FP64 residual on the device), iterations, the final FP64 residual.
-    Scalar-flux errors: at n^3 against the GPU's FP64 GMRES solve; and, when
-    the CPU leg has solved the reduced map of the same seed with the FP64
-    oracle, both methods on that map against the oracle."""
+    hexes, DG Q1, GLC S12), every method FGMRES(30)/GMRES(30) on the device:
+      fp64_gmres              plain FP64 GMRES (the reference's method);
+      fp32_fgmres_learned_dsa FP32 sweeps, FP64 restarts, right preconditioner
+                              the diffusion correction with learned_cg CG steps
+                              started from the trained network's prediction;
+      fp32_fgmres_dsa_same_cg the same without the network (zero start);
+      fp32_fgmres_dsa         the same with dsa_cg CG steps.
+    Wall time of each ouranos_solve call (right-hand side, solve and final
+    FP64 residual), iterations, final FP64 residual.  Scalar-flux errors: at
+    n^3 against the GPU's FP64 GMRES solve; and, when the CPU leg has solved
+    the reduced map of the same seed with the FP64 oracle, every method on that
+    map against the oracle."""
     import ouranos_gb300 as og
+    from ouranos_gb300.learned import Network, install
+    if not os.path.exists(LEARNED_WEIGHTS):
+        raise FileNotFoundError("trained network weights missing: %s" % LEARNED_WEIGHTS)
     prob = og.thick_3d(seed=seed, n=n, sn=12)
     out = {"workload": "3d-thick-%d^3-dgq1-glc12-seed%d" % (n, seed), "tol": tol, "dsa_cg_steps": dsa_cg,
+           "learned_cg_steps": learned_cg, "learned_weights": os.path.relpath(LEARNED_WEIGHTS, ROOT),
            "cell_dir_solves_per_sweep": prob.total_cells * prob.quad.n_dir}
+    keys = ("seconds", "iterations", "restarts", "residual", "converged")
+
+    def run_all(rt, grid):
+        sols, infos = {}, {}
+        net = Network.load(LEARNED_WEIGHTS, grid)
+        try:
+            sols["fp64_gmres"], infos["fp64_gmres"], _ = rt.solve("gmres", tol=tol, max_it=max_it, restart=30)
+            rt.set_dsa(dsa_cg)
+            sols["fp32_fgmres_dsa"], infos["fp32_fgmres_dsa"], _ = rt.solve(
+                "fgmres_mixed", tol=tol, max_it=max_it, restart=30, dsa=True)
+            rt.set_dsa(learned_cg)
+            sols["fp32_fgmres_dsa_same_cg"], infos["fp32_fgmres_dsa_same_cg"], _ = rt.solve(
+                "fgmres_mixed", tol=tol, max_it=max_it, restart=30, dsa=True)
+            install(rt, net)
+            sols["fp32_fgmres_learned_dsa"], infos["fp32_fgmres_learned_dsa"], _ = rt.solve(
+                "fgmres_learned", tol=tol, max_it=max_it, restart=30, dsa=True)
+            install(rt, None)
+        finally:
+            net.close()
+        return sols, infos
+
     with og.RadiativeTransfer(prob) as rt:
-        rt.set_dsa(dsa_cg)
-        x64, i64, _ = rt.solve("gmres", tol=tol, max_it=max_it, restart=30)
-        xd, idsa, _ = rt.solve("fgmres_mixed", tol=tol, max_it=max_it, restart=30, dsa=True)
+        sols, infos = run_all(rt, (n, n, n))
     n0 = prob.total_cells * prob.dofs_per_cell
-    for name, info in (("fp64_gmres", i64), ("fp32_fgmres_dsa", idsa)):
-        out[name] = {k: info[k] for k in ("seconds", "iterations", "restarts", "residual", "converged")}
-    out["speedup"] = i64["seconds"] / idsa["seconds"]
-    e = flux_errors(xd, x64, n0)
-    out["fp32_fgmres_dsa"]["flux_vs_gpu_fp64"] = e
-    out["flux_rel_l2_vs_fp64"] = e["rel_l2"]
+    for name, info in infos.items():
+        out[name] = {k: info[k] for k in keys}
+        if name != "fp64_gmres":
+            out[name]["flux_vs_gpu_fp64"] = flux_errors(sols[name], sols["fp64_gmres"], n0)
+            out[name]["speedup_vs_fp64_gmres"] = infos["fp64_gmres"]["seconds"] / info["seconds"]
+    out["speedup"] = out["fp32_fgmres_learned_dsa"]["speedup_vs_fp64_gmres"]
+    out["learned_gain_same_cg"] = {
+        "iterations": [infos["fp32_fgmres_dsa_same_cg"]["iterations"], infos["fp32_fgmres_learned_dsa"]["iterations"]],
+        "seconds": [infos["fp32_fgmres_dsa_same_cg"]["seconds"], infos["fp32_fgmres_learned_dsa"]["seconds"]]}
     if oracle_solve is not None:
-        small = og.thick_3d(seed=oracle_solve["seed"], n=oracle_solve["n"], sn=12)
+        m = oracle_solve["n"]
+        small = og.thick_3d(seed=oracle_solve["seed"], n=m, sn=12)
         ref = oracle_solve["solution"]
         m0 = small.total_cells * small.dofs_per_cell
-        check = {"workload": "3d-thick-%d^3-dgq1-glc12-seed%d" % (oracle_solve["n"], oracle_solve["seed"]),
+        check = {"workload": "3d-thick-%d^3-dgq1-glc12-seed%d" % (m, oracle_solve["seed"]),
                  "oracle": {k: oracle_solve[k] for k in ("iterations", "seconds", "tol")}}
         with og.RadiativeTransfer(small) as rt:
-            rt.set_dsa(dsa_cg)
-            for name, method, dsa in (("fp64_gmres", "gmres", False), ("fp32_fgmres_dsa", "fgmres_mixed", True)):
-                xs, info, _ = rt.solve(method, tol=tol, max_it=max_it, restart=30, dsa=dsa)
-                check[name] = dict(flux_errors(xs, ref, m0), iterations=info["iterations"],
-                                   residual=info["residual"])
+            ssols, sinfos = run_all(rt, (m, m, m))
+        for name, info in sinfos.items():
+            check[name] = dict(flux_errors(ssols[name], ref, m0), iterations=info["iterations"],
+                               residual=info["residual"])
         out["vs_fp64_oracle"] = check
     return out
 
@@ -595,15 +632,10 @@ def run_solve(args):
     with og.RadiativeTransfer(prob) as rt:
         res = {}
         methods = args.methods.split(",")
-        if "fgmres_learned" in methods:
+        if any(m.startswith("fgmres_learned") for m in methods):
             from ouranos_gb300.learned import Network, install
-            wpath = os.path.join(ROOT, "ouranos_gb300", "weights", "precond_thick3d.npz")
-            if os.path.exists(wpath):
-                install(rt, Network.load(wpath, (n, n, n)))
-                out["learned_weights"] = os.path.relpath(wpath, ROOT)
-            else:
-                methods.remove("fgmres_learned")
-                out["learned_weights"] = None
+            install(rt, Network.load(LEARNED_WEIGHTS, (n, n, n)))
+            out["learned_weights"] = os.path.relpath(LEARNED_WEIGHTS, ROOT)
         if any(m.endswith("+dsa") for m in methods):
             rt.set_dsa(args.dsa_cg)
             out["dsa_cg_steps"] = args.dsa_cg
@@ -760,7 +792,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
-    ap.add_argument("--fp32-contractions", default="tensor", choices=["cuda_cores", "tensor"],
+    ap.add_argument("--fp32-contractions", default="cuda_cores", choices=["cuda_cores", "tensor"],
                     help="where an FP32 run's moment/direction contractions run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-reps", type=int, default=14, help="full CPU sweeps timed (~10 s on 16 cores)")
@@ -773,7 +805,7 @@ def main():
                     help="side of the reduced thick map solved by the FP64 oracle for the error check")
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--max-it", type=int, default=3000)
-    ap.add_argument("--methods", default="gmres,fgmres_mixed,gmres+dsa,fgmres_mixed+dsa,fgmres_learned")
+    ap.add_argument("--methods", default="gmres,fgmres_mixed,gmres+dsa,fgmres_mixed+dsa,fgmres_learned+dsa")
     ap.add_argument("--dsa-cg", type=int, default=20, help="CG steps of the diffusion correction")
     ap.add_argument("--batch", action="store_true", help="batched uneven 2-D workload")
     ap.add_argument("--batch-count", type=int, default=64)

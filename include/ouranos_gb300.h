@@ -233,7 +233,10 @@ int ouranos_rt_apply_noalloc(ouranos_rt* rt, const double* x, double* y);
 #define OURANOS_SOLVER_FGMRES_MIXED 3
 /* FGMRES_MIXED with the learned right preconditioner installed by
  * ouranos_rt_set_preconditioner; falls back to the plain method for the rest of
- * the solve when a preconditioned restart cycle stagnates. */
+ * the solve when a preconditioned restart cycle stagnates.  With
+ * OURANOS_SOLVER_DSA the network's output is the initial guess of the
+ * diffusion correction's CG (ouranos_rt_pc_dsa_apply), and the diffusion
+ * correction from a zero guess is the fallback. */
 #define OURANOS_SOLVER_FGMRES_LEARNED 4
 /* OR into the solver: x holds the initial guess (not with BiCGSTAB) */
 #define OURANOS_SOLVER_WARM_START 0x100
@@ -375,6 +378,13 @@ int ouranos_rt_pc_features(ouranos_rt* rt, const double* v, float* features, dou
 int ouranos_rt_pc_target(ouranos_rt* rt, const double* v, const double* e, float* target);
 /* z = v + s g_c y, y the network output on v's features (device vectors) */
 int ouranos_rt_pc_apply(ouranos_rt* rt, const double* v, double* z);
+/* z = P v of the diffusion acceleration (ouranos_rt_set_dsa) with its CG
+ * started from the network's prediction of the correction f (vertex values
+ * s K y averaged over the cells at each vertex, scaled to their
+ * energy-norm-optimal multiple) instead of from zero (device vectors).  The
+ * CG converges to the same f from any start: the network saves CG steps, it
+ * cannot change what they converge to. */
+int ouranos_rt_pc_dsa_apply(ouranos_rt* rt, const double* v, double* z);
 
 /* ------------------------------------- diffusion synthetic acceleration
  * No counterpart in the reference (identity preconditioner, plain source

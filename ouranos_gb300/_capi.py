@@ -41,7 +41,7 @@ EXPORTS = [
     "ouranos_cnn_create", "ouranos_cnn_destroy", "ouranos_cnn_n_params", "ouranos_cnn_get_params",
     "ouranos_cnn_set_params", "ouranos_cnn_forward", "ouranos_cnn_gradients",
     "ouranos_cnn_train_step", "ouranos_cnn_last_error", "ouranos_rt_set_preconditioner",
-    "ouranos_rt_pc_features", "ouranos_rt_pc_target", "ouranos_rt_pc_apply",
+    "ouranos_rt_pc_features", "ouranos_rt_pc_target", "ouranos_rt_pc_apply", "ouranos_rt_pc_dsa_apply",
     "ouranos_batch_create", "ouranos_batch_destroy", "ouranos_batch_layout", "ouranos_batch_apply",
     "ouranos_batch_rhs", "ouranos_batch_solve", "ouranos_batch_autotune", "ouranos_batch_set_graphs",
     "ouranos_batch_stats", "ouranos_batch_last_error",

@@ -29,6 +29,10 @@
 //   matvec : w = C z, p = z + beta p, q = w + beta q, pq = p.q, alpha = rz/pq
 //   update : x += alpha p, r -= alpha q, z = r / diag, rz' = r.z, beta = rz'/rz
 // (q = C p is carried by recurrence, so the matrix is applied once per step).
+// A caller may start the CG from a guess of f (the learned preconditioner's
+// prediction): it is first scaled to its energy-norm-optimal multiple, one
+// more grid barrier, so a poor guess can never start the CG farther from the
+// solution than zero does.
 // Every block sums the per-block partials of a dot product in block order, so
 // all blocks hold the same, deterministic scalars.
 #include <algorithm>
@@ -328,7 +332,8 @@ __device__ __forceinline__ void cg_body(const DsaGeom& g, const float4* __restri
                                         long n0, const float* __restrict__ dinv, float* x, float* r, float* z,
                                         float* p, float* q, double* part_a, double* part_b, int lb, int nb,
                                         DsaSync* sync, int* status, long long limit_ns, int iters,
-                                        const float* __restrict__ fe, int n) {
+                                        const float* __restrict__ fe, int n, const float* __restrict__ x0,
+                                        double* part_c) {
   constexpr int NCORNER = DIM == 3 ? 8 : 4;
   // the cell tables: mixed mass [corner][n] (measure folded in), then the
   // interpolation of the vertex values at the nodes [n][corner]
@@ -340,16 +345,53 @@ __device__ __forceinline__ void cg_body(const DsaGeom& g, const float4* __restri
   __syncthreads();
   const int stride = nb * kCgThreads;
   const int first = lb * kCgThreads + threadIdx.x;
-  // r = rhs, z = r / diag, x = 0
+  // x = 0, r = rhs without a guess.  With a guess g (x0, written before the
+  // launch with a zero halo like z, so every block reads its neighbours'
+  // values without a barrier) the start is the multiple of g closest to the
+  // solution in the energy norm, x = a g with a = (g, rhs) / (g, C g) (a
+  // Galerkin step on span{g}: never farther from the solution than x = 0,
+  // whatever the guess), and r = rhs - a C g (C g kept in q meanwhile).
   float t = 0.f;
+  float a0 = 0.f;
+  if (x0) {
+    float t1 = 0.f, t2 = 0.f;
+    for (int vid = first; vid < g.nv; vid += stride) {
+      int I, J, K;
+      vertex_ijk(g, vid, I, J, K);
+      const float rr = assemble_rhs<DIM>(g, cell, v, I, J, K, smix, n);
+      float w = 0.f;
+#pragma unroll
+      for (int s = 0; s < kStencil<DIM>; ++s) w += coef[(long)s * g.nv + vid] * x0[vid + g.off[s]];
+      r[vid] = rr;
+      q[vid] = w;
+      t1 += x0[vid] * rr;
+      t2 += x0[vid] * w;
+    }
+    // part_c is written here only, so no later phase overwrites it while a
+    // slower block still reads it; part_a is next written after a barrier
+    const double b1 = block_sum(t1), b2 = block_sum(t2);
+    if (threadIdx.x == 0) {
+      part_a[lb] = b1;
+      part_c[lb] = b2;
+    }
+    if (!grid_barrier(sync, status, limit_ns)) return;
+    const double gb = all_sum(part_a, nb), gcg = all_sum(part_c, nb);
+    a0 = gcg > 0.0 ? (float)(gb / gcg) : 0.f;
+  }
   for (int vid = first; vid < g.nv; vid += stride) {
-    int I, J, K;
-    vertex_ijk(g, vid, I, J, K);
-    const float rr = assemble_rhs<DIM>(g, cell, v, I, J, K, smix, n);
+    float rr, xx = 0.f;
+    if (x0) {
+      xx = a0 * x0[vid];
+      rr = r[vid] - a0 * q[vid];
+    } else {
+      int I, J, K;
+      vertex_ijk(g, vid, I, J, K);
+      rr = assemble_rhs<DIM>(g, cell, v, I, J, K, smix, n);
+    }
     const float zz = rr * dinv[vid];
     r[vid] = rr;
     z[vid] = zz;
-    x[vid] = 0.f;
+    x[vid] = xx;
     t += rr * zz;
   }
   double bt = block_sum(t);
@@ -435,9 +477,10 @@ __global__ void __launch_bounds__(kCgThreads, 1) dsa_cg_kernel(DsaGeom g, const 
                                                           float* z, float* p, float* q, double* part_a,
                                                           double* part_b, DsaSync* sync, int* status,
                                                           long long limit_ns, int iters,
-                                                          const float* __restrict__ fe, int n) {
+                                                          const float* __restrict__ fe, int n,
+                                                          const float* __restrict__ x0, double* part_c) {
   cg_body<DIM>(g, cell, coef, v, out, len, n0, dinv, x, r, z, p, q, part_a, part_b, (int)blockIdx.x,
-               (int)gridDim.x, sync, status, limit_ns, iters, fe, n);
+               (int)gridDim.x, sync, status, limit_ns, iters, fe, n, x0, part_c);
 }
 
 // One problem of a batched diffusion solve: its tables, vectors and the
@@ -469,7 +512,8 @@ __global__ void __launch_bounds__(kCgThreads, 1) dsa_cg_batch_kernel(const DsaPr
   __syncthreads();
   const int lb = (int)blockIdx.x - P.block0;
   cg_body<DIM>(P.g, P.cell, P.coef, P.v, P.out, P.len, P.n0, P.dinv, P.x, P.r, P.z, P.p, P.q,
-               part_a + P.block0, part_b + P.block0, lb, P.nblk, sync, status, limit_ns, iters, P.fe, P.n);
+               part_a + P.block0, part_b + P.block0, lb, P.nblk, sync, status, limit_ns, iters, P.fe, P.n,
+               nullptr, nullptr);
 }
 
 int dfail(ouranos_rt* rt, cudaError_t e, const char* what) {
@@ -611,9 +655,10 @@ int ensure_tables(ouranos_rt* rt) {
   const int nb = nblocks(nv);
   DC(rt->d_dsa_cell.alloc(sizeof(float4) * rt->n_cells), "tables");
   const int ns = rt->dim == 3 ? kStencil<3> : kStencil<2>;
-  DC(rt->d_dsa_vec.alloc(sizeof(float) * (6 * nv + 2 * halo(g))), "vectors");
+  // x, r, p, q, 1/diag, z and the initial guess x0, the last two with zero halos
+  DC(rt->d_dsa_vec.alloc(sizeof(float) * (7 * nv + 4 * halo(g))), "vectors");
   DC(rt->d_dsa_coef.alloc(sizeof(float) * ns * nv), "stencil");
-  DC(cudaMemsetAsync(rt->d_dsa_vec.p, 0, sizeof(float) * (6 * nv + 2 * halo(g)), rt->stream), "vectors");
+  DC(cudaMemsetAsync(rt->d_dsa_vec.p, 0, sizeof(float) * (7 * nv + 4 * halo(g)), rt->stream), "vectors");
   // partials of the two phases (one per block of the cooperative grid) and the barrier
   int per_sm = 0, sms = 0;
   DC(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, rt->device), "device");
@@ -626,7 +671,8 @@ int ensure_tables(ouranos_rt* rt) {
   }
   // one block per multiprocessor keeps the grid barrier to a few participants
   rt->dsa_grid = (int)std::min<long>(sms, (nv + kCgThreads - 1) / kCgThreads);
-  DC(rt->d_dsa_red.alloc(sizeof(double) * (2 * rt->dsa_grid + 2)), "reductions");
+  // partials a, b, the barrier (two words), partials c (the guess's second sum)
+  DC(rt->d_dsa_red.alloc(sizeof(double) * (3 * rt->dsa_grid + 2)), "reductions");
   DC(cudaMemcpyAsync(rt->d_dsa_cell.p, cell.data(), sizeof(float4) * rt->n_cells, cudaMemcpyHostToDevice,
                      rt->stream),
      "tables");
@@ -651,7 +697,7 @@ int ensure_tables(ouranos_rt* rt) {
 }
 
 template <int DIM>
-int dsa_run(ouranos_rt* rt, const double* v, double* out, int iters) {
+int dsa_run(ouranos_rt* rt, const double* v, double* out, int iters, bool guess) {
   DsaGeom g = geom(rt);
   const long nv = g.nv;
   // x, r, p, q, 1/diag, then z with its halo
@@ -659,10 +705,12 @@ int dsa_run(ouranos_rt* rt, const double* v, double* out, int iters) {
   float *x = base, *r = base + nv, *p = base + 2 * nv, *q = base + 3 * nv;
   const float* dinv = base + 4 * nv;
   float* z = base + 5 * nv + halo(g);
+  const float* x0 = guess ? base + 6 * nv + 3 * halo(g) : nullptr;
   const float* coef = rt->d_dsa_coef.as<float>();
   double* part_a = rt->d_dsa_red.as<double>();
   double* part_b = part_a + rt->dsa_grid;
   DsaSync* sync = reinterpret_cast<DsaSync*>(part_b + rt->dsa_grid);
+  double* part_c = part_b + rt->dsa_grid + 2;
   int* status = rt->d_ctrl.as<int>() + 1;
   const float4* cell = rt->d_dsa_cell.as<float4>();
   long len = (long)rt->n_mom * rt->n_dofs, n0 = rt->n_cells * (long)rt->n;
@@ -672,7 +720,7 @@ int dsa_run(ouranos_rt* rt, const double* v, double* out, int iters) {
   const float* fe = rt->d_dsa_fe.as<float>();
   int n = rt->n;
   void* args[] = {&g, &cell, &coef, &v, &out, &len, &n0, &dinv, &x, &r, &z, &p, &q, &part_a, &part_b, &sync, &status,
-                  &limit, &iters, &fe, &n};
+                  &limit, &iters, &fe, &n, &x0, &part_c};
   DC(cudaLaunchCooperativeKernel((const void*)dsa_cg_kernel<DIM>, dim3(rt->dsa_grid), dim3(kCgThreads), args, 0,
                                  rt->stream),
      "solve");
@@ -840,7 +888,27 @@ int rt_dsa_apply(ouranos_rt* rt, const double* v, double* out) {
   }
   int rc = ensure_tables(rt);
   if (rc) return rc;
-  return rt->dim == 3 ? dsa_run<3>(rt, v, out, rt->dsa_iters) : dsa_run<2>(rt, v, out, rt->dsa_iters);
+  return rt->dim == 3 ? dsa_run<3>(rt, v, out, rt->dsa_iters, false) : dsa_run<2>(rt, v, out, rt->dsa_iters, false);
+}
+// The initial-guess buffer of the diffusion solve ([vertex], FP32, zero halo
+// outside): a caller writes a guess of f there before rt_dsa_apply_guess.
+int rt_dsa_guess_buffer(ouranos_rt* rt, float** guess, long* n_vertices) {
+  int rc = ensure_tables(rt);
+  if (rc) return rc;
+  const DsaGeom g = geom(rt);
+  *guess = rt->d_dsa_vec.as<float>() + 6L * g.nv + 3 * halo(g);
+  *n_vertices = g.nv;
+  return OURANOS_OK;
+}
+// out = v + f with the CG started from the guess in the guess buffer
+int rt_dsa_apply_guess(ouranos_rt* rt, const double* v, double* out) {
+  if (rt->dsa_iters < 1) {
+    rt->err = "diffusion acceleration is off (ouranos_rt_set_dsa)";
+    return OURANOS_ERR_BAD_INPUT;
+  }
+  int rc = ensure_tables(rt);
+  if (rc) return rc;
+  return rt->dim == 3 ? dsa_run<3>(rt, v, out, rt->dsa_iters, true) : dsa_run<2>(rt, v, out, rt->dsa_iters, true);
 }
 }  // namespace ouranos
 

@@ -277,6 +277,13 @@ int rt_pc_features(ouranos_rt* rt, const double* v, float* feat);
 int rt_pc_correct(ouranos_rt* rt, const double* v, const float* y, double* z);
 // diffusion synthetic acceleration (dsa.cu): out = v + f on the handle's stream
 int rt_dsa_apply(ouranos_rt* rt, const double* v, double* out);
+// the same with the CG started from a guess of f ([vertex] FP32, written by
+// the caller into the buffer rt_dsa_guess_buffer returns)
+int rt_dsa_guess_buffer(ouranos_rt* rt, float** guess, long* n_vertices);
+int rt_dsa_apply_guess(ouranos_rt* rt, const double* v, double* out);
+// learned preconditioner with the diffusion solve (precond.cu): the network's
+// correction of v as the initial guess of the diffusion CG, out = v + f
+int rt_pc_dsa_apply(ouranos_rt* rt, const double* v, double* out);
 // the network's cell grid
 void cnn_grid(const ouranos_cnn* net, int* nx, int* ny, int* nz);
 // Device-side pieces the solvers use (operator.cu).

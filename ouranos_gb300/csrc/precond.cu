@@ -86,6 +86,26 @@ __global__ void correct_kernel(const double* v, double* z, long len, const float
   }
 }
 
+// guess[vertex] = s K (mean of the network's nodal outputs y at the vertex):
+// the network's prediction of the diffusion correction f as a vertex field
+__global__ void vertex_guess_kernel(cnn::Grid g, const float* y, const double* scale, float* guess) {
+  const float sk = (float)(*scale * kGain);
+  const long nv = cnn::n_vertices(g);
+  for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < nv; v += (long)gridDim.x * blockDim.x) {
+    const int vx = (int)(v % (g.nx + 1)), vy = (int)((v / (g.nx + 1)) % (g.ny + 1));
+    const int vz = (int)(v / ((long)(g.nx + 1) * (g.ny + 1)));
+    float s = 0.f;
+    int n = 0;
+    for (int k = 0; k < kNodes; ++k) {
+      const int cx = vx - (k & 1), cy = vy - ((k >> 1) & 1), cz = vz - (k >> 2);
+      if (cx < 0 || cy < 0 || cz < 0 || cx >= g.nx || cy >= g.ny || cz >= g.nz) continue;
+      s += y[(cx + (long)g.nx * (cy + (long)g.ny * cz)) * kNodes + k];
+      ++n;
+    }
+    guess[v] = n ? sk * s / (float)n : 0.f;
+  }
+}
+
 inline int blocks(long n) {
   long b = (n + 255) / 256;
   return (int)(b < 1 ? 1 : (b > 152L * 16 ? 152L * 16 : b));
@@ -157,6 +177,35 @@ int rt_pc_features(ouranos_rt* rt, const double* v, float* feat) {
   return OURANOS_OK;
 }
 
+// The learned preconditioner inside the diffusion acceleration: the
+// network's output on v (trained to predict the diffusion correction f of
+// v) starts the diffusion CG, whose rt->dsa_iters steps then remove the
+// network's error; out = v + f.  The CG converges to the same f from any
+// guess, so a poor prediction costs CG progress, never a wrong correction.
+int rt_pc_dsa_apply(ouranos_rt* rt, const double* v, double* out) {
+  if (!rt->cnn) {
+    rt->err = "no preconditioner installed (ouranos_rt_set_preconditioner)";
+    return OURANOS_ERR_BAD_INPUT;
+  }
+  PC(rt->d_pc_feat.alloc(sizeof(float) * (kFeat + kNodes) * rt->n_cells), "preconditioner");
+  float* feat = rt->d_pc_feat.as<float>();
+  float* y = feat + (long)kFeat * rt->n_cells;
+  int rc;
+  if ((rc = rt_pc_features(rt, v, feat))) return rc;
+  PC(cudaStreamSynchronize(rt->stream), "preconditioner");
+  if ((rc = ouranos_cnn_forward(rt->cnn, feat, y))) {
+    rt->err = "network forward failed";
+    return rc;
+  }
+  float* guess = nullptr;
+  long nv = 0;
+  if ((rc = rt_dsa_guess_buffer(rt, &guess, &nv))) return rc;
+  const cnn::Grid g = pc_grid(rt);
+  vertex_guess_kernel<<<blocks(nv), 256, 0, rt->stream>>>(g, y, rt->d_pc_work.as<double>() + kPartials, guess);
+  PC(cudaGetLastError(), "guess");
+  return rt_dsa_apply_guess(rt, v, out);
+}
+
 // z = v + s * y with the normalisation of the last rt_pc_features call
 int rt_pc_correct(ouranos_rt* rt, const double* v, const float* y, double* z) {
   const long len = (long)rt->n_mom * rt->n_dofs;
@@ -216,6 +265,14 @@ int ouranos_rt_pc_target(ouranos_rt* rt, const double* v, const double* e, float
   PC(cudaGetLastError(), "target");
   PC(cudaStreamSynchronize(rt->stream), "target");
   return OURANOS_OK;
+}
+
+int ouranos_rt_pc_dsa_apply(ouranos_rt* rt, const double* v, double* z) {
+  if (!rt || !v || !z) return OURANOS_ERR_BAD_INPUT;
+  cudaSetDevice(rt->device);
+  int rc = rt_clear_status(rt);
+  if (rc || (rc = rt_pc_dsa_apply(rt, v, z))) return rc;
+  return rt_check_status(rt);
 }
 
 int ouranos_rt_pc_apply(ouranos_rt* rt, const double* v, double* z) {

@@ -115,8 +115,9 @@ int update(Work& w, int first, const std::vector<double>& y, double* x) {
 // from the FP64 true residual.  mixed: the cycle stops once its own residual
 // estimate has dropped by `inner_drop` (FP32 operator accuracy), and the FP64
 // restart refines the solution (iterative refinement).
-// dsa: the diffusion synthetic acceleration is the right preconditioner (and
-// the learned one's fallback).
+// dsa: the diffusion synthetic acceleration is the right preconditioner; with
+// learned, the network's output starts its CG (and the plain diffusion
+// correction is the fallback).
 int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double* x,
           double* hist, ouranos_solve_info* info, int inner_prec, double inner_drop,
           bool learned = false, bool warm = false, bool dsa = false) {
@@ -178,7 +179,9 @@ int gmres(ouranos_rt* rt, int m, int max_it, double tol, const double* b, double
       if (flexible) {
         // right preconditioner: z_k = P(v_k), learned correction, diffusion
         // correction or identity
-        if (use_pc) {
+        if (use_pc && dsa) {
+          RC(rt_pc_dsa_apply(rt, vin, w.v(Z0 + k)));
+        } else if (use_pc) {
           RC(ouranos_rt_pc_apply(rt, vin, w.v(Z0 + k)));
         } else if (dsa) {
           RC(rt_dsa_apply(rt, vin, w.v(Z0 + k)));

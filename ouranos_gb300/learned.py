@@ -49,6 +49,7 @@ def _lib():
             "ouranos_rt_pc_features": [vp, vp, vp, C.POINTER(C.c_double)],
             "ouranos_rt_pc_target": [vp, vp, vp, vp],
             "ouranos_rt_pc_apply": [vp, vp, vp],
+            "ouranos_rt_pc_dsa_apply": [vp, vp, vp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -370,6 +371,109 @@ def train_on_solver_pairs(n=32, maps=32, steps_per_map=60, passes=2, epochs=6, l
         for rt in rts:
             rt.close()
     return net, hist
+
+
+def guess_precondition(rt):
+    """v -> P v: the diffusion acceleration of rt (its set_dsa CG steps)
+    started from the installed network's prediction (ouranos_rt_pc_dsa_apply)."""
+    L = _lib()
+
+    def pc(v):
+        v = v.contiguous()
+        z = v.new_empty(v.shape)
+        _capi.check(L.ouranos_rt_pc_dsa_apply(rt._h, v.data_ptr(), z.data_ptr()), rt._h)
+        return z
+    return pc
+
+
+def train_dsa_guess(n=32, maps=512, steps_per_map=8, passes=2, epochs=6, lr=3e-4, seed=7, map_seed0=2000,
+                    sn=12, target_cg=100, inner_cg=3, log=print):
+    """Train the network to predict the diffusion correction f of the
+    residuals FGMRES hands its right preconditioner, for use as the initial
+    guess of the diffusion CG (ouranos_rt_pc_dsa_apply).
+
+    Maps: the seeded thick diffusive maps, seeds map_seed0 .. map_seed0 +
+    maps - 1, n^3 cells of the 64^3 workload's cell width (side 10 n / 64).
+    Pairs: (v, DSA(v) with target_cg CG steps) for the first steps_per_map
+    Krylov vectors v of FGMRES(30) on each map's right-hand side, the
+    preconditioner being the diffusion correction with inner_cg CG steps from
+    a zero guess in the first pass and from the network trained so far in
+    later passes (the vectors the learned solve meets).  Each pass is followed
+    by `epochs` epochs of Adam over every pair collected so far.  Maps are
+    visited one at a time, so memory holds one handle and the pairs.  Returns
+    (net, loss history per epoch)."""
+    import torch
+    from .transport import RadiativeTransfer
+    rng = np.random.default_rng(seed)
+    L = _lib()
+    cap = maps * steps_per_map * passes
+    cells = n ** 3
+    feats = torch.empty((cap, cells * FEATURES), dtype=torch.float32, device="cuda")
+    targets = torch.empty((cap, cells * OUTPUTS), dtype=torch.float32, device="cuda")
+    net = Network(n, n, n, seed=seed)
+    hist = []
+    filled = 0
+    for rnd in range(passes):
+        for k in range(maps):
+            with RadiativeTransfer(thick_3d(seed=map_seed0 + k, n=n, sn=sn, width=10.0 * n / 64),
+                                   precision="fp32") as rt:
+                if rnd:
+                    install(rt, net)
+                b = torch.zeros(rt.length, dtype=torch.float64, device="cuda")
+                rt.rhs(out=b)
+                start = filled
+                inner = guess_precondition(rt) if rnd else rt.dsa_apply
+
+                def pc(v, rt=rt, inner=inner, start=start):
+                    nonlocal filled
+                    v = v.contiguous()
+                    if filled - start < steps_per_map:
+                        rt.set_dsa(target_cg)
+                        e = rt.dsa_apply(v)
+                        _capi.check(L.ouranos_rt_pc_features(rt._h, v.data_ptr(), feats[filled].data_ptr(),
+                                                             None), rt._h)
+                        _capi.check(L.ouranos_rt_pc_target(rt._h, v.data_ptr(), e.data_ptr(),
+                                                           targets[filled].data_ptr()), rt._h)
+                        filled += 1
+                    rt.set_dsa(inner_cg)
+                    return inner(v)
+
+                rt.set_dsa(inner_cg)
+                fgmres_pairs(rt, b, pc, lambda w, z: None, max_it=steps_per_map)
+                if rnd:
+                    install(rt, None)
+        for ep in range(epochs):
+            order = rng.permutation(filled)
+            rate = lr * (0.5 * (1 + math.cos(math.pi * ep / epochs))) / (1 + rnd)
+            tot = 0.0
+            for i in order:
+                tot += net.train_step(feats[i], targets[i], rate)
+            hist.append(tot / filled)
+            log("pass %d epoch %d pairs %d loss %.4e" % (rnd, ep, filled, hist[-1]))
+    return net, hist
+
+
+def compare_dsa_guess(net_path, n=64, seed=7000, sn=12, cgs=(2, 3, 5, 10, 20), tol=1e-8, max_it=1000):
+    """FGMRES(30) with FP32 sweeps on the thick map (seed, n^3) to `tol`,
+    preconditioned by the diffusion acceleration with k CG steps from a zero
+    guess and from the network's prediction, for each k in cgs.  Returns
+    {k: {"dsa": info, "learned": info}} (iterations, seconds, residual)."""
+    from .transport import RadiativeTransfer
+    out = {}
+    with RadiativeTransfer(thick_3d(seed=seed, n=n, sn=sn)) as rt:
+        net = Network.load(net_path, (n, n, n))
+        for k in cgs:
+            rt.set_dsa(k)
+            row = {}
+            for name in ("dsa", "learned"):
+                install(rt, net if name == "learned" else None)
+                method = "fgmres_learned" if name == "learned" else "fgmres_mixed"
+                _, info, _ = rt.solve(method, tol=tol, max_it=max_it, restart=30, dsa=True)
+                row[name] = {key: info[key] for key in ("iterations", "seconds", "residual", "converged")}
+            install(rt, None)
+            out[k] = row
+        net.close()
+    return out
 
 
 def train(n=64, maps=128, fields_per_map=4, epochs=8, lr=3e-4, seed=7, map_seed0=2000,

@@ -182,3 +182,62 @@ def test_solver_pairs_are_exact_and_the_trainer_runs():
     net, hist = learned.train_on_solver_pairs(n=8, maps=2, steps_per_map=6, passes=2, epochs=3, lr=1e-3,
                                               sn=4, dsa=40, log=lambda s: None)
     assert len(hist) == 6 and all(np.isfinite(hist))
+
+
+def test_network_guess_of_the_diffusion_solve_converges_to_the_same_correction():
+    """The network's output starts the diffusion CG: with enough CG steps the
+    correction is the one a zero start reaches (the CG converges to the same
+    f from any start), and FGMRES with the learned guess converges."""
+    torch = pytest.importorskip("torch")
+    import ouranos_gb300 as og
+    from ouranos_gb300 import learned
+    prob = og.thick_3d(seed=2103, n=12, sn=4, block=2, width=12 * 10.0 / 64)
+    with og.RadiativeTransfer(prob) as rt:
+        net = learned.Network(12, 12, 12, seed=3)
+        learned.install(rt, net)
+        v = torch.randn(rt.length, dtype=torch.float64, device="cuda",
+                        generator=torch.Generator(device="cuda").manual_seed(4))
+        rt.set_dsa(600)
+        plain = rt.dsa_apply(v).cpu().numpy()
+        guessed = learned.guess_precondition(rt)(v).cpu().numpy()
+        assert _rel(guessed, plain) < 1e-4
+        rt.set_dsa(3)
+        xg, ig, _ = rt.solve("gmres", tol=1e-8, max_it=800)
+        xl, il, _ = rt.solve("fgmres_learned", tol=1e-8, max_it=800, dsa=True)
+    assert il["converged"] and _rel(xl, xg) < 1e-6
+
+
+def test_trainer_for_the_diffusion_guess_runs():
+    pytest.importorskip("torch")
+    from ouranos_gb300 import learned
+    net, hist = learned.train_dsa_guess(n=8, maps=2, steps_per_map=4, passes=2, epochs=2, lr=1e-3, sn=4,
+                                        target_cg=40, inner_cg=2, log=lambda s: None)
+    assert len(hist) == 4 and all(np.isfinite(hist))
+    net.close()
+
+
+def test_trained_network_gains_over_the_same_cg_budget():
+    """What the trained network gains: the committed weights (trained on the
+    seeded thick maps 2000-2511) start the diffusion CG of FGMRES with FP32
+    sweeps on the evaluation map (seed 7000, 32^3 cells of the 64^3
+    workload's width).  With the same 3 CG steps per preconditioner
+    application, the learned start needs markedly fewer FGMRES iterations than
+    the zero start, and both reach the same solution."""
+    import os
+    import ouranos_gb300 as og
+    from ouranos_gb300.learned import Network, install
+    weights = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "ouranos_gb300",
+                           "weights", "dsa_guess_thick3d.npz")
+    prob = og.thick_3d(seed=7000, n=32, sn=12, width=5.0)
+    with og.RadiativeTransfer(prob) as rt:
+        rt.set_dsa(3)
+        x0, i0, _ = rt.solve("fgmres_mixed", tol=1e-8, max_it=1000, dsa=True)
+        net = Network.load(weights, (32, 32, 32))
+        install(rt, net)
+        x1, i1, _ = rt.solve("fgmres_learned", tol=1e-8, max_it=1000, dsa=True)
+        install(rt, None)
+        net.close()
+    print("iterations without / with the network:", i0["iterations"], i1["iterations"])
+    assert i0["converged"] and i1["converged"]
+    assert i1["iterations"] <= 0.85 * i0["iterations"]
+    assert _rel(x1, x0) < 1e-6
