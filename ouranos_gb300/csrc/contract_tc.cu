@@ -283,6 +283,11 @@ cudaError_t reduce_tc_launch(const float* psi, const uint8_t* img, float* phi, i
   const cudaError_t e =
       cudaFuncSetAttribute(reduce_tc_kernel<NCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  // the whole carveout as shared memory, so that two CTAs fit on an SM (the
+  // default split left room for one)
+  const cudaError_t e2 = cudaFuncSetAttribute(reduce_tc_kernel<NCH>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                              (int)cudaSharedmemCarveoutMaxShared);
+  if (e2 != cudaSuccess) return e2;
   int dev = 0, sms = 0, per_sm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -355,6 +360,9 @@ cudaError_t launch_expand_tc(const float* T, const float* iso, const TcTables& t
   const size_t smem = std::max<size_t>(3 * (size_t)kRows * 32 + 3 * (size_t)t.npad * 32 + 64, 100 * 1024);
   const cudaError_t e = cudaFuncSetAttribute(expand_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  const cudaError_t e2 = cudaFuncSetAttribute(expand_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                              (int)cudaSharedmemCarveoutMaxShared);
+  if (e2 != cudaSuccess) return e2;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

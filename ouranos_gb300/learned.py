@@ -507,3 +507,34 @@ def install(rt, net):
     """Use `net` as the right preconditioner of rt's FGMRES_LEARNED solves."""
     _capi.check(_lib().ouranos_rt_set_preconditioner(rt._h, net._h if net else None), rt._h)
     rt._pc_net = net  # keep it alive
+
+
+def time_forward(n=64, reps=20, seed=1):
+    """Device time (ms, CUDA events) of one network forward on an n^3 grid
+    (random weights and features; the cost does not depend on the values)."""
+    import torch
+    net = Network(n, n, n, seed=seed)
+    feat = torch.randn(n ** 3 * FEATURES, device="cuda", dtype=torch.float32,
+                       generator=torch.Generator(device="cuda").manual_seed(seed))
+    out = torch.empty(n ** 3 * OUTPUTS, device="cuda", dtype=torch.float32)
+    for _ in range(3):
+        net.forward(feat, out)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        net.forward(feat, out)
+    e.record()
+    e.synchronize()
+    net.close()
+    return s.elapsed_time(e) / reps
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="time the network forward on an n^3 grid")
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--reps", type=int, default=20)
+    a = ap.parse_args()
+    print(json.dumps({"forward_ms": time_forward(a.n, a.reps), "grid": a.n}))
