@@ -39,17 +39,24 @@ constexpr int kOut = OURANOS_CNN_OUTPUTS;
 static_assert(kFeatures == kNodal + 2 && 2 * kNodal == kCin0 && kOut == 8,
               "features are 8 nodal values + 2 material fields; outputs are the 8 Q1 corners");
 
+// one voxel per thread: channels 0..7 the BF16 of the nodal values, 8..15
+// the BF16 of what that rounding lost (the first layer sees the residual to
+// ~16 bits), two 16-byte stores
 __global__ void features_kernel(const float* feat, __nv_bfloat16* x0, float2* mat, long V) {
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < V * kCin0;
-       e += (long)gridDim.x * blockDim.x) {
-    const long v = e / kCin0;
-    const int c = (int)(e % kCin0);
-    // channels 0..7: BF16 of the nodal values; 8..15: BF16 of what that
-    // rounding lost, so the first layer sees the residual to ~16 bits
-    const float f = feat[v * kFeatures + (c & 7)];
-    const float hi = __bfloat162float(__float2bfloat16(f));
-    x0[e] = __float2bfloat16(c < kNodal ? hi : f - hi);
-    if (c == 0) mat[v] = make_float2(feat[v * kFeatures + kNodal], feat[v * kFeatures + kNodal + 1]);
+  for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < V; v += (long)gridDim.x * blockDim.x) {
+    const float* f = feat + v * kFeatures;
+    uint32_t hi[4], lo[4];
+#pragma unroll
+    for (int c = 0; c < kNodal; c += 2) {
+      const __nv_bfloat162 h = __floats2bfloat162_rn(f[c], f[c + 1]);
+      const __nv_bfloat162 l = __floats2bfloat162_rn(f[c] - __low2float(h), f[c + 1] - __high2float(h));
+      hi[c / 2] = *reinterpret_cast<const uint32_t*>(&h);
+      lo[c / 2] = *reinterpret_cast<const uint32_t*>(&l);
+    }
+    uint4* o = reinterpret_cast<uint4*>(x0 + v * kCin0);
+    o[0] = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+    o[1] = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    mat[v] = make_float2(f[kNodal], f[kNodal + 1]);
   }
 }
 // 2x2x2 average pool of the material features
@@ -83,13 +90,6 @@ __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return
 __device__ __forceinline__ float gate_of(const float* a, int c, float2 m) {
   return a[3 * c] + a[3 * c + 1] * m.x + a[3 * c + 2] * m.y;
 }
-template <typename T>
-__global__ void gate_fwd_kernel(const T* o, const float2* mat, const float* a, int C, long V, T* x) {
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < V * C; e += (long)gridDim.x * blockDim.x) {
-    const int c = (int)(e % C);
-    x[e] = from_f<T>(to_f<T>(o[e]) * gate_of(a, c, mat[e / C]));
-  }
-}
 // backward of the gate: g_o = g . gamma (BF16, may alias g) and
 // da[3c+j] += sum_v g[v,c] o[v,c] (1, m0, m1)_j
 template <typename T>
@@ -117,19 +117,33 @@ __global__ void add_kernel(const __nv_bfloat16* a, const __nv_bfloat16* b, __nv_
     out[e] = __float2bfloat16(__bfloat162float(a[e]) + __bfloat162float(b[e]));
 }
 // 2x2x2 average pool (fine -> coarse) and its adjoint
+// 8 channels of one coarse voxel per thread (16-byte loads and store)
 __global__ void pool_kernel(Grid fine, const __nv_bfloat16* in, __nv_bfloat16* out, int C) {
   const Grid co{fine.nx / 2, fine.ny / 2, fine.nz / 2};
-  const long n = co.voxels() * C;
+  const int C8 = C / 8;
+  const long n = co.voxels() * C8;
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-    const long v = e / C;
-    const int c = (int)(e % C);
+    const long v = e / C8;
+    const int c = (int)(e % C8) * 8;
     const int x = (int)(v % co.nx), y = (int)((v / co.nx) % co.ny), z = (int)(v / ((long)co.nx * co.ny));
-    float s = 0.f;
+    float s[8] = {};
     for (int k = 0; k < 8; ++k) {
       const long fv = (2 * x + (k & 1)) + (long)fine.nx * ((2 * y + ((k >> 1) & 1)) + (long)fine.ny * (2 * z + (k >> 2)));
-      s += __bfloat162float(in[fv * C + c]);
+      const uint4 u = *reinterpret_cast<const uint4*>(in + fv * C + c);
+      const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        s[2 * j] += __low2float(h[j]);
+        s[2 * j + 1] += __high2float(h[j]);
+      }
     }
-    out[e] = __float2bfloat16(0.125f * s);
+    uint32_t r[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const __nv_bfloat162 q = __floats2bfloat162_rn(0.125f * s[2 * j], 0.125f * s[2 * j + 1]);
+      r[j] = *reinterpret_cast<const uint32_t*>(&q);
+    }
+    *reinterpret_cast<uint4*>(out + v * C + c) = make_uint4(r[0], r[1], r[2], r[3]);
   }
 }
 __global__ void pool_bwd_kernel(Grid fine, const __nv_bfloat16* gco, __nv_bfloat16* gfine, int C) {
@@ -144,17 +158,30 @@ __global__ void pool_bwd_kernel(Grid fine, const __nv_bfloat16* gco, __nv_bfloat
   }
 }
 // nearest upsample (coarse -> fine) plus a skip tensor on the fine grid
+// nearest upsample (coarse -> fine) plus a skip tensor on the fine grid,
+// 8 channels of one fine voxel per thread
 __global__ void up_add_kernel(Grid fine, const __nv_bfloat16* co_in, const __nv_bfloat16* skip,
                               __nv_bfloat16* out, int C) {
   const Grid co{fine.nx / 2, fine.ny / 2, fine.nz / 2};
-  const long n = fine.voxels() * C;
+  const int C8 = C / 8;
+  const long n = fine.voxels() * C8;
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-    const long v = e / C;
-    const int c = (int)(e % C);
+    const long v = e / C8;
+    const int c = (int)(e % C8) * 8;
     const int x = (int)(v % fine.nx) / 2, y = (int)((v / fine.nx) % fine.ny) / 2,
               z = (int)(v / ((long)fine.nx * fine.ny)) / 2;
-    out[e] = __float2bfloat16(__bfloat162float(co_in[(x + (long)co.nx * (y + (long)co.ny * z)) * C + c]) +
-                              __bfloat162float(skip[e]));
+    const uint4 a = *reinterpret_cast<const uint4*>(co_in + (x + (long)co.nx * (y + (long)co.ny * z)) * C + c);
+    const uint4 b = *reinterpret_cast<const uint4*>(skip + v * C + c);
+    const __nv_bfloat162* ha = reinterpret_cast<const __nv_bfloat162*>(&a);
+    const __nv_bfloat162* hb = reinterpret_cast<const __nv_bfloat162*>(&b);
+    uint32_t r[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const __nv_bfloat162 q = __floats2bfloat162_rn(__low2float(ha[j]) + __low2float(hb[j]),
+                                                     __high2float(ha[j]) + __high2float(hb[j]));
+      r[j] = *reinterpret_cast<const uint32_t*>(&q);
+    }
+    *reinterpret_cast<uint4*>(out + v * C + c) = make_uint4(r[0], r[1], r[2], r[3]);
   }
 }
 // adjoint of nearest upsample: sum the 8 children
@@ -227,29 +254,6 @@ struct Layer {
   size_t woff, goff;  // offsets into the weight and gate arrays
 };
 
-template <int CIN, int COUT, bool RELU>
-cudaError_t conv_fwd_t(const Grid& g, const __nv_bfloat16* in, const __nv_bfloat16* wt,
-                       const float* bias, __nv_bfloat16* ob, float* of, cudaStream_t s) {
-  const long warps = (g.voxels() + 15) / 16;
-  cnn::conv3_fwd<CIN, COUT, RELU><<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(g, in, wt, bias, ob, of);
-  return cudaGetLastError();
-}
-
-cudaError_t conv_fwd(int cin, int cout, bool relu, const Grid& g, const __nv_bfloat16* in,
-                     const __nv_bfloat16* wt, const float* bias, __nv_bfloat16* ob, float* of,
-                     cudaStream_t s) {
-#define CASE(CI, CO)                                                                    \
-  if (cin == CI && cout == CO)                                                          \
-    return relu ? conv_fwd_t<CI, CO, true>(g, in, wt, bias, ob, of, s)                  \
-                : conv_fwd_t<CI, CO, false>(g, in, wt, bias, ob, of, s);
-  CASE(16, 16)
-  CASE(16, 32)
-  CASE(32, 32)
-  CASE(32, 16)
-#undef CASE
-  return cudaErrorInvalidValue;
-}
-
 cudaError_t conv_wgrad(int cin, int cout, const Grid& g, const __nv_bfloat16* in,
                        const __nv_bfloat16* grad, float* dw, float* db, cudaStream_t s) {
   const int chunk = 2048;
@@ -284,6 +288,8 @@ struct ouranos_cnn {
   float* resid = nullptr;  // y - target, [voxel][kOut]
   float* vert = nullptr;   // one value per mesh vertex
   float* dloss = nullptr;
+  int* status = nullptr;   // bit 0: a convolution's bounded wait ran out
+  int* status_host = nullptr;  // page-locked copy, read after each synchronisation
   long step = 0;
   cudaStream_t stream = nullptr;
   std::string err;
@@ -327,45 +333,71 @@ int refresh_copies(ouranos_cnn* net) {
   return OURANOS_OK;
 }
 
-// layer l on `in`: o_l = W_l * in, then the gated activation into `out`
+constexpr long long kConvWaitNs = 2000000000LL;  // bound of a convolution's waits
+
+int conv_call(ouranos_cnn* net, cudaError_t e, const std::string& what) {
+  if (e == cudaSuccess) return OURANOS_OK;
+  if (net->err.empty() || net->err.compare(0, 12, "convolution:") != 0) net->err = what;
+  return cnn_fail(net, e, net->err.c_str());
+}
+
+// layer l on `in`: o_l = W_l * in and the gated activation into `out`, one launch
 int conv_layer(ouranos_cnn* net, int l, const __nv_bfloat16* in, __nv_bfloat16* out) {
   const Layer& L = net->L[l];
-  CN(conv_fwd(L.cin, L.cout, false, L.grid, in, wf_of(net, l), nullptr, net->o[l], nullptr, net->stream),
-     "conv forward");
-  gate_fwd_kernel<__nv_bfloat16><<<blocks_for(L.grid.voxels() * L.cout), 256, 0, net->stream>>>(
-      net->o[l], net->mat[L.level], net->gt + L.goff, L.cout, L.grid.voxels(), out);
-  CN(cudaGetLastError(), "gate");
+  net->err.clear();
+  return conv_call(net,
+                   cnn::conv3_tc(L.cin, L.cout, L.grid, in, wf_of(net, l), net->mat[L.level], net->gt + L.goff,
+                                 net->o[l], out, nullptr, nullptr, net->status, kConvWaitNs, net->stream, &net->err),
+                   "conv forward");
+}
+
+// bounded waits of the convolutions since the last call: the status word
+// travels with the caller's final copy, one synchronisation for both
+int conv_status(ouranos_cnn* net, bool sync = true) {
+  if (sync) {
+    CN(cudaMemcpyAsync(net->status_host, net->status, sizeof(int), cudaMemcpyDeviceToHost, net->stream), "status");
+    CN(cudaStreamSynchronize(net->stream), "status");
+  }
+  const int st = *net->status_host;
+  if (st) {
+    *net->status_host = 0;
+    CN(cudaMemsetAsync(net->status, 0, sizeof(int), net->stream), "status");
+    net->err = "convolution: a tensor-core wait timed out";
+    return OURANOS_ERR_TIMEOUT;
+  }
   return OURANOS_OK;
 }
 
 int forward(ouranos_cnn* net, const float* feat) {
   cudaStream_t s = net->stream;
   const long V0 = net->g0.voxels();
-  features_kernel<<<blocks_for(V0 * kCin0), 256, 0, s>>>(feat, net->x0, net->mat[0], V0);
+  features_kernel<<<blocks_for(V0), 256, 0, s>>>(feat, net->x0, net->mat[0], V0);
   mat_pool_kernel<<<blocks_for(net->g1.voxels()), 256, 0, s>>>(net->g0, net->mat[0], net->mat[1]);
   mat_pool_kernel<<<blocks_for(net->g2.voxels()), 256, 0, s>>>(net->g1, net->mat[1], net->mat[2]);
   int rc;
   if ((rc = conv_layer(net, A0, net->x0, net->ha0)) || (rc = conv_layer(net, B0, net->ha0, net->s0)))
     return rc;
-  pool_kernel<<<blocks_for(net->g1.voxels() * 16), 256, 0, s>>>(net->g0, net->s0, net->p0, 16);
+  pool_kernel<<<blocks_for(net->g1.voxels() * 2), 256, 0, s>>>(net->g0, net->s0, net->p0, 16);
   if ((rc = conv_layer(net, A1, net->p0, net->ha1)) || (rc = conv_layer(net, B1, net->ha1, net->s1)))
     return rc;
-  pool_kernel<<<blocks_for(net->g2.voxels() * 32), 256, 0, s>>>(net->g1, net->s1, net->p1, 32);
+  pool_kernel<<<blocks_for(net->g2.voxels() * 4), 256, 0, s>>>(net->g1, net->s1, net->p1, 32);
   if ((rc = conv_layer(net, A2, net->p1, net->ha2)) || (rc = conv_layer(net, B2, net->ha2, net->hb2)))
     return rc;
-  up_add_kernel<<<blocks_for(net->g1.voxels() * 32), 256, 0, s>>>(net->g1, net->hb2, net->s1, net->u1, 32);
+  up_add_kernel<<<blocks_for(net->g1.voxels() * 4), 256, 0, s>>>(net->g1, net->hb2, net->s1, net->u1, 32);
   if ((rc = conv_layer(net, C1, net->u1, net->hc1)) || (rc = conv_layer(net, D1, net->hc1, net->hd1)))
     return rc;
-  up_add_kernel<<<blocks_for(V0 * 16), 256, 0, s>>>(net->g0, net->hd1, net->s0, net->u0, 16);
+  up_add_kernel<<<blocks_for(V0 * 2), 256, 0, s>>>(net->g0, net->hd1, net->s0, net->u0, 16);
   if ((rc = conv_layer(net, C0, net->u0, net->hc0))) return rc;
   const Layer& LO = net->L[OUT];
-  CN(conv_fwd(LO.cin, LO.cout, false, LO.grid, net->hc0, wf_of(net, OUT), nullptr, nullptr, net->out, s),
-     "conv forward");
-  gate_fwd_kernel<float><<<blocks_for(V0 * 16), 256, 0, s>>>(net->out, net->mat[0], net->gt + LO.goff, 16, V0,
-                                                              net->outg);
+  if ((rc = conv_call(net,
+                      cnn::conv3_tc(LO.cin, LO.cout, LO.grid, net->hc0, wf_of(net, OUT), net->mat[0],
+                                    net->gt + LO.goff, nullptr, nullptr, net->out, net->outg, net->status,
+                                    kConvWaitNs, s, &net->err),
+                      "conv forward")))
+    return rc;
   const long NV = ouranos::cnn::n_vertices(net->g0);
   ouranos::cnn::vertex_average_kernel<<<blocks_for(NV), 256, 0, s>>>(net->g0, net->outg, 16, 1.f, net->vert);
-  ouranos::cnn::vertex_scatter_kernel<<<blocks_for(V0 * kOut), 256, 0, s>>>(net->g0, net->vert, net->outp);
+  ouranos::cnn::vertex_scatter_kernel<<<blocks_for(V0), 256, 0, s>>>(net->g0, net->vert, net->outp);
   CN(cudaGetLastError(), "forward");
   return OURANOS_OK;
 }
@@ -377,9 +409,14 @@ int conv_backward(ouranos_cnn* net, int l, const __nv_bfloat16* in, const __nv_b
                   __nv_bfloat16* g_in) {
   const Layer& L = net->L[l];
   CN(conv_wgrad(L.cin, L.cout, L.grid, in, g_o, net->dw + L.woff, nullptr, net->stream), "weight gradient");
-  if (g_in)
-    CN(conv_fwd(L.cout, L.cin, false, L.grid, g_o, wb_of(net, l), nullptr, g_in, nullptr, net->stream),
-       "data gradient");
+  if (g_in) {
+    const int rc = conv_call(net,
+                             cnn::conv3_tc(L.cout, L.cin, L.grid, g_o, wb_of(net, l), nullptr, nullptr, g_in,
+                                           nullptr, nullptr, nullptr, net->status, kConvWaitNs, net->stream,
+                                           &net->err),
+                             "data gradient");
+    if (rc) return rc;
+  }
   return OURANOS_OK;
 }
 
@@ -438,6 +475,8 @@ int backward(ouranos_cnn* net, const float* target, float* loss_host) {
   if ((rc = gate_backward(net, A0, ga))) return rc;
   if ((rc = conv_backward(net, A0, net->x0, ga, nullptr))) return rc;
   CN(cudaGetLastError(), "backward");
+  // the convolutions' status travels with the loss (one synchronisation)
+  CN(cudaMemcpyAsync(net->status_host, net->status, sizeof(int), cudaMemcpyDeviceToHost, s), "status");
   if (loss_host) {
     CN(cudaMemcpyAsync(loss_host, net->dloss, sizeof(float), cudaMemcpyDeviceToHost, s), "loss");
     CN(cudaStreamSynchronize(s), "loss");
@@ -482,6 +521,9 @@ int ouranos_cnn_create(int nx, int ny, int nz, unsigned long long seed, ouranos_
   if (cudaStreamCreateWithFlags(&net->stream, cudaStreamDefault) != cudaSuccess)
     return cnn_fail(net, cudaGetLastError(), "stream");
   const long V0 = net->g0.voxels(), V1 = net->g1.voxels(), V2 = net->g2.voxels();
+  CN(dalloc(net, &net->status, 1), "status");
+  CN(cudaMallocHost((void**)&net->status_host, sizeof(int)), "status");
+  *net->status_host = 0;
   CN(dalloc(net, &net->w, net->n_w), "params");
   CN(dalloc(net, &net->gt, net->n_g), "params");
   CN(dalloc(net, &net->dw, net->n_w), "grads");
@@ -550,6 +592,7 @@ int ouranos_cnn_destroy(ouranos_cnn* net) {
   if (!net) return OURANOS_OK;
   if (net->stream) cudaStreamSynchronize(net->stream);
   for (void* p : net->allocs) cudaFree(p);
+  if (net->status_host) cudaFreeHost(net->status_host);
   if (net->stream) cudaStreamDestroy(net->stream);
   delete net;
   return OURANOS_OK;
@@ -591,8 +634,9 @@ int ouranos_cnn_forward(ouranos_cnn* net, const float* features, float* out) {
   CN(cudaMemcpyAsync(out, net->outp, sizeof(float) * kOut * net->g0.voxels(), cudaMemcpyDeviceToDevice,
                      net->stream),
      "output");
+  CN(cudaMemcpyAsync(net->status_host, net->status, sizeof(int), cudaMemcpyDeviceToHost, net->stream), "status");
   CN(cudaStreamSynchronize(net->stream), "forward");
-  return OURANOS_OK;
+  return conv_status(net, false);
 }
 
 // loss and gradients without an update; grads_host (may be NULL) receives [n_params]
@@ -600,7 +644,8 @@ int ouranos_cnn_gradients(ouranos_cnn* net, const float* features, const float* 
                           float* grads_host, float* loss) {
   if (!net || !features || !target) return OURANOS_ERR_BAD_INPUT;
   int rc;
-  if ((rc = forward(net, features)) || (rc = backward(net, target, loss))) return rc;
+  if ((rc = forward(net, features)) || (rc = backward(net, target, loss)) || (rc = conv_status(net, !loss)))
+    return rc;
   if (grads_host) {
     CN(cudaStreamSynchronize(net->stream), "grads");
     CN(cudaMemcpy(grads_host, net->dw, sizeof(float) * net->n_w, cudaMemcpyDeviceToHost), "grads");
@@ -622,7 +667,10 @@ int ouranos_cnn_train_step(ouranos_cnn* net, const float* features, const float*
   // gates multiply through all ten layers: a tenth of the weights' step
   adam_kernel<<<blocks_for(net->n_g), 256, 0, net->stream>>>(net->gt, net->dgt, net->mg, net->vg, net->n_g, 0.1f * lr, b1, b2, eps, c1, c2);
   CN(cudaGetLastError(), "adam");
-  return refresh_copies(net);
+  if ((rc = refresh_copies(net))) return rc;
+  // with a loss the stream was synchronised inside backward; without one the
+  // status is read at the next synchronising call
+  return loss ? conv_status(net, false) : OURANOS_OK;
 }
 
 int ouranos_cnn_last_error(const ouranos_cnn* net, char* buf, size_t len) {

@@ -5,8 +5,8 @@
 // BF16 copies in the layouts the tensor-core kernels read.  Convolutions are
 // 3x3x3, stride 1, zero padding, written as implicit GEMMs:
 //   out[v][co] = sum_{tap, ci} in[v + off(tap)][ci] * W[tap][ci][co]
-// M = voxels, N = cout, K = 27 * cin, on mma.sync.m16n8k16 (BF16 inputs, FP32
-// accumulation); every warp owns 16 voxels and all output channels.  The
+// M = voxels, N = cout, K = 27 * cin, on tcgen05.mma (BF16 inputs, FP32
+// accumulation in tensor memory, input bricks staged by TMA; cnn_tc.cu).  The
 // gradient with respect to the input is the same implicit GEMM over the
 // output gradient with the taps mirrored; the weight gradient reduces over
 // voxels in FP32.
@@ -14,6 +14,8 @@
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+
+#include <string>
 
 namespace ouranos {
 namespace cnn {
@@ -27,100 +29,15 @@ __device__ __forceinline__ int tap_dx(int t) { return t % 3 - 1; }
 __device__ __forceinline__ int tap_dy(int t) { return (t / 3) % 3 - 1; }
 __device__ __forceinline__ int tap_dz(int t) { return t / 9 - 1; }
 
-__device__ __forceinline__ unsigned pack_bf16(float lo, float hi) {
-  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-  return *reinterpret_cast<unsigned*>(&v);
-}
-
-// D += A(16x16 bf16, row) * B(16x8 bf16, col), FP32 accumulators
-__device__ __forceinline__ void mma_bf16_16816(float* d, const unsigned* a, const unsigned* b) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-// Implicit-GEMM 3x3x3 convolution.  CIN, COUT multiples of 16 (COUT of 8).
-// wt: BF16 weights [27][COUT][CIN] (k contiguous per output channel).
-// out_bf16 (and/or out_f32) receive bias + optional ReLU.
-template <int CIN, int COUT, bool RELU>
-__global__ void __launch_bounds__(128) conv3_fwd(Grid g, const __nv_bfloat16* __restrict__ in,
-                                                 const __nv_bfloat16* __restrict__ wt,
-                                                 const float* __restrict__ bias,
-                                                 __nv_bfloat16* __restrict__ out_bf16,
-                                                 float* __restrict__ out_f32) {
-  constexpr int NT = COUT / 8;  // n tiles of 8 channels
-  const long V = g.voxels();
-  const int lane = threadIdx.x & 31;
-  const int grp = lane >> 2, tig = lane & 3;
-  const long warp_global = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
-  const long v0 = warp_global * 16;
-  if (v0 >= V) return;
-  // the two voxel rows this thread feeds into A: grp and grp + 8
-  long vr[2];
-  int xr[2], yr[2], zr[2];
-#pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    vr[h] = v0 + grp + 8 * h;
-    const long v = vr[h] < V ? vr[h] : V - 1;
-    xr[h] = (int)(v % g.nx);
-    yr[h] = (int)((v / g.nx) % g.ny);
-    zr[h] = (int)(v / ((long)g.nx * g.ny));
-  }
-  float acc[NT][4];
-#pragma unroll
-  for (int n = 0; n < NT; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
-  for (int tap = 0; tap < 27; ++tap) {
-    const int dx = tap_dx(tap), dy = tap_dy(tap), dz = tap_dz(tap);
-    const __nv_bfloat16* src[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int x = xr[h] + dx, y = yr[h] + dy, z = zr[h] + dz;
-      const bool ok = vr[h] < V && x >= 0 && x < g.nx && y >= 0 && y < g.ny && z >= 0 && z < g.nz;
-      src[h] = ok ? in + ((long)x + (long)g.nx * (y + (long)g.ny * z)) * CIN : nullptr;
-    }
-    const __nv_bfloat16* wtap = wt + (long)tap * COUT * CIN;
-#pragma unroll
-    for (int k0 = 0; k0 < CIN; k0 += 16) {
-      unsigned a[4];
-      const int c0 = k0 + tig * 2;
-      a[0] = src[0] ? *reinterpret_cast<const unsigned*>(src[0] + c0) : 0u;
-      a[1] = src[1] ? *reinterpret_cast<const unsigned*>(src[1] + c0) : 0u;
-      a[2] = src[0] ? *reinterpret_cast<const unsigned*>(src[0] + c0 + 8) : 0u;
-      a[3] = src[1] ? *reinterpret_cast<const unsigned*>(src[1] + c0 + 8) : 0u;
-#pragma unroll
-      for (int n = 0; n < NT; ++n) {
-        const __nv_bfloat16* wrow = wtap + (long)(n * 8 + grp) * CIN + c0;
-        unsigned b[2];
-        b[0] = __ldg(reinterpret_cast<const unsigned*>(wrow));
-        b[1] = __ldg(reinterpret_cast<const unsigned*>(wrow + 8));
-        mma_bf16_16816(acc[n], a, b);
-      }
-    }
-  }
-  // epilogue: C[row][col] rows grp, grp+8; cols tig*2, tig*2+1 of each n tile
-#pragma unroll
-  for (int n = 0; n < NT; ++n) {
-    const int co = n * 8 + tig * 2;
-    const float b0 = bias ? bias[co] : 0.f, b1 = bias ? bias[co + 1] : 0.f;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      if (vr[h] >= V) continue;
-      float o0 = acc[n][2 * h + 0] + b0, o1 = acc[n][2 * h + 1] + b1;
-      if (RELU) {
-        o0 = fmaxf(o0, 0.f);
-        o1 = fmaxf(o1, 0.f);
-      }
-      if (out_bf16)
-        *reinterpret_cast<unsigned*>(out_bf16 + vr[h] * COUT + co) = pack_bf16(o0, o1);
-      if (out_f32) {
-        out_f32[vr[h] * COUT + co] = o0;
-        out_f32[vr[h] * COUT + co + 1] = o1;
-      }
-    }
-  }
-}
+// 3x3x3 convolution, out[v][co] = sum_{tap, ci} in[v + off(tap)][ci] W[tap][co][ci],
+// as a tcgen05 implicit GEMM (cnn_tc.cu); cin, cout in {16, 32}; wt BF16
+// [27][cout][cin].  Outputs (each may be NULL): pre, the BF16 convolution;
+// gated, BF16 of pre times the layer's gate a[3c] + a[3c+1] m.x + a[3c+2] m.y
+// (mat per voxel, gate per channel); pre_f32 and gated_f32 the same in FP32.
+// A bounded wait that runs out sets bit 0 of *status.
+cudaError_t conv3_tc(int cin, int cout, const Grid& g, const __nv_bfloat16* in, const __nv_bfloat16* wt,
+                     const float2* mat, const float* gate, __nv_bfloat16* pre, __nv_bfloat16* gated, float* pre_f32,
+                     float* gated_f32, int* status, long long limit_ns, cudaStream_t s, std::string* err);
 
 // Weight gradient: dW[tap][ci][co] += sum_v in[v + off(tap)][ci] * g[v][co],
 // dbias[co] += sum_v g[v][co].  One block per (tap, voxel chunk); thread
@@ -217,11 +134,16 @@ __device__ __forceinline__ long corner_vertex(const Grid& g, long cell, int k) {
   return (x + (k & 1)) + (long)(g.nx + 1) * ((y + ((k >> 1) & 1)) + (long)(g.ny + 1) * (z + (k >> 2)));
 }
 
-// nodal[cell*8 + k] = vert[vertex of (cell, k)]
+// nodal[cell*8 + k] = vert[vertex of (cell, k)], one cell per thread
 static __global__ void vertex_scatter_kernel(Grid g, const float* vert, float* nodal) {
-  const long n = g.voxels() * 8;
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
-    nodal[e] = vert[corner_vertex(g, e >> 3, (int)(e & 7))];
+  const long n = g.voxels();
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n; c += (long)gridDim.x * blockDim.x) {
+    const long v0 = corner_vertex(g, c, 0);
+    const long sy = g.nx + 1, sz = (long)(g.nx + 1) * (g.ny + 1);
+    float4* o = reinterpret_cast<float4*>(nodal + c * 8);
+    o[0] = make_float4(vert[v0], vert[v0 + 1], vert[v0 + sy], vert[v0 + sy + 1]);
+    o[1] = make_float4(vert[v0 + sz], vert[v0 + sz + 1], vert[v0 + sz + sy], vert[v0 + sz + sy + 1]);
+  }
 }
 
 }  // namespace cnn

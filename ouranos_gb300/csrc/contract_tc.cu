@@ -288,12 +288,12 @@ cudaError_t reduce_tc_launch(const float* psi, const uint8_t* img, float* phi, i
   const cudaError_t e2 = cudaFuncSetAttribute(reduce_tc_kernel<NCH>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                               (int)cudaSharedmemCarveoutMaxShared);
   if (e2 != cudaSuccess) return e2;
-  int dev = 0, sms = 0, per_sm = 1;
+  int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reduce_tc_kernel<NCH>, kReduceThreads, smem);
+  const int per_sm = tc5::resident_ctas(reduce_tc_kernel<NCH>, kReduceThreads, smem, 32, dev);
   const long ntiles = (len + kRows - 1) / kRows;
-  const int grid = (int)std::max(1L, std::min(ntiles, (long)sms * std::max(per_sm, 1)));
+  const int grid = (int)std::max(1L, std::min(ntiles, (long)sms * per_sm));
   reduce_tc_kernel<NCH><<<grid, kReduceThreads, smem, s>>>(psi, img, phi, n_dir, n_mom, n_dofs, len, status,
                                                            limit_ns);
   return cudaGetLastError();

@@ -261,7 +261,7 @@ int ouranos_rt_pc_target(ouranos_rt* rt, const double* v, const double* e, float
   const cnn::Grid g = pc_grid(rt);
   target_kernel<<<blocks(n0), 256, 0, rt->stream>>>(v, e, rt->d_pc_work.as<double>() + kPartials, n0, d);
   cnn::vertex_average_kernel<<<blocks(cnn::n_vertices(g)), 256, 0, rt->stream>>>(g, d, kNodes, 1.f, vert);
-  cnn::vertex_scatter_kernel<<<blocks(n0), 256, 0, rt->stream>>>(g, vert, target);
+  cnn::vertex_scatter_kernel<<<blocks(rt->n_cells), 256, 0, rt->stream>>>(g, vert, target);
   PC(cudaGetLastError(), "target");
   PC(cudaStreamSynchronize(rt->stream), "target");
   return OURANOS_OK;

@@ -16,8 +16,31 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 namespace ouranos {
 namespace tc5 {
+
+// CTAs of a kernel that fit on one SM at the same time, from its registers,
+// its threads and its dynamic shared memory (228 KB per SM, 1 KB reserved per
+// CTA), capped by the tensor-memory columns each CTA allocates (512 per SM)
+template <typename K>
+inline int resident_ctas(K kernel, int threads, size_t smem, int tmem_cols, int device) {
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(kernel)) != cudaSuccess) return 1;
+  int smem_sm = 0, regs_sm = 0, threads_sm = 0;
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, device);
+  cudaDeviceGetAttribute(&threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, device);
+  const int warps = (threads + 31) / 32;
+  const int regs_warp = ((fa.numRegs > 0 ? fa.numRegs : 32) * 32 + 255) / 256 * 256;
+  int n = 32;
+  if (smem_sm > 0) n = std::min(n, (int)(smem_sm / (smem + fa.sharedSizeBytes + 1024)));
+  if (regs_sm > 0) n = std::min(n, regs_sm / (regs_warp * warps));
+  if (threads_sm > 0) n = std::min(n, threads_sm / threads);
+  if (tmem_cols > 0) n = std::min(n, 512 / tmem_cols);
+  return std::max(n, 1);
+}
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -106,6 +129,26 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long l
   while (!mbar_try_wait(bar, parity))
     if (globaltimer() - t0 > limit_ns) return false;
   return true;
+}
+
+// the arrival of this thread, announcing `bytes` of bulk copies that
+// complete on the barrier (the phase ends when both have happened)
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+// ------------------------------------------------------------------- TMA
+// one box of a 4-D tensor map (tmap: the generic address of a
+// __grid_constant__ CUtensorMap) into shared memory at dst, completing on
+// bar; coordinates may lie outside the tensor (those elements read as zero)
+__device__ __forceinline__ void tma_load_4d(void* dst, const void* tmap, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+      "%5}], [%6];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(bar))
+      : "memory");
 }
 
 // ------------------------------------------------------------------ MMA
