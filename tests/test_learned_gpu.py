@@ -36,14 +36,24 @@ def test_network_forward_and_gradients_match_oracle(grid):
     loss_o, grads_o, out_o = cnn_oracle.gradients(p.astype(np.float64), feat.astype(np.float64),
                                                   target.astype(np.float64), grid)
     # BF16 activations/gradients: only FP32 vs FP64 accumulation order differs
-    assert _rel(out.cpu().numpy(), out_o.reshape(-1)) < 1e-2
-    assert abs(loss - loss_o) / loss_o < 1e-2
-    off = 0
+    e_out = _rel(out.cpu().numpy(), out_o.reshape(-1))
+    e_loss = abs(loss - loss_o) / loss_o
+    off, e_w = 0, []
     for li, (cin, cout, _) in enumerate(cnn_oracle.LAYERS):
         n = 27 * cin * cout
-        assert _rel(grads[off:off + n], grads_o[off:off + n]) < 5e-2, ("weights", li)
+        e_w.append(_rel(grads[off:off + n], grads_o[off:off + n]))
         off += n
-    assert _rel(grads[off:], grads_o[off:]) < 5e-2
+    e_g = _rel(grads[off:], grads_o[off:])
+    print("network vs oracle: output %.2e loss %.2e weight grads max %.2e gate grads %.2e"
+          % (e_out, e_loss, max(e_w), e_g))
+    # measured on GB300: output 2.5e-3, loss 1.3e-6, weight gradients 7.5e-3,
+    # gate gradients 2.7e-3 (FP32 against FP64 sums, and the rare value that
+    # lands on the other side of a BF16 rounding boundary)
+    assert e_out < 1e-2
+    assert e_loss < 1e-4
+    for li, e in enumerate(e_w):
+        assert e < 2e-2, ("weights", li, e)
+    assert e_g < 1e-2
 
 
 def test_training_reduces_loss():
