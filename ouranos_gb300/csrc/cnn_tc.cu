@@ -43,7 +43,9 @@ struct TmapSet {
   CUtensorMap m[4];  // one per 8-channel chunk of the input (at most 32 channels)
 };
 
-template <int CIN, int COUT>
+// NBUF brick buffers: with two, the next-but-one tile's brick is loaded
+// while this tile's MMAs and epilogue run
+template <int CIN, int COUT, int NBUF>
 __global__ void __launch_bounds__(kThreads) conv3_tc_kernel(const __grid_constant__ TmapSet maps, Grid g,
                                                             const __nv_bfloat16* __restrict__ wt,
                                                             const float2* __restrict__ mat,
@@ -54,10 +56,11 @@ __global__ void __launch_bounds__(kThreads) conv3_tc_kernel(const __grid_constan
   constexpr uint32_t kWtap = COUT * CIN * 2;
   constexpr uint32_t kSboB = NCH * 128;
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* brick = smem;
-  uint8_t* W = smem + NCH * kPlaneStride;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(W + 27 * kWtap);  // brick loaded, MMAs done, error path
-  uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 3);
+  constexpr uint32_t kBrick = NCH * kPlaneStride;
+  uint8_t* W = smem + NBUF * kBrick;
+  // mbarriers: MMAs done [0], error path [1], brick b loaded [2 + b]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(W + 27 * kWtap);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 4);
   float* sgate = reinterpret_cast<float*>(slot + 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // W[tap][n][k] -> tap * kWtap + (n / 8) * kSboB + (k / 8) * 128 + (n % 8) * 16 + (k % 8) * 2
@@ -69,7 +72,7 @@ __global__ void __launch_bounds__(kThreads) conv3_tc_kernel(const __grid_constan
   if (gate)
     for (int i = tid; i < 3 * COUT; i += kThreads) sgate[i] = gate[i];
   if (tid == 0) {
-    for (int i = 0; i < 3; ++i) tc5::mbar_init(bar + i, 1);
+    for (int i = 0; i < 2 + NBUF; ++i) tc5::mbar_init(bar + i, 1);
     tc5::mbar_init_fence();
   }
   if (warp == 0) {
@@ -89,49 +92,60 @@ __global__ void __launch_bounds__(kThreads) conv3_tc_kernel(const __grid_constan
     y0 = (int)((t / tx) % ty) * kTy;
     z0 = (int)(t / ((long)tx * ty));
   };
-  auto load = [&](long t) {  // one thread: the brick of tile t
+  auto load = [&](long t, int b) {  // one thread: the brick of tile t into buffer b
     int x0, y0, z0;
     origin(t, x0, y0, z0);
-    tc5::mbar_arrive_expect_tx(bar, NCH * kPlaneBytes);
+    uint8_t* dst = smem + b * kBrick;
+    tc5::mbar_arrive_expect_tx(bar + 2 + b, NCH * kPlaneBytes);
 #pragma unroll
-    for (int c = 0; c < NCH; ++c) tc5::tma_load_4d(brick + c * kPlaneStride, &maps.m[c], 0, x0 - 1, y0 - 1, z0 - 1, bar);
+    for (int c = 0; c < NCH; ++c)
+      tc5::tma_load_4d(dst + c * kPlaneStride, &maps.m[c], 0, x0 - 1, y0 - 1, z0 - 1, bar + 2 + b);
   };
-  uint32_t ph_load = 0, ph_mma = 0;
-  bool ok = true, load_pending = false;
-  long tile = blockIdx.x;
-  if (tid == 0 && tile < ntiles) load(tile);
-  load_pending = tile < ntiles;
-  for (; tile < ntiles; tile += gridDim.x) {
+  uint32_t ph_load = 0, ph_mma = 0;  // ph_load bit b: the parity awaited next on brick b
+  uint32_t pending = 0;              // bit b: a load into brick b is in flight
+  bool ok = true;
+  const long stride = gridDim.x;
+  if (tid == 0)
+    for (int b = 0; b < NBUF; ++b)
+      if ((long)blockIdx.x + b * stride < ntiles) load(blockIdx.x + b * stride, b);
+  for (int b = 0; b < NBUF; ++b)
+    if ((long)blockIdx.x + b * stride < ntiles) pending |= 1u << b;
+  int it = 0;
+  for (long tile = blockIdx.x; tile < ntiles; tile += stride, ++it) {
+    const int b = NBUF == 1 ? 0 : (it & 1);
+    uint8_t* brick = smem + b * kBrick;
     bool w = true;
-    if (tid == 0) w = tc5::mbar_wait(bar, ph_load, limit_ns);
-    ph_load ^= 1u;
-    load_pending = false;
+    if (tid == 0) w = tc5::mbar_wait(bar + 2 + b, (ph_load >> b) & 1u, limit_ns);
+    ph_load ^= 1u << b;
+    pending &= ~(1u << b);
     ok = __syncthreads_and(w);
     if (!ok) break;
     if (tid == 0) {
       tc5::fence_after_sync();
-#pragma unroll 1
-      for (int tap = 0; tap < 27; ++tap) {
-        const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
-        const uint32_t shift = (uint32_t)((dz * kBy + dy) * kBx + dx) * 16u;
+      // one descriptor per operand; a tap or a K step only moves the start
+      // address (the low field, in 16-byte units), so the 27 x CIN/16 MMAs
+      // issue back to back from constant offsets
+      const uint64_t a0 = tc5::smem_desc(tc5::smem_addr(brick), kPlaneStride, kSboA);
+      const uint64_t b0 = tc5::smem_desc(tc5::smem_addr(W), 128, kSboB);
 #pragma unroll
-        for (int ks = 0; ks < CIN / 16; ++ks) {
-          const uint64_t ad =
-              tc5::smem_desc(tc5::smem_addr(brick + 2 * ks * kPlaneStride + shift), kPlaneStride, kSboA);
-          const uint64_t bd = tc5::smem_desc(tc5::smem_addr(W + tap * kWtap + ks * 256), 128, kSboB);
-          tc5::mma_bf16(tmem, ad, bd, idesc, tap > 0 || ks > 0);
-        }
+      for (int tap = 0; tap < 27; ++tap) {
+        const uint32_t shift = (uint32_t)(((tap / 9) * kBy + (tap / 3) % 3) * kBx + tap % 3);  // 16-byte units
+#pragma unroll
+        for (int ks = 0; ks < CIN / 16; ++ks)
+          tc5::mma_bf16(tmem, a0 + shift + (uint64_t)(ks * 2 * (kPlaneStride >> 4)),
+                        b0 + (uint64_t)((tap * kWtap + ks * 256) >> 4), idesc, tap > 0 || ks > 0);
       }
-      tc5::mma_commit(bar + 1);
+      tc5::mma_commit(bar);
     }
-    if (tid == 0) w = tc5::mbar_wait(bar + 1, ph_mma, limit_ns);
+    if (tid == 0) w = tc5::mbar_wait(bar, ph_mma, limit_ns);
     ph_mma ^= 1u;
     ok = __syncthreads_and(w);
     if (!ok) break;
-    // the brick is free: the next tile's load overlaps this epilogue
-    if (tile + gridDim.x < ntiles) {
-      if (tid == 0) load(tile + gridDim.x);
-      load_pending = true;
+    // this brick is free: the tile NBUF steps ahead loads into it while this
+    // epilogue (and, with two buffers, the next tile's MMAs) run
+    if (tile + NBUF * stride < ntiles) {
+      if (tid == 0) load(tile + NBUF * stride, b);
+      pending |= 1u << b;
     }
     tc5::fence_after_sync();
     int x0, y0, z0;
@@ -187,12 +201,13 @@ __global__ void __launch_bounds__(kThreads) conv3_tc_kernel(const __grid_constan
     tc5::fence_before_sync();
     __syncthreads();
   }
-  if (!ok) {  // a wait ran out: bounded waits for the MMAs and the load still in flight
+  if (!ok) {  // a wait ran out: bounded waits for the MMAs and the loads still in flight
     if (tid == 0) {
       if (status) atomicOr(status, 1);
-      tc5::mma_commit(bar + 2);
-      tc5::mbar_wait(bar + 2, 0u, limit_ns);
-      if (load_pending) tc5::mbar_wait(bar, ph_load, limit_ns);
+      tc5::mma_commit(bar + 1);
+      tc5::mbar_wait(bar + 1, 0u, limit_ns);
+      for (int b = 0; b < NBUF; ++b)
+        if ((pending >> b) & 1u) tc5::mbar_wait(bar + 2 + b, (ph_load >> b) & 1u, limit_ns);
     }
     __syncthreads();
   }
@@ -222,11 +237,11 @@ EncodeTiled encoder(std::string* err) {
   return fn;
 }
 
-template <int CIN, int COUT>
+template <int CIN, int COUT, int NBUF>
 cudaError_t launch(const TmapSet& maps, const Grid& g, const __nv_bfloat16* wt, const float2* mat, const float* gate,
                    __nv_bfloat16* pre, __nv_bfloat16* gated, float* pre_f32, float* gated_f32, int* status,
                    long long limit_ns, cudaStream_t s) {
-  constexpr size_t smem = (CIN / 8) * kPlaneStride + 27 * COUT * CIN * 2 + 3 * 8 + 16 + 3 * COUT * 4;
+  constexpr size_t smem = NBUF * (CIN / 8) * kPlaneStride + 27 * COUT * CIN * 2 + 4 * 8 + 16 + 3 * COUT * 4;
   // the function's attributes and its resident-CTA count, once per device
   // (a forward pass launches ten convolutions; host work per launch shows)
   static int slots[64] = {};  // resident CTAs per device, 0 = not configured yet
@@ -235,18 +250,18 @@ cudaError_t launch(const TmapSet& maps, const Grid& g, const __nv_bfloat16* wt, 
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   if (!slots[dev]) {
-    e = cudaFuncSetAttribute(conv3_tc_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(conv3_tc_kernel<CIN, COUT, NBUF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(conv3_tc_kernel<CIN, COUT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+      e = cudaFuncSetAttribute(conv3_tc_kernel<CIN, COUT, NBUF>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                (int)cudaSharedmemCarveoutMaxShared);
     int sms = 0;
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    slots[dev] = sms * tc5::resident_ctas(conv3_tc_kernel<CIN, COUT>, kThreads, smem, 32, dev);
+    slots[dev] = sms * tc5::resident_ctas(conv3_tc_kernel<CIN, COUT, NBUF>, kThreads, smem, 32, dev);
   }
   const long ntiles = (long)((g.nx + kTx - 1) / kTx) * ((g.ny + kTy - 1) / kTy) * g.nz;
   const int grid = (int)std::max(1L, std::min(ntiles, (long)slots[dev]));
-  conv3_tc_kernel<CIN, COUT><<<grid, kThreads, smem, s>>>(maps, g, wt, mat, gate, pre, gated, pre_f32, gated_f32,
+  conv3_tc_kernel<CIN, COUT, NBUF><<<grid, kThreads, smem, s>>>(maps, g, wt, mat, gate, pre, gated, pre_f32, gated_f32,
                                                           status, limit_ns);
   return cudaGetLastError();
 }
@@ -280,13 +295,14 @@ cudaError_t conv3_tc(int cin, int cout, const Grid& g, const __nv_bfloat16* in, 
       return cudaErrorInvalidValue;
     }
   }
+  // two brick buffers where shared memory leaves room for several CTAs per SM
   if (cin == 16 && cout == 16)
-    return launch<16, 16>(maps, g, wt, mat, gate, pre, gated, pre_f32, gated_f32, status, limit_ns, s);
+    return launch<16, 16, 2>(maps, g, wt, mat, gate, pre, gated, pre_f32, gated_f32, status, limit_ns, s);
   if (cin == 16 && cout == 32)
-    return launch<16, 32>(maps, g, wt, mat, gate, pre, gated, pre_f32, gated_f32, status, limit_ns, s);
+    return launch<16, 32, 2>(maps, g, wt, mat, gate, pre, gated, pre_f32, gated_f32, status, limit_ns, s);
   if (cin == 32 && cout == 32)
-    return launch<32, 32>(maps, g, wt, mat, gate, pre, gated, pre_f32, gated_f32, status, limit_ns, s);
-  return launch<32, 16>(maps, g, wt, mat, gate, pre, gated, pre_f32, gated_f32, status, limit_ns, s);
+    return launch<32, 32, 1>(maps, g, wt, mat, gate, pre, gated, pre_f32, gated_f32, status, limit_ns, s);
+  return launch<32, 16, 2>(maps, g, wt, mat, gate, pre, gated, pre_f32, gated_f32, status, limit_ns, s);
 }
 
 }  // namespace cnn
