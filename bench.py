@@ -78,7 +78,7 @@ def workload_config(cells, directions, moments, dofs_per_cell, world):
 # longer describes the kernel and the line reports traffic as null.
 PROFILED_TILING = (16, 1, 1)
 SWEEP_SOURCES = ("sweep.cuh", "sweep_df64.cu", "sweep_f32.cu", "df64.cuh")
-SWEEP_TRAFFIC = {"digest": "a6da536b0a95d196", "bytes": {"fp64": 701757696 + 663408384}}
+SWEEP_TRAFFIC = {"digest": "73b1cf6657cf3f76", "bytes": {"fp64": 701153280 + 663511808}}
 
 
 def sweep_source_digest():

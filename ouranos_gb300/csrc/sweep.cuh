@@ -595,11 +595,22 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
       real xr[NR];
 #pragma unroll
       for (int k = 0; k < NR; ++k) xr[k] = real(0);
+      constexpr bool kHoist = sizeof(real) == 4;
+      constexpr int NP = pad4(N), FDP = pad4(FD);  // padded row strides of the tables
+      real b[N];
+      const real* Ai = a.ainv;
+      real arow[kHoist ? NR : 1][kHoist ? N : 1];
+      // inflow-face dot products F_a psi_up,a of the x and sweep-axis faces;
+      // with two lanes per cell each lane of the pair computes one of the two
+      // (lane half 0 the x face, half 1 the sweep-axis face) and the pair
+      // exchanges them with a converged shuffle
+      real faceX[FD], faceS[FD];
+#pragma unroll
+      for (int t = 0; t < FD; ++t) faceX[t] = faceS[t] = real(0);
       if (act) {
         cp_async_wait<kPrefetch - 1>();  // plane sc has landed
         const real* v = ring + ((sc % kRing) * 32 + lane) * NVP;
         const int cls = cring[(sc % kRing) * 32 + lane];
-        real b[N];
         if (VEC) {  // 16-byte loads of the slot (physical order), then canonical order
           real t0v[N], t1v[N], isv[N];
           load_cell<real, N>(v, t0v);
@@ -640,10 +651,7 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
         // FP32: this lane's rows of A'^-1 into registers now, so their loads
         // overlap the right-hand side below (for 8-byte values the longer
         // arithmetic hides them and the registers are better spent elsewhere)
-        constexpr bool kHoist = sizeof(real) == 4;
-        constexpr int NP = pad4(N), FDP = pad4(FD);  // padded row strides of the tables
-        const real* Ai = a.ainv + ((size_t)cls * a.n_dir_class + dcls) * (N * NP);
-        real arow[kHoist ? NR : 1][kHoist ? N : 1];
+        Ai = a.ainv + ((size_t)cls * a.n_dir_class + dcls) * (N * NP);
         if constexpr (kHoist) {
 #pragma unroll
           for (int k = 0; k < NR; ++k) {
@@ -656,26 +664,58 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
             }
           }
         }
-        // inflow faces: b_face += |Omega_a| F_a psi_up
         const real* FX = a.face_mass + 0 * FD * FDP;
         const real* FS = a.face_mass + AS * FD * FDP;
+        if (H == 1) {
+#pragma unroll
+          for (int t = 0; t < FD; ++t) {
+            typename A::acc accx = A::zero(), accs = A::zero();
+            real fx[FD], fs[FD];
+            load_row<real, FD>(FX + t * FDP, fx);
+            load_row<real, FD>(FS + t * FDP, fs);
+#pragma unroll
+            for (int u = 0; u < FD; ++u) {
+              A::fma(accx, fx[u], upX[u]);
+              A::fma(accs, fs[u], upS[u]);
+            }
+            faceX[t] = A::get(accx);
+            faceS[t] = A::get(accs);
+          }
+        } else {  // one instruction stream: the face is selected by data, not by a branch
+          const real* FF = half ? FS : FX;
+          real upF[FD];
+#pragma unroll
+          for (int u = 0; u < FD; ++u) upF[u] = half ? upS[u] : upX[u];
+#pragma unroll
+          for (int t = 0; t < FD; ++t) {
+            typename A::acc acc = A::zero();
+            real f[FD];
+            load_row<real, FD>(FF + t * FDP, f);
+#pragma unroll
+            for (int u = 0; u < FD; ++u) A::fma(acc, f[u], upF[u]);
+            faceX[t] = A::get(acc);  // this lane's face; sorted out after the exchange
+          }
+        }
+      }
+      if (H == 2) {  // every lane: exchange with the pair's partner (lane ^ 1)
 #pragma unroll
         for (int t = 0; t < FD; ++t) {
-          typename A::acc accx = A::zero(), accs = A::zero();
-          real fx[FD], fs[FD];
-          load_row<real, FD>(FX + t * FDP, fx);
-          load_row<real, FD>(FS + t * FDP, fs);
+          const real mine = faceX[t];
+          const real other = A::shfl_xor(mine, 1);
+          faceX[t] = half ? other : mine;
+          faceS[t] = half ? mine : other;
+        }
+      }
+      if (act) {
+        // inflow faces: b_face += |Omega_a| F_a psi_up, one face after the
+        // other (the two inflow faces share the corner dof)
 #pragma unroll
-          for (int u = 0; u < FD; ++u) {
-            A::fma(accx, fx[u], upX[u]);
-            A::fma(accs, fs[u], upS[u]);
-          }
-          // one after the other: the two inflow faces share the corner dof
+        for (int t = 0; t < FD; ++t) {
           typename A::acc bx = A::from(b[C::x_in(t)]);
-          A::fma(bx, wX, A::get(accx));
+          A::fma(bx, wX, faceX[t]);
           b[C::x_in(t)] = A::get(bx);
           typename A::acc bs = A::from(b[C::s_in(t)]);
-          A::fma(bs, wS, A::get(accs));
+          A::fma(bs, wS, faceS[t]);
           b[C::s_in(t)] = A::get(bs);
         }
         if (DIM == 3) {
