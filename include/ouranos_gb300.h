@@ -83,7 +83,7 @@ extern "C" {
  * uniform Cartesian mesh.  All arrays are host memory and are copied. */
 typedef struct ouranos_problem_desc {
   int dim;                  /* 2 or 3 */
-  int fe_order;             /* 1..4 in 2-D, 1..2 in 3-D (DG Q_p, equidistant nodes) */
+  int fe_order;             /* 1..5 (DG Q_p, equidistant nodes) */
   int n_cells[3];           /* cells per axis */
   double lower[3];          /* box corners */
   double upper[3];
@@ -188,9 +188,10 @@ int ouranos_rt_last_sweep_ms(const ouranos_rt* rt, double* ms, int* kernels);
 /* Tiling of the sweep kernel: cells per warp along x (and y in 3-D) and
  * directions per warp, with cells_x * cells_y * dirs == 32 (one lane per cell),
  * or == 16 for cells of 9 or more dofs (2-D Q2+, 3-D Q2): two lanes share each
- * cell solve.  0s = the default (one direction per warp; 2-D 32 x 1, 3-D
- * 4 x 8; two lanes per cell and 16 cells where allowed: 2-D 16 x 1, 3-D
- * 4 x 4). */
+ * cell solve, or 1 x 1 x 1: one warp per cell (every order; the only tiling
+ * of 2-D Q5 and 3-D Q3..Q5).  0s = the default (one direction per warp; 2-D
+ * 32 x 1, 3-D 4 x 8; two lanes per cell and 16 cells where allowed: 2-D
+ * 16 x 1, 3-D 4 x 4; one warp per cell for 2-D Q5 and 3-D Q3..Q5). */
 int ouranos_rt_set_tiling(ouranos_rt* rt, int cells_x, int cells_y, int dirs_per_warp);
 int ouranos_rt_get_tiling(const ouranos_rt* rt, int* cells_x, int* cells_y, int* dirs_per_warp);
 /* Spin limit of the in-kernel dependency waits, in nanoseconds (default 2 s).

@@ -18,7 +18,8 @@ LIB = os.path.join(OUT, "libouranos_gb300.so")
 ROOT = os.path.dirname(HERE)
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["quadrature.cpp", "fe.cpp", "operator.cu", "solvers.cu", "vec.cu",
-           "sweep_f64.cu", "sweep_f32.cu", "sweep_df64.cu", "sweep_batch_f64.cu", "sweep_batch_f32.cu",
+           "sweep_f64.cu", "sweep_f32.cu", "sweep_df64.cu", "sweep_wide_f64.cu", "sweep_wide_f32.cu",
+           "sweep_wide_df64.cu", "sweep_batch_f64.cu", "sweep_batch_f32.cu",
            "batch.cu", "noalloc.cu", "cnn.cu", "precond.cu", "dsa.cu", "contract_tc.cu", "cnn_tc.cu"]
 
 

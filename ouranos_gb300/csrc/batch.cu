@@ -348,6 +348,13 @@ int ouranos_batch_create(const ouranos_problem_desc* descs, int count, int devic
       return rc;
     }
     b->rt.push_back(r);
+    if (r->lpc == 32) {
+      char buf[256];
+      std::snprintf(buf, sizeof buf,
+                    "problem %d: the batched launch covers the per-lane sweep orders (2-D Q1..Q4, 3-D Q1..Q2)", p);
+      b->err = buf;
+      return OURANOS_ERR_UNSUPPORTED;
+    }
   }
   b->device = b->rt[0]->device;
   for (ouranos_rt* r : b->rt)

@@ -96,7 +96,7 @@ struct SweepArgs {
   int n_dir_class;
   const real* abs_omega;       // [n_dir][3]
   const real* m2d;             // [n_dir][n_mom]      (moment-fused form)
-  const real* ainv;            // [n_sigma_class][n_dir_class][n][pad4(n)]
+  const real* ainv;            // [n_sigma_class][n_dir_class][n][pad4(n)]; lpc 32: [..][j][i] (transposed)
   const int* cell_class;       // [cells] sigma_t class
   const real* face_mass;       // [3][fd][pad4(fd)]
   const real* src;             // [n_mom][n_dofs] source moments T (moment-fused form)
@@ -112,7 +112,8 @@ struct SweepArgs {
   int* status;                 // 0 ok, 1 wait timeout
   long long wait_limit_ns;
   int wait_bias;
-  int lpc;                     // lanes per cell: 1, or 2 (cells of 9 or more dofs)
+  int lpc;                     // lanes per cell: 1, 2 (cells of 9 or more dofs), or 32 (one warp
+                               // per cell, sweep_wide.cuh; tiling 1 x 1 x 1, expanded source)
 };
 
 // fused_moments: 0 = read the expanded per-direction source q; 1 or 2 = apply
@@ -120,6 +121,10 @@ struct SweepArgs {
 template <typename real>
 cudaError_t launch_sweep(int dim, int p1, int fused_moments, const SweepArgs<real>& a, int grid,
                          int block, cudaStream_t s);
+// One warp per cell (a.lpc == 32), every order of both dimensions: the form
+// of the orders the per-lane kernels do not instantiate (sweep_wide.cuh)
+template <typename real>
+cudaError_t launch_sweep_wide(int dim, int p1, const SweepArgs<real>& a, int grid, int block, cudaStream_t s);
 // Many problems in one persistent launch: args[p] per problem, tmap[t] =
 // (problem, task) for ticket t, epoch read from the device (all problems of
 // the launch share it), ticket reset to 0 by the caller.

@@ -261,7 +261,7 @@ extern "C" int ouranos_rt_apply_noalloc(ouranos_rt* rt, const double* x, double*
                 "ouranos_rt_apply_noalloc takes device pointers only (no staging buffers)");
   // same form choice as the regular Apply: expand the source when it has more
   // moments than the sweep applies in place
-  const bool expand_source = !(rt->n_mom <= 2 && rt->n * (rt->n_mom + 1) <= 32);
+  const bool expand_source = !(rt->n_mom <= 2 && rt->n * (rt->n_mom + 1) <= 32) || rt->lpc == 32;
   // double, and the double-float pairs, take 8 bytes a value
   const size_t rb = rt->precision == OURANOS_FP64 ? 8 : 4;
   const Layout L = layout_for(rt, rb, expand_source);

@@ -243,13 +243,22 @@ int build_schedule(ouranos_rt* rt) {
   return OURANOS_OK;
 }
 
+// the per-lane sweep kernels are instantiated for 2-D Q1..Q4 and 3-D Q1..Q2;
+// every order (up to Q5) also runs one warp per cell
+static bool register_form(const ouranos_rt* rt) { return rt->dim == 2 ? rt->p1 <= 5 : rt->p1 <= 3; }
+
 int default_tiling(ouranos_rt* rt) {
   // one direction per warp: every lane of a warp reads the same inverse table
   // (broadcast loads); 32 cells per warp (2-D: 32 x 1, 3-D: 4 x 8), or 16
   // cells solved by two lanes each for cells of 9 or more dofs (3-D: 4 x 4).
   // Measured on GB300, 64^3 Q1 GLC S12 FP32 sweep: 4 x 8 1.80 ms, 8 x 4 1.86,
-  // 4 x 4 x 2 directions 1.94, 8 x 2 x 2 2.21
+  // 4 x 4 x 2 directions 1.94, 8 x 2 x 2 2.21.  Higher orders: one warp per cell.
   rt->kd = 1;
+  if (!register_form(rt)) {
+    rt->wx = rt->wy = 1;
+    rt->lpc = 32;
+    return OURANOS_OK;
+  }
   rt->lpc = rt->n >= 9 ? 2 : 1;
   if (rt->dim == 2) {
     rt->wx = 32 / rt->lpc;
@@ -289,8 +298,19 @@ int setup_group(ouranos_rt* rt) {
     for (int dc = 0; dc < rt->n_dir_class; ++dc)
       canonical_inverse(rt->fe, cls_val[s], &rt->class_abs_omega[3 * dc],
                         &ainv[(s * rt->n_dir_class + dc) * nn]);
-  // rows padded to whole 16-byte pieces in every precision (the sweep loads them as vectors)
-  const std::vector<double> ainv_p = pad_rows(ainv, (long)cls_val.size() * rt->n_dir_class * n, n);
+  // rows padded to whole 16-byte pieces in every precision (the per-lane sweep
+  // loads them as vectors); one warp per cell reads the transpose, whose row j
+  // holds entry (i, j) for consecutive i
+  std::vector<double> ainv_p;
+  if (rt->lpc == 32) {
+    ainv_p.resize(ainv.size());
+    const size_t mats = cls_val.size() * rt->n_dir_class;
+    for (size_t m = 0; m < mats; ++m)
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) ainv_p[m * nn + (size_t)j * n + i] = ainv[m * nn + (size_t)i * n + j];
+  } else {
+    ainv_p = pad_rows(ainv, (long)cls_val.size() * rt->n_dir_class * n, n);
+  }
   OK_OR_RETURN(upload(rt, rt->d_ainv64, ainv_p, "inverse tables"));
   OK_OR_RETURN(upload(rt, rt->d_ainv32, to_f32(ainv_p), "inverse tables"));
   OK_OR_RETURN(upload(rt, rt->d_ainvdf, to_df(ainv_p), "inverse tables"));
@@ -415,7 +435,7 @@ int sweep_prepare(ouranos_rt* rt, const real* src, const real* iso, const real* 
   fm = (rt->n_mom <= kFusedMomentsMax && rt->n * (rt->n_mom + 1) <= 32) ? rt->n_mom : 0;
   // a source sweep of a time step carries the per-direction psi^n term: expanded form
   const bool angular = iso && rt->inv_vdt > 0.0 && rt->d_psi_prev.p;
-  if (angular) fm = 0;
+  if (angular || rt->lpc == 32) fm = 0;  // (one warp per cell reads the expanded source only)
   if (fm == 0) {
     CU(rt->d_q.alloc(sizeof(real) * len_dir), "expanded source");
     a.q = rt->d_q.as<real>();
@@ -837,9 +857,8 @@ int ouranos_rt_create(const ouranos_problem_desc* D, int device, ouranos_rt** ou
     return rc;
   };
   if (D->dim != 2 && D->dim != 3) return fail(bad(rt, "dim must be 2 or 3"));
-  const int pmax = D->dim == 2 ? 4 : 2;
-  if (D->fe_order < 1 || D->fe_order > pmax) {
-    rt->err = "fe_order outside the instantiated range (2-D: 1..4, 3-D: 1..2)";
+  if (D->fe_order < 1 || D->fe_order > 5) {
+    rt->err = "fe_order outside the range of DG Q1..Q5";
     return fail(OURANOS_ERR_UNSUPPORTED);
   }
   if (D->n_groups < 1 || D->n_dir < 1 || D->n_mom < 1 || D->n_materials < 1 || D->l_max < 0 ||
@@ -1283,21 +1302,27 @@ int ouranos_rt_last_sweep_ms(const ouranos_rt* rt, double* ms, int* kernels) {
 int ouranos_rt_set_tiling(ouranos_rt* rt, int cells_x, int cells_y, int dirs) {
   if (!rt) return OURANOS_ERR_BAD_INPUT;
   cudaSetDevice(rt->device);
+  const bool was_wide = rt->lpc == 32;
   if (cells_x == 0 && cells_y == 0 && dirs == 0) {
     OK_OR_RETURN(default_tiling(rt));
   } else {
     if (rt->dim == 2) cells_y = 1;
     const int lanes = cells_x * cells_y * dirs;
+    const bool wide = lanes == 1;            // one warp per cell
     const bool two = lanes == 16 && rt->n >= 9;  // two lanes per cell
-    if (cells_x < 1 || cells_y < 1 || dirs < 1 || (lanes != 32 && !two) || (dirs & (dirs - 1)))
+    if (cells_x < 1 || cells_y < 1 || dirs < 1 || (lanes != 32 && !two && !wide) || (dirs & (dirs - 1)))
       return bad(rt, "tiling must satisfy cells_x*cells_y*dirs == 32 (or 16, two lanes per cell, for cells "
-                     "of 9 or more dofs) with dirs a power of two");
+                     "of 9 or more dofs; or 1 x 1 x 1, one warp per cell) with dirs a power of two");
+    if (!wide && !register_form(rt))
+      return bad(rt, "this DG order runs one warp per cell only (tiling 1 x 1 x 1): the per-lane sweep "
+                     "covers 2-D Q1..Q4 and 3-D Q1..Q2");
     rt->wx = cells_x;
     rt->wy = cells_y;
     rt->kd = dirs;
-    rt->lpc = two ? 2 : 1;
+    rt->lpc = wide ? 32 : (two ? 2 : 1);
   }
   OK_OR_RETURN(build_schedule(rt));
+  if (was_wide != (rt->lpc == 32)) OK_OR_RETURN(setup_group(rt));  // the inverse tables change layout
   CU(cudaStreamSynchronize(rt->stream), "tiling");
   return OURANOS_OK;
 }

@@ -1,5 +1,7 @@
 // Instantiations of the sweep kernel in double-float (FP64 accuracy on the
-// FP32 pipes): 2-D Q1..Q4, 3-D Q1..Q2.
+// FP32 pipes): 2-D Q1..Q4, 3-D Q1..Q2
+// (one warp per cell for the 1 x 1 x 1 tiling and the higher orders:
+// sweep_wide_df64.cu).
 #include "sweep.cuh"
 
 namespace ouranos {
@@ -7,6 +9,7 @@ namespace ouranos {
 template <>
 cudaError_t launch_sweep<df64>(int dim, int p1, int fm, const SweepArgs<df64>& a, int grid, int block,
                                cudaStream_t s) {
+  if (a.lpc == 32) return launch_sweep_wide<df64>(dim, p1, a, grid, block, s);
   if (dim == 2) {
     switch (p1) {
       case 2: return launch_sweep_impl<df64, 2, 2>(fm, a, grid, block, s);
