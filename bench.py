@@ -361,6 +361,8 @@ def run_ours(args):
     rt = og.RadiativeTransfer(prob, device=local, precision=args.precision)
     if args.precision == "fp32":
         rt.set_fp32_contractions(args.fp32_contractions)
+    else:
+        rt.set_fp64_contractions(args.fp64_contractions)
     stream = torch.cuda.current_stream(dev)
     rt.set_stream(stream.cuda_stream)
     L = prob.vector_length
@@ -433,11 +435,33 @@ def run_ours(args):
             ev1.record(stream)
             ev1.synchronize()
             nms.append(ev0.elapsed_time(ev1))
-        rt.set_fp64_contractions("df64_sweep")
-        rt.Apply(x, y)
-        torch.cuda.synchronize(dev)
         native = {"ms_per_step": sum(nms) / len(nms), "value": solves / (sum(nms) / len(nms) / 1e3),
                   "unit": UNIT, "steps": len(nms)}
+        # the double-float Apply with its two contractions on the CUDA cores
+        # and on the tensor cores (exact BF16 digit products)
+        engines = {}
+        for mode, key in (("df64_sweep", "cuda_cores"), ("df64_sweep_tc", "tensor")):
+            try:
+                rt.set_fp64_contractions(mode)
+            except Exception as exc:  # more directions or moments than the tensor form takes
+                engines[key] = {"unavailable": str(exc)}
+                continue
+            for _ in range(3):
+                rt.Apply(x, y)
+            ems = []
+            for _ in range(max(3, min(args.steps, 10))):
+                flush.zero_()
+                ev0.record(stream)
+                rt.Apply(x, y)
+                ev1.record(stream)
+                ev1.synchronize()
+                ems.append(ev0.elapsed_time(ev1))
+            engines[key] = {"ms_per_step": sum(ems) / len(ems), "value": solves / (sum(ems) / len(ems) / 1e3),
+                            "unit": UNIT, "steps": len(ems)}
+        native["fp64_contractions"] = engines
+        rt.set_fp64_contractions(args.fp64_contractions)
+        rt.Apply(x, y)
+        torch.cuda.synchronize(dev)
         # the FP32 Apply (the Arnoldi operator of the mixed-precision solves)
         # with its contractions on the CUDA cores and on the tensor cores
         fp32 = {}
@@ -493,8 +517,11 @@ def run_ours(args):
             "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "f32",
-            "arithmetic": ("double-float (FP32 pairs, ~48-bit significand) sweep and contractions, "
-                           "FP64 vectors" if args.precision == "fp64" else "FP32 sweep, FP64 vectors"),
+            "arithmetic": (("double-float (FP32 pairs, ~48-bit significand) sweep; contractions on the tensor "
+                            "cores as exact BF16 digit products; FP64 vectors"
+                            if args.fp64_contractions == "df64_sweep_tc" else
+                            "double-float (FP32 pairs, ~48-bit significand) sweep and contractions, FP64 vectors")
+                           if args.precision == "fp64" else "FP32 sweep, FP64 vectors"),
             "data": "synthetic (seeded SplitMix64 material map, random flux moments)",
             "config": workload_config(prob.total_cells, prob.quad.n_dir, prob.quad.n_mom,
                                       prob.dofs_per_cell, world),
@@ -519,6 +546,7 @@ def run_ours(args):
         }
         if native:
             line["fp32_apply"] = native.pop("fp32_apply")
+            line["fp64_contractions"] = native.pop("fp64_contractions")
             line["fp64_native_apply"] = native
         if parity:
             line["parity_rel_err"] = parity["rel_err"]
@@ -794,6 +822,8 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--fp32-contractions", default="cuda_cores", choices=["cuda_cores", "tensor"],
                     help="where an FP32 run's moment/direction contractions run")
+    ap.add_argument("--fp64-contractions", default="df64_sweep", choices=["df64_sweep", "df64_sweep_tc"],
+                    help="where the double-float Apply's two contractions run: CUDA cores or tensor cores")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-reps", type=int, default=14, help="full CPU sweeps timed (~10 s on 16 cores)")
     ap.add_argument("--no-solve", action="store_true",

@@ -65,11 +65,16 @@ extern "C" {
  *   NATIVE     native FP64 everywhere;
  *   DF64       moment <-> direction contractions in double-float, sweep in FP64;
  *   DF64_SWEEP contractions and the cell solves of the sweep in double-float,
- *              sources and angular fluxes stored as pairs (the default).
- * All three meet the 1e-12 parity bar against the FP64 oracle. */
+ *              sources and angular fluxes stored as pairs (the default);
+ *   DF64_SWEEP_TC  the double-float sweep with its two contractions on the
+ *              tensor cores: seven BF16 digits per value on power-of-two
+ *              grids, digit products summed exactly per level (up to 192
+ *              directions and 16 moments).
+ * All four meet the 1e-12 parity bar against the FP64 oracle. */
 #define OURANOS_FP64_NATIVE 0
 #define OURANOS_FP64_DF64 1
 #define OURANOS_FP64_DF64_SWEEP 2
+#define OURANOS_FP64_DF64_SWEEP_TC 3
 /* Where the FP32 path's moment <-> direction contractions run:
  *   CUDA_CORES FP32 multiply-adds on the CUDA cores;
  *   TENSOR     tcgen05 MMAs on the tensor cores, every FP32 operand split
@@ -137,8 +142,9 @@ int ouranos_rt_set_group(ouranos_rt* rt, int group);
 /* Sweep arithmetic: OURANOS_FP64 (default, parity path) or OURANOS_FP32. No
  * reference counterpart (the reference is FP64 only). */
 int ouranos_rt_set_precision(ouranos_rt* rt, int precision);
-/* Select OURANOS_FP64_NATIVE, OURANOS_FP64_DF64 or OURANOS_FP64_DF64_SWEEP for
- * the FP64 path.  No reference counterpart. */
+/* Select OURANOS_FP64_NATIVE, OURANOS_FP64_DF64, OURANOS_FP64_DF64_SWEEP or
+ * OURANOS_FP64_DF64_SWEEP_TC (UNSUPPORTED beyond 192 directions or 16 moments)
+ * for the FP64 path.  No reference counterpart. */
 int ouranos_rt_set_fp64_contractions(ouranos_rt* rt, int mode);
 /* Select OURANOS_FP32_CONTRACT_CUDA_CORES or OURANOS_FP32_CONTRACT_TENSOR for
  * the FP32 path (UNSUPPORTED beyond 256 directions or 16 moments).  No

@@ -21,7 +21,7 @@ BC_VACUUM, BC_ISOTROPIC, BC_MOST_NORMAL, BC_REFLECTIVE = 0, 1, 2, 3
 QUAD_LS, QUAD_GLC = 0, 1
 HARM_ORTHONORMAL, HARM_REFERENCE = 0, 1
 FP64, FP32 = 0, 1
-FP64_NATIVE, FP64_DF64, FP64_DF64_SWEEP = 0, 1, 2
+FP64_NATIVE, FP64_DF64, FP64_DF64_SWEEP, FP64_DF64_SWEEP_TC = 0, 1, 2, 3
 FP32_CONTRACT_CUDA_CORES, FP32_CONTRACT_TENSOR = 0, 1
 SOLVER_SI, SOLVER_GMRES, SOLVER_BICGSTAB, SOLVER_FGMRES_MIXED, SOLVER_FGMRES_LEARNED = 0, 1, 2, 3, 4
 SOLVER_WARM_START = 0x100

@@ -20,7 +20,7 @@ GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["quadrature.cpp", "fe.cpp", "operator.cu", "solvers.cu", "vec.cu",
            "sweep_f64.cu", "sweep_f32.cu", "sweep_df64.cu", "sweep_wide_f64.cu", "sweep_wide_f32.cu",
            "sweep_wide_df64.cu", "sweep_batch_f64.cu", "sweep_batch_f32.cu",
-           "batch.cu", "noalloc.cu", "cnn.cu", "precond.cu", "dsa.cu", "contract_tc.cu", "cnn_tc.cu"]
+           "batch.cu", "noalloc.cu", "cnn.cu", "precond.cu", "dsa.cu", "contract_tc.cu", "contract_oz.cu", "cnn_tc.cu"]
 
 
 def _nvcc():

@@ -183,6 +183,33 @@ struct TcTables {
   const uint8_t* d2m_img = nullptr;  // [3][16 moment slots][kpad directions]
   int n_dir = 0, n_mom = 0, npad = 0, kpad = 0;
 };
+// FP64-accurate contractions of the double-float sweep on the tensor cores
+// (contract_oz.cu): seven BF16 digits per value on power-of-two grids, digit
+// products summed exactly per level in FP32 accumulators.  B operand images
+// of M2D (digits per direction) and D2M (digits per moment and chunk of 48
+// directions) with their exponents, built once per handle on the host.
+struct OzHost {
+  std::vector<uint8_t> m2d_img, d2m_img;  // [7][npad][16], [nch][7][16][48] (K-major BF16)
+  std::vector<int> m2d_exp, d2m_exp;      // [npad], [nch][16]
+  int n_dir = 0, n_mom = 0, npad = 0, nch = 0;
+};
+struct OzTables {
+  const uint8_t* m2d_img = nullptr;
+  const int* m2d_exp = nullptr;
+  const uint8_t* d2m_img = nullptr;
+  const int* d2m_exp = nullptr;
+  int n_dir = 0, n_mom = 0, npad = 0, nch = 0;
+};
+bool oz_contractions_fit(int n_dir, int n_mom);
+void oz_build_tables(const std::vector<double>& m2d, const std::vector<double>& d2m, int n_dir, int n_mom,
+                     OzHost& h);
+// q (pairs) = M2D T (+ iso) and phi (double) = D2M psi over the dofs [0, len)
+// of the pointers (rows strided by n_dofs); a bounded wait that runs out sets
+// bit 4 of *status
+cudaError_t launch_expand_oz(const df64* T, const df64* iso, const OzTables& t, df64* q, long n_dofs, int* status,
+                             long long limit_ns, cudaStream_t s, long len = -1);
+cudaError_t launch_reduce_oz(const df64* psi, const OzTables& t, double* phi, long n_dofs, int* status,
+                             long long limit_ns, cudaStream_t s, long len = -1);
 bool tc_contractions_fit(int n_dir, int n_mom);
 void tc_build_images(const std::vector<double>& m2d, const std::vector<double>& d2m, int n_dir, int n_mom,
                      std::vector<uint8_t>& m2d_img, std::vector<uint8_t>& d2m_img, int& npad, int& kpad);
@@ -351,6 +378,8 @@ struct ouranos_rt {
   int fp32_contract = OURANOS_FP32_CONTRACT_CUDA_CORES;  // where the FP32 path's contractions run
   ouranos::TcTables tc;                                  // their tensor-core tables (tc.npad 0: none)
   ouranos::DevBuf d_tc_m2d, d_tc_d2m;
+  ouranos::OzTables oz;                                  // exact-digit tensor-core tables (oz.npad 0: none)
+  ouranos::DevBuf d_oz_m2d, d_oz_d2m, d_oz_m2d_exp, d_oz_d2m_exp;
   // schedule
   int wx = 0, wy = 1, kd = 0;          // 0 = not chosen yet
   int lpc = 1;                         // lanes per cell (2 only for cells of >= 9 dofs)

@@ -114,6 +114,8 @@ template <typename real>
 cudaError_t expand(const ouranos_rt* rt, const real* T, real* q, int* status, cudaStream_t st) {
   const long nd = rt->n_dofs;
   if constexpr (std::is_same<real, df64>::value) {
+    if (rt->fp64_contract == OURANOS_FP64_DF64_SWEEP_TC)
+      return launch_expand_oz(T, nullptr, rt->oz, q, nd, status, rt->wait_limit_ns, st);
     if (rt->sym.n_class) return launch_expand_sym_pairs(T, nullptr, rt->sym, q, rt->n_mom, nd, st);
     return launch_expand_source_pairs(T, nullptr, rt->d_m2d64.as<double>(), q, rt->n_dir, rt->n_mom, nd, st);
   } else if constexpr (std::is_same<real, double>::value) {
@@ -132,6 +134,8 @@ template <typename real>
 cudaError_t reduce(const ouranos_rt* rt, const real* psi, void* phi, int* status, cudaStream_t st) {
   const long nd = rt->n_dofs;
   if constexpr (std::is_same<real, df64>::value) {
+    if (rt->fp64_contract == OURANOS_FP64_DF64_SWEEP_TC)
+      return launch_reduce_oz(psi, rt->oz, (double*)phi, nd, status, rt->wait_limit_ns, st);
     if (rt->sym.n_class) return launch_reduce_sym_pairs(psi, rt->sym, (double*)phi, rt->n_mom, nd, st);
     return launch_reduce_moments_pairs(psi, rt->d_d2m64.as<double>(), (double*)phi, rt->n_dir, rt->n_mom, nd, st);
   } else if constexpr (std::is_same<real, double>::value) {
@@ -284,6 +288,7 @@ extern "C" int ouranos_rt_apply_noalloc(ouranos_rt* rt, const double* x, double*
     return fail(rt, OURANOS_ERR_CUDA, "the scratch array was not set up on this device at handle creation");
   unsigned char* b = (unsigned char*)base;
   if (rt->precision == OURANOS_FP32) return apply_noalloc<float>(rt, b, L, expand_source, x, y);
-  if (rt->fp64_contract == OURANOS_FP64_DF64_SWEEP) return apply_noalloc<df64>(rt, b, L, expand_source, x, y);
+  if (rt->fp64_contract == OURANOS_FP64_DF64_SWEEP || rt->fp64_contract == OURANOS_FP64_DF64_SWEEP_TC)
+    return apply_noalloc<df64>(rt, b, L, expand_source, x, y);
   return apply_noalloc<double>(rt, b, L, expand_source, x, y);
 }

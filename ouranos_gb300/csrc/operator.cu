@@ -72,7 +72,8 @@ std::vector<double> pad_rows(const std::vector<double>& v, long rows, int cols) 
 
 // the sweep runs in double-float with pair storage
 bool df64_sweep(const ouranos_rt* rt) {
-  return rt->precision == OURANOS_FP64 && rt->fp64_contract == OURANOS_FP64_DF64_SWEEP;
+  return rt->precision == OURANOS_FP64 &&
+         (rt->fp64_contract == OURANOS_FP64_DF64_SWEEP || rt->fp64_contract == OURANOS_FP64_DF64_SWEEP_TC);
 }
 
 // the table of the sweep's arithmetic type
@@ -367,7 +368,11 @@ int sweep_expand(ouranos_rt* rt, const real* src, const real* iso, long e0, long
   const long nd = rt->n_dofs;
   src += e0;
   if (iso) iso += e0;
-  if (std::is_same<real, df64>::value && rt->sym.n_class)  // pairs, through the octant symmetry
+  if (std::is_same<real, df64>::value && rt->fp64_contract == OURANOS_FP64_DF64_SWEEP_TC)  // tensor cores
+    CU(launch_expand_oz((const df64*)src, (const df64*)iso, rt->oz, rt->d_q.as<df64>() + e0, nd,
+                        rt->d_ctrl.as<int>() + 1, rt->wait_limit_ns, rt->stream, len),
+       "source expansion");
+  else if (std::is_same<real, df64>::value && rt->sym.n_class)  // pairs, through the octant symmetry
     CU(launch_expand_sym_pairs((const df64*)src, (const df64*)iso, rt->sym, rt->d_q.as<df64>() + e0, rt->n_mom,
                                nd, rt->stream, len),
        "source expansion");
@@ -462,7 +467,11 @@ int sweep_reduce(ouranos_rt* rt, const real* psi, void* phi, long e0 = 0, long l
   if (len < 0) len = nd;
   psi += e0;
   double* phi64 = (double*)phi + e0;
-  if (std::is_same<real, df64>::value && rt->sym.n_class)
+  if (std::is_same<real, df64>::value && rt->fp64_contract == OURANOS_FP64_DF64_SWEEP_TC)
+    CU(launch_reduce_oz((const df64*)psi, rt->oz, phi64, nd, rt->d_ctrl.as<int>() + 1, rt->wait_limit_ns,
+                        rt->stream, len),
+       "moment reduction");
+  else if (std::is_same<real, df64>::value && rt->sym.n_class)
     CU(launch_reduce_sym_pairs((const df64*)psi, rt->sym, phi64, rt->n_mom, nd, rt->stream, len),
        "moment reduction");
   else if (std::is_same<real, df64>::value)
@@ -1009,6 +1018,23 @@ int ouranos_rt_create(const ouranos_problem_desc* D, int device, ouranos_rt** ou
     rt->tc.n_dir = rt->n_dir;
     rt->tc.n_mom = rt->n_mom;
   }
+  if (oz_contractions_fit(rt->n_dir, rt->n_mom)) {
+    OzHost h;
+    oz_build_tables(rt->m2d, rt->d2m, rt->n_dir, rt->n_mom, h);
+    if ((rc = upload(rt, rt->d_oz_m2d, h.m2d_img, "tensor-core FP64 tables")) ||
+        (rc = upload(rt, rt->d_oz_d2m, h.d2m_img, "tensor-core FP64 tables")) ||
+        (rc = upload(rt, rt->d_oz_m2d_exp, h.m2d_exp, "tensor-core FP64 tables")) ||
+        (rc = upload(rt, rt->d_oz_d2m_exp, h.d2m_exp, "tensor-core FP64 tables")))
+      return fail(rc);
+    rt->oz.m2d_img = rt->d_oz_m2d.as<uint8_t>();
+    rt->oz.d2m_img = rt->d_oz_d2m.as<uint8_t>();
+    rt->oz.m2d_exp = rt->d_oz_m2d_exp.as<int>();
+    rt->oz.d2m_exp = rt->d_oz_d2m_exp.as<int>();
+    rt->oz.n_dir = h.n_dir;
+    rt->oz.n_mom = h.n_mom;
+    rt->oz.npad = h.npad;
+    rt->oz.nch = h.nch;
+  }
   if ((rc = default_tiling(rt)) || (rc = build_schedule(rt)) || (rc = setup_group(rt)))
     return fail(rc);
   if (cudaStreamSynchronize(rt->stream) != cudaSuccess)
@@ -1055,8 +1081,13 @@ int ouranos_rt_set_precision(ouranos_rt* rt, int precision) {
 
 int ouranos_rt_set_fp64_contractions(ouranos_rt* rt, int mode) {
   if (!rt) return OURANOS_ERR_BAD_INPUT;
-  if (mode != OURANOS_FP64_NATIVE && mode != OURANOS_FP64_DF64 && mode != OURANOS_FP64_DF64_SWEEP)
+  if (mode != OURANOS_FP64_NATIVE && mode != OURANOS_FP64_DF64 && mode != OURANOS_FP64_DF64_SWEEP &&
+      mode != OURANOS_FP64_DF64_SWEEP_TC)
     return bad(rt, "unknown FP64 mode");
+  if (mode == OURANOS_FP64_DF64_SWEEP_TC && !rt->oz.npad) {
+    rt->err = "tensor-core FP64 contractions take at most 192 directions and 16 moments";
+    return OURANOS_ERR_UNSUPPORTED;
+  }
   rt->fp64_contract = mode;
   return OURANOS_OK;
 }

@@ -131,6 +131,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long l
   return true;
 }
 
+// one arrival of this thread (release: its earlier shared-memory writes are
+// seen by the threads that wait for the phase)
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 // the arrival of this thread, announcing `bytes` of bulk copies that
 // complete on the barrier (the phase ends when both have happened)
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
@@ -172,7 +177,17 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 
 // ------------------------------------------------------- TMEM -> registers
 // warp w reads lanes [32 (w % 4), 32 (w % 4) + 32): thread i gets lane
-// 32 (w % 4) + i, columns [col, col + 8) / [col, col + 16)
+// 32 (w % 4) + i, columns [col, col + 4) / [col, col + 8) / [col, col + 16)
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float (&v)[4]) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr)
+               : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 4; ++k) v[k] = __uint_as_float(r[k]);
+}
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
   uint32_t r[8];
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"

@@ -90,9 +90,11 @@ class RadiativeTransfer:
     def set_fp64_contractions(self, mode):
         """FP64 path arithmetic: 'native' FP64; 'df64' (moment contractions in
         double-float on the FP32 pipes, sweep in FP64); 'df64_sweep' (the sweep's
-        cell solves too; the default)."""
+        cell solves too; the default); 'df64_sweep_tc' (the double-float sweep
+        with its contractions on the tensor cores as exact BF16 digit
+        products)."""
         m = {"native": _capi.FP64_NATIVE, "df64": _capi.FP64_DF64,
-             "df64_sweep": _capi.FP64_DF64_SWEEP}[mode]
+             "df64_sweep": _capi.FP64_DF64_SWEEP, "df64_sweep_tc": _capi.FP64_DF64_SWEEP_TC}[mode]
         self._check(_capi.lib().ouranos_rt_set_fp64_contractions(self._h, m))
 
     def set_fp32_contractions(self, mode):

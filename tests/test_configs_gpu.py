@@ -55,7 +55,9 @@ def test_small_homogeneous_source_iteration():
 def test_2d_heterogeneous_q2_s16_p3_apply_every_arithmetic():
     """256 x 256 DG Q2, LS S16 (144 directions), P3 (10 moments), 8 x 8
     seeded blocks: the benchmark's Apply in the default double-float sweep,
-    the double-float contractions with an FP64 sweep, native FP64, and FP32."""
+    the same with the contractions on the tensor cores (exact digit
+    products), the double-float contractions with an FP64 sweep, native FP64,
+    and FP32."""
     import ouranos_gb300 as og
     prob = og.heterogeneous_2d(seed=1001, n=256, fe_order=2, sn=16, l_max=3, blocks=8)
     x = np.random.default_rng(1001).standard_normal(prob.vector_length)
@@ -63,30 +65,34 @@ def test_2d_heterogeneous_q2_s16_p3_apply_every_arithmetic():
     with og.RadiativeTransfer(prob) as rt:
         assert rt.tiling() == (16, 1, 1)
         errs = {}
-        for mode in ("df64_sweep", "df64", "native"):
+        for mode in ("df64_sweep", "df64_sweep_tc", "df64", "native"):
             rt.set_fp64_contractions(mode)
             errs[mode] = rel_err(rt.apply(x), ref)
         rt.set_precision("fp32")
         errs["fp32"] = rel_err(rt.apply(x), ref)
     print(errs)
-    for mode in ("df64_sweep", "df64", "native"):
+    for mode in ("df64_sweep", "df64_sweep_tc", "df64", "native"):
         assert errs[mode] < TOL64, (mode, errs)
     assert errs["fp32"] < TOL32, errs
 
 
 def test_3d_thick_glc12_apply():
     """64^3 DG Q1, GLC S12 (168 directions, 8 octants), the thick map of the
-    time-to-solution runs (seed 7000): default FP64 arithmetic and FP32."""
+    time-to-solution runs (seed 7000): default FP64 arithmetic, the
+    tensor-core contractions (four chunks of directions), and FP32."""
     import ouranos_gb300 as og
     prob = og.thick_3d(seed=7000, n=64, sn=12)
     x = np.random.default_rng(7000).standard_normal(prob.vector_length)
     ref = _oracle_apply(prob, x)
     with og.RadiativeTransfer(prob) as rt:
         e64 = rel_err(rt.apply(x), ref)
+        rt.set_fp64_contractions("df64_sweep_tc")
+        etc = rel_err(rt.apply(x), ref)
         rt.set_precision("fp32")
         e32 = rel_err(rt.apply(x), ref)
-    print(e64, e32)
+    print(e64, etc, e32)
     assert e64 < TOL64
+    assert etc < TOL64
     assert e32 < TOL32
 
 

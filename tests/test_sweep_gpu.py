@@ -304,10 +304,11 @@ def test_wait_timeout_reports_error_and_recovers():
     assert rel_err(y, ref) < TOL64
 
 
-@pytest.mark.parametrize("mode", ["native", "df64", "df64_sweep"])
+@pytest.mark.parametrize("mode", ["native", "df64", "df64_sweep", "df64_sweep_tc"])
 def test_fp64_contraction_modes_match_oracle(mode):
     """Every FP64 arithmetic (native FP64; double-float contractions; double-float
-    contractions and cell solves) keeps the 1e-12 parity bar, on P3 (expanded
+    contractions and cell solves; the latter with the contractions on the tensor
+    cores) keeps the 1e-12 parity bar, on P3 (expanded
     source), P0 (fused moments), 2-D Q1-Q4 and 3-D Q1-Q2, Apply and RHS sweeps."""
     import ouranos_gb300 as og
     probs = [og.heterogeneous_2d(seed=61, n=20, fe_order=2, sn=8, l_max=3, blocks=4),
@@ -382,7 +383,8 @@ def test_multigroup_outer_iteration_matches_oracle(dim, method, dsa):
     assert rel_err(gf, ref) < tol
 
 
-@pytest.mark.parametrize("case", ["2d-q2-p3-df64", "2d-q2-p3-native", "2d-q2-p3-fp32", "3d-q1-fused", "ragged"])
+@pytest.mark.parametrize("case", ["2d-q2-p3-df64", "2d-q2-p3-native", "2d-q2-p3-tc", "2d-q2-p3-fp32", "3d-q1-fused",
+                                  "ragged"])
 def test_pinned_host_apply_overlaps_and_matches_the_device_apply(case):
     """Apply on page-locked host vectors moves x and y in cell ranges on a copy
     stream, overlapped with the per-cell kernels on either side of the sweep;
@@ -401,6 +403,8 @@ def test_pinned_host_apply_overlaps_and_matches_the_device_apply(case):
     with og.RadiativeTransfer(prob, precision=prec) as rt:
         if case.endswith("native"):
             rt.set_fp64_contractions("native")
+        if case.endswith("tc"):
+            rt.set_fp64_contractions("df64_sweep_tc")
         x = torch.from_numpy(np.random.default_rng(8).standard_normal(prob.vector_length)).cuda()
         yd = torch.empty_like(x)
         rt.Apply(x, yd)

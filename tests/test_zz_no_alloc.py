@@ -36,7 +36,7 @@ def _noalloc(lib, rt, x, y):
     return lib.ouranos_rt_apply_noalloc(rt._h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()))
 
 
-@pytest.mark.parametrize("arith", ["fp64", "fp64-native", "fp64-df64", "fp32"])
+@pytest.mark.parametrize("arith", ["fp64", "fp64-native", "fp64-df64", "fp64-tc", "fp32"])
 @pytest.mark.parametrize("which", ["2d-p3-expanded", "3d-p0-fused", "2d-cell-order"])
 def test_apply_noalloc_matches_apply_twice(which, arith):
     """Two calls in a row give the regular Apply's result for the handle's
@@ -53,6 +53,8 @@ def test_apply_noalloc_matches_apply_twice(which, arith):
             rt.set_fp64_contractions("native")
         elif arith == "fp64-df64":
             rt.set_fp64_contractions("df64")
+        elif arith == "fp64-tc":
+            rt.set_fp64_contractions("df64_sweep_tc")
         x = torch.randn(prob.vector_length, dtype=torch.float64, device="cuda",
                         generator=torch.Generator(device="cuda").manual_seed(7))
         y_ref = torch.empty_like(x)
