@@ -189,7 +189,9 @@ int ouranos_rt_set_stream(ouranos_rt* rt, void* stream);
 /* Copy of the last error message. */
 int ouranos_rt_last_error(const ouranos_rt* rt, char* buf, size_t len);
 /* Device time (ms) of the last sweep kernel launch, measured with CUDA events
- * on the handle's stream; and the number of kernels that sweep launched. */
+ * on the handle's stream; and the number of kernels the last call launched
+ * (an Apply: scattering source, expansion, sweep, reduction and, unless the
+ * reduction writes y = x - phi itself, the combination). */
 int ouranos_rt_last_sweep_ms(const ouranos_rt* rt, double* ms, int* kernels);
 /* Tiling of the sweep kernel: cells per warp along x (and y in 3-D) and
  * directions per warp, with cells_x * cells_y * dirs == 32 (one lane per cell),

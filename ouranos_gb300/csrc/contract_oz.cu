@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(kThreads, 1) reduce_oz_kernel(const df64* __re
                                                                const int* __restrict__ bexp,
                                                                double* __restrict__ phi, int n_dir, int n_mom,
                                                                long n_dofs, long len, int* status,
-                                                               long long limit_ns) {
+                                                               long long limit_ns, const double* __restrict__ xc) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr uint32_t kSbo = kChunk / 8 * 128;     // six core matrices of K per row group
   constexpr uint32_t kAdig = kRows / 8 * kSbo;    // 128 rows x 48 directions, BF16
@@ -549,7 +549,11 @@ __global__ void __launch_bounds__(kThreads, 1) reduce_oz_kernel(const df64* __re
           if (e < len) {
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-              if (m0 + k < n_mom) phi[(long)(m0 + k) * n_dofs + e] = df64_to(acc_result(acc[k]));
+              if (m0 + k < n_mom) {
+                const long i = (long)(m0 + k) * n_dofs + e;
+                const double p = df64_to(acc_result(acc[k]));
+                phi[i] = xc ? xc[i] - p : p;  // with xc: the Apply's y = x - phi, fused
+              }
           }
         }
       }
@@ -568,7 +572,7 @@ size_t reduce_oz_smem() {
 
 template <int NCH>
 cudaError_t reduce_oz_launch(const df64* psi, const OzTables& t, double* phi, long n_dofs, long len, int* status,
-                             long long limit_ns, cudaStream_t s) {
+                             long long limit_ns, cudaStream_t s, const double* xc) {
   const size_t smem = reduce_oz_smem<NCH>();
   cudaError_t e = cudaFuncSetAttribute(reduce_oz_kernel<NCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -578,7 +582,7 @@ cudaError_t reduce_oz_launch(const df64* psi, const OzTables& t, double* phi, lo
   const long ntiles = (len + kRows - 1) / kRows;
   const int grid = (int)std::max(1L, std::min(ntiles, (long)sms));
   reduce_oz_kernel<NCH><<<grid, kThreads, smem, s>>>(psi, t.d2m_img, t.d2m_exp, phi, t.n_dir, t.n_mom, n_dofs, len,
-                                                     status, limit_ns);
+                                                     status, limit_ns, xc);
   return cudaGetLastError();
 }
 
@@ -694,14 +698,14 @@ cudaError_t launch_expand_oz(const df64* T, const df64* iso, const OzTables& t, 
 }
 
 cudaError_t launch_reduce_oz(const df64* psi, const OzTables& t, double* phi, long n_dofs, int* status,
-                             long long limit_ns, cudaStream_t s, long len) {
+                             long long limit_ns, cudaStream_t s, long len, const double* xc) {
   if (len < 0) len = n_dofs;
   if (len == 0) return cudaSuccess;
   switch (t.nch) {
-    case 1: return reduce_oz_launch<1>(psi, t, phi, n_dofs, len, status, limit_ns, s);
-    case 2: return reduce_oz_launch<2>(psi, t, phi, n_dofs, len, status, limit_ns, s);
-    case 3: return reduce_oz_launch<3>(psi, t, phi, n_dofs, len, status, limit_ns, s);
-    case 4: return reduce_oz_launch<4>(psi, t, phi, n_dofs, len, status, limit_ns, s);
+    case 1: return reduce_oz_launch<1>(psi, t, phi, n_dofs, len, status, limit_ns, s, xc);
+    case 2: return reduce_oz_launch<2>(psi, t, phi, n_dofs, len, status, limit_ns, s, xc);
+    case 3: return reduce_oz_launch<3>(psi, t, phi, n_dofs, len, status, limit_ns, s, xc);
+    case 4: return reduce_oz_launch<4>(psi, t, phi, n_dofs, len, status, limit_ns, s, xc);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -173,8 +173,9 @@ struct SymTables {
 int sym_canonical_pattern(int P, int nm, int G, const int* mom_group, const unsigned* sign);
 cudaError_t launch_expand_sym_pairs(const df64* T, const df64* iso, const SymTables& st, df64* q, int n_mom,
                                     long n_dofs, cudaStream_t s, long len = -1);
+// with xc: writes xc - phi into phi's place (the Apply's combination, fused)
 cudaError_t launch_reduce_sym_pairs(const df64* psi, const SymTables& st, double* phi, int n_mom, long n_dofs,
-                                    cudaStream_t s, long len = -1);
+                                    cudaStream_t s, long len = -1, const double* xc = nullptr);
 // The FP32 contractions on the tensor cores (contract_tc.cu): B operand
 // images of M2D and D2M (three BF16 parts each, K-major core-matrix layout),
 // built once per handle on the host.
@@ -209,7 +210,7 @@ void oz_build_tables(const std::vector<double>& m2d, const std::vector<double>& 
 cudaError_t launch_expand_oz(const df64* T, const df64* iso, const OzTables& t, df64* q, long n_dofs, int* status,
                              long long limit_ns, cudaStream_t s, long len = -1);
 cudaError_t launch_reduce_oz(const df64* psi, const OzTables& t, double* phi, long n_dofs, int* status,
-                             long long limit_ns, cudaStream_t s, long len = -1);
+                             long long limit_ns, cudaStream_t s, long len = -1, const double* xc = nullptr);
 bool tc_contractions_fit(int n_dir, int n_mom);
 void tc_build_images(const std::vector<double>& m2d, const std::vector<double>& d2m, int n_dir, int n_mom,
                      std::vector<uint8_t>& m2d_img, std::vector<uint8_t>& d2m_img, int& npad, int& kpad);
@@ -350,7 +351,7 @@ int rt_stage_out(ouranos_rt* rt, const double* dv, double* user);
 }  // namespace ouranos
 
 // cell ranges of the host-vector Apply's overlapped copies
-#define OURANOS_OVERLAP_CHUNKS 4
+#define OURANOS_OVERLAP_CHUNKS 5
 
 struct ouranos_rt {
   int device = 0;

@@ -460,19 +460,31 @@ int sweep_prepare(ouranos_rt* rt, const real* src, const real* iso, const real* 
 
 // phi = D2M psi (the moment reduction after a sweep); phi is float for the
 // FP32 sweep, double for the FP64 and double-float sweeps
+// The double-float reductions can write the Apply's y = x - phi in phi's
+// place (one rounding, as the combine kernel): one kernel and one pass over
+// phi less per Apply
+bool fused_combine(const ouranos_rt* rt) {
+  return df64_sweep(rt) && (rt->fp64_contract == OURANOS_FP64_DF64_SWEEP_TC ? rt->oz.npad > 0 : rt->sym.n_class > 0);
+}
+
 template <typename real>
-int sweep_reduce(ouranos_rt* rt, const real* psi, void* phi, long e0 = 0, long len = -1) {
-  // dofs [e0, e0 + len): psi and phi move by e0, their row stride stays n_dofs
+int sweep_reduce(ouranos_rt* rt, const real* psi, void* phi, long e0 = 0, long len = -1, const double* xc = nullptr) {
+  // dofs [e0, e0 + len): psi and phi move by e0, their row stride stays n_dofs;
+  // with xc (fused_combine only), phi receives xc - phi
   const long nd = rt->n_dofs;
   if (len < 0) len = nd;
   psi += e0;
   double* phi64 = (double*)phi + e0;
+  if (xc) {
+    if (!std::is_same<real, df64>::value || !fused_combine(rt)) return bad(rt, "no fused combination here");
+    xc += e0;
+  }
   if (std::is_same<real, df64>::value && rt->fp64_contract == OURANOS_FP64_DF64_SWEEP_TC)
     CU(launch_reduce_oz((const df64*)psi, rt->oz, phi64, nd, rt->d_ctrl.as<int>() + 1, rt->wait_limit_ns,
-                        rt->stream, len),
+                        rt->stream, len, xc),
        "moment reduction");
   else if (std::is_same<real, df64>::value && rt->sym.n_class)
-    CU(launch_reduce_sym_pairs((const df64*)psi, rt->sym, phi64, rt->n_mom, nd, rt->stream, len),
+    CU(launch_reduce_sym_pairs((const df64*)psi, rt->sym, phi64, rt->n_mom, nd, rt->stream, len, xc),
        "moment reduction");
   else if (std::is_same<real, df64>::value)
     CU(launch_reduce_moments_pairs((const df64*)psi, rt->d_d2m64.as<double>(), phi64, rt->n_dir, rt->n_mom, nd,
@@ -526,13 +538,14 @@ int sweep_launch(ouranos_rt* rt, SweepArgs<real>& a, int fm) {
 }
 
 template <typename real>
-int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd, void* phi) {
+int run_sweep(ouranos_rt* rt, const real* src, const real* iso, const real* bnd, void* phi,
+              const double* xc = nullptr) {
   SweepArgs<real> a;
   int fm = 0, kernels = 0;
   OK_OR_RETURN(sweep_prepare<real>(rt, src, iso, bnd, a, fm, kernels));
   OK_OR_RETURN(sweep_launch<real>(rt, a, fm));
   ++kernels;
-  OK_OR_RETURN(sweep_reduce<real>(rt, a.psi, phi));
+  OK_OR_RETURN(sweep_reduce<real>(rt, a.psi, phi, 0, -1, xc));
   kernels += (rt->n_mom + 15) / 16;
   rt->last_kernels = kernels;
   return OURANOS_OK;
@@ -740,10 +753,20 @@ int apply_overlapped(ouranos_rt* rt, const double* hx, double* hy) {
   int fm = 0, kernels = 0;
   const real* src = sb.as<real>();
   OK_OR_RETURN(sweep_prepare<real>(rt, src, nullptr, nullptr, a, fm, kernels, false));
-  const long cc = (nc + K - 1) / K;
+  // cell ranges of 1/8, 1/4, 1/4, 1/4, 1/8 of the cells: only the first
+  // range's copy in and the last range's copy out wait with nothing to
+  // overlap, so those two are the short ones (the middle copies hide behind
+  // the per-cell kernels of the neighbouring ranges)
+  static_assert(K == 5, "range weights below");
+  constexpr int kWeight[K + 1] = {0, 1, 3, 5, 7, 8};  // cumulative eighths
+  auto range = [&](int k, long& c0, long& cn) {
+    c0 = nc * kWeight[k] / 8;
+    cn = nc * kWeight[k + 1] / 8 - c0;
+  };
   const size_t pitch = sizeof(double) * nd;
   for (int k = 0; k < K; ++k) {
-    const long c0 = std::min(nc, k * cc), cn = std::min(nc, c0 + cc) - c0;
+    long c0 = 0, cn = 0;
+    range(k, c0, cn);
     if (cn > 0) {
       CU(cudaMemcpy2DAsync(dx + c0 * n, pitch, hx + c0 * n, pitch, sizeof(double) * cn * n, nm,
                            cudaMemcpyHostToDevice, rt->copy_stream),
@@ -757,10 +780,14 @@ int apply_overlapped(ouranos_rt* rt, const double* hx, double* hy) {
   }
   OK_OR_RETURN(sweep_launch<real>(rt, a, fm));
   for (int k = 0; k < K; ++k) {
-    const long c0 = std::min(nc, k * cc), cn = std::min(nc, c0 + cc) - c0;
+    long c0 = 0, cn = 0;
+    range(k, c0, cn);
     if (cn > 0) {
       const long e0 = c0 * n;
-      OK_OR_RETURN(sweep_reduce<real>(rt, a.psi, pb.p, e0, cn * n));
+      if (fused_combine(rt)) {  // the reduction writes the range of y = x - phi
+        OK_OR_RETURN(sweep_reduce<real>(rt, a.psi, dy, e0, cn * n, dx));
+      } else {
+        OK_OR_RETURN(sweep_reduce<real>(rt, a.psi, pb.p, e0, cn * n));
       if (f64)
         CU(launch_combine_rows<double>(dx + e0, pb.as<double>() + e0, dy + e0, nm, cn * n, nd, 1.0, -1.0,
                                        rt->stream),
@@ -769,6 +796,7 @@ int apply_overlapped(ouranos_rt* rt, const double* hx, double* hy) {
         CU(launch_combine_rows<float>(dx + e0, pb.as<float>() + e0, dy + e0, nm, cn * n, nd, 1.0, -1.0,
                                       rt->stream),
            "combine");
+      }
     }
     CU(cudaEventRecord(ev[K + k], rt->stream), "copy order");
     CU(cudaStreamWaitEvent(rt->copy_stream, ev[K + k], 0), "copy order");
@@ -780,7 +808,9 @@ int apply_overlapped(ouranos_rt* rt, const double* hx, double* hy) {
   // later work on the handle's stream (and its synchronisation) follows the copies
   CU(cudaEventRecord(ev[2 * K + 1], rt->copy_stream), "copy order");
   CU(cudaStreamWaitEvent(rt->stream, ev[2 * K + 1], 0), "copy order");
-  rt->last_kernels = 2 * K + 1 + (fm == 0 ? K : 0);
+  // per range: scattering source, expansion (expanded form), reduction and
+  // combination (unless fused); and the sweep
+  rt->last_kernels = 2 * K + 1 + (fm == 0 ? K : 0) + (fused_combine(rt) ? 0 : K);
   return OURANOS_OK;
 }
 
@@ -792,7 +822,13 @@ namespace ouranos {
 // lexicographic numbering.  Does not synchronise.
 int rt_apply_device(ouranos_rt* rt, const double* x, double* y) {
   OK_OR_RETURN(build_source(rt, x, nullptr, df64_sweep(rt)));
+  if (fused_combine(rt)) {  // the reduction writes y = x - phi
+    OK_OR_RETURN(run_sweep<df64>(rt, rt->d_src64.as<df64>(), nullptr, nullptr, y, x));
+    rt->last_kernels += 1;  // the scattering source
+    return OURANOS_OK;
+  }
   OK_OR_RETURN(sweep_into_phi(rt, false));
+  rt->last_kernels += 2;  // the scattering source and the combination
   return phi_combine(rt, x, y, 1.0, -1.0);
 }
 // rhs = D L^-1 (q + outer + inflow) with zero in-group scattering (device).

@@ -512,9 +512,12 @@ __global__ void __launch_bounds__(256) expand_sym_kernel(const df64* __restrict_
 
 // phi[m][e]: each class's P values of psi are combined into one signed sum
 // per parity group, then every moment takes D2M_rep[m] times its group's sum
+// With xc, the kernel writes out = xc - phi instead of phi (the Apply's
+// y = x - phi, rounded once, as the combine kernel would).
 template <int NM, int P, int PAT>
 __global__ void __launch_bounds__(256) reduce_sym_kernel(const df64* __restrict__ psi, SymTables st,
-                                                         double* __restrict__ phi, int nm, long n_dofs, long len) {
+                                                         double* __restrict__ phi, int nm, long n_dofs, long len,
+                                                         const double* __restrict__ xc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   df64* srep = reinterpret_cast<df64*>(smem_raw);
   int* sdir = reinterpret_cast<int*>(srep + st.n_class * nm);
@@ -560,7 +563,11 @@ __global__ void __launch_bounds__(256) reduce_sym_kernel(const df64* __restrict_
     }
 #pragma unroll
     for (int m = 0; m < NM; ++m)
-      if (m < nm) phi[(size_t)m * n_dofs + e] = df64_to(acc_result(acc[m]));
+      if (m < nm) {
+        const size_t i = (size_t)m * n_dofs + e;
+        const double p = df64_to(acc_result(acc[m]));
+        phi[i] = xc ? xc[i] - p : p;
+      }
   }
 }
 
@@ -578,16 +585,16 @@ cudaError_t expand_sym_any(const df64* T, const df64* iso, const SymTables& st, 
 }
 template <int P, int PAT>
 cudaError_t reduce_sym_any(const df64* psi, const SymTables& st, double* phi, int nm, long n_dofs, cudaStream_t s,
-                           long len) {
+                           long len, const double* xc) {
   const size_t sh = sizeof(df64) * st.n_class * nm + sizeof(int) * (st.n_class * P + 16) + sizeof(unsigned) * 8;
   if (nm <= 1)
-    reduce_sym_kernel<1, P, PAT><<<resident_grid(reduce_sym_kernel<1, P, PAT>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
+    reduce_sym_kernel<1, P, PAT><<<resident_grid(reduce_sym_kernel<1, P, PAT>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len, xc);
   else if (nm <= 4)
-    reduce_sym_kernel<4, P, PAT><<<resident_grid(reduce_sym_kernel<4, P, PAT>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
+    reduce_sym_kernel<4, P, PAT><<<resident_grid(reduce_sym_kernel<4, P, PAT>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len, xc);
   else if (nm <= 10)
-    reduce_sym_kernel<10, P, PAT><<<resident_grid(reduce_sym_kernel<10, P, PAT>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
+    reduce_sym_kernel<10, P, PAT><<<resident_grid(reduce_sym_kernel<10, P, PAT>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len, xc);
   else
-    reduce_sym_kernel<16, P, PAT><<<resident_grid(reduce_sym_kernel<16, P, PAT>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len);
+    reduce_sym_kernel<16, P, PAT><<<resident_grid(reduce_sym_kernel<16, P, PAT>, len, sh), kBlock, sh, s>>>(psi, st, phi, nm, n_dofs, len, xc);
   return cudaGetLastError();
 }
 }  // namespace
@@ -614,13 +621,13 @@ cudaError_t launch_expand_sym_pairs(const df64* T, const df64* iso, const SymTab
   return cudaErrorInvalidValue;
 }
 cudaError_t launch_reduce_sym_pairs(const df64* psi, const SymTables& st, double* phi, int n_mom, long n_dofs,
-                                    cudaStream_t s, long len) {
+                                    cudaStream_t s, long len, const double* xc) {
   if (n_mom > 16 || st.G > st.P) return cudaErrorInvalidValue;
   if (len < 0) len = n_dofs;
-  if (st.P == 4) return st.pattern == 2 ? reduce_sym_any<4, 2>(psi, st, phi, n_mom, n_dofs, s, len)
-                                        : reduce_sym_any<4, 0>(psi, st, phi, n_mom, n_dofs, s, len);
-  if (st.P == 8) return st.pattern == 3 ? reduce_sym_any<8, 3>(psi, st, phi, n_mom, n_dofs, s, len)
-                                        : reduce_sym_any<8, 0>(psi, st, phi, n_mom, n_dofs, s, len);
+  if (st.P == 4) return st.pattern == 2 ? reduce_sym_any<4, 2>(psi, st, phi, n_mom, n_dofs, s, len, xc)
+                                        : reduce_sym_any<4, 0>(psi, st, phi, n_mom, n_dofs, s, len, xc);
+  if (st.P == 8) return st.pattern == 3 ? reduce_sym_any<8, 3>(psi, st, phi, n_mom, n_dofs, s, len, xc)
+                                        : reduce_sym_any<8, 0>(psi, st, phi, n_mom, n_dofs, s, len, xc);
   return cudaErrorInvalidValue;
 }
 
