@@ -50,6 +50,15 @@ struct df64_acc {
 __device__ __forceinline__ df64_acc acc_zero() { return {0.f, 0.f}; }
 __device__ __forceinline__ df64_acc acc_from(df64 a) { return {a.hi, a.lo}; }
 
+// acc = a * b: the product as a fresh accumulator -- the value acc_fma gives
+// from acc_zero() (TwoSum(0, p) is (p, 0)), without the additions
+__device__ __forceinline__ df64_acc acc_prod(df64 a, df64 b) {
+  const float p = a.hi * b.hi;
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return {p, e};
+}
 // acc += a * b
 __device__ __forceinline__ void acc_fma(df64_acc& acc, df64 a, df64 b) {
   const float p = a.hi * b.hi;

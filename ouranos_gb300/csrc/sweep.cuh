@@ -135,7 +135,17 @@ struct Arith {
   using acc = real;
   static __device__ __forceinline__ acc zero() { return real(0); }
   static __device__ __forceinline__ acc from(real v) { return v; }
-  static __device__ __forceinline__ void fma(acc& s, real a, real b) { s += a * b; }
+  // explicit roundings (no contraction left to the compiler), so every form
+  // of the sweep rounds a dot product the same way: s = fma(a, b, s)
+  static __device__ __forceinline__ void fma(acc& s, real a, real b) {
+    if constexpr (sizeof(real) == 4) s = __fmaf_rn(a, b, s);
+    else s = __fma_rn(a, b, s);
+  }
+  // the first term of a dot product: the value fma(zero(), a, b) gives
+  static __device__ __forceinline__ acc prod(real a, real b) {
+    if constexpr (sizeof(real) == 4) return __fmul_rn(a, b);
+    else return __dmul_rn(a, b);
+  }
   static __device__ __forceinline__ real get(acc s) { return s; }
   static __device__ __forceinline__ real ldg(const real* p) { return __ldg(p); }
   static __device__ __forceinline__ real shfl_up(real v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
@@ -147,6 +157,7 @@ struct Arith<df64> {
   static __device__ __forceinline__ acc zero() { return acc_zero(); }
   static __device__ __forceinline__ acc from(df64 v) { return acc_from(v); }
   static __device__ __forceinline__ void fma(acc& s, df64 a, df64 b) { acc_fma(s, a, b); }
+  static __device__ __forceinline__ acc prod(df64 a, df64 b) { return acc_prod(a, b); }
   static __device__ __forceinline__ df64 get(acc s) { return acc_result(s); }
   static __device__ __forceinline__ df64 ldg(const df64* p) {
     const float2 t = __ldg(reinterpret_cast<const float2*>(p));
@@ -669,12 +680,12 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
         if (H == 1) {
 #pragma unroll
           for (int t = 0; t < FD; ++t) {
-            typename A::acc accx = A::zero(), accs = A::zero();
             real fx[FD], fs[FD];
             load_row<real, FD>(FX + t * FDP, fx);
             load_row<real, FD>(FS + t * FDP, fs);
+            typename A::acc accx = A::prod(fx[0], upX[0]), accs = A::prod(fs[0], upS[0]);
 #pragma unroll
-            for (int u = 0; u < FD; ++u) {
+            for (int u = 1; u < FD; ++u) {
               A::fma(accx, fx[u], upX[u]);
               A::fma(accs, fs[u], upS[u]);
             }
@@ -688,11 +699,11 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
           for (int u = 0; u < FD; ++u) upF[u] = half ? upS[u] : upX[u];
 #pragma unroll
           for (int t = 0; t < FD; ++t) {
-            typename A::acc acc = A::zero();
             real f[FD];
             load_row<real, FD>(FF + t * FDP, f);
+            typename A::acc acc = A::prod(f[0], upF[0]);
 #pragma unroll
-            for (int u = 0; u < FD; ++u) A::fma(acc, f[u], upF[u]);
+            for (int u = 1; u < FD; ++u) A::fma(acc, f[u], upF[u]);
             faceX[t] = A::get(acc);  // this lane's face; sorted out after the exchange
           }
         }
@@ -722,11 +733,11 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
           const real* FY = a.face_mass + 1 * FD * FDP;
 #pragma unroll
           for (int t = 0; t < FD; ++t) {
-            typename A::acc acc = A::zero();
             real fy[FD];
             load_row<real, FD>(FY + t * FDP, fy);
+            typename A::acc acc = A::prod(fy[0], upY[0]);
 #pragma unroll
-            for (int u = 0; u < FD; ++u) A::fma(acc, fy[u], upY[u]);
+            for (int u = 1; u < FD; ++u) A::fma(acc, fy[u], upY[u]);
             typename A::acc by = A::from(b[C::y_in(t)]);
             A::fma(by, wY, A::get(acc));
             b[C::y_in(t)] = A::get(by);
@@ -739,13 +750,15 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
           typename A::acc acc = A::zero();
           if (H == 1 || i < N) {
             if constexpr (kHoist) {
+              acc = A::prod(arow[k][0], b[0]);
 #pragma unroll
-              for (int j = 0; j < N; ++j) A::fma(acc, arow[k][j], b[j]);
+              for (int j = 1; j < N; ++j) A::fma(acc, arow[k][j], b[j]);
             } else {
               real row[N];
               load_row<real, N>(Ai + i * NP, row);
+              acc = A::prod(row[0], b[0]);
 #pragma unroll
-              for (int j = 0; j < N; ++j) A::fma(acc, row[j], b[j]);
+              for (int j = 1; j < N; ++j) A::fma(acc, row[j], b[j]);
             }
           }
           xr[k] = A::get(acc);

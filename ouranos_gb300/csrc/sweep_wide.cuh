@@ -39,9 +39,9 @@ struct WideSlot {
 template <typename real, int FD>
 __device__ __forceinline__ real face_dot(const real* row, const real* up) {
   using A = Arith<real>;
-  typename A::acc acc = A::zero();
+  typename A::acc acc = A::prod(A::ldg(row), up[0]);
 #pragma unroll 4
-  for (int u = 0; u < FD; ++u) A::fma(acc, A::ldg(row + u), up[u]);
+  for (int u = 1; u < FD; ++u) A::fma(acc, A::ldg(row + u), up[u]);
   return A::get(acc);
 }
 
@@ -182,10 +182,13 @@ __device__ __forceinline__ void sweep_wide_task(const SweepArgs<real>& a, const 
     // ---- x = A'^-1 b, rows lane + 32 k, ascending j
     const real* AT = a.ainv + ((size_t)cls * a.n_dir_class + dcls) * (size_t)(N * N);
     typename A::acc acc[NL];
+    {
+      const real b0 = sb[0];
 #pragma unroll
-    for (int k = 0; k < NL; ++k) acc[k] = A::zero();
+      for (int k = 0; k < NL; ++k) acc[k] = lane + 32 * k < N ? A::prod(A::ldg(AT + lane + 32 * k), b0) : A::zero();
+    }
 #pragma unroll 4
-    for (int j = 0; j < N; ++j) {
+    for (int j = 1; j < N; ++j) {
       const real bj = sb[j];
       const real* col = AT + (size_t)j * N + lane;
 #pragma unroll
