@@ -459,6 +459,45 @@ __host__ __device__ constexpr unsigned sym_sign(int pat, int g) {
                      : g == 4 ? 90u : g == 5 ? 60u : g == 6 ? 102u : 150u);
 }
 
+// Member f's sign in group g is (-1)^popcount(f & mask(g)): the groups are
+// rows of the Hadamard matrix of order P, so the P signed sums of a class
+// are one Walsh-Hadamard transform (log2 P butterfly levels of P additions)
+__host__ __device__ constexpr int sym_mask(int pat, int g) {
+  return pat == 2 ? g : (int)((0x73652410u >> (4 * g)) & 7u);  // 3-D: 0 1 4 2 5 6 3 7
+}
+constexpr bool sym_masks_match(int pat, int P) {
+  for (int g = 0; g < P; ++g)
+    for (int f = 0; f < P; ++f) {
+      int par = 0;
+      for (int b = f & sym_mask(pat, g); b; b >>= 1) par ^= b & 1;
+      if ((int)((sym_sign(pat, g) >> f) & 1u) != par) return false;
+    }
+  return true;
+}
+static_assert(sym_masks_match(2, 4) && sym_masks_match(3, 8), "parity groups are Hadamard rows");
+// compensated sums without renormalisation: a + b and a - b
+__device__ __forceinline__ df64_acc acc_plus(df64_acc a, df64_acc b) {
+  const float s = a.s + b.s;
+  const float bb = s - a.s;
+  return {s, (a.c + b.c) + ((a.s - (s - bb)) + (b.s - bb))};
+}
+__device__ __forceinline__ df64_acc acc_minus(df64_acc a, df64_acc b) {
+  return acc_plus(a, df64_acc{-b.s, -b.c});
+}
+// in place: w[m] <- sum_f (-1)^popcount(f & m) w[f]
+template <int P>
+__device__ __forceinline__ void hadamard(df64_acc (&w)[P]) {
+#pragma unroll
+  for (int bit = 1; bit < P; bit <<= 1)
+#pragma unroll
+    for (int f = 0; f < P; ++f)
+      if (!(f & bit)) {
+        const df64_acc u = w[f], v = w[f | bit];
+        w[f] = acc_plus(u, v);
+        w[f | bit] = acc_minus(u, v);
+      }
+}
+
 // q[d][e] for the P members d of each class: the class's products
 // M2D_rep[m] T_m are summed per parity group once, then each member adds the
 // group sums with its signs (+ iso)
@@ -495,16 +534,31 @@ __global__ void __launch_bounds__(256) expand_sym_kernel(const df64* __restrict_
             if (grp == g) acc_fma(S[g], r, t[m]);
         }
       }
-      df64 sg[P];
+      if constexpr (PAT != 0) {  // the members' signed sums by one Hadamard transform
+        df64_acc w[P];
 #pragma unroll
-      for (int g = 0; g < P; ++g) sg[g] = acc_result(S[g]);
-#pragma unroll
-      for (int f = 0; f < P; ++f) {
-        df64_acc o = acc_from(is);
+        for (int m = 0; m < P; ++m) w[m] = acc_zero();
 #pragma unroll
         for (int g = 0; g < P; ++g)
-          if (g < G) acc_add(o, neg_if(sg[g], ((PAT ? sym_sign(PAT, g) : ssign[g]) >> f) & 1u));
-        q[(size_t)sdir[c * P + f] * n_dofs + e] = acc_result(o);
+          if (g < G) w[sym_mask(PAT, g)] = S[g];
+        hadamard<P>(w);
+#pragma unroll
+        for (int f = 0; f < P; ++f) {
+          if (iso) acc_add(w[f], is);
+          q[(size_t)sdir[c * P + f] * n_dofs + e] = acc_result(w[f]);
+        }
+      } else {
+        df64 sg[P];
+#pragma unroll
+        for (int g = 0; g < P; ++g) sg[g] = acc_result(S[g]);
+#pragma unroll
+        for (int f = 0; f < P; ++f) {
+          df64_acc o = acc_from(is);
+#pragma unroll
+          for (int g = 0; g < P; ++g)
+            if (g < G) acc_add(o, neg_if(sg[g], (ssign[g] >> f) & 1u));
+          q[(size_t)sdir[c * P + f] * n_dofs + e] = acc_result(o);
+        }
       }
     }
   }
@@ -534,15 +588,24 @@ __global__ void __launch_bounds__(256) reduce_sym_kernel(const df64* __restrict_
 #pragma unroll
       for (int f = 0; f < P; ++f) ps[f] = psi[(size_t)sdir[c * P + f] * n_dofs + e];
       df64 C[P];
+      if constexpr (PAT != 0) {  // the P signed sums by one Hadamard transform
+        df64_acc w[P];
 #pragma unroll
-      for (int g = 0; g < P; ++g) {
-        C[g] = df64(0.f);
-        if (g < G) {
-          const unsigned sg = PAT ? sym_sign(PAT, g) : ssign[g];
-          df64_acc o = acc_from(neg_if(ps[0], sg & 1u));
+        for (int f = 0; f < P; ++f) w[f] = acc_from(ps[f]);
+        hadamard<P>(w);
 #pragma unroll
-          for (int f = 1; f < P; ++f) acc_add(o, neg_if(ps[f], (sg >> f) & 1u));
-          C[g] = acc_result(o);
+        for (int g = 0; g < P; ++g) C[g] = g < G ? acc_result(w[sym_mask(PAT, g)]) : df64(0.f);
+      } else {
+#pragma unroll
+        for (int g = 0; g < P; ++g) {
+          C[g] = df64(0.f);
+          if (g < G) {
+            const unsigned sg = ssign[g];
+            df64_acc o = acc_from(neg_if(ps[0], sg & 1u));
+#pragma unroll
+            for (int f = 1; f < P; ++f) acc_add(o, neg_if(ps[f], (sg >> f) & 1u));
+            C[g] = acc_result(o);
+          }
         }
       }
       const df64* rep = srep + c * nm;
