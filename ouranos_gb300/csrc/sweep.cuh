@@ -146,6 +146,8 @@ struct Arith {
     if constexpr (sizeof(real) == 4) return __fmul_rn(a, b);
     else return __dmul_rn(a, b);
   }
+  // an intermediate that only feeds further multiply-adds
+  static __device__ __forceinline__ real raw(acc s) { return s; }
   static __device__ __forceinline__ real get(acc s) { return s; }
   static __device__ __forceinline__ real ldg(const real* p) { return __ldg(p); }
   static __device__ __forceinline__ real shfl_up(real v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
@@ -158,6 +160,9 @@ struct Arith<df64> {
   static __device__ __forceinline__ acc from(df64 v) { return acc_from(v); }
   static __device__ __forceinline__ void fma(acc& s, df64 a, df64 b) { acc_fma(s, a, b); }
   static __device__ __forceinline__ acc prod(df64 a, df64 b) { return acc_prod(a, b); }
+  // an intermediate that only feeds further compensated multiply-adds, which
+  // take any hi + lo pair with a small low part: left unrenormalised
+  static __device__ __forceinline__ df64 raw(acc s) { return df64(s.s, s.c); }
   static __device__ __forceinline__ df64 get(acc s) { return acc_result(s); }
   static __device__ __forceinline__ df64 ldg(const df64* p) {
     const float2 t = __ldg(reinterpret_cast<const float2*>(p));
@@ -642,7 +647,7 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
               typename A::acc s = A::from(isv[i]);
               A::fma(s, w0, t0v[i]);
               if (FM >= 2) A::fma(s, w1, t1v[i]);
-              b[i] = A::get(s);
+              b[i] = A::raw(s);
             }
           }
         } else {
@@ -654,7 +659,7 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
               typename A::acc s = A::from(v[FM * N + i]);
               A::fma(s, w0, v[i]);
               if (FM >= 2) A::fma(s, w1, v[N + i]);
-              b[i] = A::get(s);
+              b[i] = A::raw(s);
             }
           }
         }
@@ -689,8 +694,8 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
               A::fma(accx, fx[u], upX[u]);
               A::fma(accs, fs[u], upS[u]);
             }
-            faceX[t] = A::get(accx);
-            faceS[t] = A::get(accs);
+            faceX[t] = A::raw(accx);
+            faceS[t] = A::raw(accs);
           }
         } else {  // one instruction stream: the face is selected by data, not by a branch
           const real* FF = half ? FS : FX;
@@ -704,7 +709,7 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
             typename A::acc acc = A::prod(f[0], upF[0]);
 #pragma unroll
             for (int u = 1; u < FD; ++u) A::fma(acc, f[u], upF[u]);
-            faceX[t] = A::get(acc);  // this lane's face; sorted out after the exchange
+            faceX[t] = A::raw(acc);  // this lane's face; sorted out after the exchange
           }
         }
       }
@@ -724,10 +729,10 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
         for (int t = 0; t < FD; ++t) {
           typename A::acc bx = A::from(b[C::x_in(t)]);
           A::fma(bx, wX, faceX[t]);
-          b[C::x_in(t)] = A::get(bx);
+          b[C::x_in(t)] = A::raw(bx);
           typename A::acc bs = A::from(b[C::s_in(t)]);
           A::fma(bs, wS, faceS[t]);
-          b[C::s_in(t)] = A::get(bs);
+          b[C::s_in(t)] = A::raw(bs);
         }
         if (DIM == 3) {
           const real* FY = a.face_mass + 1 * FD * FDP;
@@ -739,8 +744,8 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
 #pragma unroll
             for (int u = 1; u < FD; ++u) A::fma(acc, fy[u], upY[u]);
             typename A::acc by = A::from(b[C::y_in(t)]);
-            A::fma(by, wY, A::get(acc));
-            b[C::y_in(t)] = A::get(by);
+            A::fma(by, wY, A::raw(acc));
+            b[C::y_in(t)] = A::raw(by);
           }
         }
         // x = A'^-1 b: this lane's rows i = k H + half

@@ -42,7 +42,7 @@ __device__ __forceinline__ real face_dot(const real* row, const real* up) {
   typename A::acc acc = A::prod(A::ldg(row), up[0]);
 #pragma unroll 4
   for (int u = 1; u < FD; ++u) A::fma(acc, A::ldg(row + u), up[u]);
-  return A::get(acc);
+  return A::raw(acc);
 }
 
 template <typename real, int DIM, int P1>
@@ -163,17 +163,17 @@ __device__ __forceinline__ void sweep_wide_task(const SweepArgs<real>& a, const 
         if (C::comp(i, 0) == 0) {  // x inflow face, transverse index i / P1
           typename A::acc bx = A::from(bi);
           A::fma(bx, wX, face_dot<real, FD>(FX + (i / P1) * FDP, sX));
-          bi = A::get(bx);
+          bi = A::raw(bx);
         }
         if (C::comp(i, AS) == 0) {  // sweep-axis inflow face, transverse index i
           typename A::acc bs = A::from(bi);
           A::fma(bs, wS, face_dot<real, FD>(FS + i * FDP, sS));
-          bi = A::get(bs);
+          bi = A::raw(bs);
         }
         if (DIM == 3 && C::comp(i, 1) == 0) {  // y inflow face, transverse c_x + P1 c_z
           typename A::acc by = A::from(bi);
           A::fma(by, wY, face_dot<real, FD>(FYm + ((i % P1) + P1 * (i / (P1 * P1))) * FDP, sY));
-          bi = A::get(by);
+          bi = A::raw(by);
         }
         sb[i] = bi;
       }

@@ -593,8 +593,10 @@ __global__ void __launch_bounds__(256) reduce_sym_kernel(const df64* __restrict_
 #pragma unroll
         for (int f = 0; f < P; ++f) w[f] = acc_from(ps[f]);
         hadamard<P>(w);
+        // (the sums feed compensated multiply-adds, which take any hi + lo
+        // pair with a small low part: no renormalisation)
 #pragma unroll
-        for (int g = 0; g < P; ++g) C[g] = g < G ? acc_result(w[sym_mask(PAT, g)]) : df64(0.f);
+        for (int g = 0; g < P; ++g) C[g] = g < G ? df64(w[sym_mask(PAT, g)].s, w[sym_mask(PAT, g)].c) : df64(0.f);
       } else {
 #pragma unroll
         for (int g = 0; g < P; ++g) {
