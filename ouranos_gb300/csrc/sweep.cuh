@@ -380,8 +380,17 @@ struct Stream {
   // on 8 different 4-bank groups
   static constexpr bool VEC = (N == 4 || N == 8) && (N * sizeof(real)) % 16 == 0;
   static constexpr int PAD = VEC && ((NV * sizeof(real) / 16) % 2 == 0) ? (int)(16 / sizeof(real)) : 0;
-  static constexpr int NVP = NV + PAD;  // per-lane stride of the ring, in values
-  static constexpr size_t warp_bytes = (size_t)Prefetch<real>::RING * 32 * (NVP * sizeof(real) + sizeof(int));
+  static constexpr int NVP = NV + PAD;  // per-slot stride of the ring, in values
+  // FP32 cells solved by two lanes share one ring slot per cell (each lane
+  // copies half of the cell's values): half the ring, so more blocks fit
+  // beside the L1 the tables need (2-D Q2 S16 FP32 sweep: 0.865 -> 0.771 ms).
+  // The 8-byte sweeps keep a slot per lane: shared slots measured slower
+  // there (1.159 -> 1.258 ms at the same two blocks per SM).
+  template <int H>
+  static constexpr bool shared_slots = H == 2 && sizeof(real) == 4;
+  template <int H>
+  static constexpr size_t warp_bytes =
+      (size_t)Prefetch<real>::RING * (shared_slots<H> ? 16 : 32) * (NVP * sizeof(real) + sizeof(int));
 };
 
 // Row r of a cell solve split over H lanes: lane `half` of the pair holds rows
@@ -417,15 +426,19 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
   using A = Arith<real>;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  real* ring = reinterpret_cast<real*>(smem_raw + warp * Stream<real, FM, N>::warp_bytes);
+  real* ring = reinterpret_cast<real*>(smem_raw + warp * Stream<real, FM, N>::template warp_bytes<H>);
   constexpr int kPrefetch = Prefetch<real>::PF;
   constexpr int kRing = Prefetch<real>::RING;
-  int* cring = reinterpret_cast<int*>(ring + kRing * 32 * NVP);
+  constexpr bool kShare = Stream<real, FM, N>::template shared_slots<H>;
+  constexpr int SL = kShare ? 16 : 32;  // ring slots per plane
+  constexpr int HS = kShare ? 2 : 1;    // lanes that fill one slot
+  int* cring = reinterpret_cast<int*>(ring + kRing * SL * NVP);
   static_assert(H == 1 || H == 2, "one or two lanes per cell");
   static_assert(H == 1 || !Stream<real, FM, N>::VEC, "16-byte cells are solved by one lane");
   constexpr int NR = (N + H - 1) / H;  // rows of the cell solve per lane
   const int cell_lane = lane / H;
   const int half = H == 2 ? (lane & 1) : 0;
+  const unsigned pair_mask = H == 2 ? (3u << (lane & 30)) : (1u << lane);
   const int wc = a.wx * a.wy;
   const int kslot = cell_lane / wc;
   const int cl = cell_lane - kslot * wc;
@@ -487,15 +500,25 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
     const bool pub_x = tx + 1 < a.tiles_x && lx == a.wx - 1;
     const bool pub_y = DIM == 3 && ty + 1 < a.tiles_y && ly == a.wy - 1;
 
-    // stream the source of plane pl into ring slot pl % kRing (one cp.async group per plane)
+    // stream the source of plane pl into ring slot pl % kRing (one cp.async
+    // group per plane).  With shared slots lane half h copies the dofs 2k + h
+    // (offsets computed once per task)
+    const int slot = kShare ? cell_lane : lane;
+    const int part = kShare ? half : 0;
+    constexpr int NH = (N + HS - 1) / HS;
+    int hoff[NH];
+#pragma unroll
+    for (int k = 0; k < NH; ++k) hoff[k] = (HS * k + part < N) ? off(HS * k + part) : 0;
     auto issue = [&](int pl) {
       if (col_ok && pl < NS) {
-        real* v = ring + ((pl % kRing) * 32 + lane) * NVP;
+        real* v = ring + ((pl % kRing) * SL + slot) * NVP;
         const long cell = cell_of(pl);
         const long cb = cell * N + base;
-        const unsigned cdst = (unsigned)__cvta_generic_to_shared(cring + (pl % kRing) * 32 + lane);
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(cdst), "l"(a.cell_class + cell)
-                     : "memory");
+        if (part == 0) {
+          const unsigned cdst = (unsigned)__cvta_generic_to_shared(cring + (pl % kRing) * SL + slot);
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(cdst), "l"(a.cell_class + cell)
+                       : "memory");
+        }
         if (VEC) {  // the cell's values in physical order, 16 bytes at a time
           const long c0 = cell * N;
           if (FM == 0) {
@@ -513,17 +536,23 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
         } else if (FM == 0) {
           const real* Q = a.q + dirbase + cb;
 #pragma unroll
-          for (int i = 0; i < N; ++i) cp_async_elem(v + i, Q + off(i));
+          for (int k = 0; k < NH; ++k) {
+            const int i = HS * k + part;
+            if (HS == 1 || i < N) cp_async_elem(v + i, Q + hoff[k]);
+          }
         } else {
           const real* T = a.src + cb;
 #pragma unroll
-          for (int i = 0; i < N; ++i) {
-            cp_async_elem(v + i, T + off(i));
-            if (FM >= 2) cp_async_elem(v + N + i, T + a.n_dofs + off(i));
-            if (a.iso)
-              cp_async_elem(v + FM * N + i, a.iso + cb + off(i));
-            else
-              v[FM * N + i] = real(0);
+          for (int k = 0; k < NH; ++k) {
+            const int i = HS * k + part;
+            if (HS == 1 || i < N) {
+              cp_async_elem(v + i, T + hoff[k]);
+              if (FM >= 2) cp_async_elem(v + N + i, T + a.n_dofs + hoff[k]);
+              if (a.iso)
+                cp_async_elem(v + FM * N + i, a.iso + cb + hoff[k]);
+              else
+                v[FM * N + i] = real(0);
+            }
           }
         }
       }
@@ -624,9 +653,10 @@ __device__ __forceinline__ void sweep_task(const SweepArgs<real> a, const int ta
 #pragma unroll
       for (int t = 0; t < FD; ++t) faceX[t] = faceS[t] = real(0);
       if (act) {
-        cp_async_wait<kPrefetch - 1>();  // plane sc has landed
-        const real* v = ring + ((sc % kRing) * 32 + lane) * NVP;
-        const int cls = cring[(sc % kRing) * 32 + lane];
+        cp_async_wait<kPrefetch - 1>();  // plane sc has landed (this lane's copies)
+        if (kShare) __syncwarp(pair_mask);  // and the partner's (both lanes of a pair share act)
+        const real* v = ring + ((sc % kRing) * SL + slot) * NVP;
+        const int cls = cring[(sc % kRing) * SL + slot];
         if (VEC) {  // 16-byte loads of the slot (physical order), then canonical order
           real t0v[N], t1v[N], isv[N];
           load_cell<real, N>(v, t0v);
@@ -909,7 +939,7 @@ constexpr int l1_keep_kb() { return Stream<real, FM, N>::VEC ? 32 : 144; }
 template <typename real, int DIM, int P1, int FM, int H>
 cudaError_t launch_sweep_fm(const SweepArgs<real>& a, int grid, int block, cudaStream_t s) {
   constexpr int N = Cell<DIM, P1>::N;
-  const size_t smem = (size_t)(block / 32) * Stream<real, FM, N>::warp_bytes;
+  const size_t smem = (size_t)(block / 32) * Stream<real, FM, N>::template warp_bytes<H>;
   static bool configured = false;  // opt in to > 48 KB once per instantiation
   static int max_per_sm = 0, carve = -2;
   if (!configured) {
@@ -936,7 +966,7 @@ cudaError_t launch_sweep_batch_fm(const SweepArgs<real>* args, const int2* tmap,
                                   const int* status, const unsigned* epoch, int grid, int block,
                                   cudaStream_t s) {
   constexpr int N = Cell<DIM, P1>::N;
-  const size_t smem = (size_t)(block / 32) * Stream<real, FM, N>::warp_bytes;
+  const size_t smem = (size_t)(block / 32) * Stream<real, FM, N>::template warp_bytes<H>;
   static bool configured = false;
   static int max_per_sm = 0, carve = -2;
   if (!configured) {
