@@ -266,6 +266,17 @@ template <>
 __device__ __forceinline__ df64 from_words<df64>(unsigned w0, unsigned w1) {
   return df64(__uint_as_float(w0), __uint_as_float(w1));
 }
+// 16 bytes through the read-only path, kept in L1 with evict-last priority:
+// the cell tables are re-read every step, while the sources streamed into
+// the ring by cp.async also pass through L1 and are read once
+__device__ __forceinline__ uint4 ldg_keep(const uint4* p) {
+  uint4 u;
+  // (not volatile: a read of read-only data, which the compiler may schedule like __ldg)
+  asm("ld.global.nc.L1::evict_last.v4.u32 {%0, %1, %2, %3}, [%4];"
+      : "=r"(u.x), "=r"(u.y), "=r"(u.z), "=r"(u.w)
+      : "l"(p));
+  return u;
+}
 // A table row of NV values stored padded to whole 16-byte pieces (p 16-byte
 // aligned): read through the read-only path in 16-byte loads
 template <typename real, int NV>
@@ -274,7 +285,7 @@ __device__ __forceinline__ void load_row(const real* p, real (&o)[NV]) {
   constexpr int W = Bits<real>::W;
 #pragma unroll
   for (int k = 0; k < (NV + PER - 1) / PER; ++k) {
-    const uint4 u = __ldg(reinterpret_cast<const uint4*>(p) + k);
+    const uint4 u = ldg_keep(reinterpret_cast<const uint4*>(p) + k);
     const unsigned w[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
     for (int t = 0; t < PER; ++t)

@@ -453,6 +453,11 @@ constexpr bool sym_pattern_is(int pat, const int* g, int n) {
 constexpr int kSymGroups2[10] = {0, 1, 2, 0, 0, 3, 1, 1, 2, 2};
 constexpr int kSymGroups3[16] = {0, 1, 2, 3, 0, 4, 0, 5, 6, 1, 2, 1, 2, 3, 7, 3};
 static_assert(sym_pattern_is(2, kSymGroups2, 10) && sym_pattern_is(3, kSymGroups3, 16), "packed group tables");
+__host__ __device__ constexpr bool sym_first_in_group(int pat, int m) {
+  for (int k = 0; k < m; ++k)
+    if (sym_group(pat, k) == sym_group(pat, m)) return false;
+  return true;
+}
 __host__ __device__ constexpr unsigned sym_sign(int pat, int g) {
   return pat == 2 ? (g == 0 ? 0u : g == 1 ? 10u : g == 2 ? 12u : 6u)
                   : (g == 0 ? 0u : g == 1 ? 170u : g == 2 ? 240u : g == 3 ? 204u
@@ -526,7 +531,10 @@ __global__ void __launch_bounds__(256) expand_sym_kernel(const df64* __restrict_
         if (m >= nm) break;
         const df64 r = rep[m];
         if (PAT) {
-          acc_fma(S[sym_group(PAT, m)], r, t[m]);
+          // a group's first moment starts its sum with the exact product
+          // (the value a zero accumulator would give)
+          if (sym_first_in_group(PAT, m)) S[sym_group(PAT, m)] = acc_prod(r, t[m]);
+          else acc_fma(S[sym_group(PAT, m)], r, t[m]);
         } else {
           const int grp = sgrp[m];  // the same for every thread: uniform branches
 #pragma unroll
@@ -778,6 +786,7 @@ struct SrcArith<float> {
   __device__ static T from(double v) { return (float)v; }
   __device__ static Acc zero() { return 0.f; }
   __device__ static void fma(Acc& a, T u, T v) { a = __fmaf_rn(u, v, a); }
+  __device__ static Acc prod(T u, T v) { return __fmul_rn(u, v); }
   __device__ static float out(Acc a, T sc) { return a * sc; }
 };
 template <>
@@ -787,6 +796,7 @@ struct SrcArith<df64> {
   __device__ static T from(double v) { return df64_from(v); }
   __device__ static Acc zero() { return acc_zero(); }
   __device__ static void fma(Acc& a, T u, T v) { acc_fma(a, u, v); }
+  __device__ static Acc prod(T u, T v) { return acc_prod(u, v); }
   __device__ static df64 out(Acc a, T sc) {
     df64_acc r = acc_zero();
     acc_fma(r, acc_result(a), sc);
@@ -822,9 +832,9 @@ __global__ void __launch_bounds__(kBlock) scatter_cell_kernel(const double* __re
     real* out = src + (size_t)m * n_dofs + c * N;
 #pragma unroll 1
     for (int i = 0; i < N; ++i) {
-      typename A::Acc acc = A::zero();
+      typename A::Acc acc = A::prod(sM[i * N], xv[0]);
 #pragma unroll
-      for (int j = 0; j < N; ++j) A::fma(acc, sM[i * N + j], xv[j]);
+      for (int j = 1; j < N; ++j) A::fma(acc, sM[i * N + j], xv[j]);
       out[i] = A::out(acc, sc);
     }
   }
