@@ -208,7 +208,8 @@ int ouranos_rt_get_tiling(const ouranos_rt* rt, int* cells_x, int* cells_y, int*
 int ouranos_rt_set_wait_limit(ouranos_rt* rt, double ns);
 /* Test hook: bias the dependency target the sweep waits for by `extra` steps
  * (0 = normal).  A positive value makes the first dependent wait unsatisfiable
- * so the timeout path can be exercised without faulting the GPU. */
+ * (the sweep's edge words and the diffusion solve's grid barriers alike) so
+ * the timeout path can be exercised without faulting the GPU. */
 int ouranos_rt_debug_wait_bias(ouranos_rt* rt, int extra);
 
 /* Apply, y = x - D L^-1 M2D S x, that allocates no device memory during the

@@ -202,3 +202,26 @@ def test_multigroup_inflow_boundaries_uneven_cells(dim):
             n0 = d.vid.shape[0] * d.nodes
             assert rel_err(z[:n0] - v[:n0], ref[:n0] - v[:n0]) < TOL_CG
             assert np.array_equal(z[n0:], v[n0:])
+
+
+def test_grid_barrier_timeout_reports_error_and_recovers():
+    """A grid barrier of the diffusion CG that cannot complete (the epoch it
+    waits for is biased past what any block publishes) runs out after the
+    wait limit: OURANOS_ERR_TIMEOUT with the diffusion message, no fault, and
+    the next call on the same handle gives the same correction as before."""
+    import ouranos_gb300 as og
+    from ouranos_gb300 import _capi
+    prob = _thick()
+    with og.RadiativeTransfer(prob) as rt:
+        v = np.random.default_rng(5).standard_normal(rt.length)
+        rt.set_dsa(5)
+        ref = rt.dsa_apply(v)
+        rt.set_wait_limit(2e7)  # 20 ms
+        rt.debug_wait_bias(1)
+        with pytest.raises(_capi.OuranosError) as e:
+            rt.dsa_apply(v)
+        assert e.value.code == _capi.ERR_TIMEOUT
+        assert "barrier" in str(e.value)
+        rt.debug_wait_bias(0)
+        rt.set_wait_limit(2e9)
+        assert np.array_equal(rt.dsa_apply(v), ref)
