@@ -12,7 +12,8 @@
 
 namespace ouranos {
 
-struct df64 {
+// 8-byte aligned, so a pair moves in one 8-byte load or store
+struct __align__(8) df64 {
   float hi, lo;
   df64() = default;
   __host__ __device__ constexpr df64(float h, float l = 0.f) : hi(h), lo(l) {}

@@ -591,10 +591,19 @@ __global__ void __launch_bounds__(256) reduce_sym_kernel(const df64* __restrict_
     df64_acc acc[NM];
 #pragma unroll
     for (int m = 0; m < NM; ++m) acc[m] = acc_zero();
+    // the next class's values are loaded while this class is combined (the
+    // loads of one class no longer wait for the arithmetic of the one before)
+    df64 pn[P];
+#pragma unroll
+    for (int f = 0; f < P; ++f) pn[f] = psi[(size_t)sdir[f] * n_dofs + e];
     for (int c = 0; c < st.n_class; ++c) {
       df64 ps[P];
 #pragma unroll
-      for (int f = 0; f < P; ++f) ps[f] = psi[(size_t)sdir[c * P + f] * n_dofs + e];
+      for (int f = 0; f < P; ++f) ps[f] = pn[f];
+      if (c + 1 < st.n_class) {
+#pragma unroll
+        for (int f = 0; f < P; ++f) pn[f] = psi[(size_t)sdir[(c + 1) * P + f] * n_dofs + e];
+      }
       df64 C[P];
       if constexpr (PAT != 0) {  // the P signed sums by one Hadamard transform
         df64_acc w[P];
