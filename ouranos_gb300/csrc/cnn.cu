@@ -254,20 +254,6 @@ struct Layer {
   size_t woff, goff;  // offsets into the weight and gate arrays
 };
 
-cudaError_t conv_wgrad(int cin, int cout, const Grid& g, const __nv_bfloat16* in,
-                       const __nv_bfloat16* grad, float* dw, float* db, cudaStream_t s) {
-  const int chunk = 2048;
-  dim3 grid((unsigned)((g.voxels() + chunk - 1) / chunk), 27);
-#define CASE(CI, CO) \
-  if (cin == CI && cout == CO) { cnn::conv3_wgrad<CI, CO><<<grid, 256, 0, s>>>(g, in, grad, dw, db, chunk); return cudaGetLastError(); }
-  CASE(16, 16)
-  CASE(16, 32)
-  CASE(32, 32)
-  CASE(32, 16)
-#undef CASE
-  return cudaErrorInvalidValue;
-}
-
 }  // namespace
 
 struct ouranos_cnn {
@@ -408,13 +394,17 @@ int forward(ouranos_cnn* net, const float* feat) {
 int conv_backward(ouranos_cnn* net, int l, const __nv_bfloat16* in, const __nv_bfloat16* g_o,
                   __nv_bfloat16* g_in) {
   const Layer& L = net->L[l];
-  CN(conv_wgrad(L.cin, L.cout, L.grid, in, g_o, net->dw + L.woff, nullptr, net->stream), "weight gradient");
+  net->err.clear();
+  int rc = conv_call(net,
+                     cnn::conv3_wgrad_tc(L.cin, L.cout, L.grid, in, g_o, net->dw + L.woff, net->status, kConvWaitNs,
+                                         net->stream),
+                     "weight gradient");
+  if (rc) return rc;
   if (g_in) {
-    const int rc = conv_call(net,
-                             cnn::conv3_tc(L.cout, L.cin, L.grid, g_o, wb_of(net, l), nullptr, nullptr, g_in,
-                                           nullptr, nullptr, nullptr, net->status, kConvWaitNs, net->stream,
-                                           &net->err),
-                             "data gradient");
+    rc = conv_call(net,
+                   cnn::conv3_tc(L.cout, L.cin, L.grid, g_o, wb_of(net, l), nullptr, nullptr, g_in, nullptr, nullptr,
+                                 nullptr, net->status, kConvWaitNs, net->stream, &net->err),
+                   "data gradient");
     if (rc) return rc;
   }
   return OURANOS_OK;

@@ -8,8 +8,8 @@
 // M = voxels, N = cout, K = 27 * cin, on tcgen05.mma (BF16 inputs, FP32
 // accumulation in tensor memory, input bricks staged by TMA; cnn_tc.cu).  The
 // gradient with respect to the input is the same implicit GEMM over the
-// output gradient with the taps mirrored; the weight gradient reduces over
-// voxels in FP32.
+// output gradient with the taps mirrored; the weight gradient is a GEMM with
+// the voxels as K (rows (tap, cin), columns cout), also on tcgen05.mma.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -39,68 +39,13 @@ cudaError_t conv3_tc(int cin, int cout, const Grid& g, const __nv_bfloat16* in, 
                      const float2* mat, const float* gate, __nv_bfloat16* pre, __nv_bfloat16* gated, float* pre_f32,
                      float* gated_f32, int* status, long long limit_ns, cudaStream_t s, std::string* err);
 
-// Weight gradient: dW[tap][ci][co] += sum_v in[v + off(tap)][ci] * g[v][co],
-// dbias[co] += sum_v g[v][co].  One block per (tap, voxel chunk); thread
-// (ci, co) pairs; FP32 accumulation, one atomicAdd per weight per block.
-template <int CIN, int COUT>
-__global__ void conv3_wgrad(Grid g, const __nv_bfloat16* __restrict__ in,
-                            const __nv_bfloat16* __restrict__ grad, float* __restrict__ dw,
-                            float* __restrict__ dbias, int chunk) {
-  constexpr int PAIRS = CIN * COUT;
-  __shared__ float s_in[64][CIN];
-  __shared__ float s_g[64][COUT];
-  const long V = g.voxels();
-  const int tap = blockIdx.y;
-  const int dx = tap_dx(tap), dy = tap_dy(tap), dz = tap_dz(tap);
-  const long vbeg = (long)blockIdx.x * chunk;
-  const long vend = vbeg + chunk < V ? vbeg + chunk : V;
-  float acc[(PAIRS + 255) / 256];
-  float bacc = 0.f;
-#pragma unroll
-  for (int k = 0; k < (PAIRS + 255) / 256; ++k) acc[k] = 0.f;
-  for (long vb = vbeg; vb < vend; vb += 64) {
-    const int nv = (int)(vend - vb < 64 ? vend - vb : 64);
-    for (int e = threadIdx.x; e < 64 * CIN; e += blockDim.x) {
-      const int r = e / CIN, c = e % CIN;
-      float val = 0.f;
-      if (r < nv) {
-        const long v = vb + r;
-        const int x = (int)(v % g.nx) + dx, y = (int)((v / g.nx) % g.ny) + dy,
-                  z = (int)(v / ((long)g.nx * g.ny)) + dz;
-        if (x >= 0 && x < g.nx && y >= 0 && y < g.ny && z >= 0 && z < g.nz)
-          val = __bfloat162float(in[((long)x + (long)g.nx * (y + (long)g.ny * z)) * CIN + c]);
-      }
-      s_in[r][c] = val;
-    }
-    for (int e = threadIdx.x; e < 64 * COUT; e += blockDim.x) {
-      const int r = e / COUT, c = e % COUT;
-      s_g[r][c] = r < nv ? __bfloat162float(grad[(vb + r) * COUT + c]) : 0.f;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < (PAIRS + 255) / 256; ++k) {
-      const int pr = threadIdx.x + 256 * k;
-      if (pr < PAIRS) {
-        const int ci = pr / COUT, co = pr % COUT;
-        float s = 0.f;
-        for (int r = 0; r < nv; ++r) s += s_in[r][ci] * s_g[r][co];
-        acc[k] += s;
-      }
-    }
-    if (tap == 13 && threadIdx.x < COUT)
-      for (int r = 0; r < nv; ++r) bacc += s_g[r][threadIdx.x];
-    __syncthreads();
-  }
-#pragma unroll
-  for (int k = 0; k < (PAIRS + 255) / 256; ++k) {
-    const int pr = threadIdx.x + 256 * k;
-    if (pr < PAIRS) {
-      const int ci = pr / COUT, co = pr % COUT;
-      atomicAdd(dw + ((long)tap * CIN + ci) * COUT + co, acc[k]);
-    }
-  }
-  if (tap == 13 && threadIdx.x < COUT && dbias) atomicAdd(dbias + threadIdx.x, bacc);
-}
+// Weight gradient dW[tap][ci][co] += sum_v in[v + off(tap)][ci] * g[v][co]
+// as a tcgen05 GEMM over voxel chunks (cnn_tc.cu): rows (tap, ci), columns
+// co, BF16 products accumulated in FP32 in tensor memory, one FP32 atomic add
+// per weight per CTA; in and g 16-byte aligned.  A bounded wait that runs out
+// sets bit 0 of *status.
+cudaError_t conv3_wgrad_tc(int cin, int cout, const Grid& g, const __nv_bfloat16* in, const __nv_bfloat16* grad,
+                           float* dw, int* status, long long limit_ns, cudaStream_t s);
 
 // ---------------------------------------------------------------- continuity projection
 // Nodal fields on a grid of Q1 cells: value k (0..7) of a cell sits at its
