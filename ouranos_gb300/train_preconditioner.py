@@ -6,7 +6,7 @@
 The committed weights ouranos_gb300/weights/dsa_guess_thick3d.npz come from
 
     python -m ouranos_gb300.train_preconditioner --pairs dsa-guess --n 32 --maps 512 \\
-        --fields 8 --passes 2 --epochs 6 --out ouranos_gb300/weights/dsa_guess_thick3d.npz
+        --fields 16 --passes 2 --epochs 8 --out ouranos_gb300/weights/dsa_guess_thick3d.npz
 
 Training maps are the seeded 3-D thick diffusive material maps (seeds
 2000, 2001, ...; GLC S12); evaluation maps use other seeds.  --pairs synthetic
