@@ -278,6 +278,13 @@ struct ouranos_cnn {
   int* status_host = nullptr;  // page-locked copy, read after each synchronisation
   long step = 0;
   cudaStream_t stream = nullptr;
+  // the forward as a CUDA graph on a caller's stream (cnn_forward_on): the
+  // buffers it was recorded with, and the calls seen with them
+  cudaGraphExec_t fwd_exec = nullptr;
+  const float* fwd_in = nullptr;
+  float* fwd_out = nullptr;
+  int fwd_calls = 0;
+  cudaEvent_t fwd_ev[2] = {nullptr, nullptr};
   std::string err;
   std::vector<void*> allocs;
 };
@@ -482,6 +489,65 @@ void cnn_grid(const ouranos_cnn* net, int* nx, int* ny, int* nz) {
   *ny = net->g0.ny;
   *nz = net->g0.nz;
 }
+
+int cnn_forward_on(ouranos_cnn* net, const float* features, float* out, cudaStream_t s) {
+  if (!net || !features || !out) return OURANOS_ERR_BAD_INPUT;
+  if (features != net->fwd_in || out != net->fwd_out) {
+    if (net->fwd_exec) cudaGraphExecDestroy(net->fwd_exec);
+    net->fwd_exec = nullptr;
+    net->fwd_in = features;
+    net->fwd_out = out;
+    net->fwd_calls = 0;
+  }
+  if (!net->fwd_exec && net->fwd_calls > 0) {
+    // second call with these buffers: every kernel is configured, record the
+    // launches and the two copies (nothing runs during the recording)
+    CN(cudaStreamBeginCapture(net->stream, cudaStreamCaptureModeThreadLocal), "forward capture");
+    int rc = forward(net, features);
+    if (!rc) {
+      const cudaError_t e1 = cudaMemcpyAsync(out, net->outp, sizeof(float) * kOut * net->g0.voxels(),
+                                             cudaMemcpyDeviceToDevice, net->stream);
+      const cudaError_t e2 = cudaMemcpyAsync(net->status_host, net->status, sizeof(int), cudaMemcpyDeviceToHost,
+                                             net->stream);
+      if (e1 != cudaSuccess || e2 != cudaSuccess) rc = cnn_fail(net, e1 != cudaSuccess ? e1 : e2, "forward capture");
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(net->stream, &graph);
+    if (!rc && e == cudaSuccess) {
+      const cudaError_t ei = cudaGraphInstantiate(&net->fwd_exec, graph, 0);
+      if (ei != cudaSuccess) {
+        net->fwd_exec = nullptr;
+        rc = cnn_fail(net, ei, "forward graph");
+      }
+    } else if (!rc) {
+      rc = cnn_fail(net, e, "forward capture");
+    }
+    if (graph) cudaGraphDestroy(graph);
+    if (rc) return rc;
+  }
+  if (net->fwd_exec) {
+    CN(cudaGraphLaunch(net->fwd_exec, s), "forward graph");
+  } else {
+    // first call: the launches run (and configure their kernels) on the
+    // network's stream, between events that order them after and before s
+    for (cudaEvent_t& ev : net->fwd_ev)
+      if (!ev) CN(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "forward");
+    CN(cudaEventRecord(net->fwd_ev[0], s), "forward");
+    CN(cudaStreamWaitEvent(net->stream, net->fwd_ev[0], 0), "forward");
+    int rc = forward(net, features);
+    if (rc) return rc;
+    CN(cudaMemcpyAsync(out, net->outp, sizeof(float) * kOut * net->g0.voxels(), cudaMemcpyDeviceToDevice,
+                       net->stream),
+       "output");
+    CN(cudaMemcpyAsync(net->status_host, net->status, sizeof(int), cudaMemcpyDeviceToHost, net->stream), "status");
+    CN(cudaEventRecord(net->fwd_ev[1], net->stream), "forward");
+    CN(cudaStreamWaitEvent(s, net->fwd_ev[1], 0), "forward");
+  }
+  ++net->fwd_calls;
+  return OURANOS_OK;
+}
+
+int cnn_forward_status(ouranos_cnn* net) { return net ? conv_status(net, false) : OURANOS_OK; }
 }  // namespace ouranos
 
 // ---------------------------------------------------------------- C-ABI
@@ -581,6 +647,9 @@ int ouranos_cnn_create(int nx, int ny, int nz, unsigned long long seed, ouranos_
 int ouranos_cnn_destroy(ouranos_cnn* net) {
   if (!net) return OURANOS_OK;
   if (net->stream) cudaStreamSynchronize(net->stream);
+  if (net->fwd_exec) cudaGraphExecDestroy(net->fwd_exec);
+  for (cudaEvent_t ev : net->fwd_ev)
+    if (ev) cudaEventDestroy(ev);
   for (void* p : net->allocs) cudaFree(p);
   if (net->status_host) cudaFreeHost(net->status_host);
   if (net->stream) cudaStreamDestroy(net->stream);

@@ -319,6 +319,16 @@ int rt_dsa_apply_guess(ouranos_rt* rt, const double* v, double* out);
 int rt_pc_dsa_apply(ouranos_rt* rt, const double* v, double* out);
 // the network's cell grid
 void cnn_grid(const ouranos_cnn* net, int* nx, int* ny, int* nz);
+// The network's forward of `features` into `out` in the order of stream s,
+// without a host synchronisation.  The first call with a pair of buffers runs
+// the launches on the network's own stream, fenced by events against s (this
+// configures every kernel); the second records the same launches, the copy
+// of the output and the copy of the status word into a CUDA graph; every
+// call from then on launches that graph on s.  The status word reaches the
+// host with the work of s: cnn_forward_status reads it once s is synchronised
+// (OURANOS_ERR_TIMEOUT if a convolution's bounded wait ran out).
+int cnn_forward_on(ouranos_cnn* net, const float* features, float* out, cudaStream_t s);
+int cnn_forward_status(ouranos_cnn* net);
 // Device-side pieces the solvers use (operator.cu).
 int rt_apply_device(ouranos_rt* rt, const double* x, double* y);
 // allocation-free Apply (noalloc.cu): resolve its scratch array on `device`,

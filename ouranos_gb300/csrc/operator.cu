@@ -571,6 +571,11 @@ int finish(ouranos_rt* rt) {
                          : "sweep dependency wait timed out";
     return OURANOS_ERR_TIMEOUT;
   }
+  // the installed network's forwards on this stream (cnn_forward_on)
+  if (rt->cnn && cnn_forward_status(rt->cnn)) {
+    rt->err = "learned preconditioner: a convolution's tensor-core wait timed out";
+    return OURANOS_ERR_TIMEOUT;
+  }
   return OURANOS_OK;
 }
 

@@ -192,8 +192,10 @@ int rt_pc_dsa_apply(ouranos_rt* rt, const double* v, double* out) {
   float* y = feat + (long)kFeat * rt->n_cells;
   int rc;
   if ((rc = rt_pc_features(rt, v, feat))) return rc;
-  PC(cudaStreamSynchronize(rt->stream), "preconditioner");
-  if ((rc = ouranos_cnn_forward(rt->cnn, feat, y))) {
+  // no host synchronisation: the forward (a CUDA graph after its first two
+  // calls) runs in the order of the handle's stream, and its status word is
+  // read with the handle's own status
+  if ((rc = cnn_forward_on(rt->cnn, feat, y, rt->stream))) {
     rt->err = "network forward failed";
     return rc;
   }
