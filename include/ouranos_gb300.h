@@ -376,7 +376,12 @@ int ouranos_cnn_train_step(ouranos_cnn* net, const float* features, const float*
                            float* loss);
 int ouranos_cnn_last_error(const ouranos_cnn* net, char* buf, size_t len);
 /* install (or, with NULL, remove) the network as the handle's preconditioner;
- * UNSUPPORTED unless the mesh is 3-D DG Q1, BAD_INPUT if the grids differ */
+ * UNSUPPORTED unless the mesh is 3-D DG Q1, BAD_INPUT if the grids differ.
+ * The learned applications run the network's forward in the order of the
+ * handle's stream (a CUDA graph from the second call on), and a timeout of
+ * one of its convolutions is reported by the handle's next synchronising
+ * call, or by this call when it replaces or removes that network (TIMEOUT,
+ * after the change).  The network must stay alive while it is installed. */
 int ouranos_rt_set_preconditioner(ouranos_rt* rt, ouranos_cnn* net);
 /* network features of a residual v ([mom][dof], device FP64) into features
  * (device [cells][OURANOS_CNN_FEATURES]); scale (host, may be NULL) gets the

@@ -490,14 +490,24 @@ void cnn_grid(const ouranos_cnn* net, int* nx, int* ny, int* nz) {
   *nz = net->g0.nz;
 }
 
+void cnn_forward_release(ouranos_cnn* net) {
+  if (!net) return;
+  if (net->fwd_exec) {
+    cudaEventSynchronize(net->fwd_ev[1]);  // the last launch of the graph has ended
+    cudaGraphExecDestroy(net->fwd_exec);
+  }
+  net->fwd_exec = nullptr;
+  net->fwd_in = nullptr;
+  net->fwd_out = nullptr;
+  net->fwd_calls = 0;
+}
+
 int cnn_forward_on(ouranos_cnn* net, const float* features, float* out, cudaStream_t s) {
   if (!net || !features || !out) return OURANOS_ERR_BAD_INPUT;
   if (features != net->fwd_in || out != net->fwd_out) {
-    if (net->fwd_exec) cudaGraphExecDestroy(net->fwd_exec);
-    net->fwd_exec = nullptr;
+    cnn_forward_release(net);
     net->fwd_in = features;
     net->fwd_out = out;
-    net->fwd_calls = 0;
   }
   if (!net->fwd_exec && net->fwd_calls > 0) {
     // second call with these buffers: every kernel is configured, record the
@@ -527,6 +537,7 @@ int cnn_forward_on(ouranos_cnn* net, const float* features, float* out, cudaStre
   }
   if (net->fwd_exec) {
     CN(cudaGraphLaunch(net->fwd_exec, s), "forward graph");
+    CN(cudaEventRecord(net->fwd_ev[1], s), "forward graph");
   } else {
     // first call: the launches run (and configure their kernels) on the
     // network's stream, between events that order them after and before s
@@ -647,7 +658,7 @@ int ouranos_cnn_create(int nx, int ny, int nz, unsigned long long seed, ouranos_
 int ouranos_cnn_destroy(ouranos_cnn* net) {
   if (!net) return OURANOS_OK;
   if (net->stream) cudaStreamSynchronize(net->stream);
-  if (net->fwd_exec) cudaGraphExecDestroy(net->fwd_exec);
+  cnn_forward_release(net);
   for (cudaEvent_t ev : net->fwd_ev)
     if (ev) cudaEventDestroy(ev);
   for (void* p : net->allocs) cudaFree(p);

@@ -329,6 +329,9 @@ void cnn_grid(const ouranos_cnn* net, int* nx, int* ny, int* nz);
 // (OURANOS_ERR_TIMEOUT if a convolution's bounded wait ran out).
 int cnn_forward_on(ouranos_cnn* net, const float* features, float* out, cudaStream_t s);
 int cnn_forward_status(ouranos_cnn* net);
+// drop the recorded graph (after its last launch has ended): the buffers it
+// was recorded with may be freed
+void cnn_forward_release(ouranos_cnn* net);
 // Device-side pieces the solvers use (operator.cu).
 int rt_apply_device(ouranos_rt* rt, const double* x, double* y);
 // allocation-free Apply (noalloc.cu): resolve its scratch array on `device`,
@@ -429,6 +432,7 @@ struct ouranos_rt {
   ouranos::DevBuf d_sym_dir, d_sym_group, d_sym_sign, d_sym_m2d, d_sym_d2m;
   // learned preconditioner
   ouranos_cnn* cnn = nullptr;
+  bool cnn_pending = false;  // a forward of cnn ran on the stream since the last status check
   int pc_group = -1;
   ouranos::DevBuf d_pc_prop, d_pc_work, d_pc_feat, d_pc_nodal, d_pc_vert;
   // diffusion synthetic acceleration: CG steps (0 = off), cell coefficients,

@@ -572,7 +572,9 @@ int finish(ouranos_rt* rt) {
     return OURANOS_ERR_TIMEOUT;
   }
   // the installed network's forwards on this stream (cnn_forward_on)
-  if (rt->cnn && cnn_forward_status(rt->cnn)) {
+  const bool pending = rt->cnn_pending;
+  rt->cnn_pending = false;
+  if (pending && rt->cnn && cnn_forward_status(rt->cnn)) {
     rt->err = "learned preconditioner: a convolution's tensor-core wait timed out";
     return OURANOS_ERR_TIMEOUT;
   }

@@ -195,6 +195,7 @@ int rt_pc_dsa_apply(ouranos_rt* rt, const double* v, double* out) {
   // no host synchronisation: the forward (a CUDA graph after its first two
   // calls) runs in the order of the handle's stream, and its status word is
   // read with the handle's own status
+  rt->cnn_pending = true;
   if ((rc = cnn_forward_on(rt->cnn, feat, y, rt->stream))) {
     rt->err = "network forward failed";
     return rc;
@@ -234,8 +235,22 @@ int ouranos_rt_set_preconditioner(ouranos_rt* rt, ouranos_cnn* cnn) {
       return OURANOS_ERR_BAD_INPUT;
     }
   }
+  // a graph of the network's forward refers to the handle's feature buffers;
+  // a timeout of forwards not yet checked is reported here, after the change
+  int rc = OURANOS_OK;
+  if (rt->cnn) {
+    cudaSetDevice(rt->device);
+    cudaStreamSynchronize(rt->stream);
+    if (rt->cnn_pending && cnn_forward_status(rt->cnn)) {
+      rt->err = "learned preconditioner: a convolution's tensor-core wait timed out";
+      rc = OURANOS_ERR_TIMEOUT;
+    }
+    rt->cnn_pending = false;
+    cnn_forward_release(rt->cnn);
+  }
+  if (cnn) cnn_forward_release(cnn);
   rt->cnn = cnn;
-  return OURANOS_OK;
+  return rc;
 }
 
 int ouranos_rt_pc_features(ouranos_rt* rt, const double* v, float* features, double* scale) {

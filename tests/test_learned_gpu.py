@@ -220,6 +220,44 @@ def test_network_guess_of_the_diffusion_solve_converges_to_the_same_correction()
     assert il["converged"] and _rel(xl, xg) < 1e-6
 
 
+def test_learned_application_as_a_graph_repeats_the_first_call():
+    """ouranos_rt_pc_dsa_apply runs the network's forward in the order of the
+    operator's stream: eagerly on the first call with the handle's buffers,
+    recorded into a CUDA graph on the second, replayed after that.  Nothing on
+    this path uses atomics, so every call on the same vector gives the same
+    bits; the graph reads each call's input; another handle (other feature
+    buffers) records its own graph, and going back records the first anew."""
+    torch = pytest.importorskip("torch")
+    import ouranos_gb300 as og
+    from ouranos_gb300 import learned
+    prob = og.thick_3d(seed=2103, n=12, sn=4, block=2, width=12 * 10.0 / 64)
+    gen = torch.Generator(device="cuda").manual_seed(8)
+    net = learned.Network(12, 12, 12, seed=3)
+    with og.RadiativeTransfer(prob) as rt:
+        learned.install(rt, net)
+        rt.set_dsa(3)
+        pc = learned.guess_precondition(rt)
+        v = torch.randn(rt.length, dtype=torch.float64, device="cuda", generator=gen)
+        w = torch.randn(rt.length, dtype=torch.float64, device="cuda", generator=gen)
+        first = pc(v).cpu().numpy()
+        for _ in range(3):  # recorded, then replayed
+            assert np.array_equal(pc(v).cpu().numpy(), first)
+        other = pc(w).cpu().numpy()
+        assert _rel(other, first) > 1e-3
+        assert np.array_equal(learned.guess_precondition(rt)(w).cpu().numpy(), other)
+        with og.RadiativeTransfer(prob) as rt2:
+            learned.install(rt2, net)
+            rt2.set_dsa(3)
+            pc2 = learned.guess_precondition(rt2)
+            for _ in range(3):
+                assert np.array_equal(pc2(v).cpu().numpy(), first)
+            learned.install(rt2, None)
+        for _ in range(3):
+            assert np.array_equal(pc(v).cpu().numpy(), first)
+        learned.install(rt, None)
+    net.close()
+
+
 def test_trainer_for_the_diffusion_guess_runs():
     pytest.importorskip("torch")
     from ouranos_gb300 import learned
